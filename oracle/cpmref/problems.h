@@ -1,0 +1,57 @@
+// ORACLE — test infrastructure only. Not part of the product library.
+//
+// Problem assembly restated from the reference's problems/:
+//   Poisson (no boundary)   problems/Poisson.cpp:12-18, 164-238 (bdy_order 0 branch)
+//   PoissonWithIBC          problems/PoissonWithIBC.cpp:8-47, 50-133, 162-192
+//   HeatWithIBC             problems/HeatWithIBC.cpp:50-103, 135-169
+//   GeodesicDistance        problems/GeodesicDistance.cpp:11-413
+#pragma once
+
+#include <functional>
+#include <memory>
+#include <vector>
+
+#include "ibc.h"
+#include "solver.h"
+
+namespace cpmref {
+
+// Row kinds of the assembled system, used to build right-hand sides:
+//   0 tube row (f at the tube closest point)
+//   1 IBC DOF row whose right-hand side is f at the DOF's IBC closest point
+//     (2nd-order Dirichlet or Neumann, problems/PoissonWithIBC.cpp:99-108)
+//   2 Dirichlet value row (identity row carrying the IBC value)
+enum RowKind { ROW_TUBE = 0, ROW_IBC_F = 1, ROW_DIRICHLET = 2, ROW_OTHER = 3 };
+
+class Problem {
+  public:
+    Problem(const SurfaceSpec &surface, const std::vector<SurfaceSpec> &ibcs, size_t p, double dx);
+    // Tube from caller-supplied closest points (parity tests: "given the same closest points").
+    template <class CPF>
+    Problem(const SurfaceSpec &surface, size_t p, double dx, CPF cpf, bool) {
+        tube.BuildWith(surface, p, dx, cpf);
+        Assemble({});
+    }
+
+    Tube tube;
+    IBCSubsets ibc;
+    bool has_ibc = false;
+    SpMat L, E, Lfull, Efull;
+    std::vector<bool> identity_rows;
+    std::vector<int> row_kind;     // RowKind per system row
+    std::vector<int> row_ibc;      // IBC index for kinds 1, 2 (else -1)
+    std::vector<V3> row_point;     // evaluation point per row
+    size_t D() const { return Lfull.rows; }
+
+    // plot interpolation (with IBC columns when IBCs are present)
+    SpMat PlotMatrix() const;
+
+    // GeodesicDistance::ComputeDistance; returns phi on the system rows (not plotted).
+    // step1_jacobi_iters = 0 selects the diagonal preconditioner for the heat solve.
+    std::vector<double> GeodesicDistance(double dt, int step1_jacobi_iters, std::vector<int> *iters = nullptr) const;
+
+    // (Re)assemble L, E and, with IBCs, the rewritten Lfull/Efull on the current tube.
+    void Assemble(const std::vector<SurfaceSpec> &ibcs);
+};
+
+}  // namespace cpmref

@@ -1,0 +1,97 @@
+"""Convergence-study problems of the reference, restated for the oracle and the GPU path.
+
+Each builder returns (surface, ibcs, m, n, f, g, exact) for one grid spacing,
+following the reference's convergence-study drivers:
+  ShiftedPoissonSphere     convergence_studies/PoissonProblems/PoissonProblems.cpp:119-137
+  PoissonSphereCircleIBC   convergence_studies/PoissonProblemsWithIBC/PoissonProblemsWithIBC.cpp:230-272
+  PoissonSpherePointIBC    convergence_studies/PoissonProblemsWithIBC/PoissonProblemsWithIBC.cpp:274-317
+  ComputeCircle3DParams    convergence_studies/PoissonProblemsWithIBC/PoissonProblemsWithIBC.cpp:117-139
+Golden average orders (the reference's own pass/fail pins, +-1e-2):
+  PoissonProblems.cpp:169 and PoissonProblemsWithIBC.cpp:375-379.
+"""
+import math
+
+import numpy as np
+
+import oracle_lib as ol
+
+GOLDEN_SHIFTED_POISSON_SPHERE = 2.18548
+# order-2 lists, PoissonProblemsWithIBC.cpp:377-378
+GOLDEN_SPHERE_CIRCLE = [2.03624, 2.20571, 2.09173, 2.0828, 2.1572, 2.10696, 1.97858, 1.97003, 2.17008, 1.9772]
+GOLDEN_SPHERE_POINT = [2.16283, 2.13198, 1.92074, 2.22093, 2.27176, 2.36021, 1.89006, 2.12619, 2.22663, 2.70325]
+# PoissonProblemsWithIBC.cpp:399-424
+RAND_NUM = [0.0, 0.170, 0.297, 0.331, 0.481, 0.511, 0.631, 0.735, 0.813, 0.973]
+RAND_NUM2 = [0.25, 0.874, 0.473, 0.973, 0.812, 0.693, 0.873, 0.912, 0.945, 1.0]
+RAND_NUM3 = [0.55, 0.123, -0.743, 0.547, -0.239, -0.693, 0.731, -0.175, 0.453, -0.364]
+DX_3D = [0.2, 0.1, 0.05]  # Helpers::ConvergenceStudy(0.2, 3, ...): dx = 0.5^i * 0.2
+
+
+def sphere_harmonic(x):
+    """u = cos(3 theta) sin^3(phi) (9 cos^2(phi) - 1) with theta = atan2(y, x), phi = acos(z)."""
+    x = np.atleast_2d(x)
+    th = np.arctan2(x[:, 1], x[:, 0])
+    ph = np.arccos(np.clip(x[:, 2] / 1.0, -1, 1))
+    return np.cos(3 * th) * np.sin(ph) ** 3 * (9 * np.cos(ph) ** 2 - 1)
+
+
+def circle3d_params(normal):
+    n = np.asarray(normal, np.float64)
+    n = n / math.sqrt(float(np.dot(n, n)))
+    r, theta, phi = 0.2, 0.1, 0.2
+    pop = np.array([r * math.cos(phi) * math.sin(theta), r * math.sin(phi) * math.sin(theta), r * math.cos(theta)])
+    rho = -float(np.dot(pop, n))
+    centre = rho * n
+    return math.sqrt(1 - rho * rho), centre, n
+
+
+def shifted_poisson_sphere(dx):
+    surf = ol.sphere_desc()
+    return dict(surface=surf, ibcs=[], m=1.0, n=1.0, f=lambda x: -29.0 * sphere_harmonic(x), g=None,
+                exact=sphere_harmonic)
+
+
+def sphere_circle_ibc(dx, i):
+    R, centre, normal = circle3d_params([RAND_NUM[i], RAND_NUM2[i], RAND_NUM3[i]])
+    ibc = ol.circle3d_desc(R, centre, normal, dx, boundary_order=2)
+    return dict(surface=ol.sphere_desc(), ibcs=[ibc], m=0.0, n=-1.0, f=lambda x: 30.0 * sphere_harmonic(x),
+                g=lambda c, x: sphere_harmonic(x), exact=sphere_harmonic)
+
+
+def sphere_point_ibc(dx, i):
+    th = 2.0 * math.pi * RAND_NUM[i] - math.pi
+    ph = 2.0 * math.pi * RAND_NUM2[i] - math.pi
+    p = [math.cos(ph) * math.cos(th), math.cos(ph) * math.sin(th), math.sin(ph)]
+    ibc = ol.point_desc(p, dx, boundary_order=2)
+    return dict(surface=ol.sphere_desc(), ibcs=[ibc], m=0.0, n=-1.0, f=lambda x: 30.0 * sphere_harmonic(x),
+                g=lambda c, x: sphere_harmonic(x), exact=sphere_harmonic)
+
+
+def build_rhs(rows, f, g):
+    """PoissonWithIBC::GetRHS (problems/PoissonWithIBC.cpp:92-133) from the exported row layout."""
+    kind, ibc, pt = rows["kind"], rows["ibc"], rows["point"]
+    b = np.zeros(len(kind))
+    m = (kind == 0) | (kind == 1)
+    b[m] = f(pt[m])
+    d = kind == 2
+    if d.any():
+        for c in np.unique(ibc[d]):
+            sel = d & (ibc == c)
+            b[sel] = g(int(c), pt[sel])
+    return b
+
+
+def convergence_order(errors, dxs):
+    """Helpers::ConvergenceOrder / AverageConvergenceOrder (src/Helpers.cpp:446-463)."""
+    orders = [math.log(errors[i - 1] / errors[i]) / math.log(dxs[i - 1] / dxs[i]) for i in range(1, len(errors))]
+    return sum(orders) / len(orders), orders
+
+
+def oracle_error(spec, dx):
+    P = ol.RefProblem(spec["surface"], spec["ibcs"], 3, dx)
+    rows = P.rows()
+    b = build_rhs(rows, spec["f"], spec["g"] or (lambda c, x: 0.0))
+    u, st = P.solve(spec["m"], spec["n"], b)
+    ptr, idx, val = P.csr(4)
+    uplot = ol.csr_matvec(ptr, idx, val, u)
+    err = float(np.max(np.abs(uplot - spec["exact"](P.xp()))))
+    return err, st
