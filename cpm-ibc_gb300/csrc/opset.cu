@@ -1,0 +1,977 @@
+// Operator-set assembly: Lfull / Efull rows for the device operator.
+//
+//   no IBC:  Helpers::SetupMatrices (src/Helpers.cpp:86-93) — every tube row is
+//            the regular brick stencil, nothing is stored per row but the base
+//            point and the 12 weights already held by the tube.
+//   IBCs:    IBCSubsets::Initialize (src/IBCSubsets.cpp:11-116) and
+//            IBCMatrixManipulations::AddIBCFiniteDifference / AddIBCExtension
+//            (src/IBCMatrixManipulations.cpp:12-251,424-463) as a patch:
+//            moved stencil columns per tube row, extra IBC DOF rows whose E row
+//            is the tricubic stencil at cp-bar (negated, + 2 g), identity rows.
+// Per-node work runs in kernels (K6 IBC distance of every tube node, K7
+// closest-point Jacobian + 3x3 eigen frames of every tube node, cp-bar and
+// stencil weights); the host orders the small IBC subsets in the reference's
+// BFS order and assembles the patch lists (K8).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+#include "eig3.h"
+#include "opset.h"
+
+namespace cpm {
+
+template <class T>
+static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, const T *lval, const T *ldiag) {
+    OpView<T> v;
+    v.bv = o->tube->view();
+    v.N = o->N;
+    v.D = o->D;
+    v.key = o->tube->key.p;
+    v.base = o->base.p;
+    v.w = w;
+    v.flags = o->flags.p;
+    v.patch = o->patch.p;
+    v.p_emask = o->p_emask.p;
+    v.p_eoff = o->p_eoff.p;
+    v.p_lmask = o->p_lmask.p;
+    v.p_loff = o->p_loff.p;
+    v.moved = o->moved.p;
+    v.p_xcol = o->p_xcol.p;
+    v.p_xval = xval;
+    v.lptr = o->lptr.p;
+    v.lcol = o->lcol.p;
+    v.lval = lval;
+    v.ldiag = ldiag;
+    // FDMatrices::BuildLaplacianMatrix: -2*dim and 1, then L /= dx*dx (src/FDMatrices.cpp:28-48)
+    v.Ldiag = (T)(-6.0 / (o->dx * o->dx));
+    v.Loff = (T)(1.0 / (o->dx * o->dx));
+    return v;
+}
+
+}  // namespace cpm
+
+template <>
+cpm::OpView<double> cpm_opset_s::view<double>() const {
+    return cpm::make_view<double>(this, w.p, p_xval.p, lval.p, ldiag.p);
+}
+template <>
+cpm::OpView<float> cpm_opset_s::view<float>() const {
+    return cpm::make_view<float>(this, w32.p, p_xval32.p, lval32.p, ldiag32.p);
+}
+
+namespace cpm {
+
+// ---------------------------------------------------------------- host mirror of the tube tables
+struct HostTube {
+    std::vector<int32_t> bmap, bstart;
+    std::vector<uint64_t> bmask;
+    std::vector<uint32_t> key;
+    std::vector<double> cp;
+    int NB = 0, N1d = 0;
+    double dx = 0, xstart = 0, radius = 0;
+    int64_t N = 0;
+    int load(const cpm_tube_s *t) {
+        NB = t->g.NB;
+        N1d = t->g.N1d;
+        dx = t->g.dx;
+        xstart = t->g.xstart;
+        radius = t->g.radius;
+        N = t->N;
+        CPM_TRY(t->bmap.download(bmap, (size_t)NB * NB * NB));
+        CPM_TRY(t->bstart.download(bstart, t->nbricks));
+        CPM_TRY(t->bmask.download(bmask, t->nbricks));
+        CPM_TRY(t->key.download(key, N));
+        CPM_TRY(t->cp.download(cp, 3 * N));
+        return 0;
+    }
+    int node(int i, int j, int k) const {
+        if (i < 0 || j < 0 || k < 0 || i >= N1d || j >= N1d || k >= N1d) return -1;
+        int r = bmap[((size_t)(i >> 2) * NB + (j >> 2)) * NB + (k >> 2)];
+        if (r < 0) return -1;
+        int l = ((i & 3) << 4) | ((j & 3) << 2) | (k & 3);
+        uint64_t m = bmask[r];
+        if (!((m >> l) & 1ull)) return -1;
+        return bstart[r] + __builtin_popcountll(m & ((1ull << l) - 1ull));
+    }
+    // Node::neighbour(nbr), order +x,-x,+y,-y,+z,-z
+    int nbr(int64_t q, int d) const {
+        uint32_t kk = key[q];
+        int i = unpack_i(kk) + (d == 0) - (d == 1), j = unpack_j(kk) + (d == 2) - (d == 3), k = unpack_k(kk) + (d == 4) - (d == 5);
+        return node(i, j, k);
+    }
+    void x(int64_t q, double out[3]) const {
+        uint32_t kk = key[q];
+        out[0] = xstart + (double)unpack_i(kk) * dx;
+        out[1] = xstart + (double)unpack_j(kk) * dx;
+        out[2] = xstart + (double)unpack_k(kk) * dx;
+    }
+    // Tube::NearestTubeIndex (src/Tube.h:116-121)
+    int64_t nearest(const double p[3]) const {
+        int t[3];
+        for (int d = 0; d < 3; ++d) t[d] = (int)std::round((p[d] - xstart) / dx);
+        return node(t[0], t[1], t[2]);
+    }
+};
+
+static inline double hdot(const double *a, const double *b) {
+    double s = 0.0;
+    for (int d = 0; d < 3; ++d) s += a[d] * b[d];
+    return s;
+}
+
+// ---------------------------------------------------------------- K7: Jcp frames of the whole tube
+// Dc_c cp_r per node (FDMatrices::BuildGradientMatrices, src/FDMatrices.cpp:66-92).
+__global__ void k_cp_gradients(BrickView bv, int64_t N, const uint32_t *__restrict__ key, const double *__restrict__ cp, double dx,
+                               double *__restrict__ g) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    uint32_t kk = key[q];
+    int i = unpack_i(kk), j = unpack_j(kk), k = unpack_k(kk);
+    const double cplus = 0.5 / dx, cminus = -0.5 / dx;
+    for (int c = 0; c < 3; ++c) {
+        int np = node_at(bv, i + (c == 0), j + (c == 1), k + (c == 2));
+        int nm = node_at(bv, i - (c == 0), j - (c == 1), k - (c == 2));
+        for (int r = 0; r < 3; ++r) {
+            double s = 0.0;
+            if (np >= 0) s += cplus * cp[3 * (int64_t)np + r];
+            if (nm >= 0) s += cminus * cp[3 * (int64_t)nm + r];
+            g[9 * q + 3 * r + c] = s;
+        }
+    }
+}
+
+// (E g) for a 9-wide row-major vector on the plain tube stencil.
+__global__ void k_extend9(OpView<double> op, const double *__restrict__ g, double *__restrict__ J) {
+    int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t r = gid / 9;
+    int s = (int)(gid % 9);
+    if (r >= op.N) return;
+    J[r * 9 + s] = e_row<double, 9>(op, r, s, g);
+}
+
+// Eigenvector of the smallest eigenvalue of 0.5 (J + J^T): the unoriented surface normal
+// (IBCSubset::ComputeFrameBasedDirections, src/IBCSubset.cpp:192-228).
+__global__ void k_jcp_normals(int64_t N, const double *__restrict__ J, double *__restrict__ nrm) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    double A[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) A[r][c] = 0.5 * (J[9 * q + 3 * r + c] + J[9 * q + 3 * c + r]);
+    Eig3 e = sym_eig3(A);
+    for (int r = 0; r < 3; ++r) nrm[3 * q + r] = e.vec[r][0];
+}
+
+__global__ void k_node_coords(int64_t N, const uint32_t *__restrict__ key, double xstart, double dx, double *__restrict__ x) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    uint32_t kk = key[q];
+    x[3 * q] = xstart + (double)unpack_i(kk) * dx;
+    x[3 * q + 1] = xstart + (double)unpack_j(kk) * dx;
+    x[3 * q + 2] = xstart + (double)unpack_k(kk) * dx;
+}
+
+// ---------------------------------------------------------------- host helpers for the IBC subsets
+
+struct QueryRows {  // base points + weights of query points (computed on the device)
+    std::vector<uint32_t> base;
+    std::vector<double> w;
+};
+
+static int query_weights(const cpm_tube_s *t, const std::vector<double> &pts, QueryRows &out) {
+    int64_t n = (int64_t)pts.size() / 3;
+    out.base.clear();
+    out.w.clear();
+    if (n == 0) return 0;
+    DBuf<double> dp, dw;
+    DBuf<uint32_t> db;
+    DBuf<int32_t> err;
+    CPM_TRY(dp.upload(pts));
+    CPM_TRY(db.alloc(n));
+    CPM_TRY(dw.alloc(12 * n));
+    CPM_TRY(err.alloc(1));
+    CPM_TRY(err.zero());
+    CPM_TRY(interp_weights_dev(t, n, dp.p, db.p, dw.p, err.p));
+    std::vector<int32_t> he;
+    CPM_TRY(err.download(he, 1));
+    if (he[0]) return fail(CPM_ERR_BASEPOINT_OUTSIDE_TUBE, "Tube::ComputeBasePoints - Interpolation base point is not within the tube");
+    CPM_TRY(db.download(out.base, n));
+    CPM_TRY(dw.download(out.w, 12 * n));
+    return 0;
+}
+
+// Stencil node of sidx = 16 i + 4 j + k and its E value w2[k]*w1[j]*w0[i]
+// (src/Interpolation.cpp:99).
+static inline void stencil_entry(const HostTube &ht, const QueryRows &qr, int64_t q, int sidx, int &col, double &val) {
+    int i = sidx >> 4, j = (sidx >> 2) & 3, k = sidx & 3;
+    uint32_t b = qr.base[q];
+    col = ht.node(unpack_i(b) + i, unpack_j(b) + j, unpack_k(b) + k);
+    const double *w = &qr.w[12 * q];
+    val = w[8 + k] * w[4 + j] * w[i];
+}
+
+struct IBCData {
+    cpm_surface_desc desc;
+    std::vector<int64_t> tag_set;       // tube indices, BFS order
+    std::vector<int64_t> tag_sub;       // N -> tagging index or -1
+    std::vector<double> tag_cpc, tag_dist, tag_cpdiff, tag_dir, tag_binormal;
+    std::vector<uint8_t> tag_bdy;
+    std::vector<int64_t> dof_of_tag;    // tagging index -> dof index or -1
+    std::vector<int64_t> dof_set;       // tube indices
+    std::vector<int64_t> dof_sub;       // N -> dof index or -1
+    std::vector<double> dof_cp, dof_cpbar, dof_dir;
+    QueryRows dof_rows;                 // E_ibc stencils (at cp or cp-bar)
+    bool order2 = false, dirichlet = true;
+};
+
+// Geometry::InterpolateUnorientedVectorFromNeighbours (src/Geometry.cpp:146-188).
+static void interp_from_neighbours(const HostTube &ht, std::vector<double> &vec, const std::vector<int64_t> &set,
+                                   const std::vector<int64_t> &sub, size_t i, double tol) {
+    double acc[3] = {0, 0, 0}, first[3] = {0, 0, 0};
+    size_t num = 0;
+    for (int d = 0; d < 6; ++d) {
+        int nb = ht.nbr(set[i], d);
+        if (nb < 0) continue;
+        int64_t s = sub[nb];
+        if (s < 0) continue;
+        const double *v = &vec[3 * s];
+        if (std::sqrt(hdot(v, v)) >= tol) {
+            if (num == 0)
+                for (int k = 0; k < 3; ++k) first[k] = v[k];
+            double sg = hdot(first, v) > 0 ? 1.0 : -1.0;
+            for (int k = 0; k < 3; ++k) acc[k] = (sg > 0) ? acc[k] + v[k] : acc[k] - v[k];
+            ++num;
+        }
+    }
+    if (num > 0)
+        for (int k = 0; k < 3; ++k) vec[3 * i + k] = acc[k] / (double)num;
+}
+
+// Geometry::InterpolateUnorientedVectors + ApplyInterpolationToUnorientedVectors
+// (src/Geometry.cpp:205-266), normalised; columns restricted by colmap (-1 drops).
+static std::vector<double> interp_unoriented(const HostTube &ht, const QueryRows &qr, const std::vector<double> &vecs,
+                                             const std::vector<int64_t> *colmap) {
+    size_t n = qr.base.size();
+    std::vector<double> out(3 * n, 0.0);
+    std::vector<std::pair<int64_t, double>> ent;
+    for (size_t q = 0; q < n; ++q) {
+        ent.clear();
+        for (int s = 0; s < 64; ++s) {
+            int col;
+            double val;
+            stencil_entry(ht, qr, (int64_t)q, s, col, val);
+            if (col < 0) continue;
+            int64_t c = colmap ? (*colmap)[col] : col;
+            if (c >= 0) ent.push_back({c, val});
+        }
+        std::sort(ent.begin(), ent.end(), [](const std::pair<int64_t, double> &a, const std::pair<int64_t, double> &b) {
+            return a.first < b.first;
+        });
+        double first[3] = {0, 0, 0}, acc[3] = {0, 0, 0};
+        for (size_t e = 0; e < ent.size(); ++e) {
+            const double *v = &vecs[3 * ent[e].first];
+            if (e == 0)
+                for (int k = 0; k < 3; ++k) first[k] = v[k];
+            bool plus = hdot(first, v) > 0.0;
+            for (int k = 0; k < 3; ++k) acc[k] = plus ? acc[k] + ent[e].second * v[k] : acc[k] - ent[e].second * v[k];
+        }
+        double nn = std::sqrt(hdot(acc, acc));
+        for (int k = 0; k < 3; ++k) out[3 * q + k] = (nn > 0.0) ? acc[k] / nn : 0.0;
+    }
+    return out;
+}
+
+// Geometry::EigenDecompositionOfJcp on a subset (src/Geometry.cpp:27-69): Dc and E
+// restricted to the subset, J = E (Dc_c cp_r), frames of 0.5 (J + J^T).
+static std::vector<Eig3> subset_jcp(const HostTube &ht, const IBCData &ib, const QueryRows &qr) {
+    size_t ns = ib.tag_set.size();
+    std::vector<double> g(9 * ns, 0.0);
+    const double cplus = 0.5 / ht.dx, cminus = -0.5 / ht.dx;
+    for (size_t i = 0; i < ns; ++i)
+        for (int c = 0; c < 3; ++c) {
+            int np = ht.nbr(ib.tag_set[i], 2 * c), nm = ht.nbr(ib.tag_set[i], 2 * c + 1);
+            int64_t sp = np >= 0 ? ib.tag_sub[np] : -1, sm = nm >= 0 ? ib.tag_sub[nm] : -1;
+            for (int r = 0; r < 3; ++r) {
+                double s = 0.0;
+                if (sp >= 0) s += cplus * ib.tag_cpc[3 * sp + r];
+                if (sm >= 0) s += cminus * ib.tag_cpc[3 * sm + r];
+                g[9 * i + 3 * r + c] = s;
+            }
+        }
+    std::vector<Eig3> out(ns);
+    for (size_t i = 0; i < ns; ++i) {
+        double J[9] = {0};
+        for (int s = 0; s < 64; ++s) {
+            int col;
+            double val;
+            stencil_entry(ht, qr, (int64_t)i, s, col, val);
+            if (col < 0) continue;
+            int64_t c = ib.tag_sub[col];
+            if (c < 0) continue;
+            for (int t = 0; t < 9; ++t) J[t] += val * g[9 * c + t];
+        }
+        double A[3][3];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) A[r][c] = 0.5 * (J[3 * r + c] + J[3 * c + r]);
+        out[i] = sym_eig3(A);
+    }
+    return out;
+}
+
+// First parameterisation point of an IBC (IBCSubset::FindStartingPoint uses xp()[0]):
+// paramCircle3D vertex 0 (src/Surface.cpp:1883-1904), the point itself, or vertex 0.
+static void ibc_xp0(const cpm_surface_desc &d, const std::vector<double> &verts, double out[3]) {
+    if (d.kind == CPM_CIRCLE3D) {
+        const double *p = d.params;
+        double n[3] = {p[4], p[5], p[6]}, t1[3], t2[3];
+        if (std::fabs(n[0]) > std::fabs(n[1])) {
+            t1[0] = -n[2]; t1[1] = 0; t1[2] = n[0];
+        } else {
+            t1[0] = 0; t1[1] = n[2]; t1[2] = -n[1];
+        }
+        t2[0] = n[1] * t1[2] - n[2] * t1[1];
+        t2[1] = n[2] * t1[0] - n[0] * t1[2];
+        t2[2] = n[0] * t1[1] - n[1] * t1[0];
+        double n1 = std::sqrt(hdot(t1, t1)), n2 = std::sqrt(hdot(t2, t2));
+        for (int k = 0; k < 3; ++k) {
+            t1[k] = n1 > 0 ? t1[k] / n1 : 0;
+            t2[k] = n2 > 0 ? t2[k] / n2 : 0;
+        }
+        double c0 = std::cos(0.0), s0 = std::sin(0.0);
+        for (int k = 0; k < 3; ++k) out[k] = p[1 + k] + p[0] * (c0 * t1[k] + s0 * t2[k]);
+    } else if (d.kind == CPM_POINT) {
+        for (int k = 0; k < 3; ++k) out[k] = d.params[k];
+    } else {
+        for (int k = 0; k < 3; ++k) out[k] = verts[k];
+    }
+}
+
+static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_desc &desc, const std::vector<double> &normals,
+                          const DBuf<double> &xdev, IBCData &ib) {
+    const int64_t N = ht.N;
+    const double r = ht.radius;
+    ib.desc = desc;
+    ib.order2 = desc.boundary_order == 2;
+    if (desc.is_oriented) return fail(CPM_ERR_UNSUPPORTED, "oriented IBCs are not implemented on the device path");
+    ib.dirichlet = desc.boundary_type[0] == 0;
+    // K6: IBC closest point + distance of every tube node (bounded at 2r for meshes)
+    SurfaceObj s;
+    CPM_TRY(surface_init(s, &desc, r));
+    std::vector<double> verts;
+    if (desc.kind == CPM_TRIANGULATION || desc.kind == CPM_POLYLINE) verts.assign(desc.verts, desc.verts + 3 * desc.nverts);
+    DBuf<double> dcp, dd;
+    CPM_TRY(dcp.alloc(3 * N));
+    CPM_TRY(dd.alloc(N));
+    CPM_TRY(closest_points_dev(s.params(), N, xdev.p, dcp.p, dd.p, 2.0 * r * (1.0 + 1e-12)));
+    std::vector<double> cpc, distc;
+    CPM_TRY(dcp.download(cpc, 3 * N));
+    CPM_TRY(dd.download(distc, N));
+    // open polylines tag closest points at their end points (src/Surface.cpp:2614-2637)
+    bool open_poly = false;
+    if (desc.kind == CPM_POLYLINE && desc.nverts > 1) {
+        const double *v0 = desc.verts, *vl = desc.verts + 3 * (desc.nverts - 1);
+        bool same = v0[0] == vl[0] && v0[1] == vl[1] && v0[2] == vl[2];
+        const int64_t *lastf = desc.prims + 2 * (desc.nprims - 1);
+        open_poly = !(same || lastf[0] == 0 || lastf[1] == 0);
+    }
+    // IBCSubset::ComputeSubsetNearIBC (src/IBCSubset.cpp:39-109): BFS over tube
+    // neighbours from the node nearest xp[0], keeping dist < 2r, in queue order.
+    double xp0[3];
+    ibc_xp0(desc, verts, xp0);
+    int64_t start = ht.nearest(xp0);
+    if (start < 0) return fail(CPM_ERR_INVALID_ARG, "IBC start point is not near the tube");
+    ib.tag_sub.assign(N, -1);
+    std::vector<uint8_t> visited(N, 0);
+    std::vector<int64_t> queue{start};
+    for (size_t h = 0; h < queue.size(); ++h) {
+        int64_t cur = queue[h];
+        for (int d = 0; d < 6; ++d) {
+            int nb = ht.nbr(cur, d);
+            if (nb < 0 || visited[nb]) continue;
+            visited[nb] = 1;
+            if (distc[nb] < 2.0 * r) {
+                ib.tag_sub[nb] = (int64_t)ib.tag_set.size();
+                ib.tag_set.push_back(nb);
+                queue.push_back(nb);
+            }
+        }
+    }
+    const size_t nt = ib.tag_set.size();
+    ib.tag_cpc.resize(3 * nt);
+    ib.tag_dist.resize(nt);
+    ib.tag_bdy.assign(nt, 0);
+    for (size_t i = 0; i < nt; ++i) {
+        int64_t q = ib.tag_set[i];
+        for (int k = 0; k < 3; ++k) ib.tag_cpc[3 * i + k] = cpc[3 * q + k];
+        ib.tag_dist[i] = distc[q];
+        if (open_poly) {
+            const double *v0 = desc.verts, *vl = desc.verts + 3 * (desc.nverts - 1);
+            double d0 = 0, d1 = 0;
+            for (int k = 0; k < 3; ++k) {
+                d0 += (v0[k] - cpc[3 * q + k]) * (v0[k] - cpc[3 * q + k]);
+                d1 += (vl[k] - cpc[3 * q + k]) * (vl[k] - cpc[3 * q + k]);
+            }
+            if (std::sqrt(d0) < 1e-7)
+                ib.tag_bdy[i] = 1;
+            else if (std::sqrt(d1) < 1e-7)
+                ib.tag_bdy[i] = 2;
+        }
+    }
+    // ComputeCPdiff (src/IBCSubset.cpp:156-187) with the S-perp fix-up.
+    ib.tag_cpdiff.resize(3 * nt);
+    for (size_t i = 0; i < nt; ++i) {
+        int64_t q = ib.tag_set[i];
+        for (int k = 0; k < 3; ++k) ib.tag_cpdiff[3 * i + k] = ht.cp[3 * q + k] - ib.tag_cpc[3 * i + k];
+    }
+    if (desc.use_cp_diff_directions) return fail(CPM_ERR_UNSUPPORTED, "cp_diff directions are not implemented on the device path");
+    for (size_t i = 0; i < nt; ++i)
+        if (std::sqrt(hdot(&ib.tag_cpdiff[3 * i], &ib.tag_cpdiff[3 * i])) < desc.on_ibc_tolerance)
+            interp_from_neighbours(ht, ib.tag_cpdiff, ib.tag_set, ib.tag_sub, i, desc.on_ibc_tolerance);
+    // ComputeFrameBasedDirections (src/IBCSubset.cpp:190-268)
+    QueryRows qc;
+    CPM_TRY(query_weights(t, ib.tag_cpc, qc));
+    std::vector<double> nrm = interp_unoriented(ht, qc, normals, nullptr);
+    std::vector<Eig3> eig = subset_jcp(ht, ib, qc);
+    ib.tag_dir.assign(3 * nt, 0.0);
+    ib.tag_binormal.assign(3 * nt, 0.0);
+    for (size_t i = 0; i < nt; ++i) {
+        const double *n = &nrm[3 * i], *cd = &ib.tag_cpdiff[3 * i];
+        if (std::fabs(eig[i].val[2]) < 1e-8) {
+            double dn = hdot(n, cd);
+            for (int k = 0; k < 3; ++k) ib.tag_dir[3 * i + k] = cd[k] - dn * n[k];
+        } else {
+            double tg[3] = {eig[i].vec[0][2], eig[i].vec[1][2], eig[i].vec[2][2]};
+            double b[3] = {tg[1] * n[2] - tg[2] * n[1], tg[2] * n[0] - tg[0] * n[2], tg[0] * n[1] - tg[1] * n[0]};
+            double bc = hdot(b, cd);
+            for (int k = 0; k < 3; ++k) {
+                ib.tag_binormal[3 * i + k] = b[k];
+                ib.tag_dir[3 * i + k] = bc * b[k];
+            }
+        }
+    }
+    // IBCDOFSubset::ComputeDOFSubset (src/IBCDOFSubset.cpp:10-93)
+    const double rad = desc.dof_radius_scale * r;
+    ib.dof_sub.assign(N, -1);
+    ib.dof_of_tag.assign(nt, -1);
+    for (size_t i = 0; i < nt; ++i)
+        if (ib.tag_dist[i] < rad) {
+            ib.dof_of_tag[i] = (int64_t)ib.dof_set.size();
+            ib.dof_sub[ib.tag_set[i]] = (int64_t)ib.dof_set.size();
+            ib.dof_set.push_back(ib.tag_set[i]);
+            for (int k = 0; k < 3; ++k) {
+                ib.dof_cp.push_back(ib.tag_cpc[3 * i + k]);
+                ib.dof_dir.push_back(ib.tag_dir[3 * i + k]);
+            }
+        }
+    const size_t nd = ib.dof_set.size();
+    if (ib.order2) {
+        // cp-bar = cp_S(2 cp_c - x)  (src/IBCDOFSubset.cpp:63-73)
+        std::vector<double> proj(3 * nd);
+        for (size_t i = 0; i < nd; ++i) {
+            double x[3];
+            ht.x(ib.dof_set[i], x);
+            for (int k = 0; k < 3; ++k) proj[3 * i + k] = 2.0 * ib.dof_cp[3 * i + k] - x[k];
+        }
+        DBuf<double> dp, dc, ddist;
+        CPM_TRY(dp.upload(proj));
+        CPM_TRY(dc.alloc(3 * nd));
+        CPM_TRY(ddist.alloc(nd));
+        CPM_TRY(closest_points_dev(t->surf.params(), (int64_t)nd, dp.p, dc.p, ddist.p, 4.0 * r));
+        CPM_TRY(dc.download(ib.dof_cpbar, 3 * nd));
+        CPM_TRY(query_weights(t, ib.dof_cpbar, ib.dof_rows));
+    } else {
+        CPM_TRY(query_weights(t, ib.dof_cp, ib.dof_rows));
+    }
+    return 0;
+}
+
+// tag of the stencil entry (row director dir_r, column node col) for one IBC
+// (TagStencils, src/IBCMatrixManipulations.cpp:424-463).
+static inline bool tagged(const IBCData &ib, const double *dir_r, int col, double flip) {
+    int64_t sp = ib.tag_sub[col];
+    if (sp < 0 || ib.tag_bdy[sp] != 0) return false;
+    return flip * hdot(dir_r, &ib.tag_dir[3 * sp]) < 0.0;
+}
+
+static int build_base(cpm_opset_s *o) {
+    cpm_tube_s *t = o->tube;
+    o->N = t->N;
+    o->D = t->N;
+    o->dx = t->g.dx;
+    CPM_TRY(o->base.alloc(o->D));
+    CPM_CUDA_TRY(cudaMemcpyAsync(o->base.p, t->base.p, o->D * 4, cudaMemcpyDeviceToDevice, stream()));
+    CPM_TRY(o->w.alloc(12 * o->D));
+    CPM_CUDA_TRY(cudaMemcpyAsync(o->w.p, t->w.p, 12 * o->D * 8, cudaMemcpyDeviceToDevice, stream()));
+    CPM_TRY(o->flags.alloc(o->D));
+    CPM_TRY(o->flags.zero());
+    CPM_TRY(o->patch.alloc(o->D));
+    CPM_CUDA_TRY(cudaMemsetAsync(o->patch.p, 0xff, o->D * 4, stream()));
+    for (auto *b : {&o->p_eoff, &o->p_loff, &o->moved, &o->p_xcol, &o->lptr, &o->lcol}) CPM_TRY(b->alloc(1));
+    CPM_TRY(o->p_emask.alloc(1));
+    CPM_TRY(o->p_lmask.alloc(1));
+    for (auto *b : {&o->p_xval, &o->lval, &o->ldiag}) CPM_TRY(b->alloc(1));
+    for (auto *b : {&o->p_xval32, &o->lval32, &o->ldiag32}) CPM_TRY(b->alloc(1));
+    o->h_identity.assign(o->D, 0);
+    o->h_kind.assign(o->D, 0);
+    o->h_ibc.assign(o->D, -1);
+    CPM_TRY(t->cp.download(o->h_point, 3 * o->D));
+    return 0;
+}
+
+__global__ void k_to_float(int64_t n, const double *__restrict__ a, float *__restrict__ b) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+static int make_float_copies(cpm_opset_s *o) {
+    auto conv = [&](DBuf<double> &a, DBuf<float> &b) -> int {
+        CPM_TRY(b.alloc(a.n));
+        k_to_float<<<(unsigned)((a.n + 255) / 256), 256, 0, stream()>>>((int64_t)a.n, a.p, b.p);
+        CPM_CUDA_TRY(cudaGetLastError());
+        return 0;
+    };
+    CPM_TRY(conv(o->w, o->w32));
+    CPM_TRY(conv(o->p_xval, o->p_xval32));
+    CPM_TRY(conv(o->lval, o->lval32));
+    CPM_TRY(conv(o->ldiag, o->ldiag32));
+    return 0;
+}
+
+// Whole-tube Jcp normals (K7) on the plain (IBC-free) operator rows.
+static int tube_normals(cpm_opset_s *base, std::vector<double> &normals) {
+    cpm_tube_s *t = base->tube;
+    const int64_t N = t->N;
+    DBuf<double> g, J, nrm;
+    CPM_TRY(g.alloc(9 * N));
+    CPM_TRY(J.alloc(9 * N));
+    CPM_TRY(nrm.alloc(3 * N));
+    k_cp_gradients<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(t->view(), N, t->key.p, t->cp.p, t->g.dx, g.p);
+    k_extend9<<<(unsigned)((9 * N + 255) / 256), 256, 0, stream()>>>(base->view<double>(), g.p, J.p);
+    k_jcp_normals<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, J.p, nrm.p);
+    CPM_CUDA_TRY(cudaGetLastError());
+    CPM_TRY(nrm.download(normals, 3 * N));
+    return 0;
+}
+
+static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs) {
+    cpm_tube_s *t = o->tube;
+    HostTube ht;
+    CPM_TRY(ht.load(t));
+    const int64_t N = ht.N;
+    bool need_normals = false;
+    for (int c = 0; c < n_ibc; ++c)
+        if (!descs[c].use_cp_diff_directions) need_normals = true;
+    std::vector<double> normals;
+    if (need_normals) CPM_TRY(tube_normals(o, normals));
+    DBuf<double> xdev;
+    CPM_TRY(xdev.alloc(3 * N));
+    k_node_coords<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, t->key.p, t->g.xstart, t->g.dx, xdev.p);
+    CPM_CUDA_TRY(cudaGetLastError());
+    std::vector<IBCData> ibs(n_ibc);
+    for (int c = 0; c < n_ibc; ++c) CPM_TRY(build_ibc_data(t, ht, descs[c], normals, xdev, ibs[c]));
+
+    // column layout: IBCStartingColumns / TotalDOFs (src/IBCSubsets.cpp:74-116)
+    o->n_ibc = n_ibc;
+    o->col_start.assign(n_ibc, 0);
+    o->dcol_start.assign(n_ibc, 0);
+    if (n_ibc > 0) o->col_start[0] = o->dcol_start[0] = N;
+    for (int c = 1; c < n_ibc; ++c) {
+        if (ibs[c].order2 != ibs[0].order2)
+            return fail(CPM_ERR_UNSUPPORTED, "IBCs of mixed boundary order are not implemented on the device path");
+        o->col_start[c] = o->col_start[c - 1] + (int64_t)ibs[c - 1].dof_set.size();
+        int64_t prev_dirichlet = (ibs[c - 1].dirichlet && ibs[c - 1].order2) ? (int64_t)ibs[c - 1].dof_set.size() : 0;
+        if (ibs[c].dirichlet && ibs[c].order2) o->dcol_start[c] = o->dcol_start[c - 1] + prev_dirichlet;
+    }
+    int64_t total = 0, num2 = 0, idstart = 0;
+    for (int c = 0; c < n_ibc; ++c) {
+        if (ibs[c].dirichlet && ibs[c].order2) {
+            idstart += 1;
+            num2 += (int64_t)ibs[c].dof_set.size();
+        }
+        total += (int64_t)ibs[c].dof_set.size();
+    }
+    if (idstart) idstart = total;
+    o->total_ibc = total;
+    o->num2 = num2;
+    o->identity_rows_start = idstart;
+    const int64_t D = N + total + num2;
+    o->D = D;
+    auto value_row = [&](int c, int64_t i) -> int64_t {  // DirichletValueRow
+        if (ibs[c].order2) return idstart + i + o->dcol_start[c];
+        return idstart + i + o->col_start[c];
+    };
+
+    // ---- host row structures
+    std::vector<uint32_t> base(D, 0);
+    std::vector<double> w(12 * D, 0.0);
+    std::vector<uint8_t> flags(D, 0);
+    std::vector<int32_t> patch(D, -1);
+    std::vector<uint64_t> p_emask;
+    std::vector<uint8_t> p_lmask;
+    std::vector<int32_t> p_eoff, p_loff, moved, p_xcol, lptr{0}, lcol;
+    std::vector<double> p_xval, lval, ldiag;
+    {
+        std::vector<uint32_t> tb;
+        std::vector<double> tw;
+        CPM_TRY(t->base.download(tb, N));
+        CPM_TRY(t->w.download(tw, 12 * N));
+        std::copy(tb.begin(), tb.end(), base.begin());
+        std::copy(tw.begin(), tw.end(), w.begin());
+    }
+    std::vector<uint8_t> ident(D, 0);
+    std::vector<int32_t> kind(D, 3), rowibc(D, -1);
+    std::vector<double> point(3 * D, 0.0);
+    for (int64_t q = 0; q < N; ++q) {
+        kind[q] = 0;
+        for (int k = 0; k < 3; ++k) point[3 * q + k] = ht.cp[3 * q + k];
+    }
+
+    // ---- tube rows: moved E / L columns (MoveToIBCColumns, src/IBCMatrixManipulations.cpp:189-216)
+    int64_t nmoved = 0;
+    for (int64_t q = 0; q < N; ++q) {
+        uint64_t emask = 0;
+        uint8_t lmask = 0;
+        std::vector<int32_t> etarget, ltarget;
+        bool any = false;
+        for (int c = 0; c < n_ibc && !any; ++c)
+            if (ibs[c].tag_sub[q] >= 0) any = true;
+        if (!any) continue;
+        // E row of q: stencil at cp(q) in s order
+        for (int s = 0; s < 64; ++s) {
+            int i = s >> 4, j = (s >> 2) & 3, k = s & 3;
+            int col = ht.node(unpack_i(base[q]) + i, unpack_j(base[q]) + j, unpack_k(base[q]) + k);
+            int hits = 0;
+            int64_t tgt = -1;
+            for (int c = 0; c < n_ibc; ++c) {
+                int64_t tq = ibs[c].tag_sub[q];
+                if (tq < 0 || col < 0) continue;
+                if (tagged(ibs[c], &ibs[c].tag_dir[3 * tq], col, 1.0) && ibs[c].dof_sub[col] >= 0) {
+                    ++hits;
+                    tgt = o->col_start[c] + ibs[c].dof_sub[col];
+                }
+            }
+            if (hits > 1) return fail(CPM_ERR_UNSUPPORTED, "IBCs too close together: a stencil entry moves to two IBCs");
+            if (hits == 1) {
+                emask |= 1ull << s;
+                etarget.push_back((int32_t)tgt);
+            }
+        }
+        for (int d = 0; d < 6; ++d) {
+            int col = ht.nbr(q, d);
+            if (col < 0) continue;
+            int hits = 0;
+            int64_t tgt = -1;
+            for (int c = 0; c < n_ibc; ++c) {
+                int64_t tq = ibs[c].tag_sub[q];
+                if (tq < 0) continue;
+                if (tagged(ibs[c], &ibs[c].tag_dir[3 * tq], col, 1.0) && ibs[c].dof_sub[col] >= 0) {
+                    ++hits;
+                    tgt = o->col_start[c] + ibs[c].dof_sub[col];
+                }
+            }
+            if (hits > 1) return fail(CPM_ERR_UNSUPPORTED, "IBCs too close together: a stencil entry moves to two IBCs");
+            if (hits == 1) {
+                lmask |= (uint8_t)(1u << d);
+                ltarget.push_back((int32_t)tgt);
+            }
+        }
+        if (!emask && !lmask) continue;
+        patch[q] = (int32_t)p_emask.size();
+        p_emask.push_back(emask);
+        p_lmask.push_back(lmask);
+        p_eoff.push_back((int32_t)moved.size());
+        moved.insert(moved.end(), etarget.begin(), etarget.end());
+        p_loff.push_back((int32_t)moved.size());
+        moved.insert(moved.end(), ltarget.begin(), ltarget.end());
+        p_xcol.push_back(0);
+        p_xval.push_back(0.0);
+        if (emask) flags[q] |= F_EMOVE;
+        if (lmask) flags[q] |= F_LMOVE;
+        nmoved += (int64_t)etarget.size() + (int64_t)ltarget.size();
+    }
+    const int64_t n_tube_patched = (int64_t)p_emask.size();
+
+    // ---- IBC DOF rows and Dirichlet value rows
+    const double Ldg = -6.0 / (ht.dx * ht.dx), Lof = 1.0 / (ht.dx * ht.dx);
+    for (int c = 0; c < n_ibc; ++c) {
+        const IBCData &ib = ibs[c];
+        const int64_t nd = (int64_t)ib.dof_set.size();
+        for (int64_t i = 0; i < nd; ++i) {
+            const int64_t row = o->col_start[c] + i;
+            const int64_t node = ib.dof_set[i];
+            for (int k = 0; k < 3; ++k) point[3 * row + k] = ib.dof_cp[3 * i + k];
+            rowibc[row] = c;
+            if (ib.dirichlet && !ib.order2) {
+                // order-1 Dirichlet: identity DOF rows carrying the value
+                flags[row] = F_IDENT;
+                ident[row] = 1;
+                kind[row] = 2;
+                lptr.push_back((int32_t)lcol.size());
+                ldiag.push_back(0.0);
+                continue;
+            }
+            kind[row] = 1;
+            // E row: E_ibc stencil (at cp-bar for order 2), tags with the DOF
+            // direction and flip -1, scaled by -1 for Dirichlet
+            // (AddExtensionIBCRows, src/IBCMatrixManipulations.cpp:118-186).
+            base[row] = ib.dof_rows.base[i];
+            for (int k = 0; k < 12; ++k) w[12 * row + k] = ib.dof_rows.w[12 * i + k];
+            uint64_t emask = 0;
+            std::vector<int32_t> etarget;
+            for (int s = 0; s < 64; ++s) {
+                int ii = s >> 4, jj = (s >> 2) & 3, kk = s & 3;
+                uint32_t b = base[row];
+                int col = ht.node(unpack_i(b) + ii, unpack_j(b) + jj, unpack_k(b) + kk);
+                if (col >= 0 && tagged(ib, &ib.dof_dir[3 * i], col, -1.0) && ib.dof_sub[col] >= 0) {
+                    emask |= 1ull << s;
+                    etarget.push_back((int32_t)(o->col_start[c] + ib.dof_sub[col]));
+                }
+            }
+            patch[row] = (int32_t)p_emask.size();
+            p_emask.push_back(emask);
+            p_lmask.push_back(0);
+            p_eoff.push_back((int32_t)moved.size());
+            moved.insert(moved.end(), etarget.begin(), etarget.end());
+            p_loff.push_back((int32_t)moved.size());
+            nmoved += (int64_t)etarget.size();
+            uint8_t f = F_LCSR;
+            if (emask) f |= F_EMOVE;
+            if (ib.dirichlet) {
+                f |= F_ENEG | F_EXTRA;
+                p_xcol.push_back((int32_t)value_row(c, i));
+                p_xval.push_back(2.0);
+            } else {
+                p_xcol.push_back(0);
+                p_xval.push_back(0.0);
+            }
+            flags[row] = f;
+            // L row (AddFiniteDifferenceIBCRows, src/IBCMatrixManipulations.cpp:219-251):
+            // across the curve -> the original tube node; same side and in the DOF
+            // subset -> that DOF's column; otherwise dropped.
+            const int64_t tq = ib.tag_sub[node];
+            for (int d = 0; d < 6; ++d) {
+                int col = ht.nbr(node, d);
+                if (col < 0) continue;
+                bool tg = tq >= 0 && tagged(ib, &ib.tag_dir[3 * tq], col, 1.0);
+                if (tg) {
+                    lcol.push_back(col);
+                    lval.push_back(Lof);
+                } else if (ib.dof_sub[col] >= 0) {
+                    lcol.push_back((int32_t)(o->col_start[c] + ib.dof_sub[col]));
+                    lval.push_back(Lof);
+                }
+            }
+            lptr.push_back((int32_t)lcol.size());
+            ldiag.push_back(Ldg);
+        }
+    }
+    // Dirichlet value rows of 2nd-order IBCs: identity
+    for (int64_t row = N + total; row < D; ++row) {
+        flags[row] = F_IDENT;
+        lptr.push_back((int32_t)lcol.size());
+        ldiag.push_back(0.0);
+    }
+    for (int c = 0; c < n_ibc; ++c)
+        if (ibs[c].dirichlet)
+            for (int64_t i = 0; i < (int64_t)ibs[c].dof_set.size(); ++i) {
+                int64_t vr = value_row(c, i);
+                ident[vr] = 1;
+                kind[vr] = 2;
+                rowibc[vr] = c;
+                for (int k = 0; k < 3; ++k) point[3 * vr + k] = ibs[c].dof_cp[3 * i + k];
+            }
+    if ((int64_t)lptr.size() != D - N + 1) return fail(CPM_ERR_CUDA, "internal: IBC row count mismatch");
+    o->n_patched = n_tube_patched;
+    o->n_moved = nmoved;
+
+    // ---- upload
+    CPM_TRY(o->base.upload(base));
+    CPM_TRY(o->w.upload(w));
+    CPM_TRY(o->flags.upload(flags));
+    CPM_TRY(o->patch.upload(patch));
+    if (p_emask.empty()) {
+        p_emask.push_back(0);
+        p_lmask.push_back(0);
+        p_eoff.push_back(0);
+        p_loff.push_back(0);
+        p_xcol.push_back(0);
+        p_xval.push_back(0);
+    }
+    if (moved.empty()) moved.push_back(0);
+    if (lcol.empty()) {
+        lcol.push_back(0);
+        lval.push_back(0);
+    }
+    CPM_TRY(o->p_emask.upload(p_emask));
+    CPM_TRY(o->p_lmask.upload(p_lmask));
+    CPM_TRY(o->p_eoff.upload(p_eoff));
+    CPM_TRY(o->p_loff.upload(p_loff));
+    CPM_TRY(o->moved.upload(moved));
+    CPM_TRY(o->p_xcol.upload(p_xcol));
+    CPM_TRY(o->p_xval.upload(p_xval));
+    CPM_TRY(o->lptr.upload(lptr));
+    CPM_TRY(o->lcol.upload(lcol));
+    CPM_TRY(o->lval.upload(lval));
+    CPM_TRY(o->ldiag.upload(ldiag));
+    o->h_identity = ident;
+    o->h_kind = kind;
+    o->h_ibc = rowibc;
+    o->h_point = point;
+    o->tag_set.resize(n_ibc);
+    o->dof_set.resize(n_ibc);
+    o->dof_cp.resize(n_ibc);
+    for (int c = 0; c < n_ibc; ++c) {
+        o->tag_set[c] = ibs[c].tag_set;
+        o->dof_set[c] = ibs[c].dof_set;
+        o->dof_cp[c] = ibs[c].dof_cp;
+    }
+    return 0;
+}
+
+}  // namespace cpm
+
+using namespace cpm;
+
+extern "C" int cpm_opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, cpm_opset_t *out) {
+    if (!t || !out || n_ibc < 0 || (n_ibc > 0 && !ibcs)) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
+    *out = nullptr;
+    cpm_opset_s *o = new cpm_opset_s();
+    o->tube = t;
+    int rc = build_base(o);
+    if (!rc && n_ibc > 0) rc = build_ibc(o, n_ibc, ibcs);
+    if (!rc) rc = make_float_copies(o);
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(stream());
+        if (e != cudaSuccess) rc = fail(CPM_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (rc) {
+        delete o;
+        return rc;
+    }
+    *out = o;
+    return 0;
+}
+
+extern "C" int cpm_opset_sizes(cpm_opset_t o, int64_t *s) {
+    if (!o || !s) return fail(CPM_ERR_INVALID_ARG, "null argument");
+    s[0] = o->D;
+    s[1] = o->N;
+    s[2] = o->total_ibc;
+    s[3] = o->num2;
+    s[4] = o->n_ibc;
+    s[5] = o->n_patched;
+    s[6] = o->n_moved;
+    return 0;
+}
+
+extern "C" int cpm_opset_rows(cpm_opset_t o, uint8_t *identity, int32_t *kind, int32_t *ibc, double *point) {
+    if (!o) return fail(CPM_ERR_INVALID_ARG, "null opset");
+    for (int64_t r = 0; r < o->D; ++r) {
+        if (identity) identity[r] = o->h_identity[r];
+        if (kind) kind[r] = o->h_kind[r];
+        if (ibc) ibc[r] = o->h_ibc[r];
+        if (point)
+            for (int k = 0; k < 3; ++k) point[3 * r + k] = o->h_point[3 * r + k];
+    }
+    return 0;
+}
+
+extern "C" int cpm_opset_ibc_sizes(cpm_opset_t o, int32_t c, int64_t *s) {
+    if (!o || c < 0 || c >= o->n_ibc || !s) return fail(CPM_ERR_INVALID_ARG, "invalid IBC index");
+    s[0] = (int64_t)o->tag_set[c].size();
+    s[1] = (int64_t)o->dof_set[c].size();
+    s[2] = o->col_start[c];
+    s[3] = o->dcol_start[c];
+    s[4] = o->identity_rows_start;
+    return 0;
+}
+
+extern "C" int cpm_opset_ibc_export(cpm_opset_t o, int32_t c, int64_t *tag_set, int64_t *dof_set, double *dof_cp) {
+    if (!o || c < 0 || c >= o->n_ibc) return fail(CPM_ERR_INVALID_ARG, "invalid IBC index");
+    if (tag_set) std::copy(o->tag_set[c].begin(), o->tag_set[c].end(), tag_set);
+    if (dof_set) std::copy(o->dof_set[c].begin(), o->dof_set[c].end(), dof_set);
+    if (dof_cp) std::copy(o->dof_cp[c].begin(), o->dof_cp[c].end(), dof_cp);
+    return 0;
+}
+
+// Lfull / Efull as CSR (sorted columns) reconstructed from the device rows.
+extern "C" int cpm_opset_export_csr(cpm_opset_t o, int32_t which, int64_t *nnz, int64_t *ptr, int64_t *idx, double *val) {
+    if (!o || !nnz || (which != 0 && which != 1)) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
+    HostTube ht;
+    CPM_TRY(ht.load(o->tube));
+    const int64_t D = o->D, N = o->N;
+    std::vector<uint32_t> base;
+    std::vector<double> w, p_xval, lval, ldiag;
+    std::vector<uint8_t> flags, p_lmask;
+    std::vector<int32_t> patch, p_eoff, p_loff, moved, p_xcol, lptr, lcol;
+    std::vector<uint64_t> p_emask;
+    CPM_TRY(o->base.download(base, D));
+    CPM_TRY(o->w.download(w, 12 * D));
+    CPM_TRY(o->flags.download(flags, D));
+    CPM_TRY(o->patch.download(patch, D));
+    CPM_TRY(o->p_emask.download(p_emask, o->p_emask.n));
+    CPM_TRY(o->p_lmask.download(p_lmask, o->p_lmask.n));
+    CPM_TRY(o->p_eoff.download(p_eoff, o->p_eoff.n));
+    CPM_TRY(o->p_loff.download(p_loff, o->p_loff.n));
+    CPM_TRY(o->moved.download(moved, o->moved.n));
+    CPM_TRY(o->p_xcol.download(p_xcol, o->p_xcol.n));
+    CPM_TRY(o->p_xval.download(p_xval, o->p_xval.n));
+    CPM_TRY(o->lptr.download(lptr, o->lptr.n));
+    CPM_TRY(o->lcol.download(lcol, o->lcol.n));
+    CPM_TRY(o->lval.download(lval, o->lval.n));
+    CPM_TRY(o->ldiag.download(ldiag, o->ldiag.n));
+    const double Ldg = -6.0 / (o->dx * o->dx), Lof = 1.0 / (o->dx * o->dx);
+    std::vector<std::pair<int64_t, double>> row;
+    int64_t count = 0;
+    if (ptr) ptr[0] = 0;
+    for (int64_t r = 0; r < D; ++r) {
+        row.clear();
+        uint8_t f = flags[r];
+        if (f & F_IDENT) {
+            row.push_back({r, 1.0});
+        } else if (which == 1) {
+            int pi = patch[r];
+            uint64_t emask = (pi >= 0) ? p_emask[pi] : 0;
+            int eoff = (pi >= 0) ? p_eoff[pi] : 0;
+            uint32_t b = base[r];
+            double sg = (f & F_ENEG) ? -1.0 : 1.0;
+            for (int s = 0; s < 64; ++s) {
+                int i = s >> 4, j = (s >> 2) & 3, k = s & 3;
+                int64_t col = ((emask >> s) & 1ull) ? moved[eoff + __builtin_popcountll(emask & ((1ull << s) - 1ull))]
+                                                    : ht.node(unpack_i(b) + i, unpack_j(b) + j, unpack_k(b) + k);
+                row.push_back({col, sg * (w[12 * r + 8 + k] * w[12 * r + 4 + j] * w[12 * r + i])});
+            }
+            if (f & F_EXTRA) row.push_back({p_xcol[pi], p_xval[pi]});
+        } else if (r < N) {
+            int pi = patch[r];
+            uint8_t lm = (pi >= 0) ? p_lmask[pi] : 0;
+            int loff = (pi >= 0) ? p_loff[pi] : 0;
+            row.push_back({r, Ldg});
+            for (int d = 0; d < 6; ++d) {
+                int64_t col = ((lm >> d) & 1) ? moved[loff + __builtin_popcount((unsigned)lm & ((1u << d) - 1u))] : ht.nbr(r, d);
+                if (col >= 0) row.push_back({col, Lof});
+            }
+        } else {
+            int64_t q = r - N;
+            row.push_back({r, ldiag[q]});
+            for (int e = lptr[q]; e < lptr[q + 1]; ++e) row.push_back({lcol[e], lval[e]});
+        }
+        std::sort(row.begin(), row.end(),
+                  [](const std::pair<int64_t, double> &a, const std::pair<int64_t, double> &b) { return a.first < b.first; });
+        if (idx)
+            for (size_t e = 0; e < row.size(); ++e) {
+                idx[count + e] = row[e].first;
+                val[count + e] = row[e].second;
+            }
+        count += (int64_t)row.size();
+        if (ptr) ptr[r + 1] = count;
+    }
+    *nnz = count;
+    return 0;
+}
+
+extern "C" int cpm_opset_destroy(cpm_opset_t o) {
+    delete o;
+    return 0;
+}

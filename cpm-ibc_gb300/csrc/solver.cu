@@ -1,0 +1,784 @@
+// BiCGStab on the device, batched over K slot columns (row-major [D][K]).
+//
+//   K9   E pass  t = E~ x                          (Interpolation, src/GeneralizedBiCGStabSystem.h:235-261)
+//        L pass  y = m x + n (Ldiag x + Loff t)    (LnodiagTimesX/LdiagTimesX/FinalizeMultiplication :65-189)
+//        with the BiCGStab dot products fused into the L pass epilogue
+//   K10  vector updates of BiCGStab::Solve (src/BiCGStab.h:41-103) fused with
+//        their reductions; per-slot scalars stay on the device; reductions are
+//        accumulated in FP64 with a fixed-order two-level tree (deterministic
+//        and independent of the other slots' contents)
+//   K11  FP64 iterative refinement around an FP32 inner BiCGStab: r = b - A x
+//        in FP64, inner solve on r/||r|| in FP32, x += ||r|| d
+// Every slot is an independent state machine (idle / iterating / refine /
+// restart / done), so slots can start and finish at different times.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+#include "opset.h"
+
+namespace cpm {
+
+enum Phase : int { PH_IDLE = 0, PH_ITER = 1, PH_REFINE = 2, PH_DONE = 3, PH_RESTART = 4, PH_INNER_INIT = 5 };
+
+struct Slot {
+    double rho, rho_old, alpha, omega, beta;
+    double bnorm2, r0norm2, rr, tol2;
+    double scale, rnorm64, outer_tol2, b64norm2;
+    int phase, iters, inner_iters, refinements, restarts, status, pad0, pad1;
+};
+
+struct SolveParams {
+    double tol, inner_tol;
+    int max_iters, max_inner, max_refine, mixed;
+};
+
+constexpr int BS = 256;
+
+template <int K>
+__device__ __forceinline__ bool slot_in(const Slot *sl, int s, int ph) {
+    return sl[s].phase == ph;
+}
+
+// ---- fixed-order block + grid reduction with a last-block finaliser
+template <int K, int NDOT>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NDOT], double *partial, unsigned int *counter, double (&out)[NDOT]) {
+    __shared__ double sh[NDOT][BS];
+    __shared__ bool last;
+    const int tid = threadIdx.x;
+    constexpr int RPB = BS / K;
+#pragma unroll
+    for (int d = 0; d < NDOT; ++d) sh[d][tid] = v[d];
+    __syncthreads();
+    const int rib = tid / K;
+    for (int h = RPB / 2; h > 0; h >>= 1) {
+        if (rib < h)
+#pragma unroll
+            for (int d = 0; d < NDOT; ++d) sh[d][tid] += sh[d][tid + h * K];
+        __syncthreads();
+    }
+    if (tid < K)
+#pragma unroll
+        for (int d = 0; d < NDOT; ++d) partial[((size_t)blockIdx.x * K + tid) * NDOT + d] = sh[d][tid];
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    // fixed order: chunk c sums blocks c, c+RPB, ... ; then a tree over chunks
+    const int slot = tid % K, chunk = tid / K;
+    double acc[NDOT];
+#pragma unroll
+    for (int d = 0; d < NDOT; ++d) acc[d] = 0.0;
+    for (unsigned b = chunk; b < gridDim.x; b += RPB)
+#pragma unroll
+        for (int d = 0; d < NDOT; ++d) acc[d] += ((volatile double *)partial)[((size_t)b * K + slot) * NDOT + d];
+#pragma unroll
+    for (int d = 0; d < NDOT; ++d) sh[d][tid] = acc[d];
+    __syncthreads();
+    for (int h = RPB / 2; h > 0; h >>= 1) {
+        if (chunk < h)
+#pragma unroll
+            for (int d = 0; d < NDOT; ++d) sh[d][tid] += sh[d][tid + h * K];
+        __syncthreads();
+    }
+    if (tid < K)
+#pragma unroll
+        for (int d = 0; d < NDOT; ++d) out[d] = sh[d][tid];
+    if (tid == 0) *counter = 0u;
+    return tid < K;
+}
+
+// ================================================================= kernels
+
+// E pass for the slots in phase `ph` (ph < 0: every slot).
+template <class T, int K>
+__global__ void k_epass(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x, T *__restrict__ t) {
+    int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t r = gid / K;
+    int s = (int)(gid % K);
+    if (r >= op.D) return;
+    if (ph >= 0 && sl[s].phase != ph) return;
+    t[r * K + s] = e_row<T, K>(op, r, s, x);
+}
+
+// plain L pass (apply API)
+template <class T, int K>
+__global__ void k_lpass(OpView<T> op, T m, T n, const T *__restrict__ x, const T *__restrict__ t, T *__restrict__ y) {
+    int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t r = gid / K;
+    int s = (int)(gid % K);
+    if (r >= op.D) return;
+    y[r * K + s] = l_row<T, K>(op, r, s, m, n, x, t);
+}
+
+#define GRID_LOOP                                                  \
+    constexpr int RPB = BS / K;                                    \
+    const int s = threadIdx.x % K;                                 \
+    const int64_t r0i = (int64_t)blockIdx.x * RPB + threadIdx.x / K; \
+    const int64_t rstride = (int64_t)gridDim.x * RPB;
+
+// --- plain FP64 / inner init: x = 0, r = r0 = rhs, p = v = 0; ||rhs||^2
+// rhs = b (plain) or (T)(r64 / scale) (inner init)
+template <class T, int K>
+__global__ void k_init(OpView<T> op, Slot *sl, SolveParams P, int from_phase, const double *__restrict__ rhs64,
+                       T *__restrict__ x, T *__restrict__ r, T *__restrict__ r0, T *__restrict__ p, T *__restrict__ v,
+                       double *partial, unsigned int *counter) {
+    GRID_LOOP
+    const bool act = sl[s].phase == from_phase;
+    const double inv = (from_phase == PH_INNER_INIT) ? 1.0 / sl[s].scale : 1.0;
+    double acc[1] = {0.0};
+    if (act)
+        for (int64_t row = r0i; row < op.D; row += rstride) {
+            int64_t i = row * K + s;
+            T bv = (T)(rhs64[i] * inv);
+            x[i] = 0;
+            r[i] = bv;
+            r0[i] = bv;
+            p[i] = 0;
+            v[i] = 0;
+            acc[0] += (double)bv * (double)bv;
+        }
+    double tot[1];
+    if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
+        Slot &S = sl[threadIdx.x];
+        if (S.phase != from_phase) return;
+        double b2 = tot[0];
+        S.bnorm2 = b2;
+        S.r0norm2 = b2;
+        S.rr = b2;
+        S.rho_old = 1.0;
+        S.alpha = 1.0;
+        S.omega = 1.0;
+        S.inner_iters = 0;
+        if (from_phase == PH_INNER_INIT) {
+            S.tol2 = P.inner_tol * P.inner_tol * b2;
+        } else {
+            S.tol2 = P.tol * P.tol * b2;  // BiCGStab::Solve: tol2 = tol^2 ||b||^2 (src/BiCGStab.h:56)
+            S.iters = 0;
+            S.restarts = 0;
+            S.refinements = 0;
+        }
+        if (b2 == 0.0) {  // src/BiCGStab.h:53: x = 0, converged
+            S.phase = (from_phase == PH_INNER_INIT) ? PH_REFINE : PH_DONE;
+            S.status = 0;
+            return;
+        }
+        if (!(S.rr > S.tol2)) {
+            S.phase = (from_phase == PH_INNER_INIT) ? PH_REFINE : PH_DONE;
+            return;
+        }
+        S.rho = b2;  // r0 . r for the first iteration
+        S.beta = (S.rho / S.rho_old) * (S.alpha / S.omega);
+        S.phase = PH_ITER;
+    }
+}
+
+// p = (p - w v) beta + r ; y = D^-1 p   (src/BiCGStab.h:74-78)
+template <class T, int K>
+__global__ void k_update_p(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, const T *__restrict__ r,
+                           const T *__restrict__ v, T *__restrict__ p, T *__restrict__ y) {
+    int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t row = gid / K;
+    int s = (int)(gid % K);
+    if (row >= D || sl[s].phase != PH_ITER) return;
+    const T w = (T)sl[s].omega, beta = (T)sl[s].beta;
+    int64_t i = row * K + s;
+    T pi = -w * v[i] + p[i];
+    pi *= beta;
+    pi = pi + r[i];
+    p[i] = pi;
+    y[i] = pi / pden[row];
+}
+
+// v = A y with r0 . v  ->  alpha = rho / (r0 . v)   (src/BiCGStab.h:79-80)
+template <class T, int K>
+__global__ void k_apply_alpha(OpView<T> op, Slot *sl, T m, T n, const T *__restrict__ y, const T *__restrict__ te,
+                              const T *__restrict__ r0, T *__restrict__ v, double *partial, unsigned int *counter) {
+    GRID_LOOP
+    const bool act = sl[s].phase == PH_ITER;
+    double acc[1] = {0.0};
+    if (act)
+        for (int64_t row = r0i; row < op.D; row += rstride) {
+            T vv = l_row<T, K>(op, row, s, m, n, y, te);
+            v[row * K + s] = vv;
+            acc[0] += (double)r0[row * K + s] * (double)vv;
+        }
+    double tot[1];
+    if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
+        Slot &S = sl[threadIdx.x];
+        if (S.phase != PH_ITER) return;
+        S.alpha = S.rho / tot[0];
+    }
+}
+
+// s = r - alpha v ; z = D^-1 s   (src/BiCGStab.h:82-84)
+template <class T, int K>
+__global__ void k_update_s(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, const T *__restrict__ r,
+                           const T *__restrict__ v, T *__restrict__ sv, T *__restrict__ z) {
+    int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t row = gid / K;
+    int s = (int)(gid % K);
+    if (row >= D || sl[s].phase != PH_ITER) return;
+    const T a = (T)sl[s].alpha;
+    int64_t i = row * K + s;
+    T si = -a * v[i] + r[i];
+    sv[i] = si;
+    z[i] = si / pden[row];
+}
+
+// t = A z with t.t and t.s  ->  omega   (src/BiCGStab.h:85-95)
+template <class T, int K>
+__global__ void k_apply_omega(OpView<T> op, Slot *sl, T m, T n, const T *__restrict__ z, const T *__restrict__ te,
+                              const T *__restrict__ sv, T *__restrict__ tv, double *partial, unsigned int *counter) {
+    GRID_LOOP
+    const bool act = sl[s].phase == PH_ITER;
+    double acc[2] = {0.0, 0.0};
+    if (act)
+        for (int64_t row = r0i; row < op.D; row += rstride) {
+            T tt = l_row<T, K>(op, row, s, m, n, z, te);
+            tv[row * K + s] = tt;
+            acc[0] += (double)tt * (double)tt;
+            acc[1] += (double)tt * (double)sv[row * K + s];
+        }
+    double tot[2];
+    if (grid_reduce<K, 2>(acc, partial, counter, tot)) {
+        Slot &S = sl[threadIdx.x];
+        if (S.phase != PH_ITER) return;
+        S.omega = (tot[0] > 0.0) ? tot[1] / tot[0] : 0.0;
+    }
+}
+
+// x += alpha y + w z ; r = s - w t ; r.r and r0.r -> convergence test, rho, beta
+// (src/BiCGStab.h:97-103 and the loop head :59-73)
+template <class T, int K>
+__global__ void k_update_xr(int64_t D, Slot *sl, SolveParams P, const T *__restrict__ y, const T *__restrict__ z,
+                            const T *__restrict__ sv, const T *__restrict__ tv, const T *__restrict__ r0, T *__restrict__ x,
+                            T *__restrict__ r, double *partial, unsigned int *counter) {
+    GRID_LOOP
+    const bool act = sl[s].phase == PH_ITER;
+    double acc[2] = {0.0, 0.0};
+    if (act) {
+        const T a = (T)sl[s].alpha, w = (T)sl[s].omega;
+        for (int64_t row = r0i; row < D; row += rstride) {
+            int64_t i = row * K + s;
+            T xi = a * y[i] + x[i];
+            x[i] = w * z[i] + xi;
+            T ri = -w * tv[i] + sv[i];
+            r[i] = ri;
+            acc[0] += (double)ri * (double)ri;
+            acc[1] += (double)r0[i] * (double)ri;
+        }
+    }
+    double tot[2];
+    if (grid_reduce<K, 2>(acc, partial, counter, tot)) {
+        Slot &S = sl[threadIdx.x];
+        if (S.phase != PH_ITER) return;
+        S.iters += 1;
+        S.inner_iters += 1;
+        S.rr = tot[0];
+        const bool conv = !(S.rr > S.tol2);
+        if (P.mixed) {
+            if (conv || S.inner_iters >= P.max_inner || S.iters >= P.max_iters || !isfinite(S.rr)) {
+                S.phase = PH_REFINE;
+                return;
+            }
+        } else {
+            if (conv) {
+                S.phase = PH_DONE;
+                S.status = 0;
+                return;
+            }
+            if (S.iters >= P.max_iters || !isfinite(S.rr)) {
+                S.phase = PH_DONE;
+                S.status = isfinite(S.rr) ? CPM_ERR_NOT_CONVERGED : CPM_ERR_BREAKDOWN;
+                return;
+            }
+        }
+        S.rho_old = S.rho;
+        S.rho = tot[1];
+        const double eps = 2.220446049250313e-16;
+        if (fabs(S.rho) < eps * eps * S.r0norm2) {  // restart on rho breakdown (src/BiCGStab.h:62-71)
+            S.phase = P.mixed ? PH_REFINE : PH_RESTART;
+            return;
+        }
+        S.beta = (S.rho / S.rho_old) * (S.alpha / S.omega);
+    }
+}
+
+// plain-path restart: r = b - A x ; r0 = r ; rho = r0norm2 = ||r||^2
+template <class T, int K>
+__global__ void k_restart(OpView<T> op, Slot *sl, T m, T n, const double *__restrict__ b, const T *__restrict__ x,
+                          const T *__restrict__ te, T *__restrict__ r, T *__restrict__ r0, double *partial,
+                          unsigned int *counter) {
+    GRID_LOOP
+    const bool act = sl[s].phase == PH_RESTART;
+    double acc[1] = {0.0};
+    if (act)
+        for (int64_t row = r0i; row < op.D; row += rstride) {
+            T ax = l_row<T, K>(op, row, s, m, n, x, te);
+            T ri = (T)b[row * K + s] - ax;
+            r[row * K + s] = ri;
+            r0[row * K + s] = ri;
+            acc[0] += (double)ri * (double)ri;
+        }
+    double tot[1];
+    if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
+        Slot &S = sl[threadIdx.x];
+        if (S.phase != PH_RESTART) return;
+        S.rho = S.r0norm2 = tot[0];
+        if (S.restarts++ == 0) S.iters = 0;
+        S.beta = (S.rho / S.rho_old) * (S.alpha / S.omega);
+        S.phase = PH_ITER;
+    }
+}
+
+// refinement: x64 += scale * u32 for slots in PH_REFINE
+template <int K>
+__global__ void k_refine_accumulate(int64_t D, const Slot *__restrict__ sl, const float *__restrict__ u, double *__restrict__ x64) {
+    int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t row = gid / K;
+    int s = (int)(gid % K);
+    if (row >= D || sl[s].phase != PH_REFINE) return;
+    x64[row * K + s] += sl[s].scale * (double)u[row * K + s];
+}
+
+// r64 = b - A x64 (FP64) and ||r64||: done, or a new inner solve on r64 / ||r64||
+template <int K>
+__global__ void k_refine_residual(OpView<double> op, Slot *sl, SolveParams P, double m, double n, const double *__restrict__ b,
+                                  const double *__restrict__ x64, const double *__restrict__ te, double *__restrict__ r64,
+                                  double *partial, unsigned int *counter) {
+    GRID_LOOP
+    const bool act = sl[s].phase == PH_REFINE;
+    double acc[1] = {0.0};
+    if (act)
+        for (int64_t row = r0i; row < op.D; row += rstride) {
+            double ax = l_row<double, K>(op, row, s, m, n, x64, te);
+            double ri = b[row * K + s] - ax;
+            r64[row * K + s] = ri;
+            acc[0] += ri * ri;
+        }
+    double tot[1];
+    if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
+        Slot &S = sl[threadIdx.x];
+        if (S.phase != PH_REFINE) return;
+        S.refinements += 1;
+        S.rnorm64 = sqrt(tot[0]);
+        if (!(tot[0] > S.outer_tol2)) {
+            S.phase = PH_DONE;
+            S.status = 0;
+        } else if (S.refinements >= P.max_refine || S.iters >= P.max_iters || !isfinite(tot[0])) {
+            S.phase = PH_DONE;
+            S.status = isfinite(tot[0]) ? CPM_ERR_NOT_CONVERGED : CPM_ERR_BREAKDOWN;
+        } else {
+            S.scale = S.rnorm64;
+            S.phase = PH_INNER_INIT;
+        }
+    }
+}
+
+// mixed-path start: x64 = 0, r64 = b, ||b||
+template <int K>
+__global__ void k_mixed_start(int64_t D, Slot *sl, SolveParams P, const double *__restrict__ b, double *__restrict__ x64,
+                              double *__restrict__ r64, double *partial, unsigned int *counter) {
+    GRID_LOOP
+    const bool act = sl[s].phase == PH_REFINE;
+    double acc[1] = {0.0};
+    if (act)
+        for (int64_t row = r0i; row < D; row += rstride) {
+            int64_t i = row * K + s;
+            x64[i] = 0.0;
+            r64[i] = b[i];
+            acc[0] += b[i] * b[i];
+        }
+    double tot[1];
+    if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
+        Slot &S = sl[threadIdx.x];
+        if (S.phase != PH_REFINE) return;
+        S.b64norm2 = tot[0];
+        S.outer_tol2 = P.tol * P.tol * tot[0];
+        S.iters = 0;
+        S.refinements = 0;
+        S.restarts = 0;
+        S.rnorm64 = sqrt(tot[0]);
+        if (tot[0] == 0.0) {
+            S.phase = PH_DONE;
+            S.status = 0;
+            return;
+        }
+        S.scale = S.rnorm64;
+        S.phase = PH_INNER_INIT;
+    }
+}
+
+// D^-1 denominators m + n L_rr (src/GeneralizedBiCGStabSystem.h:281-340); identity rows 1
+template <class T>
+__global__ void k_pden(OpView<T> op, double m, double n, T *__restrict__ pden) {
+    int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= op.D) return;
+    if (op.flags[r] & F_IDENT) {
+        pden[r] = (T)1;
+        return;
+    }
+    double ld = (r < op.N) ? (double)op.Ldiag : (double)op.ldiag[r - op.N];
+    pden[r] = (T)(m + ld * n);
+}
+
+// layout transposes between RHS-major host arrays and [D][K] slot layout
+__global__ void k_scatter_cols(int64_t D, int K, int k, const double *__restrict__ src, double *__restrict__ dst) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= D * K) return;
+    int64_t row = i / K;
+    int s = (int)(i % K);
+    dst[i] = (s < k) ? src[(int64_t)s * D + row] : 0.0;
+}
+__global__ void k_gather_cols(int64_t D, int K, int k, const double *__restrict__ src, double *__restrict__ dst) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= D * (int64_t)k) return;
+    int s = (int)(i / D);
+    int64_t row = i % D;
+    dst[i] = src[row * K + s];
+}
+template <class T>
+__global__ void k_copy_cast(int64_t n, const T *__restrict__ a, double *__restrict__ b) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (double)a[i];
+}
+
+}  // namespace cpm
+
+using namespace cpm;
+
+// ================================================================= solver object
+
+struct cpm_solver_s {
+    cpm_opset_s *op = nullptr;
+    double m = 0, n = 0;
+    int K = 1;
+    int64_t D = 0;
+    int G = 1;
+    cudaStream_t st = nullptr;
+    DBuf<Slot> slots;
+    std::vector<Slot> h_slots;
+    DBuf<double> partial;
+    DBuf<unsigned int> counter;
+    // FP64 Krylov vectors (plain path) and FP64 refinement state (mixed path)
+    DBuf<double> b64, x64, r64, te64, pden64;
+    DBuf<double> dr, dr0, dp, dv, ds, dt, dy, dz;
+    // FP32 Krylov vectors (inner solves of the mixed path)
+    DBuf<float> fx, fr, fr0, fp, fv, fs, ft, fy, fz, fte, pden32;
+    bool have64 = false, have32 = false;
+    // captured iteration graphs
+    cudaGraphExec_t g_plain = nullptr, g_mixed = nullptr;
+    int chunk = 16;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~cpm_solver_s() {
+        if (g_plain) cudaGraphExecDestroy(g_plain);
+        if (g_mixed) cudaGraphExecDestroy(g_mixed);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    }
+};
+
+namespace cpm {
+
+static inline unsigned nblk(int64_t n) { return (unsigned)((n + BS - 1) / BS); }
+
+template <int K>
+static int plain_iteration(cpm_solver_s *s, const SolveParams &P) {
+    auto op = s->op->view<double>();
+    const int64_t D = s->D;
+    cudaStream_t st = stream();
+    Slot *sl = s->slots.p;
+    k_update_p<double, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden64.p, s->dr.p, s->dv.p, s->dp.p, s->dy.p);
+    k_epass<double, K><<<nblk(D * K), BS, 0, st>>>(op, sl, PH_ITER, s->dy.p, s->te64.p);
+    k_apply_alpha<double, K><<<s->G, BS, 0, st>>>(op, sl, s->m, s->n, s->dy.p, s->te64.p, s->dr0.p, s->dv.p, s->partial.p,
+                                                  s->counter.p);
+    k_update_s<double, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden64.p, s->dr.p, s->dv.p, s->ds.p, s->dz.p);
+    k_epass<double, K><<<nblk(D * K), BS, 0, st>>>(op, sl, PH_ITER, s->dz.p, s->te64.p);
+    k_apply_omega<double, K><<<s->G, BS, 0, st>>>(op, sl, s->m, s->n, s->dz.p, s->te64.p, s->ds.p, s->dt.p, s->partial.p,
+                                                  s->counter.p);
+    k_update_xr<double, K><<<s->G, BS, 0, st>>>(D, sl, P, s->dy.p, s->dz.p, s->ds.p, s->dt.p, s->dr0.p, s->x64.p, s->dr.p,
+                                                s->partial.p, s->counter.p);
+    return 0;
+}
+
+template <int K>
+static int plain_restart(cpm_solver_s *s) {
+    auto op = s->op->view<double>();
+    cudaStream_t st = stream();
+    k_epass<double, K><<<nblk(s->D * K), BS, 0, st>>>(op, s->slots.p, PH_RESTART, s->x64.p, s->te64.p);
+    k_restart<double, K><<<s->G, BS, 0, st>>>(op, s->slots.p, s->m, s->n, s->b64.p, s->x64.p, s->te64.p, s->dr.p, s->dr0.p,
+                                              s->partial.p, s->counter.p);
+    return 0;
+}
+
+template <int K>
+static int mixed_iteration(cpm_solver_s *s, const SolveParams &P) {
+    auto op = s->op->view<float>();
+    const int64_t D = s->D;
+    cudaStream_t st = stream();
+    Slot *sl = s->slots.p;
+    const float m = (float)s->m, n = (float)s->n;
+    k_update_p<float, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden32.p, s->fr.p, s->fv.p, s->fp.p, s->fy.p);
+    k_epass<float, K><<<nblk(D * K), BS, 0, st>>>(op, sl, PH_ITER, s->fy.p, s->fte.p);
+    k_apply_alpha<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p, s->counter.p);
+    k_update_s<float, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden32.p, s->fr.p, s->fv.p, s->fs.p, s->fz.p);
+    k_epass<float, K><<<nblk(D * K), BS, 0, st>>>(op, sl, PH_ITER, s->fz.p, s->fte.p);
+    k_apply_omega<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p, s->counter.p);
+    k_update_xr<float, K><<<s->G, BS, 0, st>>>(D, sl, P, s->fy.p, s->fz.p, s->fs.p, s->ft.p, s->fr0.p, s->fx.p, s->fr.p,
+                                               s->partial.p, s->counter.p);
+    return 0;
+}
+
+// FP64 refinement for slots whose inner solve finished, then inner restarts.
+template <int K>
+static int mixed_refine(cpm_solver_s *s, const SolveParams &P) {
+    auto op64 = s->op->view<double>();
+    auto op32 = s->op->view<float>();
+    const int64_t D = s->D;
+    cudaStream_t st = stream();
+    Slot *sl = s->slots.p;
+    k_refine_accumulate<K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->fx.p, s->x64.p);
+    k_epass<double, K><<<nblk(D * K), BS, 0, st>>>(op64, sl, PH_REFINE, s->x64.p, s->te64.p);
+    k_refine_residual<K><<<s->G, BS, 0, st>>>(op64, sl, P, s->m, s->n, s->b64.p, s->x64.p, s->te64.p, s->r64.p, s->partial.p,
+                                              s->counter.p);
+    k_init<float, K><<<s->G, BS, 0, st>>>(op32, sl, P, PH_INNER_INIT, s->r64.p, s->fx.p, s->fr.p, s->fr0.p, s->fp.p, s->fv.p,
+                                          s->partial.p, s->counter.p);
+    return 0;
+}
+
+static int alloc_vectors(cpm_solver_s *s, bool want64, bool want32) {
+    const size_t n = (size_t)s->D * s->K;
+    if (want64 && !s->have64) {
+        for (auto *b : {&s->dr, &s->dr0, &s->dp, &s->dv, &s->ds, &s->dt, &s->dy, &s->dz}) CPM_TRY(b->alloc(n));
+        s->have64 = true;
+    }
+    if (want32 && !s->have32) {
+        for (auto *b : {&s->fx, &s->fr, &s->fr0, &s->fp, &s->fv, &s->fs, &s->ft, &s->fy, &s->fz, &s->fte}) CPM_TRY(b->alloc(n));
+        CPM_TRY(s->pden32.alloc(s->D));
+        k_pden<float><<<nblk(s->D), BS, 0, stream()>>>(s->op->view<float>(), s->m, s->n, s->pden32.p);
+        CPM_CUDA_TRY(cudaGetLastError());
+        s->have32 = true;
+    }
+    return 0;
+}
+
+template <int K>
+static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_stats *stats) {
+    SolveParams P;
+    P.tol = o->tol > 0 ? o->tol : 1e-10;
+    P.max_iters = o->max_iters > 0 ? o->max_iters : 100000;
+    P.mixed = o->precision == 1;
+    P.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
+    P.max_refine = o->max_refine > 0 ? o->max_refine : 40;
+    P.max_inner = 4000;
+    if (o->precond != 1) return fail(CPM_ERR_UNSUPPORTED, "the device solver implements the diagonal preconditioner");
+    CPM_TRY(alloc_vectors(s, !P.mixed, P.mixed));
+    cudaStream_t st = stream();
+    // slot phases: 0..k-1 start, others idle
+    for (int j = 0; j < K; ++j) {
+        memset(&s->h_slots[j], 0, sizeof(Slot));
+        s->h_slots[j].phase = (j < k) ? (P.mixed ? PH_REFINE : PH_ITER) : PH_IDLE;
+    }
+    CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p, s->h_slots.data(), sizeof(Slot) * K, cudaMemcpyHostToDevice, st));
+    CPM_CUDA_TRY(cudaEventRecord(s->e0, st));
+    if (!P.mixed) {
+        k_init<double, K><<<s->G, BS, 0, st>>>(s->op->view<double>(), s->slots.p, P, PH_ITER, s->b64.p, s->x64.p, s->dr.p,
+                                               s->dr0.p, s->dp.p, s->dv.p, s->partial.p, s->counter.p);
+    } else {
+        k_mixed_start<K><<<s->G, BS, 0, st>>>(s->D, s->slots.p, P, s->b64.p, s->x64.p, s->r64.p, s->partial.p, s->counter.p);
+        k_init<float, K><<<s->G, BS, 0, st>>>(s->op->view<float>(), s->slots.p, P, PH_INNER_INIT, s->r64.p, s->fx.p, s->fr.p,
+                                              s->fr0.p, s->fp.p, s->fv.p, s->partial.p, s->counter.p);
+    }
+    CPM_CUDA_TRY(cudaGetLastError());
+    // one captured graph = `chunk` iterations (+ the refinement step for the mixed path)
+    cudaGraphExec_t &gexec = P.mixed ? s->g_mixed : s->g_plain;
+    if (gexec) {
+        cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+    }
+    {
+        cudaGraph_t graph;
+        CPM_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int it = 0; it < s->chunk; ++it) {
+            if (P.mixed) {
+                mixed_iteration<K>(s, P);
+                // slots whose inner solve finished are refined every 4 iterations
+                if ((it & 3) == 3) mixed_refine<K>(s, P);
+            } else {
+                plain_iteration<K>(s, P);
+            }
+        }
+        cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        if (ce != cudaSuccess) return fail(CPM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+        ce = cudaGraphInstantiate(&gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return fail(CPM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+    }
+    const int64_t max_chunks = (int64_t)P.max_iters / s->chunk + 2 * P.max_refine + 4;
+    // kernels per graph: 7 per BiCGStab iteration (+ 4 per refinement step)
+    const long long per_graph = 7LL * s->chunk + (P.mixed ? 4LL * (s->chunk / 4) : 0);
+    count_launches(P.mixed ? 2 : 1);
+    bool done = false;
+    for (int64_t c = 0; c < max_chunks && !done; ++c) {
+        CPM_CUDA_TRY(cudaGraphLaunch(gexec, st));
+        count_launches(per_graph);
+        CPM_CUDA_TRY(cudaMemcpyAsync(s->h_slots.data(), s->slots.p, sizeof(Slot) * K, cudaMemcpyDeviceToHost, st));
+        CPM_CUDA_TRY(cudaStreamSynchronize(st));
+        done = true;
+        bool restart = false;
+        for (int j = 0; j < K; ++j) {
+            int ph = s->h_slots[j].phase;
+            if (ph != PH_DONE && ph != PH_IDLE) done = false;
+            if (ph == PH_RESTART) restart = true;
+        }
+        if (restart && !P.mixed) {
+            plain_restart<K>(s);
+            count_launches(2);
+            CPM_CUDA_TRY(cudaGetLastError());
+        }
+    }
+    CPM_CUDA_TRY(cudaEventRecord(s->e1, st));
+    CPM_CUDA_TRY(cudaEventSynchronize(s->e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->e0, s->e1);
+    int rc = 0;
+    for (int j = 0; j < k; ++j) {
+        const Slot &S = s->h_slots[j];
+        int status = (S.phase == PH_DONE) ? S.status : CPM_ERR_TIMEOUT;
+        if (status != 0 && rc == 0) rc = status;
+        if (stats) {
+            stats[j].iterations = S.iters;
+            stats[j].refinements = S.refinements;
+            stats[j].restarts = S.restarts;
+            stats[j].status = status;
+            stats[j].rel_residual = P.mixed ? (S.b64norm2 > 0 ? S.rnorm64 / std::sqrt(S.b64norm2) : 0.0)
+                                            : (S.bnorm2 > 0 ? std::sqrt(S.rr / S.bnorm2) : 0.0);
+            stats[j].seconds = ms * 1e-3;
+        }
+    }
+    if (rc) set_error("solve did not converge for every right-hand side (see per-RHS status)");
+    return rc;
+}
+
+}  // namespace cpm
+
+extern "C" int cpm_solver_create(cpm_opset_t op, double m, double n, int32_t kslots, cpm_solver_t *out) {
+    if (!op || !out || kslots < 1 || kslots > 32) return fail(CPM_ERR_INVALID_ARG, "kslots must be in [1, 32]");
+    *out = nullptr;
+    cpm_solver_s *s = new cpm_solver_s();
+    s->op = op;
+    s->m = m;
+    s->n = n;
+    s->K = (kslots == 1) ? 1 : 32;
+    s->D = op->D;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t need = (s->D * s->K + BS - 1) / BS;
+    s->G = (int)std::max<int64_t>(1, std::min<int64_t>(need, 8LL * sms));
+    s->h_slots.assign(s->K, Slot());
+    auto bail = [&](int rc) {
+        delete s;
+        return rc;
+    };
+    int rc;
+    if ((rc = s->slots.alloc(s->K)) || (rc = s->partial.alloc((size_t)s->G * s->K * 2)) || (rc = s->counter.alloc(1)) ||
+        (rc = s->counter.zero()) || (rc = s->b64.alloc((size_t)s->D * s->K)) || (rc = s->x64.alloc((size_t)s->D * s->K)) ||
+        (rc = s->r64.alloc((size_t)s->D * s->K)) || (rc = s->te64.alloc((size_t)s->D * s->K)) || (rc = s->pden64.alloc(s->D)))
+        return bail(rc);
+    k_pden<double><<<nblk(s->D), BS, 0, stream()>>>(op->view<double>(), m, n, s->pden64.p);
+    if (cudaGetLastError() != cudaSuccess) return bail(fail(CPM_ERR_CUDA, "pden kernel"));
+    cudaEventCreate(&s->e0);
+    cudaEventCreate(&s->e1);
+    *out = s;
+    return 0;
+}
+
+extern "C" int cpm_solve_device(cpm_solver_t s, int32_t k, const void *b_dev, void *x_dev, const cpm_solve_opts *opts,
+                                cpm_solve_stats *stats) {
+    if (!s || !opts || k < 1 || k > s->K) return fail(CPM_ERR_INVALID_ARG, "invalid solve arguments");
+    const size_t bytes = (size_t)s->D * s->K * sizeof(double);
+    if (b_dev != s->b64.p) CPM_CUDA_TRY(cudaMemcpyAsync(s->b64.p, b_dev, bytes, cudaMemcpyDeviceToDevice, stream()));
+    int rc = (s->K == 1) ? run_solve<1>(s, k, opts, stats) : run_solve<32>(s, k, opts, stats);
+    if (x_dev) CPM_CUDA_TRY(cudaMemcpyAsync(x_dev, s->x64.p, bytes, cudaMemcpyDeviceToDevice, stream()));
+    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
+    return rc;
+}
+
+extern "C" int cpm_solve(cpm_solver_t s, int32_t k, const double *b, double *x, const cpm_solve_opts *opts, cpm_solve_stats *stats) {
+    if (!s || !b || !x || !opts || k < 1 || k > s->K) return fail(CPM_ERR_INVALID_ARG, "invalid solve arguments");
+    DBuf<double> stage;
+    CPM_TRY(stage.upload(b, (size_t)s->D * k));
+    k_scatter_cols<<<nblk(s->D * s->K), BS, 0, stream()>>>(s->D, s->K, k, stage.p, s->b64.p);
+    CPM_CUDA_TRY(cudaGetLastError());
+    int rc = (s->K == 1) ? run_solve<1>(s, k, opts, stats) : run_solve<32>(s, k, opts, stats);
+    k_gather_cols<<<nblk(s->D * (int64_t)k), BS, 0, stream()>>>(s->D, s->K, k, s->x64.p, stage.p);
+    CPM_CUDA_TRY(cudaGetLastError());
+    CPM_CUDA_TRY(cudaMemcpyAsync(x, stage.p, sizeof(double) * s->D * k, cudaMemcpyDeviceToHost, stream()));
+    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
+    return rc;
+}
+
+extern "C" int cpm_solver_destroy(cpm_solver_t s) {
+    delete s;
+    return 0;
+}
+
+// ================================================================= apply
+
+extern "C" int cpm_apply(cpm_opset_t op, double m, double n, int32_t k, const double *x, double *y) {
+    if (!op || !x || !y || k < 1) return fail(CPM_ERR_INVALID_ARG, "invalid apply arguments");
+    const int64_t D = op->D;
+    DBuf<double> dx, dt, dy;
+    CPM_TRY(dx.alloc(D));
+    CPM_TRY(dt.alloc(D));
+    CPM_TRY(dy.alloc(D));
+    auto v = op->view<double>();
+    for (int j = 0; j < k; ++j) {
+        CPM_CUDA_TRY(cudaMemcpyAsync(dx.p, x + (size_t)j * D, D * 8, cudaMemcpyHostToDevice, stream()));
+        k_epass<double, 1><<<nblk(D), BS, 0, stream()>>>(v, nullptr, -1, dx.p, dt.p);
+        k_lpass<double, 1><<<nblk(D), BS, 0, stream()>>>(v, m, n, dx.p, dt.p, dy.p);
+        CPM_CUDA_TRY(cudaGetLastError());
+        CPM_CUDA_TRY(cudaMemcpyAsync(y + (size_t)j * D, dy.p, D * 8, cudaMemcpyDeviceToHost, stream()));
+    }
+    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
+    return 0;
+}
+
+extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslots, int32_t fp32, const void *x_dev, void *t_dev,
+                                void *y_dev) {
+    if (!op || !x_dev || !t_dev || !y_dev || (kslots != 1 && kslots != 32))
+        return fail(CPM_ERR_INVALID_ARG, "apply_device: null pointer or kslots not 1 / 32");
+    const int64_t D = op->D;
+    cudaStream_t st = stream();
+    if (fp32) {
+        auto v = op->view<float>();
+        const float *x = (const float *)x_dev;
+        float *t = (float *)t_dev, *y = (float *)y_dev;
+        if (kslots == 1) {
+            k_epass<float, 1><<<nblk(D), BS, 0, st>>>(v, nullptr, -1, x, t);
+            k_lpass<float, 1><<<nblk(D), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
+        } else {
+            k_epass<float, 32><<<nblk(D * 32), BS, 0, st>>>(v, nullptr, -1, x, t);
+            k_lpass<float, 32><<<nblk(D * 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
+        }
+    } else {
+        auto v = op->view<double>();
+        const double *x = (const double *)x_dev;
+        double *t = (double *)t_dev, *y = (double *)y_dev;
+        if (kslots == 1) {
+            k_epass<double, 1><<<nblk(D), BS, 0, st>>>(v, nullptr, -1, x, t);
+            k_lpass<double, 1><<<nblk(D), BS, 0, st>>>(v, m, n, x, t, y);
+        } else {
+            k_epass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, nullptr, -1, x, t);
+            k_lpass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, m, n, x, t, y);
+        }
+    }
+    count_launches(2);
+    CPM_CUDA_TRY(cudaGetLastError());
+    return 0;
+}

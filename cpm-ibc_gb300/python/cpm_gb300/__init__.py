@@ -1,0 +1,320 @@
+"""ctypes binding of libcpmgpu.so, the C-ABI of the GB300 closest-point solve path.
+
+Class and method names follow the reference's C++ interface (Tube, Solver,
+problems) so that tests read like the reference's drivers.  There is no CPU
+fallback: if the CUDA library is missing or no GPU is present the calls fail.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(os.path.dirname(HERE))  # .../cpm-ibc_gb300
+LIB_PATH = os.path.join(PKG, "_build", "libcpmgpu.so")
+
+SPHERE, TORUS, CIRCLE3D, POINT, TRIANGULATION, POLYLINE = range(6)
+STATUS = {0: "OK", -1: "INVALID_ARG", -2: "CUDA_ERROR", -3: "OOM", -4: "BASEPOINT_OUTSIDE_TUBE", -5: "NOT_CONVERGED",
+          -6: "BREAKDOWN", -7: "UNSUPPORTED", -8: "ADMISSION", -9: "TIMEOUT"}
+
+
+class CpmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SurfaceDesc(ctypes.Structure):
+    """struct cpm_surface_desc (include/cpm_gpu.h)."""
+
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("nparams", ctypes.c_int32),
+        ("params", ctypes.c_double * 8),
+        ("bbox", ctypes.c_double * 2),
+        ("nverts", ctypes.c_int64),
+        ("verts", ctypes.POINTER(ctypes.c_double)),
+        ("nprims", ctypes.c_int64),
+        ("prims", ctypes.POINTER(ctypes.c_int64)),
+        ("boundary_order", ctypes.c_int32),
+        ("boundary_type", ctypes.c_int32 * 2),
+        ("is_oriented", ctypes.c_int32),
+        ("has_point_on_side1", ctypes.c_int32),
+        ("use_cp_diff_directions", ctypes.c_int32),
+        ("use_Jcp_surface_normals", ctypes.c_int32),
+        ("pad0", ctypes.c_int32),
+        ("on_ibc_tolerance", ctypes.c_double),
+        ("point_on_side1", ctypes.c_double * 3),
+        ("dof_radius_scale", ctypes.c_double),
+    ]
+
+
+class TubeInfo(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_int64), ("n1d", ctypes.c_int64), ("n_bricks", ctypes.c_int64),
+                ("n_visited", ctypes.c_int64), ("dx", ctypes.c_double), ("xstart", ctypes.c_double),
+                ("radius", ctypes.c_double), ("p", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("max_iters", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("precond", ctypes.c_int32), ("precond_iters", ctypes.c_int32), ("inner_tol", ctypes.c_double),
+                ("max_refine", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("refinements", ctypes.c_int32), ("restarts", ctypes.c_int32),
+                ("status", ctypes.c_int32), ("rel_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+
+def desc(kind, params=(), bbox=(-1.0, 1.0), boundary_order=1, on_ibc_tolerance=0.0, verts=None, prims=None,
+         boundary_type=(0, 0)):
+    d = SurfaceDesc()
+    d.kind = kind
+    d.nparams = len(params)
+    for i, p in enumerate(params):
+        d.params[i] = float(p)
+    d.bbox[0], d.bbox[1] = bbox
+    d.boundary_order = boundary_order
+    d.boundary_type[0], d.boundary_type[1] = boundary_type
+    d.use_Jcp_surface_normals = 1
+    d.on_ibc_tolerance = on_ibc_tolerance
+    d.dof_radius_scale = 1.0
+    d._keep = []
+    if verts is not None:
+        v = np.ascontiguousarray(verts, dtype=np.float64)
+        p = np.ascontiguousarray(prims, dtype=np.int64)
+        d._keep += [v, p]
+        d.nverts = v.shape[0]
+        d.verts = v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.nprims = p.shape[0]
+        d.prims = p.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    return d
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise CpmError(-2, f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, P = ctypes.c_void_p, ctypes.POINTER
+        L.cpm_last_error.restype = ctypes.c_char_p
+        L.cpm_device_info.argtypes = [ctypes.c_char_p, ctypes.c_int64, vp, vp, vp]
+        L.cpm_tube_build.argtypes = [P(SurfaceDesc), ctypes.c_int32, ctypes.c_double, P(vp)]
+        L.cpm_tube_build_from_cp.argtypes = [P(SurfaceDesc), ctypes.c_int32, ctypes.c_double, ctypes.c_int64, vp, vp, vp,
+                                             P(vp)]
+        L.cpm_tube_info_get.argtypes = [vp, P(TubeInfo)]
+        L.cpm_tube_export.argtypes = [vp] * 8
+        L.cpm_interp_query.argtypes = [vp, ctypes.c_int64, vp, vp, vp]
+        L.cpm_tube_destroy.argtypes = [vp]
+        L.cpm_opset_create.argtypes = [vp, ctypes.c_int32, P(SurfaceDesc), P(vp)]
+        L.cpm_opset_sizes.argtypes = [vp, vp]
+        L.cpm_opset_rows.argtypes = [vp] * 5
+        L.cpm_opset_ibc_sizes.argtypes = [vp, ctypes.c_int32, vp]
+        L.cpm_opset_ibc_export.argtypes = [vp, ctypes.c_int32, vp, vp, vp]
+        L.cpm_opset_export_csr.argtypes = [vp, ctypes.c_int32, vp, vp, vp, vp]
+        L.cpm_opset_destroy.argtypes = [vp]
+        L.cpm_apply.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, vp, vp]
+        L.cpm_apply_device.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, vp, vp]
+        L.cpm_get_stream.restype = ctypes.c_void_p
+        L.cpm_launch_count.restype = ctypes.c_int64
+        L.cpm_sync.restype = ctypes.c_int
+        L.cpm_solver_create.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, P(vp)]
+        L.cpm_solve.argtypes = [vp, ctypes.c_int32, vp, vp, P(SolveOpts), P(SolveStats)]
+        L.cpm_solve_device.argtypes = [vp, ctypes.c_int32, vp, vp, P(SolveOpts), P(SolveStats)]
+        L.cpm_solver_destroy.argtypes = [vp]
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise CpmError(rc, lib().cpm_last_error().decode())
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def device_info():
+    name = ctypes.create_string_buffer(256)
+    fr, to, sm = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
+    _check(lib().cpm_device_info(name, 256, ctypes.byref(fr), ctypes.byref(to), ctypes.byref(sm)))
+    return dict(name=name.value.decode(), free=fr.value, total=to.value, sms=sm.value)
+
+
+class Tube:
+    """Tube(SurfaceSpecifier&, p, dx) (src/Tube.h:45) built on the device."""
+
+    def __init__(self, surface, p=3, dx=0.1, _handle=None):
+        self.surface = surface
+        if _handle is None:
+            h = ctypes.c_void_p()
+            _check(lib().cpm_tube_build(ctypes.byref(surface), p, dx, ctypes.byref(h)))
+            _handle = h
+        self.h = _handle
+        info = TubeInfo()
+        _check(lib().cpm_tube_info_get(self.h, ctypes.byref(info)))
+        self.N, self.N1d, self.n_bricks, self.n_visited = info.n_nodes, info.n1d, info.n_bricks, info.n_visited
+        self.dx, self.xstart, self.radius, self.p = info.dx, info.xstart, info.radius, info.p
+
+    @classmethod
+    def from_closest_points(cls, surface, p, dx, keys, cp, dist):
+        keys = np.asarray(keys, np.int64)
+        o = np.argsort(keys, kind="stable")
+        k = np.ascontiguousarray(keys[o])
+        c = np.ascontiguousarray(np.asarray(cp, np.float64)[o])
+        d = np.ascontiguousarray(np.asarray(dist, np.float64)[o])
+        h = ctypes.c_void_p()
+        _check(lib().cpm_tube_build_from_cp(ctypes.byref(surface), p, dx, len(k), _p(k), _p(c), _p(d), ctypes.byref(h)))
+        return cls(surface, _handle=h)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().cpm_tube_destroy(self.h)
+        except Exception:
+            pass
+
+    def export(self):
+        N = self.N
+        out = dict(rec=np.zeros(N, np.int64), x=np.zeros((N, 3)), cp=np.zeros((N, 3)), dist=np.zeros(N),
+                   bpt=np.zeros(N, np.int64), nbr=np.zeros((N, 6), np.int64), w=np.zeros((N, 3, 4)))
+        _check(lib().cpm_tube_export(self.h, _p(out["rec"]), _p(out["x"]), _p(out["cp"]), _p(out["dist"]),
+                                     _p(out["bpt"]), _p(out["nbr"]), _p(out["w"])))
+        return out
+
+    def interp_query(self, xq):
+        """Interpolation(Tube&, xq) rows: 64 (column, value) per query point."""
+        xq = np.ascontiguousarray(xq, np.float64)
+        n = xq.shape[0]
+        cols = np.zeros((n, 64), np.int64)
+        vals = np.zeros((n, 64))
+        _check(lib().cpm_interp_query(self.h, n, _p(xq), _p(cols), _p(vals)))
+        return cols, vals
+
+
+class OpSet:
+    """Lfull / Efull / identity rows (Helpers::SetupMatrices + IBCMatrixManipulations) on the device."""
+
+    def __init__(self, tube, ibcs=()):
+        self.tube = tube
+        self.ibcs = list(ibcs)
+        h = ctypes.c_void_p()
+        arr = (SurfaceDesc * max(1, len(ibcs)))(*ibcs) if ibcs else None
+        _check(lib().cpm_opset_create(tube.h, len(ibcs), arr, ctypes.byref(h)))
+        self.h = h
+        s = np.zeros(7, np.int64)
+        _check(lib().cpm_opset_sizes(self.h, _p(s)))
+        self.D, self.N, self.total_ibc_dofs, self.num2, self.n_ibc, self.n_patched, self.n_moved = [int(v) for v in s]
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().cpm_opset_destroy(self.h)
+        except Exception:
+            pass
+
+    def rows(self):
+        D = self.D
+        ident = np.zeros(D, np.uint8)
+        kind = np.zeros(D, np.int32)
+        ibc = np.zeros(D, np.int32)
+        point = np.zeros((D, 3))
+        _check(lib().cpm_opset_rows(self.h, _p(ident), _p(kind), _p(ibc), _p(point)))
+        return dict(identity=ident.astype(bool), kind=kind, ibc=ibc, point=point)
+
+    def ibc_subsets(self, c):
+        s = np.zeros(5, np.int64)
+        _check(lib().cpm_opset_ibc_sizes(self.h, c, _p(s)))
+        tag = np.zeros(int(s[0]), np.int64)
+        dof = np.zeros(int(s[1]), np.int64)
+        cp = np.zeros((int(s[1]), 3))
+        _check(lib().cpm_opset_ibc_export(self.h, c, _p(tag), _p(dof), _p(cp)))
+        return dict(tag_set=tag, dof_set=dof, dof_cp=cp, col_start=int(s[2]), dcol_start=int(s[3]),
+                    identity_rows_start=int(s[4]))
+
+    def csr(self, which):
+        nnz = ctypes.c_int64()
+        _check(lib().cpm_opset_export_csr(self.h, which, ctypes.byref(nnz), None, None, None))
+        ptr = np.zeros(self.D + 1, np.int64)
+        idx = np.zeros(nnz.value, np.int64)
+        val = np.zeros(nnz.value)
+        _check(lib().cpm_opset_export_csr(self.h, which, ctypes.byref(nnz), _p(ptr), _p(idx), _p(val)))
+        return ptr, idx, val
+
+    def apply(self, m, n, x):
+        """Solver::Multiply (src/Solver.cpp:122-138); x: (D,) or (k, D)."""
+        x = np.ascontiguousarray(np.atleast_2d(x), np.float64)
+        y = np.zeros_like(x)
+        _check(lib().cpm_apply(self.h, m, n, x.shape[0], _p(x), _p(y)))
+        return y
+
+    def apply_device(self, m, n, kslots, fp32, x_ptr, t_ptr, y_ptr):
+        """Asynchronous device apply on the library stream ([D][kslots] arrays)."""
+        _check(lib().cpm_apply_device(self.h, m, n, kslots, int(fp32), x_ptr, t_ptr, y_ptr))
+
+
+def set_device(dev):
+    lib().cpm_set_device.argtypes = [ctypes.c_int32]
+    _check(lib().cpm_set_device(int(dev)))
+
+
+def stream_ptr():
+    """The library's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+    return lib().cpm_get_stream()
+
+
+def launch_count():
+    return int(lib().cpm_launch_count())
+
+
+def sync():
+    _check(lib().cpm_sync())
+
+
+class Solver:
+    """Solver::Init(m, n, ...) + Solve (src/Solver.cpp:8-114), k right-hand sides per call."""
+
+    def __init__(self, opset, m, n, kslots=1):
+        self.opset = opset
+        self.m, self.n, self.kslots = m, n, kslots
+        h = ctypes.c_void_p()
+        _check(lib().cpm_solver_create(opset.h, m, n, kslots, ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().cpm_solver_destroy(self.h)
+        except Exception:
+            pass
+
+    def solve(self, b, tol=1e-10, precision=0, max_iters=100000, inner_tol=1e-4, max_refine=40, raise_on_error=True):
+        b = np.ascontiguousarray(np.atleast_2d(b), np.float64)
+        k = b.shape[0]
+        x = np.zeros_like(b)
+        o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=1, precond_iters=0,
+                      inner_tol=inner_tol, max_refine=max_refine)
+        st = (SolveStats * k)()
+        rc = lib().cpm_solve(self.h, k, _p(b), _p(x), ctypes.byref(o), st)
+        stats = [dict(iterations=s.iterations, refinements=s.refinements, restarts=s.restarts, status=s.status,
+                      rel_residual=s.rel_residual, seconds=s.seconds) for s in st]
+        if rc != 0 and raise_on_error:
+            raise CpmError(rc, lib().cpm_last_error().decode() + f" stats={stats}")
+        return x, stats
+
+    def solve_device(self, b_ptr, x_ptr, k, tol=1e-10, precision=0, max_iters=100000, inner_tol=1e-4, max_refine=40):
+        o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=1, precond_iters=0,
+                      inner_tol=inner_tol, max_refine=max_refine)
+        st = (SolveStats * k)()
+        rc = lib().cpm_solve_device(self.h, k, b_ptr, x_ptr, ctypes.byref(o), st)
+        stats = [dict(iterations=s.iterations, refinements=s.refinements, restarts=s.restarts, status=s.status,
+                      rel_residual=s.rel_residual, seconds=s.seconds) for s in st]
+        if rc != 0:
+            raise CpmError(rc, lib().cpm_last_error().decode() + f" stats={stats}")
+        return stats

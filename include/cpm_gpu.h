@@ -1,0 +1,216 @@
+/*
+ * cpm_gpu.h — C-ABI of the GB300-native closest-point-method solve path.
+ *
+ * The entry points replace the reference's BUILD_CUSTOM_SOLVER path
+ * (nathandking/cpm-ibc).  Every declaration names the reference interface it
+ * stands in for.  Plain pointers and sizes only; host buffers are caller-owned
+ * and copied in/out; device state is owned by opaque handles.  All functions
+ * return 0 on success or a negative cpm_status; cpm_last_error() describes the
+ * last failure of the calling thread.
+ */
+#ifndef CPM_GPU_H
+#define CPM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference throws std::runtime_error for a base point
+ * outside the tube (src/Tube.cpp:477-480) and for unknown surfaces
+ * (src/Surface.cpp:188), and silently returns after 100000 BiCGStab
+ * iterations (src/BiCGStab.h:107); here each is a status. */
+enum cpm_status {
+    CPM_OK = 0,
+    CPM_ERR_INVALID_ARG = -1,
+    CPM_ERR_CUDA = -2,
+    CPM_ERR_OOM = -3,
+    CPM_ERR_BASEPOINT_OUTSIDE_TUBE = -4,
+    CPM_ERR_NOT_CONVERGED = -5,
+    CPM_ERR_BREAKDOWN = -6,
+    CPM_ERR_UNSUPPORTED = -7,
+    CPM_ERR_ADMISSION = -8,
+    CPM_ERR_TIMEOUT = -9
+};
+
+/* Surface kinds: the reference dispatches on a name string
+ * (src/Surface.cpp:61-190); the in-scope kinds are numbered. */
+enum cpm_surface_kind {
+    CPM_SPHERE = 0,        /* cpSphere    src/Surface.cpp:710-741  params R [, centre] */
+    CPM_TORUS = 1,         /* cpTorus     src/Surface.cpp:800-838  params R, r          */
+    CPM_CIRCLE3D = 2,      /* cpCircle3D  src/Surface.cpp:464-504  params R, centre, normal */
+    CPM_POINT = 3,         /* cpPoint     src/Surface.cpp:840-848  params x, y, z       */
+    CPM_TRIANGULATION = 4, /* cpTri       src/Surface.cpp:1751-1780 (fcpw in the reference) */
+    CPM_POLYLINE = 5       /* cpTri on line segments, same lines                          */
+};
+
+/* SurfaceSpecifier (src/SurfaceSpecifier.h:198-216) + IBCMetaData
+ * (src/IBCMetaData.h:9-24) in one plain struct. */
+typedef struct cpm_surface_desc {
+    int32_t kind;
+    int32_t nparams;
+    double params[8];
+    double bbox[2];
+    int64_t nverts;
+    const double *verts;   /* 3*nverts, host memory */
+    int64_t nprims;
+    const int64_t *prims;  /* 3*nprims triangles or 2*nprims segments */
+    int32_t boundary_order;         /* IBCMetaData::boundary_order (1 or 2) */
+    int32_t boundary_type[2];       /* 0 Dirichlet, 1 Neumann */
+    int32_t is_oriented;
+    int32_t has_point_on_side1;
+    int32_t use_cp_diff_directions;
+    int32_t use_Jcp_surface_normals;
+    int32_t pad0;
+    double on_ibc_tolerance;
+    double point_on_side1[3];
+    double dof_radius_scale;        /* IBCMetaData::ibc_DOFSubset_radius_scale */
+} cpm_surface_desc;
+
+typedef struct cpm_tube_s *cpm_tube_t;
+typedef struct cpm_opset_s *cpm_opset_t;
+typedef struct cpm_solver_s *cpm_solver_t;
+
+typedef struct cpm_tube_info {
+    int64_t n_nodes;     /* Tube::nNodes            src/Tube.h:51 */
+    int64_t n1d;         /* Tube::N1d               src/Tube.h:54 */
+    int64_t n_bricks;    /* occupied 4^3 bricks */
+    int64_t n_visited;   /* grid nodes whose closest point was evaluated */
+    double dx;           /* Tube::dx */
+    double xstart;       /* Tube::xstart()[d] (equal in every dimension) */
+    double radius;       /* Tube::TubeRadius        src/Tube.cpp:131-138 */
+    int32_t p;           /* interpolation degree */
+    int32_t pad;
+} cpm_tube_info;
+
+/* ---- errors / device ---------------------------------------------------- */
+const char *cpm_last_error(void);
+/* Select the CUDA device for this process's library state; call before any
+ * other entry point (the library stream is created on the current device). */
+int cpm_set_device(int32_t device);
+int cpm_device_info(char *name, int64_t name_len, int64_t *free_bytes, int64_t *total_bytes, int32_t *sm_count);
+
+/* ---- Tube ----------------------------------------------------------------
+ * Tube(SurfaceSpecifier&, size_t p, Scalar dx)  src/Tube.h:45, src/Tube.cpp:46-55,295-461.
+ * Builds the band on the device: analytic (or mesh) closest points, band test
+ * |dist| <= r, 6-connected component of the seed node, Morton-ordered 4^3
+ * bricks, neighbour / brick tables, base points and tricubic weights. */
+int cpm_tube_build(const cpm_surface_desc *surface, int32_t p, double dx, cpm_tube_t *out);
+
+/* Same tube, but the closest point and distance of every grid node the build
+ * evaluates come from the caller (keys = grid linear indices i*N1d^2+j*N1d+k,
+ * sorted ascending).  "Given the same closest points" parity entry point. */
+int cpm_tube_build_from_cp(const cpm_surface_desc *surface, int32_t p, double dx, int64_t n, const int64_t *keys,
+                           const double *cp, const double *dist, cpm_tube_t *out);
+
+int cpm_tube_info_get(cpm_tube_t t, cpm_tube_info *info);
+
+/* Tube accessors, exported in device (Morton-brick) order together with each
+ * node's grid linear index `rec` (Node::recIndex, src/Node.h:11), so callers
+ * can permute to the reference's BFS order.  Any pointer may be NULL.
+ *   x, cp: 3*n; dist: n; bpt_rec: n (grid linear index of the base point,
+ *   Tube::bpt src/Tube.h:147 as a grid index); nbr: 6*n tube indices or -1
+ *   (Node::neighbour order +x,-x,+y,-y,+z,-z, src/Node.h:23);
+ *   w: 12*n tricubic 1-D weights [d][j] (Interpolation m_w, src/Interpolation.h:29). */
+int cpm_tube_export(cpm_tube_t t, int64_t *rec, double *x, double *cp, double *dist, int64_t *bpt_rec, int64_t *nbr,
+                    double *w);
+
+/* Interpolation(Tube&, xq) + BuildInterpolationMatrix (src/Interpolation.cpp:23-36,52-121):
+ * per query point the 64 column indices (device tube order) and E entries
+ * (w2[k]*w1[j]*w0[i], walk +x outer, +y, +z inner).  Returns
+ * CPM_ERR_BASEPOINT_OUTSIDE_TUBE like Tube::ComputeBasePoints. */
+int cpm_interp_query(cpm_tube_t t, int64_t n, const double *xq, int64_t *cols, double *vals);
+
+int cpm_tube_destroy(cpm_tube_t t);
+
+/* ---- Operator set (Lfull, Efull, identity rows) -------------------------
+ * Helpers::SetupMatrices (src/Helpers.cpp:86-93), IBCSubsets::Initialize
+ * (src/IBCSubsets.h:23) and IBCMatrixManipulations::AddIBCFiniteDifference /
+ * AddIBCExtension (src/IBCMatrixManipulations.cpp:12-71) as one object whose
+ * rows are: tube rows (device order), then IBC DOF rows and Dirichlet value
+ * rows in the reference's column layout (src/IBCSubsets.cpp:74-116). */
+int cpm_opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, cpm_opset_t *out);
+
+/* sizes: [D, N, total_ibc_dofs, num_2nd_order_rows, n_ibc, n_patched_rows, n_moved_entries] */
+int cpm_opset_sizes(cpm_opset_t op, int64_t *sizes);
+
+/* Row layout for right-hand sides (PoissonWithIBC::GetRHS, problems/PoissonWithIBC.cpp:92-133):
+ * kind 0 tube row (f at its closest point), 1 IBC DOF row (f at the DOF's IBC
+ * closest point), 2 Dirichlet value row (IBC value), 3 other.  point: 3*D. */
+int cpm_opset_rows(cpm_opset_t op, uint8_t *identity, int32_t *kind, int32_t *ibc, double *point);
+
+/* IBC subsets of IBC c (IBCSubset / IBCDOFSubset, src/IBCSubset.h, src/IBCDOFSubset.h):
+ * sizes [tagging, dof, column start, dirichlet column start, identity rows start]
+ * and the subsets as device tube indices in the reference's BFS order. */
+int cpm_opset_ibc_sizes(cpm_opset_t op, int32_t c, int64_t *sizes);
+int cpm_opset_ibc_export(cpm_opset_t op, int32_t c, int64_t *tag_set, int64_t *dof_set, double *dof_cp);
+
+/* Assembled Lfull / Efull (which = 0 / 1) as CSR in device row/column order,
+ * for oracle comparison (columns sorted ascending). nnz query with ptr = NULL. */
+int cpm_opset_export_csr(cpm_opset_t op, int32_t which, int64_t *nnz, int64_t *ptr, int64_t *idx, double *val);
+
+int cpm_opset_destroy(cpm_opset_t op);
+
+/* ---- Operator apply and solve --------------------------------------------
+ * GeneralizedBiCGStabSystem::Multiply (src/GeneralizedBiCGStabSystem.h:191-233)
+ * = Solver::Multiply (src/Solver.cpp:122-138):
+ *   y = x on identity rows, else m x + n (L_qq x_q + sum_{c!=q} L_qc (E~x)_c).
+ * x, y: host arrays of D*k doubles, RHS-major (x[j*D + r] is row r of RHS j). */
+int cpm_apply(cpm_opset_t op, double m, double n, int32_t k, const double *x, double *y);
+/* Same with device pointers: row-major [D][kslots] arrays (kslots 1 or 32),
+ * FP64 or FP32 (fp32 = 1), t_dev a caller-owned scratch array of the same
+ * shape for E~x.  Enqueued on the library stream, asynchronous (cpm_sync). */
+int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslots, int32_t fp32, const void *x_dev, void *t_dev,
+                     void *y_dev);
+
+typedef struct cpm_solve_opts {
+    double tol;             /* relative residual, reference 1e-10 (src/Solver.cpp:110) */
+    int32_t max_iters;      /* reference 100000 */
+    int32_t precision;      /* 0 plain FP64 BiCGStab, 1 FP32 inner BiCGStab + FP64 refinement */
+    int32_t precond;        /* 0 identity, 1 diagonal, 2 jacobi (Defines.h:13-18) */
+    int32_t precond_iters;  /* jacobi sweeps (Solver::SetPrecond, src/Solver.cpp:115-120) */
+    double inner_tol;       /* FP32 inner relative tolerance per refinement step */
+    int32_t max_refine;     /* FP64 refinement steps */
+    int32_t pad;
+} cpm_solve_opts;
+
+typedef struct cpm_solve_stats {
+    int32_t iterations;      /* total BiCGStab iterations (inner iterations for precision 1) */
+    int32_t refinements;     /* FP64 residual evaluations */
+    int32_t restarts;
+    int32_t status;          /* cpm_status of this right-hand side */
+    double rel_residual;     /* final ||b - A x|| / ||b|| in FP64 */
+    double seconds;          /* device time of the solve */
+} cpm_solve_stats;
+
+/* Solver::Init(m, n, L, E, precond, identity_rows) (src/Solver.cpp:8-68):
+ * binds (m, n) to an operator set and allocates k slot columns of solver state. */
+int cpm_solver_create(cpm_opset_t op, double m, double n, int32_t kslots, cpm_solver_t *out);
+
+/* Solver::Solve (src/Solver.cpp:69-114) for k right-hand sides at once (k <= kslots);
+ * b, x: host, RHS-major D*k.  stats: k entries (may be NULL). */
+int cpm_solve(cpm_solver_t s, int32_t k, const double *b, double *x, const cpm_solve_opts *opts, cpm_solve_stats *stats);
+/* Device-resident variant: b_dev/x_dev are row-major [D][kslots] FP64 device arrays. */
+int cpm_solve_device(cpm_solver_t s, int32_t k, const void *b_dev, void *x_dev, const cpm_solve_opts *opts,
+                     cpm_solve_stats *stats);
+
+int cpm_solver_destroy(cpm_solver_t s);
+
+/* Synchronise the library stream. */
+int cpm_sync(void);
+
+/* The library's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or timing events with the library's. */
+void *cpm_get_stream(void);
+
+/* Number of kernels this library has launched in this process (graph
+ * launches count their kernel nodes). */
+int64_t cpm_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPM_GPU_H */

@@ -1,0 +1,155 @@
+"""Device tube / weights / IBC subsets against the oracle.
+
+Bit-exact given the same closest points (the tube is built from the oracle's
+closest points through cpm_tube_build_from_cp), and within 1e-14 for the
+device's own closest points (CUDA's libm may differ from glibc by an ulp)."""
+import math
+
+import numpy as np
+import pytest
+
+import studies as S
+
+pytestmark = pytest.mark.gpu
+
+
+def ref_to_gpu_index(ref_rec, gpu_rec):
+    o = np.argsort(gpu_rec)
+    pos = np.searchsorted(gpu_rec[o], ref_rec)
+    assert np.all(gpu_rec[o][pos] == ref_rec)
+    return o[pos]
+
+
+@pytest.mark.parametrize("kind,dx", [("sphere", 0.1), ("sphere", 0.05), ("torus", 0.05)])
+def test_tube_bit_exact_given_same_closest_points(gpu, oracle, kind, dx):
+    if kind == "sphere":
+        od, gd = oracle.sphere_desc(), gpu.desc(gpu.SPHERE, [1.0], (-1.0, 1.0))
+    else:
+        od, gd = oracle.torus_desc(1.0, 0.4, (-1.4, 1.4)), gpu.desc(gpu.TORUS, [1.0, 0.4], (-1.4, 1.4))
+    P = oracle.RefProblem(od, [], 3, dx, record_visited=True)
+    rec, cp, dist = P.visited()
+    T = gpu.Tube.from_closest_points(gd, 3, dx, rec, cp, dist)
+    ref = P.tube()
+    g = T.export()
+    assert T.N == P.N and T.N1d == P.N1d
+    assert T.n_visited == P.n_visited
+    assert T.xstart == P.xstart and T.radius == P.radius
+    # membership
+    assert np.array_equal(np.sort(g["rec"]), np.sort(ref["rec"]))
+    m = ref_to_gpu_index(ref["rec"], g["rec"])
+    # grid coordinates and closest points
+    assert np.array_equal(g["x"][m], ref["x"])
+    assert np.array_equal(g["cp"][m], ref["cp"])
+    # base points (as grid keys) bit-exact
+    assert np.array_equal(g["bpt"][m], ref["rec"][ref["bpt"]])
+    # tricubic weights bit-exact
+    assert np.array_equal(g["w"][m], P.weights())
+    # neighbours, mapped to reference indices
+    inv = np.empty(T.N, np.int64)
+    inv[m] = np.arange(T.N)
+    gn = g["nbr"][m]
+    gn_ref = np.where(gn >= 0, inv[np.maximum(gn, 0)], -1)
+    assert np.array_equal(gn_ref, ref["nbr"])
+
+
+@pytest.mark.parametrize("kind,dx", [("sphere", 0.1), ("torus", 0.05)])
+def test_device_closest_points_match_oracle(gpu, oracle, kind, dx):
+    if kind == "sphere":
+        od, gd = oracle.sphere_desc(), gpu.desc(gpu.SPHERE, [1.0], (-1.0, 1.0))
+    else:
+        od, gd = oracle.torus_desc(1.0, 0.4, (-1.4, 1.4)), gpu.desc(gpu.TORUS, [1.0, 0.4], (-1.4, 1.4))
+    P = oracle.RefProblem(od, [], 3, dx)
+    T = gpu.Tube(gd, 3, dx)
+    ref, g = P.tube(), T.export()
+    assert np.array_equal(np.sort(g["rec"]), np.sort(ref["rec"]))
+    m = ref_to_gpu_index(ref["rec"], g["rec"])
+    assert np.max(np.abs(g["cp"][m] - ref["cp"])) < 1e-14
+    assert np.max(np.abs(g["dist"][m] - ref["dist"])) < 1e-14
+    # base points: floor((cp - xstart)/dx) can only differ where a closest-point
+    # coordinate lies within rounding of a grid plane
+    diff = g["bpt"][m] != ref["rec"][ref["bpt"]]
+    f = (ref["cp"][diff] - P.xstart) / dx
+    assert np.all(np.min(np.abs(f - np.round(f)), axis=1) < 1e-9)
+    assert diff.sum() <= max(2, P.N // 1000)
+    w_ok = ~diff
+    assert np.max(np.abs(g["w"][m][w_ok] - P.weights()[w_ok])) < 1e-12
+
+
+def test_interp_query_matches_oracle_rows(gpu, oracle):
+    dx = 0.1
+    P = oracle.RefProblem(oracle.sphere_desc(), [], 3, dx)
+    T = gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx)
+    ref, g = P.tube(), T.export()
+    m = ref_to_gpu_index(ref["rec"], g["rec"])
+    inv = np.empty(T.N, np.int64)
+    inv[m] = np.arange(T.N)
+    ptr, idx, val = P.csr(3)  # E
+    cols, vals = T.interp_query(ref["cp"])
+    for q in range(0, P.N, 97):
+        a = sorted(zip(idx[ptr[q]:ptr[q + 1]].tolist(), val[ptr[q]:ptr[q + 1]].tolist()))
+        b = sorted(zip(inv[cols[q]].tolist(), vals[q].tolist()))
+        assert [c for c, _ in a] == [c for c, _ in b]
+        assert np.max(np.abs(np.array([v for _, v in a]) - np.array([v for _, v in b]))) < 1e-14
+
+
+def c2_ibcs(mod, dx, order=2):
+    """Config C2: circles z = 0.3 (u = 1) and z = -0.5 (u = 0) on the unit sphere."""
+    mk = (lambda R, c, n: mod.circle3d_desc(R, c, n, dx, order)) if hasattr(mod, "circle3d_desc") else (
+        lambda R, c, n: mod.desc(mod.CIRCLE3D, [R, *c, *n], (-1.0, 1.0), boundary_order=order, on_ibc_tolerance=0.1 * dx * dx))
+    return [mk(math.sqrt(1 - 0.09), (0, 0, 0.3), (0, 0, 1)), mk(math.sqrt(1 - 0.25), (0, 0, -0.5), (0, 0, 1))]
+
+
+@pytest.mark.parametrize("dx,order", [(0.1, 2), (0.05, 2), (0.05, 1)])
+def test_ibc_subsets_bit_exact(gpu, oracle, dx, order):
+    P = oracle.RefProblem(oracle.sphere_desc(), c2_ibcs(oracle, dx, order), 3, dx, record_visited=True)
+    T = gpu.Tube.from_closest_points(gpu.desc(gpu.SPHERE, [1.0]), 3, dx, *P.visited())
+    O = gpu.OpSet(T, c2_ibcs(gpu, dx, order))
+    ref, g = P.tube(), T.export()
+    assert O.D == P.D and O.total_ibc_dofs == P.total_ibc_dofs and O.num2 == P.num2
+    for c in range(2):
+        rs, gs = P.ibc_subsets(c), O.ibc_subsets(c)
+        # same nodes in the same (BFS) order, compared as grid keys
+        assert np.array_equal(g["rec"][gs["tag_set"]], ref["rec"][rs["tag_set"]])
+        assert np.array_equal(g["rec"][gs["dof_set"]], ref["rec"][rs["dof_set"]])
+        assert gs["col_start"] == rs["col_start"] and gs["identity_rows_start"] == rs["identity_rows_start"]
+    rr, gr = P.rows(), O.rows()
+    assert np.array_equal(rr["identity"][P.N:], gr["identity"][P.N:])
+    assert np.array_equal(rr["kind"][P.N:], gr["kind"][P.N:])
+
+
+def _permuted_csr(gpu_csr, m_inv_full, D):
+    ptr, idx, val = gpu_csr
+    rows = {}
+    for r in range(D):
+        rows[r] = (m_inv_full[idx[ptr[r]:ptr[r + 1]]], val[ptr[r]:ptr[r + 1]])
+    return rows
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_ibc_operator_rows_match_oracle(gpu, oracle, which):
+    """Lfull / Efull rows (with IBC column moves) equal the oracle's up to rounding of the weights' products."""
+    dx = 0.1
+    P = oracle.RefProblem(oracle.sphere_desc(), c2_ibcs(oracle, dx), 3, dx, record_visited=True)
+    T = gpu.Tube.from_closest_points(gpu.desc(gpu.SPHERE, [1.0]), 3, dx, *P.visited())
+    O = gpu.OpSet(T, c2_ibcs(gpu, dx))
+    ref, g = P.tube(), T.export()
+    m = ref_to_gpu_index(ref["rec"], g["rec"])
+    full = np.arange(O.D)
+    full[m] = np.arange(P.N)  # gpu tube row -> reference row; IBC rows unchanged
+    # gpu row index for each reference row
+    g_of_ref = np.arange(O.D)
+    g_of_ref[:P.N] = m
+    rp, ri, rv = P.csr(which)
+    gp, gi, gv = O.csr(which)
+    for r in range(P.D):
+        gr = g_of_ref[r]
+        a = dict(zip(ri[rp[r]:rp[r + 1]].tolist(), rv[rp[r]:rp[r + 1]].tolist()))
+        b = dict(zip(full[gi[gp[gr]:gp[gr + 1]]].tolist(), gv[gp[gr]:gp[gr + 1]].tolist()))
+        a = {k: v for k, v in a.items() if v != 0.0}
+        b = {k: v for k, v in b.items() if v != 0.0}
+        assert a.keys() == b.keys(), (r, sorted(set(a) ^ set(b)))
+        # tube rows are bit-exact given the same closest points; IBC DOF rows
+        # interpolate at cp-bar, which the device computes with CUDA's libm
+        tol = 0.0 if r < P.N else 1e-13
+        for k in a:
+            assert abs(a[k] - b[k]) <= tol * max(1.0, abs(a[k])), (r, k, a[k], b[k])

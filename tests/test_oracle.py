@@ -1,0 +1,86 @@
+"""The oracle (CPU restatement of the reference's solve path) against the
+reference's own known answers: the golden average convergence orders its
+convergence studies assert (+-1e-2), and its compile-time self-checks
+(row sums of E equal 1, src/Interpolation.cpp:232-239; BFS IBC subset equals
+the brute-force subset, src/IBCSubset.cpp:86-153)."""
+import math
+
+import numpy as np
+import pytest
+
+import studies as S
+
+
+def test_shifted_poisson_sphere_golden_order(oracle):
+    # convergence_studies/PoissonProblems/PoissonProblems.cpp:119-137,169,230,233
+    errs = [S.oracle_error(S.shifted_poisson_sphere(dx), dx)[0] for dx in S.DX_3D]
+    order, _ = S.convergence_order(errs, S.DX_3D)
+    assert abs(order - S.GOLDEN_SHIFTED_POISSON_SPHERE) < 1e-2
+    assert abs(order - S.GOLDEN_SHIFTED_POISSON_SPHERE) < 1e-4  # tighter than the reference asks
+
+
+@pytest.mark.parametrize("i", [0, 1])
+def test_sphere_circle_ibc_golden_order(oracle, i):
+    # PoissonProblemsWithIBC.cpp:230-272 (order-2 Dirichlet Circle3D IBC), golden list :377
+    errs = [S.oracle_error(S.sphere_circle_ibc(dx, i), dx)[0] for dx in S.DX_3D]
+    order, _ = S.convergence_order(errs, S.DX_3D)
+    assert abs(order - S.GOLDEN_SPHERE_CIRCLE[i]) < 1e-2
+
+
+@pytest.mark.parametrize("i", [0, 1])
+def test_sphere_point_ibc_golden_order(oracle, i):
+    # PoissonProblemsWithIBC.cpp:274-317 (order-2 Dirichlet Point IBC), golden list :378
+    errs = [S.oracle_error(S.sphere_point_ibc(dx, i), dx)[0] for dx in S.DX_3D]
+    order, _ = S.convergence_order(errs, S.DX_3D)
+    assert abs(order - S.GOLDEN_SPHERE_POINT[i]) < 1e-2
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("i", range(2, 10))
+def test_sphere_circle_ibc_golden_order_all(oracle, i):
+    errs = [S.oracle_error(S.sphere_circle_ibc(dx, i), dx)[0] for dx in S.DX_3D]
+    assert abs(S.convergence_order(errs, S.DX_3D)[0] - S.GOLDEN_SPHERE_CIRCLE[i]) < 1e-2
+
+
+def test_interpolation_rows_sum_to_one(oracle):
+    P = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1)
+    ptr, idx, val = P.csr(3)
+    sums = np.add.reduceat(val, ptr[:-1])
+    assert np.allclose(sums, 1.0, atol=1e-13)
+    assert np.all(np.diff(ptr) == 64)
+
+
+def test_tube_is_band_component(oracle):
+    """Tube = 6-connected component of {|d| <= r} containing the seed (src/Tube.cpp:429-454)."""
+    P = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1, record_visited=True)
+    t = P.tube()
+    rec, cp, dist = P.visited()
+    inside = np.abs(dist) <= P.radius
+    tube_keys = set(t["rec"].tolist())
+    assert tube_keys <= set(rec[inside].tolist())
+    # every visited node outside the tube is either out of the band or not adjacent... it was visited
+    # because it neighbours a tube node; nodes of the band that were visited are all in the tube
+    assert set(rec[inside].tolist()) == tube_keys
+    assert abs(P.N - 10900) < 400  # about 10.9k nodes at dx = 0.1
+
+
+def test_ibc_subset_equals_brute_force(oracle):
+    """IBC_TESTS idea (src/IBCSubset.cpp:86-108): BFS subset = brute-force {dist_C < 2r}."""
+    dx = 0.1
+    R, c, n = S.circle3d_params([0.3, 0.2, 0.9])
+    ibc = oracle.circle3d_desc(R, c, n, dx)
+    P = oracle.RefProblem(oracle.sphere_desc(), [ibc], 3, dx)
+    sub = P.ibc_subsets(0)
+    t = P.tube()
+    _, d = oracle.closest_points(ibc, t["x"])
+    brute = np.nonzero(d < 2 * P.radius)[0]
+    assert sorted(sub["tag_set"].tolist()) == sorted(brute.tolist())
+    dof = sorted(sub["dof_set"].tolist())
+    assert dof == sorted(np.nonzero(d < P.radius)[0].tolist())
+
+
+def test_grid_sizing_matches_survey_table(oracle):
+    """Tube::ConstructTube sizing (src/Tube.cpp:131-157) at the sphere and torus configs."""
+    P = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1)
+    assert P.N1d == 33 and abs(P.xstart - (-1.6)) < 1e-15
+    assert abs(P.radius - 1.0001 * math.sqrt(17) * 0.1) < 1e-15
