@@ -190,6 +190,41 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(what):
+    """Short, self-contained workload runs for ncu captures: 3 + 5 FP32 32-RHS
+    applies and 3 + 5 FP64 1-RHS applies, or one batched mixed-precision solve."""
+    import torch
+
+    import build_ext
+
+    build_ext.build()
+    import cpm_gb300 as cg
+
+    cg.set_device(0)
+    dev = torch.device("cuda", 0)
+    T = cg.Tube(cg.desc(cg.SPHERE, [1.0]), 3, DX)
+    O = cg.OpSet(T, circles(cg, DX))
+    D = O.D
+    if what == "apply":
+        for k, fp32 in ((KSLOTS, True), (1, False)):
+            dt = torch.float32 if fp32 else torch.float64
+            x = torch.randn((D, k), dtype=dt, device=dev)
+            t = torch.empty_like(x)
+            y = torch.empty_like(x)
+            for _ in range(8):
+                O.apply_device(0.0, -1.0, k, fp32, x.data_ptr(), t.data_ptr(), y.data_ptr())
+            cg.sync()
+    else:
+        rows = O.rows()
+        rng = np.random.default_rng(5)
+        B = np.stack([rhs_from_rows(rows, rng.uniform(0, 1, 2)) for _ in range(KSLOTS)], axis=1)
+        b = torch.from_numpy(B).to(dev)
+        x = torch.zeros_like(b)
+        st = cg.Solver(O, 0.0, -1.0, kslots=KSLOTS).solve_device(b.data_ptr(), x.data_ptr(), KSLOTS, tol=TOL, precision=1)
+        print(json.dumps({"iterations": max(s["iterations"] for s in st)}))
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -198,9 +233,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-solves", type=int, default=8)
+    ap.add_argument("--profile", choices=["apply", "solve"], default=None,
+                    help="run only a few applies (or one batched solve) of the workload, for ncu")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile:
+        return run_profile(args.profile)
     args.warmup = max(3, args.warmup)
 
     world, rank, local, dist = dist_setup()

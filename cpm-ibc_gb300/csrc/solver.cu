@@ -7,10 +7,18 @@
 //        their reductions; per-slot scalars stay on the device; reductions are
 //        accumulated in FP64 with a fixed-order two-level tree (deterministic
 //        and independent of the other slots' contents)
-//   K11  FP64 iterative refinement around an FP32 inner BiCGStab: r = b - A x
-//        in FP64, inner solve on r/||r|| in FP32, x += ||r|| d
+//   K11  mixed precision: the Krylov iteration runs in FP32 (FP32 weights and
+//        vectors, FP64 reductions) and is refined in FP64 by reliable updates
+//        (Sleijpen & van der Vorst, "Reliable updated residuals in hybrid Bi-CG
+//        methods", Computing 56, 1996; the mixed-precision form of Clark et al.,
+//        Comput. Phys. Commun. 181, 2010): whenever the FP32 residual has
+//        dropped by delta since the last update, or claims convergence, the
+//        FP32 solution increment is added to the FP64 solution, the FP64 true
+//        residual b - A x replaces the FP32 recursive one and the iteration
+//        continues with its search directions; the solve ends when the FP64
+//        true residual meets ||b - A x|| <= tol ||b||.
 // Every slot is an independent state machine (idle / iterating / refine /
-// restart / done), so slots can start and finish at different times.
+// reliable-update / restart / done), so slots start and finish independently.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -20,25 +28,46 @@
 
 namespace cpm {
 
-enum Phase : int { PH_IDLE = 0, PH_ITER = 1, PH_REFINE = 2, PH_DONE = 3, PH_RESTART = 4, PH_INNER_INIT = 5 };
+enum Phase : int { PH_IDLE = 0, PH_ITER = 1, PH_REFINE = 2, PH_DONE = 3, PH_RESTART = 4, PH_INNER_INIT = 5, PH_RELIABLE = 6 };
 
 struct Slot {
     double rho, rho_old, alpha, omega, beta;
-    double bnorm2, r0norm2, rr, tol2;
+    double bnorm2, r0norm2, rr, tol2, rr_max;
     double scale, rnorm64, outer_tol2, b64norm2;
-    int phase, iters, inner_iters, refinements, restarts, status, pad0, pad1;
+    int phase, iters, inner_iters, refinements, restarts, status, krylov_restart, pad1;
 };
 
 struct SolveParams {
-    double tol, inner_tol;
-    int max_iters, max_inner, max_refine, mixed;
+    double tol, delta;
+    int max_iters, max_refine, mixed, pad;
 };
 
 constexpr int BS = 256;
+constexpr unsigned FULL = 0xffffffffu;
 
+// row functions: warp-per-row for 32 slots, thread-per-row otherwise
+template <class T, int K>
+__device__ __forceinline__ T E_ROW(const OpView<T> &op, int64_t r, int s, const T *__restrict__ x) {
+    if constexpr (K == 32)
+        return e_row_warp<T>(op, r, s, x);
+    else
+        return e_row_thread<T, K>(op, r, s, x);
+}
+template <class T, int K>
+__device__ __forceinline__ T L_ROW(const OpView<T> &op, int64_t r, int s, T m, T n, const T *__restrict__ x,
+                                   const T *__restrict__ t) {
+    if constexpr (K == 32)
+        return l_row_warp<T>(op, r, s, m, n, x, t);
+    else
+        return l_row<T, K>(op, r, s, m, n, x, t);
+}
+// whether this thread's loop body runs: for 32 slots the whole warp runs if any slot is active
 template <int K>
-__device__ __forceinline__ bool slot_in(const Slot *sl, int s, int ph) {
-    return sl[s].phase == ph;
+__device__ __forceinline__ bool run_rows(bool act) {
+    if constexpr (K == 32)
+        return __any_sync(FULL, act);
+    else
+        return act;
 }
 
 // ---- fixed-order block + grid reduction with a last-block finaliser
@@ -99,9 +128,11 @@ __global__ void k_epass(OpView<T> op, const Slot *__restrict__ sl, int ph, const
     int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int64_t r = gid / K;
     int s = (int)(gid % K);
-    if (r >= op.D) return;
-    if (ph >= 0 && sl[s].phase != ph) return;
-    t[r * K + s] = e_row<T, K>(op, r, s, x);
+    if (r >= op.D) return;  // warp-uniform for K = 32
+    const bool act = (ph < 0) || sl[s].phase == ph;
+    if (!run_rows<K>(act)) return;
+    T v = E_ROW<T, K>(op, r, s, x);
+    if (act) t[r * K + s] = v;
 }
 
 // plain L pass (apply API)
@@ -111,17 +142,17 @@ __global__ void k_lpass(OpView<T> op, T m, T n, const T *__restrict__ x, const T
     int64_t r = gid / K;
     int s = (int)(gid % K);
     if (r >= op.D) return;
-    y[r * K + s] = l_row<T, K>(op, r, s, m, n, x, t);
+    y[r * K + s] = L_ROW<T, K>(op, r, s, m, n, x, t);
 }
 
-#define GRID_LOOP                                                  \
-    constexpr int RPB = BS / K;                                    \
-    const int s = threadIdx.x % K;                                 \
+#define GRID_LOOP                                                    \
+    constexpr int RPB = BS / K;                                      \
+    const int s = threadIdx.x % K;                                   \
     const int64_t r0i = (int64_t)blockIdx.x * RPB + threadIdx.x / K; \
     const int64_t rstride = (int64_t)gridDim.x * RPB;
 
-// --- plain FP64 / inner init: x = 0, r = r0 = rhs, p = v = 0; ||rhs||^2
-// rhs = b (plain) or (T)(r64 / scale) (inner init)
+// --- start of a (plain or mixed) Krylov iteration: x = 0, r = r0 = rhs, p = v = 0
+// rhs = b (plain) or (T)(r64 / scale) (mixed)
 template <class T, int K>
 __global__ void k_init(OpView<T> op, Slot *sl, SolveParams P, int from_phase, const double *__restrict__ rhs64,
                        T *__restrict__ x, T *__restrict__ r, T *__restrict__ r0, T *__restrict__ p, T *__restrict__ v,
@@ -149,12 +180,15 @@ __global__ void k_init(OpView<T> op, Slot *sl, SolveParams P, int from_phase, co
         S.bnorm2 = b2;
         S.r0norm2 = b2;
         S.rr = b2;
+        S.rr_max = b2;
         S.rho_old = 1.0;
         S.alpha = 1.0;
         S.omega = 1.0;
         S.inner_iters = 0;
+        S.krylov_restart = 0;
         if (from_phase == PH_INNER_INIT) {
-            S.tol2 = P.inner_tol * P.inner_tol * b2;
+            // claimed convergence of the FP32 residual, in the scaled system
+            S.tol2 = P.tol * P.tol * S.b64norm2 / (S.scale * S.scale);
         } else {
             S.tol2 = P.tol * P.tol * b2;  // BiCGStab::Solve: tol2 = tol^2 ||b||^2 (src/BiCGStab.h:56)
             S.iters = 0;
@@ -200,11 +234,13 @@ __global__ void k_apply_alpha(OpView<T> op, Slot *sl, T m, T n, const T *__restr
     GRID_LOOP
     const bool act = sl[s].phase == PH_ITER;
     double acc[1] = {0.0};
-    if (act)
+    if (run_rows<K>(act))
         for (int64_t row = r0i; row < op.D; row += rstride) {
-            T vv = l_row<T, K>(op, row, s, m, n, y, te);
-            v[row * K + s] = vv;
-            acc[0] += (double)r0[row * K + s] * (double)vv;
+            T vv = L_ROW<T, K>(op, row, s, m, n, y, te);
+            if (act) {
+                v[row * K + s] = vv;
+                acc[0] += (double)r0[row * K + s] * (double)vv;
+            }
         }
     double tot[1];
     if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
@@ -236,12 +272,14 @@ __global__ void k_apply_omega(OpView<T> op, Slot *sl, T m, T n, const T *__restr
     GRID_LOOP
     const bool act = sl[s].phase == PH_ITER;
     double acc[2] = {0.0, 0.0};
-    if (act)
+    if (run_rows<K>(act))
         for (int64_t row = r0i; row < op.D; row += rstride) {
-            T tt = l_row<T, K>(op, row, s, m, n, z, te);
-            tv[row * K + s] = tt;
-            acc[0] += (double)tt * (double)tt;
-            acc[1] += (double)tt * (double)sv[row * K + s];
+            T tt = L_ROW<T, K>(op, row, s, m, n, z, te);
+            if (act) {
+                tv[row * K + s] = tt;
+                acc[0] += (double)tt * (double)tt;
+                acc[1] += (double)tt * (double)sv[row * K + s];
+            }
         }
     double tot[2];
     if (grid_reduce<K, 2>(acc, partial, counter, tot)) {
@@ -281,7 +319,10 @@ __global__ void k_update_xr(int64_t D, Slot *sl, SolveParams P, const T *__restr
         S.rr = tot[0];
         const bool conv = !(S.rr > S.tol2);
         if (P.mixed) {
-            if (conv || S.inner_iters >= P.max_inner || S.iters >= P.max_iters || !isfinite(S.rr)) {
+            S.rr_max = fmax(S.rr_max, S.rr);
+            // reliable update when the FP32 residual fell by delta or claims convergence
+            if (conv || S.rr <= P.delta * P.delta * S.rr_max || S.iters >= P.max_iters || !isfinite(S.rr)) {
+                S.rho_old = S.rho;
                 S.phase = PH_REFINE;
                 return;
             }
@@ -301,7 +342,12 @@ __global__ void k_update_xr(int64_t D, Slot *sl, SolveParams P, const T *__restr
         S.rho = tot[1];
         const double eps = 2.220446049250313e-16;
         if (fabs(S.rho) < eps * eps * S.r0norm2) {  // restart on rho breakdown (src/BiCGStab.h:62-71)
-            S.phase = P.mixed ? PH_REFINE : PH_RESTART;
+            if (P.mixed) {
+                S.krylov_restart = 1;
+                S.phase = PH_REFINE;
+            } else {
+                S.phase = PH_RESTART;
+            }
             return;
         }
         S.beta = (S.rho / S.rho_old) * (S.alpha / S.omega);
@@ -316,13 +362,15 @@ __global__ void k_restart(OpView<T> op, Slot *sl, T m, T n, const double *__rest
     GRID_LOOP
     const bool act = sl[s].phase == PH_RESTART;
     double acc[1] = {0.0};
-    if (act)
+    if (run_rows<K>(act))
         for (int64_t row = r0i; row < op.D; row += rstride) {
-            T ax = l_row<T, K>(op, row, s, m, n, x, te);
-            T ri = (T)b[row * K + s] - ax;
-            r[row * K + s] = ri;
-            r0[row * K + s] = ri;
-            acc[0] += (double)ri * (double)ri;
+            T ax = L_ROW<T, K>(op, row, s, m, n, x, te);
+            if (act) {
+                T ri = (T)b[row * K + s] - ax;
+                r[row * K + s] = ri;
+                r0[row * K + s] = ri;
+                acc[0] += (double)ri * (double)ri;
+            }
         }
     double tot[1];
     if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
@@ -335,17 +383,18 @@ __global__ void k_restart(OpView<T> op, Slot *sl, T m, T n, const double *__rest
     }
 }
 
-// refinement: x64 += scale * u32 for slots in PH_REFINE
+// reliable update, step 1: x64 += scale * u32, u32 = 0
 template <int K>
-__global__ void k_refine_accumulate(int64_t D, const Slot *__restrict__ sl, const float *__restrict__ u, double *__restrict__ x64) {
+__global__ void k_refine_accumulate(int64_t D, const Slot *__restrict__ sl, float *__restrict__ u, double *__restrict__ x64) {
     int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int64_t row = gid / K;
     int s = (int)(gid % K);
     if (row >= D || sl[s].phase != PH_REFINE) return;
     x64[row * K + s] += sl[s].scale * (double)u[row * K + s];
+    u[row * K + s] = 0.0f;
 }
 
-// r64 = b - A x64 (FP64) and ||r64||: done, or a new inner solve on r64 / ||r64||
+// step 2: r64 = b - A x64 (FP64) and ||r64||: done, or replace the FP32 residual
 template <int K>
 __global__ void k_refine_residual(OpView<double> op, Slot *sl, SolveParams P, double m, double n, const double *__restrict__ b,
                                   const double *__restrict__ x64, const double *__restrict__ te, double *__restrict__ r64,
@@ -353,12 +402,14 @@ __global__ void k_refine_residual(OpView<double> op, Slot *sl, SolveParams P, do
     GRID_LOOP
     const bool act = sl[s].phase == PH_REFINE;
     double acc[1] = {0.0};
-    if (act)
+    if (run_rows<K>(act))
         for (int64_t row = r0i; row < op.D; row += rstride) {
-            double ax = l_row<double, K>(op, row, s, m, n, x64, te);
-            double ri = b[row * K + s] - ax;
-            r64[row * K + s] = ri;
-            acc[0] += ri * ri;
+            double ax = L_ROW<double, K>(op, row, s, m, n, x64, te);
+            if (act) {
+                double ri = b[row * K + s] - ax;
+                r64[row * K + s] = ri;
+                acc[0] += ri * ri;
+            }
         }
     double tot[1];
     if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
@@ -373,9 +424,52 @@ __global__ void k_refine_residual(OpView<double> op, Slot *sl, SolveParams P, do
             S.phase = PH_DONE;
             S.status = isfinite(tot[0]) ? CPM_ERR_NOT_CONVERGED : CPM_ERR_BREAKDOWN;
         } else {
-            S.scale = S.rnorm64;
-            S.phase = PH_INNER_INIT;
+            S.phase = PH_RELIABLE;
         }
+    }
+}
+
+// step 3: r32 = r64 / scale; keep p, v, r0 and the scalars, recompute rho = r0 . r
+// (after a rho breakdown the Krylov space restarts from the true residual instead)
+template <int K>
+__global__ void k_reliable(int64_t D, Slot *sl, const double *__restrict__ r64, float *__restrict__ r, float *__restrict__ r0,
+                           float *__restrict__ p, float *__restrict__ v, double *partial, unsigned int *counter) {
+    GRID_LOOP
+    const bool act = sl[s].phase == PH_RELIABLE;
+    const bool fresh = act && sl[s].krylov_restart;
+    double acc[2] = {0.0, 0.0};
+    if (act) {
+        const double inv = 1.0 / sl[s].scale;
+        for (int64_t row = r0i; row < D; row += rstride) {
+            int64_t i = row * K + s;
+            float ri = (float)(r64[i] * inv);
+            r[i] = ri;
+            if (fresh) {
+                r0[i] = ri;
+                p[i] = 0.0f;
+                v[i] = 0.0f;
+            }
+            acc[0] += (double)ri * (double)ri;
+            acc[1] += (double)(fresh ? ri : r0[i]) * (double)ri;
+        }
+    }
+    double tot[2];
+    if (grid_reduce<K, 2>(acc, partial, counter, tot)) {
+        Slot &S = sl[threadIdx.x];
+        if (S.phase != PH_RELIABLE) return;
+        S.rr = tot[0];
+        S.rr_max = tot[0];
+        if (S.krylov_restart) {
+            S.krylov_restart = 0;
+            S.restarts += 1;
+            S.r0norm2 = tot[0];
+            S.rho_old = 1.0;
+            S.alpha = 1.0;
+            S.omega = 1.0;
+        }
+        S.rho = tot[1];
+        S.beta = (S.rho / S.rho_old) * (S.alpha / S.omega);
+        S.phase = PH_ITER;
     }
 }
 
@@ -441,11 +535,6 @@ __global__ void k_gather_cols(int64_t D, int K, int k, const double *__restrict_
     int64_t row = i % D;
     dst[i] = src[row * K + s];
 }
-template <class T>
-__global__ void k_copy_cast(int64_t n, const T *__restrict__ a, double *__restrict__ b) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (double)a[i];
-}
 
 }  // namespace cpm
 
@@ -459,7 +548,6 @@ struct cpm_solver_s {
     int K = 1;
     int64_t D = 0;
     int G = 1;
-    cudaStream_t st = nullptr;
     DBuf<Slot> slots;
     std::vector<Slot> h_slots;
     DBuf<double> partial;
@@ -467,11 +555,13 @@ struct cpm_solver_s {
     // FP64 Krylov vectors (plain path) and FP64 refinement state (mixed path)
     DBuf<double> b64, x64, r64, te64, pden64;
     DBuf<double> dr, dr0, dp, dv, ds, dt, dy, dz;
-    // FP32 Krylov vectors (inner solves of the mixed path)
+    // FP32 Krylov vectors of the mixed path
     DBuf<float> fx, fr, fr0, fp, fv, fs, ft, fy, fz, fte, pden32;
     bool have64 = false, have32 = false;
-    // captured iteration graphs
+    // captured iteration graphs (kernel arguments are fixed pointers; per-solve
+    // parameters live in device memory, so a graph is reused while they match)
     cudaGraphExec_t g_plain = nullptr, g_mixed = nullptr;
+    SolveParams gp_plain{}, gp_mixed{};
     int chunk = 16;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     ~cpm_solver_s() {
@@ -487,7 +577,7 @@ namespace cpm {
 static inline unsigned nblk(int64_t n) { return (unsigned)((n + BS - 1) / BS); }
 
 template <int K>
-static int plain_iteration(cpm_solver_s *s, const SolveParams &P) {
+static void plain_iteration(cpm_solver_s *s, const SolveParams &P) {
     auto op = s->op->view<double>();
     const int64_t D = s->D;
     cudaStream_t st = stream();
@@ -502,21 +592,19 @@ static int plain_iteration(cpm_solver_s *s, const SolveParams &P) {
                                                   s->counter.p);
     k_update_xr<double, K><<<s->G, BS, 0, st>>>(D, sl, P, s->dy.p, s->dz.p, s->ds.p, s->dt.p, s->dr0.p, s->x64.p, s->dr.p,
                                                 s->partial.p, s->counter.p);
-    return 0;
 }
 
 template <int K>
-static int plain_restart(cpm_solver_s *s) {
+static void plain_restart(cpm_solver_s *s) {
     auto op = s->op->view<double>();
     cudaStream_t st = stream();
     k_epass<double, K><<<nblk(s->D * K), BS, 0, st>>>(op, s->slots.p, PH_RESTART, s->x64.p, s->te64.p);
     k_restart<double, K><<<s->G, BS, 0, st>>>(op, s->slots.p, s->m, s->n, s->b64.p, s->x64.p, s->te64.p, s->dr.p, s->dr0.p,
                                               s->partial.p, s->counter.p);
-    return 0;
 }
 
 template <int K>
-static int mixed_iteration(cpm_solver_s *s, const SolveParams &P) {
+static void mixed_iteration(cpm_solver_s *s, const SolveParams &P) {
     auto op = s->op->view<float>();
     const int64_t D = s->D;
     cudaStream_t st = stream();
@@ -530,14 +618,12 @@ static int mixed_iteration(cpm_solver_s *s, const SolveParams &P) {
     k_apply_omega<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p, s->counter.p);
     k_update_xr<float, K><<<s->G, BS, 0, st>>>(D, sl, P, s->fy.p, s->fz.p, s->fs.p, s->ft.p, s->fr0.p, s->fx.p, s->fr.p,
                                                s->partial.p, s->counter.p);
-    return 0;
 }
 
-// FP64 refinement for slots whose inner solve finished, then inner restarts.
+// reliable update (FP64) for slots that asked for one
 template <int K>
-static int mixed_refine(cpm_solver_s *s, const SolveParams &P) {
+static void mixed_refine(cpm_solver_s *s, const SolveParams &P) {
     auto op64 = s->op->view<double>();
-    auto op32 = s->op->view<float>();
     const int64_t D = s->D;
     cudaStream_t st = stream();
     Slot *sl = s->slots.p;
@@ -545,9 +631,7 @@ static int mixed_refine(cpm_solver_s *s, const SolveParams &P) {
     k_epass<double, K><<<nblk(D * K), BS, 0, st>>>(op64, sl, PH_REFINE, s->x64.p, s->te64.p);
     k_refine_residual<K><<<s->G, BS, 0, st>>>(op64, sl, P, s->m, s->n, s->b64.p, s->x64.p, s->te64.p, s->r64.p, s->partial.p,
                                               s->counter.p);
-    k_init<float, K><<<s->G, BS, 0, st>>>(op32, sl, P, PH_INNER_INIT, s->r64.p, s->fx.p, s->fr.p, s->fr0.p, s->fp.p, s->fv.p,
-                                          s->partial.p, s->counter.p);
-    return 0;
+    k_reliable<K><<<s->G, BS, 0, st>>>(D, sl, s->r64.p, s->fr.p, s->fr0.p, s->fp.p, s->fv.p, s->partial.p, s->counter.p);
 }
 
 static int alloc_vectors(cpm_solver_s *s, bool want64, bool want32) {
@@ -566,19 +650,26 @@ static int alloc_vectors(cpm_solver_s *s, bool want64, bool want32) {
     return 0;
 }
 
+static bool same_params(const SolveParams &a, const SolveParams &b) {
+    return a.tol == b.tol && a.delta == b.delta && a.max_iters == b.max_iters && a.max_refine == b.max_refine &&
+           a.mixed == b.mixed;
+}
+
+// mixed graphs interleave a reliable-update step every 2 iterations
+constexpr int REFINE_EVERY = 2;
+
 template <int K>
 static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_stats *stats) {
     SolveParams P;
+    memset(&P, 0, sizeof(P));
     P.tol = o->tol > 0 ? o->tol : 1e-10;
     P.max_iters = o->max_iters > 0 ? o->max_iters : 100000;
     P.mixed = o->precision == 1;
-    P.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
-    P.max_refine = o->max_refine > 0 ? o->max_refine : 40;
-    P.max_inner = 4000;
+    P.delta = o->inner_tol > 0 ? o->inner_tol : 0.1;
+    P.max_refine = o->max_refine > 0 ? o->max_refine : 200;
     if (o->precond != 1) return fail(CPM_ERR_UNSUPPORTED, "the device solver implements the diagonal preconditioner");
     CPM_TRY(alloc_vectors(s, !P.mixed, P.mixed));
     cudaStream_t st = stream();
-    // slot phases: 0..k-1 start, others idle
     for (int j = 0; j < K; ++j) {
         memset(&s->h_slots[j], 0, sizeof(Slot));
         s->h_slots[j].phase = (j < k) ? (P.mixed ? PH_REFINE : PH_ITER) : PH_IDLE;
@@ -594,20 +685,19 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
                                               s->fr0.p, s->fp.p, s->fv.p, s->partial.p, s->counter.p);
     }
     CPM_CUDA_TRY(cudaGetLastError());
-    // one captured graph = `chunk` iterations (+ the refinement step for the mixed path)
     cudaGraphExec_t &gexec = P.mixed ? s->g_mixed : s->g_plain;
-    if (gexec) {
+    SolveParams &gpar = P.mixed ? s->gp_mixed : s->gp_plain;
+    if (gexec && !same_params(gpar, P)) {
         cudaGraphExecDestroy(gexec);
         gexec = nullptr;
     }
-    {
+    if (!gexec) {
         cudaGraph_t graph;
         CPM_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < s->chunk; ++it) {
             if (P.mixed) {
                 mixed_iteration<K>(s, P);
-                // slots whose inner solve finished are refined every 4 iterations
-                if ((it & 3) == 3) mixed_refine<K>(s, P);
+                if (it % REFINE_EVERY == REFINE_EVERY - 1) mixed_refine<K>(s, P);
             } else {
                 plain_iteration<K>(s, P);
             }
@@ -617,10 +707,10 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
         ce = cudaGraphInstantiate(&gexec, graph, 0);
         cudaGraphDestroy(graph);
         if (ce != cudaSuccess) return fail(CPM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+        gpar = P;
     }
     const int64_t max_chunks = (int64_t)P.max_iters / s->chunk + 2 * P.max_refine + 4;
-    // kernels per graph: 7 per BiCGStab iteration (+ 4 per refinement step)
-    const long long per_graph = 7LL * s->chunk + (P.mixed ? 4LL * (s->chunk / 4) : 0);
+    const long long per_graph = 7LL * s->chunk + (P.mixed ? 4LL * (s->chunk / REFINE_EVERY) : 0);
     count_launches(P.mixed ? 2 : 1);
     bool done = false;
     for (int64_t c = 0; c < max_chunks && !done; ++c) {

@@ -141,15 +141,29 @@ def test_ibc_operator_rows_match_oracle(gpu, oracle, which):
     g_of_ref[:P.N] = m
     rp, ri, rv = P.csr(which)
     gp, gi, gv = O.csr(which)
+    # cp-bar of every IBC DOF row (oracle), to recognise base points on a grid plane
+    cpbar = {}
+    for c in range(2):
+        s = P.ibc_subsets(c)
+        for i, q in enumerate(range(s["col_start"], s["col_start"] + len(s["dof_set"]))):
+            cpbar[q] = s["dof_cpbar"][i]
+    on_plane = 0
     for r in range(P.D):
         gr = g_of_ref[r]
         a = dict(zip(ri[rp[r]:rp[r + 1]].tolist(), rv[rp[r]:rp[r + 1]].tolist()))
         b = dict(zip(full[gi[gp[gr]:gp[gr + 1]]].tolist(), gv[gp[gr]:gp[gr + 1]].tolist()))
         a = {k: v for k, v in a.items() if v != 0.0}
         b = {k: v for k, v in b.items() if v != 0.0}
+        if a.keys() != b.keys() and r in cpbar:
+            # the device's cp-bar (CUDA libm) and the oracle's may straddle a grid plane
+            f = (cpbar[r] - P.xstart) / dx
+            assert np.min(np.abs(f - np.round(f))) < 1e-9, (r, cpbar[r])
+            on_plane += 1
+            continue
         assert a.keys() == b.keys(), (r, sorted(set(a) ^ set(b)))
         # tube rows are bit-exact given the same closest points; IBC DOF rows
         # interpolate at cp-bar, which the device computes with CUDA's libm
         tol = 0.0 if r < P.N else 1e-13
         for k in a:
             assert abs(a[k] - b[k]) <= tol * max(1.0, abs(a[k])), (r, k, a[k], b[k])
+    assert on_plane <= 8
