@@ -23,6 +23,8 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <mutex>
+#include <string>
 
 #include "opset.h"
 
@@ -866,6 +868,75 @@ extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslo
         } else {
             k_epass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, nullptr, -1, x, t);
             k_lpass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, m, n, x, t, y);
+        }
+    }
+    count_launches(2);
+    CPM_CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+// ================================================================= allocation-free apply
+// The E~x scratch of cpm_apply_device_noalloc: one fixed array per device,
+// shared by every call (see include/cpm_gpu.h for the contract).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[CPM_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+void *g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// device address of the scratch array on the current device, looked up once per device
+int noalloc_scratch(void **out) {
+    int dev = 0;
+    CPM_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(CPM_ERR_INVALID_ARG, "apply_device_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(CPM_ERR_CUDA, std::string("apply_device_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return 0;
+}
+}  // namespace
+
+extern "C" int cpm_apply_device_noalloc(cpm_opset_t op, double m, double n, int32_t kslots, int32_t fp32, const void *x_dev,
+                                        void *y_dev) {
+    if (!op || !x_dev || !y_dev || (kslots != 1 && kslots != 32))
+        return fail(CPM_ERR_INVALID_ARG, "apply_device_noalloc: null pointer or kslots not 1 / 32");
+    const size_t need = (size_t)op->D * (size_t)kslots * (fp32 ? sizeof(float) : sizeof(double));
+    if (need > (size_t)CPM_NOALLOC_SCRATCH_BYTES)
+        return fail(CPM_ERR_INVALID_ARG, "apply_device_noalloc: scratch of " + std::to_string(need) +
+                                             " bytes exceeds the fixed " + std::to_string(CPM_NOALLOC_SCRATCH_BYTES) +
+                                             "-byte array; use cpm_apply_device with caller scratch");
+    void *t = nullptr;
+    CPM_TRY(noalloc_scratch(&t));
+    const int64_t D = op->D;
+    cudaStream_t st = stream();
+    if (fp32) {
+        auto v = op->view<float>();
+        const float *x = (const float *)x_dev;
+        float *tt = (float *)t, *y = (float *)y_dev;
+        if (kslots == 1) {
+            k_epass<float, 1><<<nblk(D), BS, 0, st>>>(v, nullptr, -1, x, tt);
+            k_lpass<float, 1><<<nblk(D), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
+        } else {
+            k_epass<float, 32><<<nblk(D * 32), BS, 0, st>>>(v, nullptr, -1, x, tt);
+            k_lpass<float, 32><<<nblk(D * 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
+        }
+    } else {
+        auto v = op->view<double>();
+        const double *x = (const double *)x_dev;
+        double *tt = (double *)t, *y = (double *)y_dev;
+        if (kslots == 1) {
+            k_epass<double, 1><<<nblk(D), BS, 0, st>>>(v, nullptr, -1, x, tt);
+            k_lpass<double, 1><<<nblk(D), BS, 0, st>>>(v, m, n, x, tt, y);
+        } else {
+            k_epass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, nullptr, -1, x, tt);
+            k_lpass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, m, n, x, tt, y);
         }
     }
     count_launches(2);

@@ -165,6 +165,24 @@ int cpm_apply(cpm_opset_t op, double m, double n, int32_t k, const double *x, do
 int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslots, int32_t fp32, const void *x_dev, void *t_dev,
                      void *y_dev);
 
+/* Allocation-free variant of cpm_apply_device.  It has no counterpart in the
+ * reference; it exists for callers that cannot allocate device memory when
+ * they apply the operator: applications whose device memory is entirely owned
+ * by their own pool, and latency-critical loops in which a cudaMalloc or
+ * cudaFree would synchronise the device and stall other streams.
+ * Inputs and outputs are caller-owned as in cpm_apply_device; the E~x scratch
+ * lives in one fixed device array of CPM_NOALLOC_SCRATCH_BYTES (32 MiB) that
+ * every GPU which loads this library holds until the process exits.
+ * D * kslots * (4 or 8 bytes) above that limit returns CPM_ERR_INVALID_ARG.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture, with the library's device current.
+ * All calls share the one array, which keeps the previous call's contents
+ * (every entry is rewritten before it is read, nothing needs clearing):
+ * calls that overlap on the GPU race. */
+#define CPM_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int cpm_apply_device_noalloc(cpm_opset_t op, double m, double n, int32_t kslots, int32_t fp32, const void *x_dev,
+                             void *y_dev);
+
 typedef struct cpm_solve_opts {
     double tol;             /* relative residual, reference 1e-10 (src/Solver.cpp:110) */
     int32_t max_iters;      /* reference 100000 */
