@@ -23,7 +23,7 @@
 namespace cpm {
 
 template <class T>
-static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, const T *lval, const T *ldiag) {
+static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, const T *lval, const T *ldiag, const T *w_ord) {
     OpView<T> v;
     v.bv = o->tube->view();
     v.N = o->N;
@@ -47,6 +47,16 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
     // FDMatrices::BuildLaplacianMatrix: -2*dim and 1, then L /= dx*dx (src/FDMatrices.cpp:28-48)
     v.Ldiag = (T)(-6.0 / (o->dx * o->dx));
     v.Loff = (T)(1.0 / (o->dx * o->dx));
+    v.nbr6 = o->nbr6.p;
+    v.ord = o->ord.p;
+    v.grp = o->grp.p;
+    v.ident = o->ident.p;
+    v.gcols = o->gcols.p;
+    v.w_ord = w_ord;
+    v.fl_ord = o->fl_ord.p;
+    v.n_ord = o->n_ord;
+    v.n_grp = o->n_grp;
+    v.n_ident = o->n_ident;
     return v;
 }
 
@@ -54,11 +64,11 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
 
 template <>
 cpm::OpView<double> cpm_opset_s::view<double>() const {
-    return cpm::make_view<double>(this, w.p, p_xval.p, lval.p, ldiag.p);
+    return cpm::make_view<double>(this, w.p, p_xval.p, lval.p, ldiag.p, w_ord.p);
 }
 template <>
 cpm::OpView<float> cpm_opset_s::view<float>() const {
-    return cpm::make_view<float>(this, w32.p, p_xval32.p, lval32.p, ldiag32.p);
+    return cpm::make_view<float>(this, w32.p, p_xval32.p, lval32.p, ldiag32.p, w_ord32.p);
 }
 
 namespace cpm {
@@ -532,6 +542,7 @@ static int make_float_copies(cpm_opset_s *o) {
         return 0;
     };
     CPM_TRY(conv(o->w, o->w32));
+    CPM_TRY(conv(o->w_ord, o->w_ord32));
     CPM_TRY(conv(o->p_xval, o->p_xval32));
     CPM_TRY(conv(o->lval, o->lval32));
     CPM_TRY(conv(o->ldiag, o->ldiag32));
@@ -829,6 +840,99 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs) {
     return 0;
 }
 
+// The six L columns of every tube row with IBC moves applied (-1: no neighbour).
+__global__ void k_build_nbr6(OpView<double> op, int32_t *__restrict__ nbr6) {
+    int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= op.N) return;
+    const uint32_t kk = op.key[r];
+    const int i = unpack_i(kk), j = unpack_j(kk), k = unpack_k(kk);
+    uint8_t lmask = 0;
+    int loff = 0;
+    if (op.flags[r] & F_LMOVE) {
+        int pi = op.patch[r];
+        lmask = op.p_lmask[pi];
+        loff = op.p_loff[pi];
+    }
+    for (int d = 0; d < 6; ++d) {
+        int col;
+        if ((lmask >> d) & 1)
+            col = op.moved[loff + __popc((unsigned)lmask & ((1u << d) - 1u))];
+        else
+            col = node_at(op.bv, i + (d == 0) - (d == 1), j + (d == 2) - (d == 3), k + (d == 4) - (d == 5));
+        nbr6[6 * r + d] = col;
+    }
+}
+
+// 64 bulk stencil columns of each base group (s = 16 i + 4 j + k)
+__global__ void k_group_cols(OpView<double> op, int64_t n_grp, int32_t *__restrict__ gcols) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= 64 * n_grp) return;
+    int64_t g = e >> 6;
+    int s = (int)(e & 63);
+    uint32_t b = op.base[op.ord[op.grp[g]]];
+    int col = node_at(op.bv, unpack_i(b) + (s >> 4), unpack_j(b) + ((s >> 2) & 3), unpack_k(b) + (s & 3));
+    gcols[e] = col >= 0 ? col : 0;  // missing stencil nodes are rejected at tube build time
+}
+
+// weights and flags in base-sorted row order
+__global__ void k_sorted_rows(OpView<double> op, int64_t n_ord, double *__restrict__ w_ord, uint8_t *__restrict__ fl_ord) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= 12 * n_ord) return;
+    int64_t p = e / 12;
+    int a = (int)(e % 12);
+    int64_t r = op.ord[p];
+    w_ord[e] = op.w[12 * r + a];
+    if (a == 0) fl_ord[p] = op.flags[r];
+}
+
+// Apply schedule: neighbour table, rows sorted by base point with their groups,
+// identity rows.  Rows sharing a base point read the same 64 values of x.
+static int build_schedule(cpm_opset_s *o) {
+    const int64_t N = o->N, D = o->D;
+    CPM_TRY(o->nbr6.alloc(6 * N));
+    k_build_nbr6<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(o->view<double>(), o->nbr6.p);
+    CPM_CUDA_TRY(cudaGetLastError());
+    std::vector<uint8_t> flags;
+    std::vector<uint32_t> base;
+    CPM_TRY(o->flags.download(flags, D));
+    CPM_TRY(o->base.download(base, D));
+    std::vector<std::pair<uint32_t, int32_t>> rows;
+    std::vector<int32_t> ident;
+    rows.reserve(D);
+    for (int64_t r = 0; r < D; ++r) {
+        if (flags[r] & F_IDENT)
+            ident.push_back((int32_t)r);
+        else
+            rows.push_back({base[r], (int32_t)r});
+    }
+    std::sort(rows.begin(), rows.end());
+    std::vector<int32_t> ord(rows.size()), grp;
+    for (size_t p = 0; p < rows.size(); ++p) {
+        ord[p] = rows[p].second;
+        if (p == 0 || rows[p].first != rows[p - 1].first) grp.push_back((int32_t)p);
+    }
+    grp.push_back((int32_t)rows.size());
+    o->n_ord = (int64_t)ord.size();
+    o->n_grp = (int64_t)grp.size() - 1;
+    o->n_ident = (int64_t)ident.size();
+    if (ord.empty()) ord.push_back(0);
+    if (ident.empty()) ident.push_back(0);
+    CPM_TRY(o->ord.upload(ord));
+    CPM_TRY(o->grp.upload(grp));
+    CPM_TRY(o->ident.upload(ident));
+    // per group: its 64 bulk stencil columns; per sorted row: weights and flags
+    CPM_TRY(o->gcols.alloc(64 * std::max<int64_t>(1, o->n_grp)));
+    CPM_TRY(o->w_ord.alloc(12 * std::max<int64_t>(1, o->n_ord)));
+    CPM_TRY(o->fl_ord.alloc(std::max<int64_t>(1, o->n_ord)));
+    if (o->n_grp > 0) {
+        k_group_cols<<<(unsigned)((64 * o->n_grp + 255) / 256), 256, 0, stream()>>>(o->view<double>(), o->n_grp, o->gcols.p);
+        k_sorted_rows<<<(unsigned)((12 * o->n_ord + 255) / 256), 256, 0, stream()>>>(o->view<double>(), o->n_ord, o->w_ord.p,
+                                                                                    o->fl_ord.p);
+        CPM_CUDA_TRY(cudaGetLastError());
+    }
+    return 0;
+}
+
 }  // namespace cpm
 
 using namespace cpm;
@@ -840,6 +944,7 @@ extern "C" int cpm_opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_d
     o->tube = t;
     int rc = build_base(o);
     if (!rc && n_ibc > 0) rc = build_ibc(o, n_ibc, ibcs);
+    if (!rc) rc = build_schedule(o);
     if (!rc) rc = make_float_copies(o);
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(stream());

@@ -61,7 +61,7 @@ __device__ __forceinline__ T L_ROW(const OpView<T> &op, int64_t r, int s, T m, T
     if constexpr (K == 32)
         return l_row_warp<T>(op, r, s, m, n, x, t);
     else
-        return l_row<T, K>(op, r, s, m, n, x, t);
+        return l_row_nbr<T, K>(op, r, s, m, n, x, t);
 }
 // whether this thread's loop body runs: for 32 slots the whole warp runs if any slot is active
 template <int K>
@@ -125,16 +125,74 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NDOT], double *partial, 
 // ================================================================= kernels
 
 // E pass for the slots in phase `ph` (ph < 0: every slot).
+// 32 slots: one warp per base group, then one warp per identity row.  The
+// group's 64 x 32 block lives in registers (~150 per thread), so blocks are
+// two warps wide: an SM then keeps ~6 independent blocks resident instead of
+// one 8-warp block that waits for its slowest group.
+constexpr int BS_E32 = 64;
+template <class T>
+__global__ void __launch_bounds__(BS_E32) k_epass32(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x,
+                                                    T *__restrict__ t) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const bool act = (ph < 0) || sl[lane].phase == ph;
+    if (!__any_sync(FULL, act)) return;
+    if (w < op.n_grp) {
+        e_group_warp<T>(op, w, lane, act, x, t);
+        return;
+    }
+    const int64_t q = w - op.n_grp;
+    if (q < op.n_ident && act) {
+        const int64_t r = op.ident[q];
+        t[r * 32 + lane] = x[r * 32 + lane];
+    }
+}
+
+// 32 slots, plane-split: one 4-warp block per base group (grid-stride), then
+// identity rows copied warp per row.
+template <class T>
+__global__ void __launch_bounds__(128) k_epass32s(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x,
+                                                  T *__restrict__ t) {
+    __shared__ EGShared<T> sh;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool act = (ph < 0) || sl[lane].phase == ph;
+    if (!__any_sync(FULL, act)) return;  // the same 32 slots in every warp: block-uniform
+    for (int64_t g = blockIdx.x; g < op.n_grp; g += gridDim.x) e_group_split<T>(op, g, warp, lane, act, sh, x, t);
+    if (act)
+        for (int64_t q = (int64_t)blockIdx.x * 4 + warp; q < op.n_ident; q += (int64_t)gridDim.x * 4) {
+            const uint32_t r = (uint32_t)op.ident[q];
+            t[r * 32u + lane] = x[r * 32u + lane];
+        }
+}
+
+// 1 slot: one thread per row, rows visited in base-point order so that the
+// threads of a warp that share a base read the same cache lines.
+template <class T>
+__global__ void k_epass1(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x, T *__restrict__ t) {
+    if (ph >= 0 && sl[0].phase != ph) return;
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p < op.n_ord) {
+        const int64_t r = op.ord[p];
+        t[r] = e_row_thread<T, 1>(op, r, 0, x);
+        return;
+    }
+    const int64_t q = p - op.n_ord;
+    if (q < op.n_ident) {
+        const int64_t r = op.ident[q];
+        t[r] = x[r];
+    }
+}
+
 template <class T, int K>
-__global__ void k_epass(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x, T *__restrict__ t) {
-    int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t r = gid / K;
-    int s = (int)(gid % K);
-    if (r >= op.D) return;  // warp-uniform for K = 32
-    const bool act = (ph < 0) || sl[s].phase == ph;
-    if (!run_rows<K>(act)) return;
-    T v = E_ROW<T, K>(op, r, s, x);
-    if (act) t[r * K + s] = v;
+static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x, T *t, cudaStream_t st) {
+    static_assert(K == 1 || K == 32, "slot widths 1 and 32");
+    if constexpr (K == 32) {
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(op.n_grp, 152LL * 16));
+        k_epass32s<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
+    } else {
+        const int64_t threads = op.n_ord + op.n_ident;
+        k_epass1<T><<<(unsigned)((threads + BS - 1) / BS), BS, 0, st>>>(op, sl, ph, x, t);
+    }
 }
 
 // plain L pass (apply API)
@@ -585,11 +643,11 @@ static void plain_iteration(cpm_solver_s *s, const SolveParams &P) {
     cudaStream_t st = stream();
     Slot *sl = s->slots.p;
     k_update_p<double, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden64.p, s->dr.p, s->dv.p, s->dp.p, s->dy.p);
-    k_epass<double, K><<<nblk(D * K), BS, 0, st>>>(op, sl, PH_ITER, s->dy.p, s->te64.p);
+    launch_epass<double, K>(op, sl, PH_ITER, s->dy.p, s->te64.p, st);
     k_apply_alpha<double, K><<<s->G, BS, 0, st>>>(op, sl, s->m, s->n, s->dy.p, s->te64.p, s->dr0.p, s->dv.p, s->partial.p,
                                                   s->counter.p);
     k_update_s<double, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden64.p, s->dr.p, s->dv.p, s->ds.p, s->dz.p);
-    k_epass<double, K><<<nblk(D * K), BS, 0, st>>>(op, sl, PH_ITER, s->dz.p, s->te64.p);
+    launch_epass<double, K>(op, sl, PH_ITER, s->dz.p, s->te64.p, st);
     k_apply_omega<double, K><<<s->G, BS, 0, st>>>(op, sl, s->m, s->n, s->dz.p, s->te64.p, s->ds.p, s->dt.p, s->partial.p,
                                                   s->counter.p);
     k_update_xr<double, K><<<s->G, BS, 0, st>>>(D, sl, P, s->dy.p, s->dz.p, s->ds.p, s->dt.p, s->dr0.p, s->x64.p, s->dr.p,
@@ -600,7 +658,7 @@ template <int K>
 static void plain_restart(cpm_solver_s *s) {
     auto op = s->op->view<double>();
     cudaStream_t st = stream();
-    k_epass<double, K><<<nblk(s->D * K), BS, 0, st>>>(op, s->slots.p, PH_RESTART, s->x64.p, s->te64.p);
+    launch_epass<double, K>(op, s->slots.p, PH_RESTART, s->x64.p, s->te64.p, st);
     k_restart<double, K><<<s->G, BS, 0, st>>>(op, s->slots.p, s->m, s->n, s->b64.p, s->x64.p, s->te64.p, s->dr.p, s->dr0.p,
                                               s->partial.p, s->counter.p);
 }
@@ -613,10 +671,10 @@ static void mixed_iteration(cpm_solver_s *s, const SolveParams &P) {
     Slot *sl = s->slots.p;
     const float m = (float)s->m, n = (float)s->n;
     k_update_p<float, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden32.p, s->fr.p, s->fv.p, s->fp.p, s->fy.p);
-    k_epass<float, K><<<nblk(D * K), BS, 0, st>>>(op, sl, PH_ITER, s->fy.p, s->fte.p);
+    launch_epass<float, K>(op, sl, PH_ITER, s->fy.p, s->fte.p, st);
     k_apply_alpha<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p, s->counter.p);
     k_update_s<float, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden32.p, s->fr.p, s->fv.p, s->fs.p, s->fz.p);
-    k_epass<float, K><<<nblk(D * K), BS, 0, st>>>(op, sl, PH_ITER, s->fz.p, s->fte.p);
+    launch_epass<float, K>(op, sl, PH_ITER, s->fz.p, s->fte.p, st);
     k_apply_omega<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p, s->counter.p);
     k_update_xr<float, K><<<s->G, BS, 0, st>>>(D, sl, P, s->fy.p, s->fz.p, s->fs.p, s->ft.p, s->fr0.p, s->fx.p, s->fr.p,
                                                s->partial.p, s->counter.p);
@@ -630,7 +688,7 @@ static void mixed_refine(cpm_solver_s *s, const SolveParams &P) {
     cudaStream_t st = stream();
     Slot *sl = s->slots.p;
     k_refine_accumulate<K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->fx.p, s->x64.p);
-    k_epass<double, K><<<nblk(D * K), BS, 0, st>>>(op64, sl, PH_REFINE, s->x64.p, s->te64.p);
+    launch_epass<double, K>(op64, sl, PH_REFINE, s->x64.p, s->te64.p, st);
     k_refine_residual<K><<<s->G, BS, 0, st>>>(op64, sl, P, s->m, s->n, s->b64.p, s->x64.p, s->te64.p, s->r64.p, s->partial.p,
                                               s->counter.p);
     k_reliable<K><<<s->G, BS, 0, st>>>(D, sl, s->r64.p, s->fr.p, s->fr0.p, s->fp.p, s->fv.p, s->partial.p, s->counter.p);
@@ -667,8 +725,8 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
     P.tol = o->tol > 0 ? o->tol : 1e-10;
     P.max_iters = o->max_iters > 0 ? o->max_iters : 100000;
     P.mixed = o->precision == 1;
-    P.delta = o->inner_tol > 0 ? o->inner_tol : 0.1;
-    P.max_refine = o->max_refine > 0 ? o->max_refine : 200;
+    P.delta = o->inner_tol > 0 ? o->inner_tol : 0.2;
+    P.max_refine = o->max_refine > 0 ? o->max_refine : 400;
     if (o->precond != 1) return fail(CPM_ERR_UNSUPPORTED, "the device solver implements the diagonal preconditioner");
     CPM_TRY(alloc_vectors(s, !P.mixed, P.mixed));
     cudaStream_t st = stream();
@@ -832,7 +890,7 @@ extern "C" int cpm_apply(cpm_opset_t op, double m, double n, int32_t k, const do
     auto v = op->view<double>();
     for (int j = 0; j < k; ++j) {
         CPM_CUDA_TRY(cudaMemcpyAsync(dx.p, x + (size_t)j * D, D * 8, cudaMemcpyHostToDevice, stream()));
-        k_epass<double, 1><<<nblk(D), BS, 0, stream()>>>(v, nullptr, -1, dx.p, dt.p);
+        launch_epass<double, 1>(v, nullptr, -1, dx.p, dt.p, stream());
         k_lpass<double, 1><<<nblk(D), BS, 0, stream()>>>(v, m, n, dx.p, dt.p, dy.p);
         CPM_CUDA_TRY(cudaGetLastError());
         CPM_CUDA_TRY(cudaMemcpyAsync(y + (size_t)j * D, dy.p, D * 8, cudaMemcpyDeviceToHost, stream()));
@@ -852,10 +910,10 @@ extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslo
         const float *x = (const float *)x_dev;
         float *t = (float *)t_dev, *y = (float *)y_dev;
         if (kslots == 1) {
-            k_epass<float, 1><<<nblk(D), BS, 0, st>>>(v, nullptr, -1, x, t);
+            launch_epass<float, 1>(v, nullptr, -1, x, t, st);
             k_lpass<float, 1><<<nblk(D), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
         } else {
-            k_epass<float, 32><<<nblk(D * 32), BS, 0, st>>>(v, nullptr, -1, x, t);
+            launch_epass<float, 32>(v, nullptr, -1, x, t, st);
             k_lpass<float, 32><<<nblk(D * 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
         }
     } else {
@@ -863,10 +921,10 @@ extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslo
         const double *x = (const double *)x_dev;
         double *t = (double *)t_dev, *y = (double *)y_dev;
         if (kslots == 1) {
-            k_epass<double, 1><<<nblk(D), BS, 0, st>>>(v, nullptr, -1, x, t);
+            launch_epass<double, 1>(v, nullptr, -1, x, t, st);
             k_lpass<double, 1><<<nblk(D), BS, 0, st>>>(v, m, n, x, t, y);
         } else {
-            k_epass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, nullptr, -1, x, t);
+            launch_epass<double, 32>(v, nullptr, -1, x, t, st);
             k_lpass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, m, n, x, t, y);
         }
     }
@@ -921,10 +979,10 @@ extern "C" int cpm_apply_device_noalloc(cpm_opset_t op, double m, double n, int3
         const float *x = (const float *)x_dev;
         float *tt = (float *)t, *y = (float *)y_dev;
         if (kslots == 1) {
-            k_epass<float, 1><<<nblk(D), BS, 0, st>>>(v, nullptr, -1, x, tt);
+            launch_epass<float, 1>(v, nullptr, -1, x, tt, st);
             k_lpass<float, 1><<<nblk(D), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
         } else {
-            k_epass<float, 32><<<nblk(D * 32), BS, 0, st>>>(v, nullptr, -1, x, tt);
+            launch_epass<float, 32>(v, nullptr, -1, x, tt, st);
             k_lpass<float, 32><<<nblk(D * 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
         }
     } else {
@@ -932,10 +990,10 @@ extern "C" int cpm_apply_device_noalloc(cpm_opset_t op, double m, double n, int3
         const double *x = (const double *)x_dev;
         double *tt = (double *)t, *y = (double *)y_dev;
         if (kslots == 1) {
-            k_epass<double, 1><<<nblk(D), BS, 0, st>>>(v, nullptr, -1, x, tt);
+            launch_epass<double, 1>(v, nullptr, -1, x, tt, st);
             k_lpass<double, 1><<<nblk(D), BS, 0, st>>>(v, m, n, x, tt, y);
         } else {
-            k_epass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, nullptr, -1, x, tt);
+            launch_epass<double, 32>(v, nullptr, -1, x, tt, st);
             k_lpass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, m, n, x, tt, y);
         }
     }

@@ -294,7 +294,7 @@ class Solver:
         except Exception:
             pass
 
-    def solve(self, b, tol=1e-10, precision=0, max_iters=100000, inner_tol=1e-4, max_refine=40, raise_on_error=True):
+    def solve(self, b, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.2, max_refine=400, raise_on_error=True):
         b = np.ascontiguousarray(np.atleast_2d(b), np.float64)
         k = b.shape[0]
         x = np.zeros_like(b)
@@ -308,7 +308,7 @@ class Solver:
             raise CpmError(rc, lib().cpm_last_error().decode() + f" stats={stats}")
         return x, stats
 
-    def solve_device(self, b_ptr, x_ptr, k, tol=1e-10, precision=0, max_iters=100000, inner_tol=1e-4, max_refine=40):
+    def solve_device(self, b_ptr, x_ptr, k, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.2, max_refine=400):
         o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=1, precond_iters=0,
                       inner_tol=inner_tol, max_refine=max_refine)
         st = (SolveStats * k)()

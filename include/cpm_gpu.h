@@ -189,9 +189,9 @@ typedef struct cpm_solve_opts {
     int32_t precision;      /* 0 plain FP64 BiCGStab, 1 FP32 BiCGStab refined in FP64 (reliable updates) */
     int32_t precond;        /* 0 identity, 1 diagonal, 2 jacobi (Defines.h:13-18) */
     int32_t precond_iters;  /* jacobi sweeps (Solver::SetPrecond, src/Solver.cpp:115-120) */
-    double inner_tol;       /* precision 1: the FP32 residual reduction (default 0.1) after which the
+    double inner_tol;       /* precision 1: the FP32 residual reduction (default 0.2) after which the
                                FP64 true residual replaces it (one refinement step) */
-    int32_t max_refine;     /* FP64 refinement steps (default 200) */
+    int32_t max_refine;     /* FP64 refinement steps (default 400) */
     int32_t pad;
 } cpm_solve_opts;
 
