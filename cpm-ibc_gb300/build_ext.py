@@ -23,6 +23,7 @@ UNITS = {
     "tube.cu": ["-fmad=false"],
     "opset.cu": ["-fmad=false"],
     "solver.cu": [],
+    "geodesic.cu": [],
 }
 
 

@@ -230,7 +230,7 @@ struct IBCData {
     std::vector<int64_t> dof_of_tag;    // tagging index -> dof index or -1
     std::vector<int64_t> dof_set;       // tube indices
     std::vector<int64_t> dof_sub;       // N -> dof index or -1
-    std::vector<double> dof_cp, dof_cpbar, dof_dir;
+    std::vector<double> dof_cp, dof_cpbar, dof_dir, dof_cpdiff;
     QueryRows dof_rows;                 // E_ibc stencils (at cp or cp-bar)
     bool order2 = false, dirichlet = true;
 };
@@ -471,6 +471,7 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
             ib.dof_set.push_back(ib.tag_set[i]);
             for (int k = 0; k < 3; ++k) {
                 ib.dof_cp.push_back(ib.tag_cpc[3 * i + k]);
+                ib.dof_cpdiff.push_back(ib.tag_cpdiff[3 * i + k]);
                 ib.dof_dir.push_back(ib.tag_dir[3 * i + k]);
             }
         }
@@ -574,7 +575,10 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs) {
     for (int c = 0; c < n_ibc; ++c)
         if (!descs[c].use_cp_diff_directions) need_normals = true;
     std::vector<double> normals;
-    if (need_normals) CPM_TRY(tube_normals(o, normals));
+    if (need_normals) {
+        CPM_TRY(tube_normals(o, normals));
+        CPM_TRY(o->normals.upload(normals));
+    }
     DBuf<double> xdev;
     CPM_TRY(xdev.alloc(3 * N));
     k_node_coords<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, t->key.p, t->g.xstart, t->g.dx, xdev.p);
@@ -832,10 +836,12 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs) {
     o->tag_set.resize(n_ibc);
     o->dof_set.resize(n_ibc);
     o->dof_cp.resize(n_ibc);
+    o->dof_cpdiff.resize(n_ibc);
     for (int c = 0; c < n_ibc; ++c) {
         o->tag_set[c] = ibs[c].tag_set;
         o->dof_set[c] = ibs[c].dof_set;
         o->dof_cp[c] = ibs[c].dof_cp;
+        o->dof_cpdiff[c] = ibs[c].dof_cpdiff;
     }
     return 0;
 }

@@ -474,7 +474,10 @@ __device__ __forceinline__ void e_group_split(const OpView<T> &op, int64_t g, in
     if (lane < 16) sh.cols[sidx] = mycol;
     T xb[16];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) xb[q] = x[(uint32_t)__shfl_sync(FULL, mycol, q) * 32u + lane];
+    for (int q = 0; q < 16; ++q) {
+        const uint32_t cq = (uint32_t)__shfl_sync(FULL, mycol, q);
+        xb[q] = act ? x[cq * 32u + lane] : T(0);  // inactive slots issue no memory requests
+    }
     for (int c0 = p0; c0 < p1; c0 += EG_ROWS) {
         const int nr = min(p1 - c0, EG_ROWS);
         // stage the chunk's sorted weights, row ids and flags (coalesced, independent loads)
@@ -544,11 +547,12 @@ __device__ __forceinline__ void e_group_split(const OpView<T> &op, int64_t g, in
 // broadcasts them.
 template <class T>
 __device__ __forceinline__ T l_row_warp(const OpView<T> &op, int64_t r, int lane, T m, T n, const T *__restrict__ x,
-                                        const T *__restrict__ t) {
+                                        const T *__restrict__ t, bool act = true) {
     const unsigned FULL = 0xffffffffu;
-    // flags, x and the neighbour columns are independent loads: issue them together
+    // flags, x and the neighbour columns are independent loads: issue them together;
+    // inactive slots issue no memory requests for x and t
     const uint8_t fl = op.flags[r];
-    const T xr = x[(uint32_t)r * 32u + lane];
+    const T xr = act ? x[(uint32_t)r * 32u + lane] : T(0);
     int col = -1;
     if (r < op.N && lane < 6) col = __ldg(op.nbr6 + 6 * r + lane);
     if (fl & F_IDENT) return xr;
@@ -557,7 +561,7 @@ __device__ __forceinline__ T l_row_warp(const OpView<T> &op, int64_t r, int lane
 #pragma unroll
         for (int d = 0; d < 6; ++d) {
             const int c = __shfl_sync(FULL, col, d);
-            if (c >= 0) off += t[(uint32_t)c * 32u + lane];
+            if (c >= 0 && act) off += t[(uint32_t)c * 32u + lane];
         }
         return m * xr + n * (op.Ldiag * xr + op.Loff * off);
     }
@@ -575,7 +579,7 @@ __device__ __forceinline__ T l_row_warp(const OpView<T> &op, int64_t r, int lane
         for (int e = 0; e < cnt; ++e) {
             const int ce = __shfl_sync(FULL, c, e);
             const T ve = __shfl_sync(FULL, v, e);
-            off += ve * t[(uint32_t)ce * 32u + lane];
+            if (act) off += ve * t[(uint32_t)ce * 32u + lane];
         }
     }
     return m * xr + n * (op.ldiag[q] * xr + off);
@@ -607,7 +611,10 @@ struct cpm_opset_s {
     std::vector<double> h_point;
     // IBC subsets (device tube indices, reference BFS order)
     std::vector<std::vector<int64_t>> tag_set, dof_set;
-    std::vector<std::vector<double>> dof_cp;
+    std::vector<std::vector<double>> dof_cp, dof_cpdiff;
+    // unoriented surface normals of the tube nodes (eigenvector 0 of the
+    // symmetrised closest-point Jacobian), kept when IBC frames needed them
+    cpm::DBuf<double> normals;
     std::vector<int64_t> col_start, dcol_start;
     int64_t identity_rows_start = 0;
 

@@ -41,8 +41,13 @@ struct Slot {
 
 struct SolveParams {
     double tol, delta;
-    int max_iters, max_refine, mixed, pad;
+    int max_iters, max_refine, mixed;
+    int precond;  // 0 identity, 1 diagonal, 2 damped Jacobi with `sweeps` sweeps
+    int sweeps, pad;
 };
+
+// damping of the Jacobi preconditioner (src/GeneralizedBiCGStabSystem.h:365)
+constexpr double JACOBI_OMEGA = 2.0 / 3.0;
 
 constexpr int BS = 256;
 constexpr unsigned FULL = 0xffffffffu;
@@ -57,9 +62,9 @@ __device__ __forceinline__ T E_ROW(const OpView<T> &op, int64_t r, int s, const 
 }
 template <class T, int K>
 __device__ __forceinline__ T L_ROW(const OpView<T> &op, int64_t r, int s, T m, T n, const T *__restrict__ x,
-                                   const T *__restrict__ t) {
+                                   const T *__restrict__ t, bool act = true) {
     if constexpr (K == 32)
-        return l_row_warp<T>(op, r, s, m, n, x, t);
+        return l_row_warp<T>(op, r, s, m, n, x, t, act);
     else
         return l_row_nbr<T, K>(op, r, s, m, n, x, t);
 }
@@ -270,9 +275,12 @@ __global__ void k_init(OpView<T> op, Slot *sl, SolveParams P, int from_phase, co
     }
 }
 
-// p = (p - w v) beta + r ; y = D^-1 p   (src/BiCGStab.h:74-78)
+// p = (p - w v) beta + r ; y = M^-1 p   (src/BiCGStab.h:74-78)
+// M^-1 here is the diagonal inverse (ys = 1, pden = m + n L_rr), the identity
+// (pden = null) or the first Jacobi sweep from zero, y = omega (p / pden)
+// (src/GeneralizedBiCGStabSystem.h:358-377 with result = 0 and A 0 = 0)
 template <class T, int K>
-__global__ void k_update_p(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, const T *__restrict__ r,
+__global__ void k_update_p(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, T ys, const T *__restrict__ r,
                            const T *__restrict__ v, T *__restrict__ p, T *__restrict__ y) {
     int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int64_t row = gid / K;
@@ -284,7 +292,7 @@ __global__ void k_update_p(int64_t D, const Slot *__restrict__ sl, const T *__re
     pi *= beta;
     pi = pi + r[i];
     p[i] = pi;
-    y[i] = pi / pden[row];
+    y[i] = pden ? ys * (pi / pden[row]) : pi;
 }
 
 // v = A y with r0 . v  ->  alpha = rho / (r0 . v)   (src/BiCGStab.h:79-80)
@@ -296,7 +304,7 @@ __global__ void k_apply_alpha(OpView<T> op, Slot *sl, T m, T n, const T *__restr
     double acc[1] = {0.0};
     if (run_rows<K>(act))
         for (int64_t row = r0i; row < op.D; row += rstride) {
-            T vv = L_ROW<T, K>(op, row, s, m, n, y, te);
+            T vv = L_ROW<T, K>(op, row, s, m, n, y, te, act);
             if (act) {
                 v[row * K + s] = vv;
                 acc[0] += (double)r0[row * K + s] * (double)vv;
@@ -310,9 +318,9 @@ __global__ void k_apply_alpha(OpView<T> op, Slot *sl, T m, T n, const T *__restr
     }
 }
 
-// s = r - alpha v ; z = D^-1 s   (src/BiCGStab.h:82-84)
+// s = r - alpha v ; z = M^-1 s   (src/BiCGStab.h:82-84), M^-1 as in k_update_p
 template <class T, int K>
-__global__ void k_update_s(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, const T *__restrict__ r,
+__global__ void k_update_s(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, T ys, const T *__restrict__ r,
                            const T *__restrict__ v, T *__restrict__ sv, T *__restrict__ z) {
     int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int64_t row = gid / K;
@@ -322,7 +330,25 @@ __global__ void k_update_s(int64_t D, const Slot *__restrict__ sl, const T *__re
     int64_t i = row * K + s;
     T si = -a * v[i] + r[i];
     sv[i] = si;
-    z[i] = si / pden[row];
+    z[i] = pden ? ys * (si / pden[row]) : si;
+}
+
+// one further damped Jacobi sweep on A y = c, after the E pass te = E~ y:
+// y += omega ((c - A y) / pden)   (src/GeneralizedBiCGStabSystem.h:366-376).
+// Row r of A y reads y only at row r, so the update is in place.
+template <class T, int K>
+__global__ void k_jacobi_sweep(OpView<T> op, const Slot *__restrict__ sl, T m, T n, const T *__restrict__ c,
+                               const T *__restrict__ te, const T *__restrict__ pden, T omega, T *y) {
+    GRID_LOOP
+    const bool act = sl[s].phase == PH_ITER;
+    if (run_rows<K>(act))
+        for (int64_t row = r0i; row < op.D; row += rstride) {
+            const T ay = L_ROW<T, K>(op, row, s, m, n, y, te, act);
+            if (act) {
+                const int64_t i = row * K + s;
+                y[i] = y[i] + omega * ((c[i] - ay) / pden[row]);
+            }
+        }
 }
 
 // t = A z with t.t and t.s  ->  omega   (src/BiCGStab.h:85-95)
@@ -334,7 +360,7 @@ __global__ void k_apply_omega(OpView<T> op, Slot *sl, T m, T n, const T *__restr
     double acc[2] = {0.0, 0.0};
     if (run_rows<K>(act))
         for (int64_t row = r0i; row < op.D; row += rstride) {
-            T tt = L_ROW<T, K>(op, row, s, m, n, z, te);
+            T tt = L_ROW<T, K>(op, row, s, m, n, z, te, act);
             if (act) {
                 tv[row * K + s] = tt;
                 acc[0] += (double)tt * (double)tt;
@@ -424,7 +450,7 @@ __global__ void k_restart(OpView<T> op, Slot *sl, T m, T n, const double *__rest
     double acc[1] = {0.0};
     if (run_rows<K>(act))
         for (int64_t row = r0i; row < op.D; row += rstride) {
-            T ax = L_ROW<T, K>(op, row, s, m, n, x, te);
+            T ax = L_ROW<T, K>(op, row, s, m, n, x, te, act);
             if (act) {
                 T ri = (T)b[row * K + s] - ax;
                 r[row * K + s] = ri;
@@ -464,7 +490,7 @@ __global__ void k_refine_residual(OpView<double> op, Slot *sl, SolveParams P, do
     double acc[1] = {0.0};
     if (run_rows<K>(act))
         for (int64_t row = r0i; row < op.D; row += rstride) {
-            double ax = L_ROW<double, K>(op, row, s, m, n, x64, te);
+            double ax = L_ROW<double, K>(op, row, s, m, n, x64, te, act);
             if (act) {
                 double ri = b[row * K + s] - ax;
                 r64[row * K + s] = ri;
@@ -636,17 +662,33 @@ namespace cpm {
 
 static inline unsigned nblk(int64_t n) { return (unsigned)((n + BS - 1) / BS); }
 
+// Jacobi sweeps 2..n of the preconditioner on A y = c (sweep 1 is fused into
+// k_update_p / k_update_s)
+template <int K>
+static void jacobi_rest(cpm_solver_s *s, const SolveParams &P, const double *c, double *y) {
+    auto op = s->op->view<double>();
+    cudaStream_t st = stream();
+    for (int j = 1; j < P.sweeps; ++j) {
+        launch_epass<double, K>(op, s->slots.p, PH_ITER, y, s->te64.p, st);
+        k_jacobi_sweep<double, K><<<s->G, BS, 0, st>>>(op, s->slots.p, s->m, s->n, c, s->te64.p, s->pden64.p, JACOBI_OMEGA, y);
+    }
+}
+
 template <int K>
 static void plain_iteration(cpm_solver_s *s, const SolveParams &P) {
     auto op = s->op->view<double>();
     const int64_t D = s->D;
     cudaStream_t st = stream();
     Slot *sl = s->slots.p;
-    k_update_p<double, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden64.p, s->dr.p, s->dv.p, s->dp.p, s->dy.p);
+    const double *pden = P.precond == 0 ? nullptr : s->pden64.p;
+    const double ys = P.precond == 2 ? JACOBI_OMEGA : 1.0;
+    k_update_p<double, K><<<nblk(D * K), BS, 0, st>>>(D, sl, pden, ys, s->dr.p, s->dv.p, s->dp.p, s->dy.p);
+    if (P.precond == 2) jacobi_rest<K>(s, P, s->dp.p, s->dy.p);
     launch_epass<double, K>(op, sl, PH_ITER, s->dy.p, s->te64.p, st);
     k_apply_alpha<double, K><<<s->G, BS, 0, st>>>(op, sl, s->m, s->n, s->dy.p, s->te64.p, s->dr0.p, s->dv.p, s->partial.p,
                                                   s->counter.p);
-    k_update_s<double, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden64.p, s->dr.p, s->dv.p, s->ds.p, s->dz.p);
+    k_update_s<double, K><<<nblk(D * K), BS, 0, st>>>(D, sl, pden, ys, s->dr.p, s->dv.p, s->ds.p, s->dz.p);
+    if (P.precond == 2) jacobi_rest<K>(s, P, s->ds.p, s->dz.p);
     launch_epass<double, K>(op, sl, PH_ITER, s->dz.p, s->te64.p, st);
     k_apply_omega<double, K><<<s->G, BS, 0, st>>>(op, sl, s->m, s->n, s->dz.p, s->te64.p, s->ds.p, s->dt.p, s->partial.p,
                                                   s->counter.p);
@@ -670,10 +712,11 @@ static void mixed_iteration(cpm_solver_s *s, const SolveParams &P) {
     cudaStream_t st = stream();
     Slot *sl = s->slots.p;
     const float m = (float)s->m, n = (float)s->n;
-    k_update_p<float, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden32.p, s->fr.p, s->fv.p, s->fp.p, s->fy.p);
+    const float *pden = P.precond == 0 ? nullptr : s->pden32.p;
+    k_update_p<float, K><<<nblk(D * K), BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fp.p, s->fy.p);
     launch_epass<float, K>(op, sl, PH_ITER, s->fy.p, s->fte.p, st);
     k_apply_alpha<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p, s->counter.p);
-    k_update_s<float, K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->pden32.p, s->fr.p, s->fv.p, s->fs.p, s->fz.p);
+    k_update_s<float, K><<<nblk(D * K), BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fs.p, s->fz.p);
     launch_epass<float, K>(op, sl, PH_ITER, s->fz.p, s->fte.p, st);
     k_apply_omega<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p, s->counter.p);
     k_update_xr<float, K><<<s->G, BS, 0, st>>>(D, sl, P, s->fy.p, s->fz.p, s->fs.p, s->ft.p, s->fr0.p, s->fx.p, s->fr.p,
@@ -712,7 +755,7 @@ static int alloc_vectors(cpm_solver_s *s, bool want64, bool want32) {
 
 static bool same_params(const SolveParams &a, const SolveParams &b) {
     return a.tol == b.tol && a.delta == b.delta && a.max_iters == b.max_iters && a.max_refine == b.max_refine &&
-           a.mixed == b.mixed;
+           a.mixed == b.mixed && a.precond == b.precond && a.sweeps == b.sweeps;
 }
 
 // mixed graphs interleave a reliable-update step every 2 iterations
@@ -727,7 +770,16 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
     P.mixed = o->precision == 1;
     P.delta = o->inner_tol > 0 ? o->inner_tol : 0.2;
     P.max_refine = o->max_refine > 0 ? o->max_refine : 400;
-    if (o->precond != 1) return fail(CPM_ERR_UNSUPPORTED, "the device solver implements the diagonal preconditioner");
+    P.precond = o->precond;
+    P.sweeps = o->precond_iters;
+    if (P.precond < 0 || P.precond > 2) return fail(CPM_ERR_INVALID_ARG, "precond must be 0 (identity), 1 (diagonal) or 2 (jacobi)");
+    if (P.precond == 2 && (P.sweeps < 1 || P.sweeps > 20000))
+        return fail(CPM_ERR_INVALID_ARG, "the jacobi preconditioner needs 1 <= precond_iters <= 20000");
+    // FP32 cannot hold the far-field values that many Jacobi sweeps resolve (a
+    // heat kernel decays below 1e-38 within a few hundred cells), so the Jacobi
+    // preconditioner is an FP64 solve
+    if (P.precond == 2 && P.mixed)
+        return fail(CPM_ERR_UNSUPPORTED, "the jacobi preconditioner runs in FP64 (precision 0) only");
     CPM_TRY(alloc_vectors(s, !P.mixed, P.mixed));
     cudaStream_t st = stream();
     for (int j = 0; j < K; ++j) {
@@ -754,7 +806,8 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
     if (!gexec) {
         cudaGraph_t graph;
         CPM_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        for (int it = 0; it < s->chunk; ++it) {
+        const int chunk = (P.precond == 2) ? 1 : s->chunk;
+        for (int it = 0; it < chunk; ++it) {
             if (P.mixed) {
                 mixed_iteration<K>(s, P);
                 if (it % REFINE_EVERY == REFINE_EVERY - 1) mixed_refine<K>(s, P);
@@ -769,8 +822,10 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
         if (ce != cudaSuccess) return fail(CPM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
         gpar = P;
     }
-    const int64_t max_chunks = (int64_t)P.max_iters / s->chunk + 2 * P.max_refine + 4;
-    const long long per_graph = 7LL * s->chunk + (P.mixed ? 4LL * (s->chunk / REFINE_EVERY) : 0);
+    const int chunk = (P.precond == 2) ? 1 : s->chunk;
+    const int64_t max_chunks = (int64_t)P.max_iters / chunk + 2 * P.max_refine + 4;
+    const long long per_graph = (7LL + (P.precond == 2 ? 4LL * (P.sweeps - 1) : 0)) * chunk +
+                                (P.mixed ? 4LL * (chunk / REFINE_EVERY) : 0);
     count_launches(P.mixed ? 2 : 1);
     bool done = false;
     for (int64_t c = 0; c < max_chunks && !done; ++c) {

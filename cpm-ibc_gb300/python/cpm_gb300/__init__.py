@@ -259,6 +259,36 @@ class OpSet:
         _check(lib().cpm_apply_device(self.h, m, n, kslots, int(fp32), x_ptr, t_ptr, y_ptr))
 
 
+class Geodesic:
+    """GeodesicDistance::ComputeDistance (problems/GeodesicDistance.cpp:11-69) from a point source."""
+
+    def __init__(self, tube, source):
+        L = lib()
+        L.cpm_geodesic_create.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
+                                          ctypes.POINTER(ctypes.c_int64)]
+        L.cpm_geodesic_run.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_double,
+                                       ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+        L.cpm_geodesic_destroy.argtypes = [ctypes.c_void_p]
+        self.tube = tube
+        src = np.ascontiguousarray(source, np.float64)
+        h, D = ctypes.c_void_p(), ctypes.c_int64()
+        _check(L.cpm_geodesic_create(tube.h, _p(src), ctypes.byref(h), ctypes.byref(D)))
+        self.h, self.D = h, D.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().cpm_geodesic_destroy(self.h)
+        except Exception:
+            pass
+
+    def run(self, dt, precision=0, tol=1e-10, heat_sweeps=2000):
+        phi = np.zeros(self.D)
+        its = np.zeros(4, np.int32)
+        _check(lib().cpm_geodesic_run(self.h, dt, precision, tol, heat_sweeps, _p(phi), _p(its)))
+        return phi, its.tolist()
+
+
 def set_device(dev):
     lib().cpm_set_device.argtypes = [ctypes.c_int32]
     _check(lib().cpm_set_device(int(dev)))
@@ -275,6 +305,10 @@ def launch_count():
 
 def sync():
     _check(lib().cpm_sync())
+
+
+# preconditioners (src/Defines.h:13-18)
+IDENTITY, DIAGONAL, JACOBI = 0, 1, 2
 
 
 class Solver:
@@ -294,11 +328,12 @@ class Solver:
         except Exception:
             pass
 
-    def solve(self, b, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.2, max_refine=400, raise_on_error=True):
+    def solve(self, b, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.2, max_refine=400, raise_on_error=True,
+              precond=DIAGONAL, precond_iters=0):
         b = np.ascontiguousarray(np.atleast_2d(b), np.float64)
         k = b.shape[0]
         x = np.zeros_like(b)
-        o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=1, precond_iters=0,
+        o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=precond, precond_iters=precond_iters,
                       inner_tol=inner_tol, max_refine=max_refine)
         st = (SolveStats * k)()
         rc = lib().cpm_solve(self.h, k, _p(b), _p(x), ctypes.byref(o), st)
@@ -308,8 +343,9 @@ class Solver:
             raise CpmError(rc, lib().cpm_last_error().decode() + f" stats={stats}")
         return x, stats
 
-    def solve_device(self, b_ptr, x_ptr, k, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.2, max_refine=400):
-        o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=1, precond_iters=0,
+    def solve_device(self, b_ptr, x_ptr, k, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.2, max_refine=400,
+                     precond=DIAGONAL, precond_iters=0):
+        o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=precond, precond_iters=precond_iters,
                       inner_tol=inner_tol, max_refine=max_refine)
         st = (SolveStats * k)()
         rc = lib().cpm_solve_device(self.h, k, b_ptr, x_ptr, ctypes.byref(o), st)

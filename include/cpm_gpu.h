@@ -217,6 +217,24 @@ int cpm_solve_device(cpm_solver_t s, int32_t k, const void *b_dev, void *x_dev, 
 
 int cpm_solver_destroy(cpm_solver_t s);
 
+/* ---- Heat-method geodesic distance -----------------------------------------
+ * GeodesicDistance::ComputeDistance(Tube&, IBCSubsets&, dt)
+ * (problems/GeodesicDistance.cpp:11-69) from a point source (a Point IBC,
+ * order 1, on_ibc_tolerance 0.1 dx^2): heat solve (m = 1, n = -dt), normalised
+ * normal-projected gradient, divergence, Poisson solve (m = 0, n = 1),
+ * phi -= min phi, repeated twice more on E phi.  create builds the IBC system
+ * (D rows, returned in D_out).  run solves the heat step in FP64 with
+ * `heat_sweeps` damped Jacobi sweeps per preconditioner call (<= 0: 2000, as
+ * problems/GeodesicDistance.cpp:117-119), and the three Poisson steps with
+ * `precision` 0 (plain FP64) or 1 (FP32 + FP64 reliable updates), all to
+ * relative residual `tol`; it writes phi on the D rows (tube rows in device
+ * order) and the 4 iteration counts. */
+typedef struct cpm_geodesic_s *cpm_geodesic_t;
+int cpm_geodesic_create(cpm_tube_t t, const double *source, cpm_geodesic_t *out, int64_t *D_out);
+int cpm_geodesic_run(cpm_geodesic_t g, double dt, int32_t precision, double tol, int32_t heat_sweeps, double *phi_out,
+                     int32_t *iters_out);
+int cpm_geodesic_destroy(cpm_geodesic_t g);
+
 /* Synchronise the library stream. */
 int cpm_sync(void);
 

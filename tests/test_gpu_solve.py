@@ -82,6 +82,31 @@ def test_plain_fp64_ibc_solve_matches_oracle(gpu, oracle):
     assert _rel_inf(x_gpu[0][gr], x_ref) <= 1e-9
 
 
+@pytest.mark.parametrize("kslots", [1, 32])
+@pytest.mark.parametrize("precond,sweeps", [(0, 0), (2, 1), (2, 25)])
+def test_preconditioners_match_oracle(gpu, oracle, precond, sweeps, kslots):
+    """Identity and damped-Jacobi preconditioning (src/GeneralizedBiCGStabSystem.h:350-385)
+    on the backward-Euler heat operator with the C2 IBCs at dx = 0.1."""
+    dx = 0.1
+    P, T, O, gr = _pair(gpu, oracle, dx, ibc=True)
+    rows = P.rows()
+    b = S.build_rhs(rows, lambda x: x[:, 0], lambda c, x: np.full(len(x), 0.25 + 0.5 * c))
+    dt = dx * dx
+    x_ref, st_ref = P.solve(1.0, -dt, b, precond=precond, precond_iters=sweeps)
+    bg = np.empty(O.D)
+    bg[gr] = b
+    x_gpu, st = gpu.Solver(O, 1.0, -dt, kslots=kslots).solve(bg, precond=precond, precond_iters=sweeps)
+    assert st[0]["status"] == 0
+    assert abs(st[0]["iterations"] - st_ref["iterations"]) <= 1
+    assert _rel_inf(x_gpu[0][gr], x_ref) <= 1e-9
+
+
+def test_jacobi_rejects_fp32(gpu, oracle):
+    P, T, O, gr = _pair(gpu, oracle, 0.1)
+    with pytest.raises(gpu.CpmError):
+        gpu.Solver(O, 1.0, -0.01).solve(np.ones(O.D), precision=1, precond=2, precond_iters=10)
+
+
 def test_mixed_precision_matches_fp64_oracle(gpu, oracle):
     dx = 0.05
     P, T, O, gr = _pair(gpu, oracle, dx, ibc=True)
