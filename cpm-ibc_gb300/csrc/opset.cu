@@ -869,6 +869,20 @@ __global__ void k_build_nbr6(OpView<double> op, int32_t *__restrict__ nbr6) {
     }
 }
 
+// rows >= N: the IBC DOF rows' L columns (AddFiniteDifferenceIBCRows keeps at
+// most the six neighbours, each with weight 1/dx^2 and the diagonal -6/dx^2),
+// so every row's L has the tube-row form; identity rows get none.  err = 1 if a
+// row has more than six off-diagonal entries.
+__global__ void k_build_nbr6_ibc(OpView<double> op, int32_t *__restrict__ nbr6, int *__restrict__ err) {
+    int64_t r = op.N + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= op.D) return;
+    const int64_t q = r - op.N;
+    const int e0 = op.lptr[q], e1 = op.lptr[q + 1];
+    const bool ident = op.flags[r] & F_IDENT;
+    if (!ident && e1 - e0 > 6) atomicOr(err, 1);
+    for (int d = 0; d < 6; ++d) nbr6[6 * r + d] = (!ident && e0 + d < e1) ? op.lcol[e0 + d] : -1;
+}
+
 // 64 bulk stencil columns of each base group (s = 16 i + 4 j + k)
 __global__ void k_group_cols(OpView<double> op, int64_t n_grp, int32_t *__restrict__ gcols) {
     int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -895,9 +909,19 @@ __global__ void k_sorted_rows(OpView<double> op, int64_t n_ord, double *__restri
 // identity rows.  Rows sharing a base point read the same 64 values of x.
 static int build_schedule(cpm_opset_s *o) {
     const int64_t N = o->N, D = o->D;
-    CPM_TRY(o->nbr6.alloc(6 * N));
+    CPM_TRY(o->nbr6.alloc(6 * D));
     k_build_nbr6<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(o->view<double>(), o->nbr6.p);
     CPM_CUDA_TRY(cudaGetLastError());
+    if (D > N) {
+        DBuf<int> err;
+        CPM_TRY(err.alloc(1));
+        CPM_TRY(err.zero());
+        k_build_nbr6_ibc<<<(unsigned)((D - N + 255) / 256), 256, 0, stream()>>>(o->view<double>(), o->nbr6.p, err.p);
+        CPM_CUDA_TRY(cudaGetLastError());
+        std::vector<int> he;
+        CPM_TRY(err.download(he, 1));
+        if (he[0]) return fail(CPM_ERR_CUDA, "internal: an IBC L row has more than six off-diagonal entries");
+    }
     std::vector<uint8_t> flags;
     std::vector<uint32_t> base;
     CPM_TRY(o->flags.download(flags, D));

@@ -37,7 +37,8 @@ struct OpView {
     const T *ldiag;         // rows >= N: L diagonal
     T Ldiag, Loff;          // tube rows: -6/dx^2 and 1/dx^2
     // apply schedule
-    const int32_t *nbr6;    // tube rows: the six L columns (moves applied, -1 absent)
+    const int32_t *nbr6;    // D x 6: each row's L columns (moves applied, -1 absent); all rows'
+                            // L rows are Ldiag on the diagonal and Loff off it
     const int32_t *ord;     // non-identity rows sorted by base point (stable in row order)
     const int32_t *grp;     // base groups: ord[grp[g] .. grp[g+1]) share one base point
     const int32_t *gcols;   // 64 bulk stencil columns per group, s = 16 i + 4 j + k
@@ -150,72 +151,6 @@ __device__ __forceinline__ T e_row_thread(const OpView<T> &op, int64_t r, int s,
     return acc;
 }
 
-// Warp-per-row gather for a 32-slot batch: lanes 0..7 resolve one corner brick
-// each, every lane resolves the columns of stencil points lane and lane+32 and
-// the warp broadcasts them with shuffles; each gather then reads one 128-byte
-// row of the batch (all 32 right-hand sides of one node) — fully coalesced.
-template <class T>
-__device__ __forceinline__ T e_row_warp(const OpView<T> &op, int64_t r, int lane, const T *__restrict__ x) {
-    const unsigned FULL = 0xffffffffu;
-    const uint8_t fl = op.flags[r];
-    if (fl & F_IDENT) return x[r * 32 + lane];
-    const uint32_t b = op.base[r];
-    const int bi = unpack_i(b), bj = unpack_j(b), bk = unpack_k(b);
-    const int X0 = bi >> 2, Y0 = bj >> 2, Z0 = bk >> 2;
-    Corner mine{0, 0ull};
-    if (lane < 8) mine = load_corner(op.bv, X0 + (lane & 1), Y0 + ((lane >> 1) & 1), Z0 + (lane >> 2));
-    uint64_t emask = 0;
-    int eoff = 0, pi = -1;
-    if (fl & (F_EMOVE | F_EXTRA)) {
-        pi = op.patch[r];
-        emask = op.p_emask[pi];
-        eoff = op.p_eoff[pi];
-    }
-    int col2[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int sidx = lane + 32 * h;
-        const int gi = bi + (sidx >> 4), gj = bj + ((sidx >> 2) & 3), gk = bk + (sidx & 3);
-        const int cc = ((gi >> 2) - X0) | (((gj >> 2) - Y0) << 1) | (((gk >> 2) - Z0) << 2);
-        Corner c;
-        c.start = __shfl_sync(FULL, mine.start, cc);
-        c.mask = ((uint64_t)__shfl_sync(FULL, (unsigned)(mine.mask >> 32), cc) << 32) |
-                 (uint64_t)__shfl_sync(FULL, (unsigned)mine.mask, cc);
-        int col = corner_node(c, ((gi & 3) << 4) | ((gj & 3) << 2) | (gk & 3));
-        if ((emask >> sidx) & 1ull) col = op.moved[eoff + __popcll(emask & ((1ull << sidx) - 1ull))];
-        col2[h] = col;
-    }
-    const T *w = op.w + 12 * r;
-    T wx[4], wy[4], wz[4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        wx[a] = w[a];
-        wy[a] = w[4 + a];
-        wz[a] = w[8 + a];
-    }
-    T acc = 0;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        T ay = 0;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            T az = 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int sidx = 16 * i + 4 * j + k;
-                const int col = __shfl_sync(FULL, col2[sidx >> 5], sidx & 31);
-                T xv = (col >= 0) ? x[(int64_t)col * 32 + lane] : T(0);
-                az += wz[k] * xv;
-            }
-            ay += wy[j] * az;
-        }
-        acc += wx[i] * ay;
-    }
-    if (fl & F_ENEG) acc = -acc;
-    if (fl & F_EXTRA) acc += op.p_xval[pi] * x[(int64_t)op.p_xcol[pi] * 32 + lane];
-    return acc;
-}
-
 // (E~ x)_r for slot s of a K-wide row-major batch (reference per-point walk;
 // kept for odd widths such as the 9-wide Jacobian extension).
 template <class T, int K>
@@ -266,68 +201,6 @@ __device__ __forceinline__ T e_row(const OpView<T> &op, int64_t r, int s, const 
     return acc;
 }
 
-// y_r = m x_r + n (L_rr x_r + sum_{c != r} L_rc t_c), identity rows y = x
-// (GeneralizedBiCGStabSystem::Multiply, src/GeneralizedBiCGStabSystem.h:191-233).
-template <class T, int K>
-__device__ __forceinline__ T l_row(const OpView<T> &op, int64_t r, int s, T m, T n, const T *__restrict__ x,
-                                   const T *__restrict__ t) {
-    const uint8_t fl = op.flags[r];
-    const T xr = x[r * K + s];
-    if (fl & F_IDENT) return xr;
-    if (r < op.N) {
-        const uint32_t kk = op.key[r];
-        const int i = unpack_i(kk), j = unpack_j(kk), k = unpack_k(kk);
-        uint8_t lmask = 0;
-        int loff = 0;
-        if (fl & F_LMOVE) {
-            int pi = op.patch[r];
-            lmask = op.p_lmask[pi];
-            loff = op.p_loff[pi];
-        }
-        T off = 0;
-#pragma unroll
-        for (int d = 0; d < 6; ++d) {
-            int col;
-            if ((lmask >> d) & 1)
-                col = op.moved[loff + __popc((unsigned)lmask & ((1u << d) - 1u))];
-            else {
-                const int di = (d == 0) - (d == 1), dj = (d == 2) - (d == 3), dk = (d == 4) - (d == 5);
-                col = node_at(op.bv, i + di, j + dj, k + dk);
-            }
-            if (col >= 0) off += t[(int64_t)col * K + s];
-        }
-        return m * xr + n * (op.Ldiag * xr + op.Loff * off);
-    }
-    const int64_t q = r - op.N;
-    T off = 0;
-    for (int e = op.lptr[q]; e < op.lptr[q + 1]; ++e) off += op.lval[e] * t[(int64_t)op.lcol[e] * K + s];
-    return m * xr + n * (op.ldiag[q] * xr + off);
-}
-
-// L row from the precomputed neighbour table (thread per row and slot).
-template <class T, int K>
-__device__ __forceinline__ T l_row_nbr(const OpView<T> &op, int64_t r, int s, T m, T n, const T *__restrict__ x,
-                                       const T *__restrict__ t) {
-    const uint8_t fl = op.flags[r];
-    const T xr = x[r * K + s];
-    if (fl & F_IDENT) return xr;
-    if (r < op.N) {
-        const int2 a = __ldg((const int2 *)(op.nbr6 + 6 * r));
-        const int2 b = __ldg((const int2 *)(op.nbr6 + 6 * r + 2));
-        const int2 c = __ldg((const int2 *)(op.nbr6 + 6 * r + 4));
-        const int cols[6] = {a.x, a.y, b.x, b.y, c.x, c.y};
-        T off = 0;
-#pragma unroll
-        for (int d = 0; d < 6; ++d)
-            if (cols[d] >= 0) off += t[(int64_t)cols[d] * K + s];
-        return m * xr + n * (op.Ldiag * xr + op.Loff * off);
-    }
-    const int64_t q = r - op.N;
-    T off = 0;
-    for (int e = op.lptr[q]; e < op.lptr[q + 1]; ++e) off += op.lval[e] * t[(int64_t)op.lcol[e] * K + s];
-    return m * xr + n * (op.ldiag[q] * xr + off);
-}
-
 // the 12 tricubic weights of a row (48 or 96 bytes, 16-byte aligned) as vectors
 __device__ __forceinline__ void load_w12(const float *w, float (&o)[12]) {
     const float4 *v = (const float4 *)w;
@@ -347,103 +220,6 @@ __device__ __forceinline__ void load_w12(const double *w, double (&o)[12]) {
         double2 a = __ldg(v + q);
         o[2 * q] = a.x;
         o[2 * q + 1] = a.y;
-    }
-}
-
-// IBC patch of one row in the 32-slot group kernel: moved stencil points add
-// w_s (x[moved] - x[orig]); 2nd-order Dirichlet rows are negated and add 2 g.
-template <class T>
-__device__ __forceinline__ T e_patch_warp(const OpView<T> &op, int r, uint8_t fl, const T (&w)[12], const int (&col2)[2],
-                                          int lane, const T *__restrict__ x, T acc) {
-    const unsigned FULL = 0xffffffffu;
-    if (fl & (F_EMOVE | F_EXTRA)) {
-        const int pi = op.patch[r];
-        uint64_t em = op.p_emask[pi];
-        int mo = op.p_eoff[pi];
-        const T wx[4] = {w[0], w[1], w[2], w[3]}, wy[4] = {w[4], w[5], w[6], w[7]}, wz[4] = {w[8], w[9], w[10], w[11]};
-        while (em) {  // warp-uniform: one row per warp
-            const int s = __ffsll((long long)em) - 1;
-            em &= em - 1;
-            const int orig = __shfl_sync(FULL, (s < 32) ? col2[0] : col2[1], s & 31);
-            const int nc = op.moved[mo++];
-            const T ws = pick4(wx, s >> 4) * pick4(wy, (s >> 2) & 3) * pick4(wz, s & 3);
-            acc += ws * (x[(uint32_t)nc * 32u + lane] - x[(uint32_t)orig * 32u + lane]);
-        }
-        if (fl & F_ENEG) acc = -acc;
-        if (fl & F_EXTRA) acc += op.p_xval[pi] * x[(uint32_t)op.p_xcol[pi] * 32u + lane];
-    } else if (fl & F_ENEG) {
-        acc = -acc;
-    }
-    return acc;
-}
-
-// Warp-per-group E pass for a 32-slot batch.  Rows sharing a base point read
-// the same 64 nodes: the warp gathers that 64 x 32 block once into registers
-// (lane = slot; lanes 0..7 resolve the corner bricks, every lane two stencil
-// columns, broadcast by shuffles) and evaluates every row of the group from
-// registers with its own weights.  A row whose stencil has columns moved to
-// IBC DOF columns adds w_s (x[moved] - x[orig]) per moved point.
-template <class T>
-__device__ __forceinline__ void e_group_warp(const OpView<T> &op, int64_t g, int lane, bool act, const T *__restrict__ x,
-                                             T *__restrict__ t) {
-    const unsigned FULL = 0xffffffffu;
-    const int p0 = op.grp[g], p1 = op.grp[g + 1];
-    const uint32_t b = op.base[op.ord[p0]];
-    const int bi = unpack_i(b), bj = unpack_j(b), bk = unpack_k(b);
-    const int X0 = bi >> 2, Y0 = bj >> 2, Z0 = bk >> 2;
-    Corner mine{0, 0ull};
-    if (lane < 8) mine = load_corner(op.bv, X0 + (lane & 1), Y0 + ((lane >> 1) & 1), Z0 + (lane >> 2));
-    int col2[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int sidx = lane + 32 * h;
-        const int gi = bi + (sidx >> 4), gj = bj + ((sidx >> 2) & 3), gk = bk + (sidx & 3);
-        const int cc = ((gi >> 2) - X0) | (((gj >> 2) - Y0) << 1) | (((gk >> 2) - Z0) << 2);
-        Corner c;
-        c.start = __shfl_sync(FULL, mine.start, cc);
-        c.mask = ((uint64_t)__shfl_sync(FULL, (unsigned)(mine.mask >> 32), cc) << 32) |
-                 (uint64_t)__shfl_sync(FULL, (unsigned)mine.mask, cc);
-        const int l = ((gi & 3) << 4) | ((gj & 3) << 2) | (gk & 3);
-        // a missing node reads row 0 (tubes with missing stencil nodes are rejected at build time)
-        col2[h] = ((c.mask >> l) & 1ull) ? c.start + __popcll(c.mask & ((1ull << l) - 1ull)) : 0;
-    }
-    // row-major [D][32] batches are addressed with 32-bit element offsets (D < 2^26)
-    T xb[64];
-#pragma unroll
-    for (int s = 0; s < 64; ++s) xb[s] = x[(uint32_t)__shfl_sync(FULL, col2[s >> 5], s & 31) * 32u + lane];
-    // two rows of the group in flight per iteration (independent load and FMA chains)
-    for (int p = p0; p < p1; p += 2) {
-        const bool two = p + 1 < p1;
-        const int ra = op.ord[p];
-        const int rb = two ? op.ord[p + 1] : ra;
-        T wa[12], wb[12];
-        load_w12(op.w + 12 * (size_t)ra, wa);
-        load_w12(op.w + 12 * (size_t)rb, wb);
-        const uint8_t fla = op.flags[ra], flb = op.flags[rb];
-        T acc_a = 0, acc_b = 0;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            T ay_a = 0, ay_b = 0;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                T az_a = 0, az_b = 0;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    az_a += wa[8 + k] * xb[16 * i + 4 * j + k];
-                    az_b += wb[8 + k] * xb[16 * i + 4 * j + k];
-                }
-                ay_a += wa[4 + j] * az_a;
-                ay_b += wb[4 + j] * az_b;
-            }
-            acc_a += wa[i] * ay_a;
-            acc_b += wb[i] * ay_b;
-        }
-        acc_a = e_patch_warp(op, ra, fla, wa, col2, lane, x, acc_a);
-        if (act) t[(uint32_t)ra * 32u + lane] = acc_a;
-        if (two) {
-            acc_b = e_patch_warp(op, rb, flb, wb, col2, lane, x, acc_b);
-            if (act) t[(uint32_t)rb * 32u + lane] = acc_b;
-        }
     }
 }
 
@@ -542,47 +318,63 @@ __device__ __forceinline__ void e_group_split(const OpView<T> &op, int64_t g, in
     }
 }
 
-// Warp-per-row L row for a 32-slot batch: lanes 0..5 read the six neighbour
-// columns (or the CSR entries of an IBC DOF row, 32 at a time) and the warp
-// broadcasts them.
-template <class T>
-__device__ __forceinline__ T l_row_warp(const OpView<T> &op, int64_t r, int lane, T m, T n, const T *__restrict__ x,
-                                        const T *__restrict__ t, bool act = true) {
-    const unsigned FULL = 0xffffffffu;
-    // flags, x and the neighbour columns are independent loads: issue them together;
-    // inactive slots issue no memory requests for x and t
-    const uint8_t fl = op.flags[r];
-    const T xr = act ? x[(uint32_t)r * 32u + lane] : T(0);
-    int col = -1;
-    if (r < op.N && lane < 6) col = __ldg(op.nbr6 + 6 * r + lane);
-    if (fl & F_IDENT) return xr;
-    if (r < op.N) {
-        T off = 0;
+// y_r = m x_r + n (Ldiag x_r + Loff sum_d t_{c_d}), identity rows y = x
+// (GeneralizedBiCGStabSystem::Multiply, src/GeneralizedBiCGStabSystem.h:191-233)
+// for slot s of a K-wide row-major batch and U rows at once: the flags, x and
+// neighbour columns of all U rows are loaded first, then their 6 U gathers of
+// t, so U rows' memory requests are in flight together.  Rows >= D produce
+// nothing; an inactive slot (act false) reads nothing.
+template <class T, int K, int U>
+__device__ __forceinline__ void l_rows(const OpView<T> &op, const int64_t (&r)[U], int s, T m, T n, const T *__restrict__ x,
+                                       const T *__restrict__ t, bool act, T (&y)[U]) {
+    uint8_t fl[U];
+    T xr[U];
+    int c[U][6];
 #pragma unroll
-        for (int d = 0; d < 6; ++d) {
-            const int c = __shfl_sync(FULL, col, d);
-            if (c >= 0 && act) off += t[(uint32_t)c * 32u + lane];
+    for (int u = 0; u < U; ++u) {
+        const bool ok = r[u] < op.D;
+        fl[u] = ok ? __ldg(op.flags + r[u]) : (uint8_t)F_IDENT;
+        xr[u] = (ok && act) ? x[r[u] * K + s] : T(0);
+        int2 a = make_int2(-1, -1), b = a, e = a;
+        if (ok) {
+            a = __ldg((const int2 *)(op.nbr6 + 6 * r[u]));
+            b = __ldg((const int2 *)(op.nbr6 + 6 * r[u] + 2));
+            e = __ldg((const int2 *)(op.nbr6 + 6 * r[u] + 4));
         }
-        return m * xr + n * (op.Ldiag * xr + op.Loff * off);
+        c[u][0] = a.x;
+        c[u][1] = a.y;
+        c[u][2] = b.x;
+        c[u][3] = b.y;
+        c[u][4] = e.x;
+        c[u][5] = e.y;
     }
-    const int64_t q = r - op.N;
-    const int e0 = op.lptr[q], e1 = op.lptr[q + 1];
-    T off = 0;
-    for (int base = e0; base < e1; base += 32) {
-        int c = -1;
-        T v = 0;
-        if (base + lane < e1) {
-            c = op.lcol[base + lane];
-            v = op.lval[base + lane];
+    if constexpr (sizeof(T) == 8) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            T off = 0;
+#pragma unroll
+            for (int d = 0; d < 6; ++d)
+                if (c[u][d] >= 0 && act && !(fl[u] & F_IDENT)) off += t[(int64_t)c[u][d] * K + s];
+            y[u] = (fl[u] & F_IDENT) ? xr[u] : m * xr[u] + n * (op.Ldiag * xr[u] + op.Loff * off);
         }
-        const int cnt = min(32, e1 - base);
-        for (int e = 0; e < cnt; ++e) {
-            const int ce = __shfl_sync(FULL, c, e);
-            const T ve = __shfl_sync(FULL, v, e);
-            if (act) off += ve * t[(uint32_t)ce * 32u + lane];
+    } else {
+        // FP32: the same row as Loff (sum_d (t_d - x) + (k - 6) x) with k present
+        // neighbours (Ldiag = -6 Loff).  The differences of a smooth field are
+        // exact, so the O(1/dx^2) terms no longer cancel in FP32 arithmetic.
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            T off = 0;
+            int k = 0;
+#pragma unroll
+            for (int d = 0; d < 6; ++d)
+                if (c[u][d] >= 0 && act && !(fl[u] & F_IDENT)) {
+                    off += t[(int64_t)c[u][d] * K + s] - xr[u];
+                    ++k;
+                }
+            off += (T)(k - 6) * xr[u];
+            y[u] = (fl[u] & F_IDENT) ? xr[u] : m * xr[u] + n * (op.Loff * off);
         }
     }
-    return m * xr + n * (op.ldiag[q] * xr + off);
 }
 
 }  // namespace cpm

@@ -43,83 +43,143 @@ struct SolveParams {
     double tol, delta;
     int max_iters, max_refine, mixed;
     int precond;  // 0 identity, 1 diagonal, 2 damped Jacobi with `sweeps` sweeps
-    int sweeps, pad;
+    int sweeps, refine_every;
 };
 
 // damping of the Jacobi preconditioner (src/GeneralizedBiCGStabSystem.h:365)
 constexpr double JACOBI_OMEGA = 2.0 / 3.0;
 
 constexpr int BS = 256;
+constexpr int UNR = 4;       // rows in flight per thread in the row loops
+constexpr int RGROUP = 32;   // blocks per first-level group of the grid reduction
 constexpr unsigned FULL = 0xffffffffu;
 
-// row functions: warp-per-row for 32 slots, thread-per-row otherwise
-template <class T, int K>
-__device__ __forceinline__ T E_ROW(const OpView<T> &op, int64_t r, int s, const T *__restrict__ x) {
-    if constexpr (K == 32)
-        return e_row_warp<T>(op, r, s, x);
-    else
-        return e_row_thread<T, K>(op, r, s, x);
+// grid size of the row-loop kernels: UNR rows per thread per trip, at most
+// four 256-thread blocks per SM (the reduction tree is fixed by this size)
+static inline int sm_count() {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
 }
-template <class T, int K>
-__device__ __forceinline__ T L_ROW(const OpView<T> &op, int64_t r, int s, T m, T n, const T *__restrict__ x,
-                                   const T *__restrict__ t, bool act = true) {
-    if constexpr (K == 32)
-        return l_row_warp<T>(op, r, s, m, n, x, t, act);
-    else
-        return l_row_nbr<T, K>(op, r, s, m, n, x, t);
+static inline int row_grid(int64_t D, int K) {
+    const int sms = sm_count();
+    const int64_t rpb = BS / K;
+    const int64_t need = (D + rpb * UNR - 1) / (rpb * UNR);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(need, 4LL * sms));
 }
-// whether this thread's loop body runs: for 32 slots the whole warp runs if any slot is active
-template <int K>
-__device__ __forceinline__ bool run_rows(bool act) {
-    if constexpr (K == 32)
-        return __any_sync(FULL, act);
-    else
-        return act;
-}
+static inline int64_t reduce_groups(int G) { return (G + RGROUP - 1) / RGROUP; }
 
-// ---- fixed-order block + grid reduction with a last-block finaliser
+// ---- per-thread dot products.  FP64 vectors accumulate in FP64.  FP32 vectors
+// accumulate in a double-float pair on the FP32 pipes (FP64 units are scarce on
+// this GPU): each product a*b is split exactly into p + e by an FMA, p is added
+// to the running sum by TwoSum (Knuth), and the rounding errors and e collect
+// in the low word, about 48 significant bits in all.  Across threads the
+// sums are FP64.
+template <class T, int N>
+struct Dot;
+template <int N>
+struct Dot<double, N> {
+    double a[N];
+    __device__ __forceinline__ Dot() {
+#pragma unroll
+        for (int d = 0; d < N; ++d) a[d] = 0.0;
+    }
+    __device__ __forceinline__ void add(int d, double x, double y) { a[d] += x * y; }
+    __device__ __forceinline__ void get(double (&o)[N]) const {
+#pragma unroll
+        for (int d = 0; d < N; ++d) o[d] = a[d];
+    }
+};
+template <int N>
+struct Dot<float, N> {
+    float hi[N], lo[N];
+    __device__ __forceinline__ Dot() {
+#pragma unroll
+        for (int d = 0; d < N; ++d) hi[d] = lo[d] = 0.0f;
+    }
+    __device__ __forceinline__ void add(int d, float x, float y) {
+        const float p = __fmul_rn(x, y);
+        const float e = __fmaf_rn(x, y, -p);  // x*y = p + e exactly
+        const float s = __fadd_rn(hi[d], p);
+        const float bp = __fsub_rn(s, hi[d]);
+        const float err = __fadd_rn(__fsub_rn(hi[d], __fsub_rn(s, bp)), __fsub_rn(p, bp));  // hi + p = s + err
+        hi[d] = s;
+        lo[d] = __fadd_rn(lo[d], __fadd_rn(err, e));
+    }
+    __device__ __forceinline__ void get(double (&o)[N]) const {
+#pragma unroll
+        for (int d = 0; d < N; ++d) o[d] = (double)hi[d] + (double)lo[d];
+    }
+};
+
+// ---- fixed-order grid reduction of NDOT FP64 sums per slot.  Blocks reduce
+// their rows with a tree, groups of RGROUP blocks are summed in block order by
+// the group's last block, and the groups in group order by the last group: the
+// result depends only on the grid size, never on timing or on other slots.
+// partial holds (G + groups) * K * NDOT doubles, counter 1 + groups zeros.
 template <int K, int NDOT>
 __device__ __forceinline__ bool grid_reduce(double (&v)[NDOT], double *partial, unsigned int *counter, double (&out)[NDOT]) {
     __shared__ double sh[NDOT][BS];
     __shared__ bool last;
     const int tid = threadIdx.x;
     constexpr int RPB = BS / K;
+    const int slot = tid % K, chunk = tid / K;
+    auto tree = [&]() {
+        __syncthreads();
+        for (int h = RPB / 2; h > 0; h >>= 1) {
+            if (chunk < h)
+#pragma unroll
+                for (int d = 0; d < NDOT; ++d) sh[d][tid] += sh[d][tid + h * K];
+            __syncthreads();
+        }
+    };
 #pragma unroll
     for (int d = 0; d < NDOT; ++d) sh[d][tid] = v[d];
-    __syncthreads();
-    const int rib = tid / K;
-    for (int h = RPB / 2; h > 0; h >>= 1) {
-        if (rib < h)
-#pragma unroll
-            for (int d = 0; d < NDOT; ++d) sh[d][tid] += sh[d][tid + h * K];
-        __syncthreads();
-    }
+    tree();
+    const unsigned G = gridDim.x, grp = blockIdx.x / RGROUP, ngrp = (G + RGROUP - 1) / RGROUP;
+    double *gpart = partial + (size_t)G * K * NDOT;
     if (tid < K)
 #pragma unroll
         for (int d = 0; d < NDOT; ++d) partial[((size_t)blockIdx.x * K + tid) * NDOT + d] = sh[d][tid];
     __threadfence();
     __syncthreads();
-    if (tid == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    const unsigned b0 = grp * RGROUP, b1 = min(b0 + RGROUP, G);
+    if (tid == 0) last = (atomicAdd(counter + 1 + grp, 1u) == b1 - b0 - 1);
     __syncthreads();
     if (!last) return false;
     __threadfence();
-    // fixed order: chunk c sums blocks c, c+RPB, ... ; then a tree over chunks
-    const int slot = tid % K, chunk = tid / K;
     double acc[NDOT];
 #pragma unroll
     for (int d = 0; d < NDOT; ++d) acc[d] = 0.0;
-    for (unsigned b = chunk; b < gridDim.x; b += RPB)
 #pragma unroll
-        for (int d = 0; d < NDOT; ++d) acc[d] += ((volatile double *)partial)[((size_t)b * K + slot) * NDOT + d];
+    for (int q = 0; q < (RGROUP + RPB - 1) / RPB; ++q) {
+        const unsigned b = b0 + chunk + q * RPB;
+        if (b < b1)
+#pragma unroll
+            for (int d = 0; d < NDOT; ++d) acc[d] += __ldcg(partial + ((size_t)b * K + slot) * NDOT + d);
+    }
 #pragma unroll
     for (int d = 0; d < NDOT; ++d) sh[d][tid] = acc[d];
-    __syncthreads();
-    for (int h = RPB / 2; h > 0; h >>= 1) {
-        if (chunk < h)
+    tree();
+    if (tid < K)
 #pragma unroll
-            for (int d = 0; d < NDOT; ++d) sh[d][tid] += sh[d][tid + h * K];
-        __syncthreads();
-    }
+        for (int d = 0; d < NDOT; ++d) gpart[((size_t)grp * K + tid) * NDOT + d] = sh[d][tid];
+    if (tid == 0) counter[1 + grp] = 0u;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = (atomicAdd(counter, 1u) == ngrp - 1);
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+#pragma unroll
+    for (int d = 0; d < NDOT; ++d) acc[d] = 0.0;
+    for (unsigned g = chunk; g < ngrp; g += RPB)
+#pragma unroll
+        for (int d = 0; d < NDOT; ++d) acc[d] += __ldcg(gpart + ((size_t)g * K + slot) * NDOT + d);
+#pragma unroll
+    for (int d = 0; d < NDOT; ++d) sh[d][tid] = acc[d];
+    tree();
     if (tid < K)
 #pragma unroll
         for (int d = 0; d < NDOT; ++d) out[d] = sh[d][tid];
@@ -129,32 +189,8 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NDOT], double *partial, 
 
 // ================================================================= kernels
 
-// E pass for the slots in phase `ph` (ph < 0: every slot).
-// 32 slots: one warp per base group, then one warp per identity row.  The
-// group's 64 x 32 block lives in registers (~150 per thread), so blocks are
-// two warps wide: an SM then keeps ~6 independent blocks resident instead of
-// one 8-warp block that waits for its slowest group.
-constexpr int BS_E32 = 64;
-template <class T>
-__global__ void __launch_bounds__(BS_E32) k_epass32(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x,
-                                                    T *__restrict__ t) {
-    const int lane = threadIdx.x & 31;
-    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const bool act = (ph < 0) || sl[lane].phase == ph;
-    if (!__any_sync(FULL, act)) return;
-    if (w < op.n_grp) {
-        e_group_warp<T>(op, w, lane, act, x, t);
-        return;
-    }
-    const int64_t q = w - op.n_grp;
-    if (q < op.n_ident && act) {
-        const int64_t r = op.ident[q];
-        t[r * 32 + lane] = x[r * 32 + lane];
-    }
-}
-
 // 32 slots, plane-split: one 4-warp block per base group (grid-stride), then
-// identity rows copied warp per row.
+// identity rows copied warp per row.  ph < 0: every slot.
 template <class T>
 __global__ void __launch_bounds__(128) k_epass32s(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x,
                                                   T *__restrict__ t) {
@@ -192,7 +228,7 @@ template <class T, int K>
 static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x, T *t, cudaStream_t st) {
     static_assert(K == 1 || K == 32, "slot widths 1 and 32");
     if constexpr (K == 32) {
-        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(op.n_grp, 152LL * 16));
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(op.n_grp, 16LL * sm_count()));
         k_epass32s<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
     } else {
         const int64_t threads = op.n_ord + op.n_ident;
@@ -200,45 +236,70 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
     }
 }
 
-// plain L pass (apply API)
-template <class T, int K>
-__global__ void k_lpass(OpView<T> op, T m, T n, const T *__restrict__ x, const T *__restrict__ t, T *__restrict__ y) {
-    int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t r = gid / K;
-    int s = (int)(gid % K);
-    if (r >= op.D) return;
-    y[r * K + s] = L_ROW<T, K>(op, r, s, m, n, x, t);
-}
-
+// Row loops: thread (row group, slot s) with K slots per row; each trip
+// handles UNR rows rb + u * rstride, all of whose loads are issued first.
 #define GRID_LOOP                                                    \
     constexpr int RPB = BS / K;                                      \
     const int s = threadIdx.x % K;                                   \
     const int64_t r0i = (int64_t)blockIdx.x * RPB + threadIdx.x / K; \
     const int64_t rstride = (int64_t)gridDim.x * RPB;
+#define ROWS_UNR_N(Dn, UN) for (int64_t rb = r0i; rb < (Dn); rb += (int64_t)(UN) * rstride)
+#define ROWS_OF_TRIP_N(rr, UN)                                        \
+    int64_t rr[UN];                                                   \
+    _Pragma("unroll") for (int u = 0; u < (UN); ++u) rr[u] = rb + (int64_t)u * rstride;
+#define ROWS_UNR(Dn) ROWS_UNR_N(Dn, UNR)
+#define ROWS_OF_TRIP(rr) ROWS_OF_TRIP_N(rr, UNR)
+// FP64 streams of six vectors keep two rows in flight within 64 registers
+template <class T>
+constexpr int unr_stream6() { return sizeof(T) == 8 ? 2 : UNR; }
+
+// y = m x + n (Ldiag x + Loff E~-gathered neighbours): the L pass of one apply
+template <class T, int K>
+__global__ void __launch_bounds__(BS, 4) k_lpass(OpView<T> op, T m, T n, const T *__restrict__ x, const T *__restrict__ t,
+                                              T *__restrict__ y) {
+    GRID_LOOP
+    ROWS_UNR(op.D) {
+        ROWS_OF_TRIP(rr)
+        T v[UNR];
+        l_rows<T, K, UNR>(op, rr, s, m, n, x, t, true, v);
+#pragma unroll
+        for (int u = 0; u < UNR; ++u)
+            if (rr[u] < op.D) y[rr[u] * K + s] = v[u];
+    }
+}
 
 // --- start of a (plain or mixed) Krylov iteration: x = 0, r = r0 = rhs, p = v = 0
 // rhs = b (plain) or (T)(r64 / scale) (mixed)
 template <class T, int K>
-__global__ void k_init(OpView<T> op, Slot *sl, SolveParams P, int from_phase, const double *__restrict__ rhs64,
+__global__ void __launch_bounds__(BS, 4) k_init(OpView<T> op, Slot *sl, SolveParams P, int from_phase, const double *__restrict__ rhs64,
                        T *__restrict__ x, T *__restrict__ r, T *__restrict__ r0, T *__restrict__ p, T *__restrict__ v,
                        double *partial, unsigned int *counter) {
     GRID_LOOP
     const bool act = sl[s].phase == from_phase;
     const double inv = (from_phase == PH_INNER_INIT) ? 1.0 / sl[s].scale : 1.0;
-    double acc[1] = {0.0};
+    Dot<T, 1> acc;
     if (act)
-        for (int64_t row = r0i; row < op.D; row += rstride) {
-            int64_t i = row * K + s;
-            T bv = (T)(rhs64[i] * inv);
-            x[i] = 0;
-            r[i] = bv;
-            r0[i] = bv;
-            p[i] = 0;
-            v[i] = 0;
-            acc[0] += (double)bv * (double)bv;
+        ROWS_UNR(op.D) {
+            ROWS_OF_TRIP(rr)
+            double bb[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) bb[u] = rr[u] < op.D ? rhs64[rr[u] * K + s] : 0.0;
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+                if (rr[u] < op.D) {
+                    const int64_t i = rr[u] * K + s;
+                    T bv = (T)(bb[u] * inv);
+                    x[i] = 0;
+                    r[i] = bv;
+                    r0[i] = bv;
+                    p[i] = 0;
+                    v[i] = 0;
+                    acc.add(0, bv, bv);
+                }
         }
-    double tot[1];
-    if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
+    double av[1], tot[1];
+    acc.get(av);
+    if (grid_reduce<K, 1>(av, partial, counter, tot)) {
         Slot &S = sl[threadIdx.x];
         if (S.phase != from_phase) return;
         double b2 = tot[0];
@@ -280,38 +341,63 @@ __global__ void k_init(OpView<T> op, Slot *sl, SolveParams P, int from_phase, co
 // (pden = null) or the first Jacobi sweep from zero, y = omega (p / pden)
 // (src/GeneralizedBiCGStabSystem.h:358-377 with result = 0 and A 0 = 0)
 template <class T, int K>
-__global__ void k_update_p(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, T ys, const T *__restrict__ r,
-                           const T *__restrict__ v, T *__restrict__ p, T *__restrict__ y) {
-    int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t row = gid / K;
-    int s = (int)(gid % K);
-    if (row >= D || sl[s].phase != PH_ITER) return;
+__global__ void __launch_bounds__(BS, 4) k_update_p(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, T ys,
+                                                 const T *__restrict__ r, const T *__restrict__ v, T *__restrict__ p,
+                                                 T *__restrict__ y) {
+    GRID_LOOP
+    constexpr int UN = unr_stream6<T>();
+    if (sl[s].phase != PH_ITER) return;
     const T w = (T)sl[s].omega, beta = (T)sl[s].beta;
-    int64_t i = row * K + s;
-    T pi = -w * v[i] + p[i];
-    pi *= beta;
-    pi = pi + r[i];
-    p[i] = pi;
-    y[i] = pden ? ys * (pi / pden[row]) : pi;
+    ROWS_UNR_N(D, UN) {
+        ROWS_OF_TRIP_N(rr, UN)
+        T pv[UN], vv[UN], rv[UN], dv[UN];
+#pragma unroll
+        for (int u = 0; u < UN; ++u)
+            if (rr[u] < D) {
+                const int64_t i = rr[u] * K + s;
+                pv[u] = p[i];
+                vv[u] = v[i];
+                rv[u] = r[i];
+                dv[u] = pden ? pden[rr[u]] : T(1);
+            }
+#pragma unroll
+        for (int u = 0; u < UN; ++u)
+            if (rr[u] < D) {
+                const int64_t i = rr[u] * K + s;
+                T pi = -w * vv[u] + pv[u];
+                pi *= beta;
+                pi = pi + rv[u];
+                p[i] = pi;
+                y[i] = pden ? ys * (pi / dv[u]) : pi;
+            }
+    }
 }
 
 // v = A y with r0 . v  ->  alpha = rho / (r0 . v)   (src/BiCGStab.h:79-80)
 template <class T, int K>
-__global__ void k_apply_alpha(OpView<T> op, Slot *sl, T m, T n, const T *__restrict__ y, const T *__restrict__ te,
-                              const T *__restrict__ r0, T *__restrict__ v, double *partial, unsigned int *counter) {
+__global__ void __launch_bounds__(BS, 4) k_apply_alpha(OpView<T> op, Slot *sl, T m, T n, const T *__restrict__ y,
+                                                    const T *__restrict__ te, const T *__restrict__ r0, T *__restrict__ v,
+                                                    double *partial, unsigned int *counter) {
     GRID_LOOP
     const bool act = sl[s].phase == PH_ITER;
-    double acc[1] = {0.0};
-    if (run_rows<K>(act))
-        for (int64_t row = r0i; row < op.D; row += rstride) {
-            T vv = L_ROW<T, K>(op, row, s, m, n, y, te, act);
-            if (act) {
-                v[row * K + s] = vv;
-                acc[0] += (double)r0[row * K + s] * (double)vv;
-            }
+    Dot<T, 1> acc;
+    if (act)
+        ROWS_UNR(op.D) {
+            ROWS_OF_TRIP(rr)
+            T r0v[UNR], vv[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) r0v[u] = rr[u] < op.D ? r0[rr[u] * K + s] : T(0);
+            l_rows<T, K, UNR>(op, rr, s, m, n, y, te, true, vv);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+                if (rr[u] < op.D) {
+                    v[rr[u] * K + s] = vv[u];
+                    acc.add(0, r0v[u], vv[u]);
+                }
         }
-    double tot[1];
-    if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
+    double av[1], tot[1];
+    acc.get(av);
+    if (grid_reduce<K, 1>(av, partial, counter, tot)) {
         Slot &S = sl[threadIdx.x];
         if (S.phase != PH_ITER) return;
         S.alpha = S.rho / tot[0];
@@ -320,55 +406,88 @@ __global__ void k_apply_alpha(OpView<T> op, Slot *sl, T m, T n, const T *__restr
 
 // s = r - alpha v ; z = M^-1 s   (src/BiCGStab.h:82-84), M^-1 as in k_update_p
 template <class T, int K>
-__global__ void k_update_s(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, T ys, const T *__restrict__ r,
-                           const T *__restrict__ v, T *__restrict__ sv, T *__restrict__ z) {
-    int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t row = gid / K;
-    int s = (int)(gid % K);
-    if (row >= D || sl[s].phase != PH_ITER) return;
+__global__ void __launch_bounds__(BS, 4) k_update_s(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, T ys,
+                                                 const T *__restrict__ r, const T *__restrict__ v, T *__restrict__ sv,
+                                                 T *__restrict__ z) {
+    GRID_LOOP
+    if (sl[s].phase != PH_ITER) return;
     const T a = (T)sl[s].alpha;
-    int64_t i = row * K + s;
-    T si = -a * v[i] + r[i];
-    sv[i] = si;
-    z[i] = pden ? ys * (si / pden[row]) : si;
+    ROWS_UNR(D) {
+        ROWS_OF_TRIP(rr)
+        T vv[UNR], rv[UNR], dv[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u)
+            if (rr[u] < D) {
+                const int64_t i = rr[u] * K + s;
+                vv[u] = v[i];
+                rv[u] = r[i];
+                dv[u] = pden ? pden[rr[u]] : T(1);
+            }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u)
+            if (rr[u] < D) {
+                const int64_t i = rr[u] * K + s;
+                T si = -a * vv[u] + rv[u];
+                sv[i] = si;
+                z[i] = pden ? ys * (si / dv[u]) : si;
+            }
+    }
 }
 
 // one further damped Jacobi sweep on A y = c, after the E pass te = E~ y:
 // y += omega ((c - A y) / pden)   (src/GeneralizedBiCGStabSystem.h:366-376).
 // Row r of A y reads y only at row r, so the update is in place.
 template <class T, int K>
-__global__ void k_jacobi_sweep(OpView<T> op, const Slot *__restrict__ sl, T m, T n, const T *__restrict__ c,
-                               const T *__restrict__ te, const T *__restrict__ pden, T omega, T *y) {
+__global__ void __launch_bounds__(BS, 4) k_jacobi_sweep(OpView<T> op, const Slot *__restrict__ sl, T m, T n,
+                                                     const T *__restrict__ c, const T *__restrict__ te,
+                                                     const T *__restrict__ pden, T omega, T *y) {
     GRID_LOOP
-    const bool act = sl[s].phase == PH_ITER;
-    if (run_rows<K>(act))
-        for (int64_t row = r0i; row < op.D; row += rstride) {
-            const T ay = L_ROW<T, K>(op, row, s, m, n, y, te, act);
-            if (act) {
-                const int64_t i = row * K + s;
-                y[i] = y[i] + omega * ((c[i] - ay) / pden[row]);
+    if (sl[s].phase != PH_ITER) return;
+    ROWS_UNR(op.D) {
+        ROWS_OF_TRIP(rr)
+        T cv[UNR], dv[UNR], ay[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u)
+            if (rr[u] < op.D) {
+                cv[u] = c[rr[u] * K + s];
+                dv[u] = pden[rr[u]];
             }
-        }
+        l_rows<T, K, UNR>(op, rr, s, m, n, y, te, true, ay);
+#pragma unroll
+        for (int u = 0; u < UNR; ++u)
+            if (rr[u] < op.D) {
+                const int64_t i = rr[u] * K + s;
+                y[i] = y[i] + omega * ((cv[u] - ay[u]) / dv[u]);
+            }
+    }
 }
 
 // t = A z with t.t and t.s  ->  omega   (src/BiCGStab.h:85-95)
 template <class T, int K>
-__global__ void k_apply_omega(OpView<T> op, Slot *sl, T m, T n, const T *__restrict__ z, const T *__restrict__ te,
-                              const T *__restrict__ sv, T *__restrict__ tv, double *partial, unsigned int *counter) {
+__global__ void __launch_bounds__(BS, 4) k_apply_omega(OpView<T> op, Slot *sl, T m, T n, const T *__restrict__ z,
+                                                    const T *__restrict__ te, const T *__restrict__ sv, T *__restrict__ tv,
+                                                    double *partial, unsigned int *counter) {
     GRID_LOOP
     const bool act = sl[s].phase == PH_ITER;
-    double acc[2] = {0.0, 0.0};
-    if (run_rows<K>(act))
-        for (int64_t row = r0i; row < op.D; row += rstride) {
-            T tt = L_ROW<T, K>(op, row, s, m, n, z, te, act);
-            if (act) {
-                tv[row * K + s] = tt;
-                acc[0] += (double)tt * (double)tt;
-                acc[1] += (double)tt * (double)sv[row * K + s];
-            }
+    Dot<T, 2> acc;
+    if (act)
+        ROWS_UNR(op.D) {
+            ROWS_OF_TRIP(rr)
+            T svv[UNR], tt[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) svv[u] = rr[u] < op.D ? sv[rr[u] * K + s] : T(0);
+            l_rows<T, K, UNR>(op, rr, s, m, n, z, te, true, tt);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+                if (rr[u] < op.D) {
+                    tv[rr[u] * K + s] = tt[u];
+                    acc.add(0, tt[u], tt[u]);
+                    acc.add(1, tt[u], svv[u]);
+                }
         }
-    double tot[2];
-    if (grid_reduce<K, 2>(acc, partial, counter, tot)) {
+    double av[2], tot[2];
+    acc.get(av);
+    if (grid_reduce<K, 2>(av, partial, counter, tot)) {
         Slot &S = sl[threadIdx.x];
         if (S.phase != PH_ITER) return;
         S.omega = (tot[0] > 0.0) ? tot[1] / tot[0] : 0.0;
@@ -378,26 +497,46 @@ __global__ void k_apply_omega(OpView<T> op, Slot *sl, T m, T n, const T *__restr
 // x += alpha y + w z ; r = s - w t ; r.r and r0.r -> convergence test, rho, beta
 // (src/BiCGStab.h:97-103 and the loop head :59-73)
 template <class T, int K>
-__global__ void k_update_xr(int64_t D, Slot *sl, SolveParams P, const T *__restrict__ y, const T *__restrict__ z,
-                            const T *__restrict__ sv, const T *__restrict__ tv, const T *__restrict__ r0, T *__restrict__ x,
-                            T *__restrict__ r, double *partial, unsigned int *counter) {
+__global__ void __launch_bounds__(BS, 4) k_update_xr(int64_t D, Slot *sl, SolveParams P, const T *__restrict__ y,
+                                                  const T *__restrict__ z, const T *__restrict__ sv,
+                                                  const T *__restrict__ tv, const T *__restrict__ r0, T *__restrict__ x,
+                                                  T *__restrict__ r, double *partial, unsigned int *counter) {
     GRID_LOOP
     const bool act = sl[s].phase == PH_ITER;
-    double acc[2] = {0.0, 0.0};
+    Dot<T, 2> acc;
     if (act) {
         const T a = (T)sl[s].alpha, w = (T)sl[s].omega;
-        for (int64_t row = r0i; row < D; row += rstride) {
-            int64_t i = row * K + s;
-            T xi = a * y[i] + x[i];
-            x[i] = w * z[i] + xi;
-            T ri = -w * tv[i] + sv[i];
-            r[i] = ri;
-            acc[0] += (double)ri * (double)ri;
-            acc[1] += (double)r0[i] * (double)ri;
+        constexpr int UN = unr_stream6<T>();
+        ROWS_UNR_N(D, UN) {
+            ROWS_OF_TRIP_N(rr, UN)
+            T yv[UN], zv[UN], xv[UN], tw[UN], sw[UN], r0v[UN];
+#pragma unroll
+            for (int u = 0; u < UN; ++u)
+                if (rr[u] < D) {
+                    const int64_t i = rr[u] * K + s;
+                    yv[u] = y[i];
+                    zv[u] = z[i];
+                    xv[u] = x[i];
+                    tw[u] = tv[i];
+                    sw[u] = sv[i];
+                    r0v[u] = r0[i];
+                }
+#pragma unroll
+            for (int u = 0; u < UN; ++u)
+                if (rr[u] < D) {
+                    const int64_t i = rr[u] * K + s;
+                    T xi = a * yv[u] + xv[u];
+                    x[i] = w * zv[u] + xi;
+                    T ri = -w * tw[u] + sw[u];
+                    r[i] = ri;
+                    acc.add(0, ri, ri);
+                    acc.add(1, r0v[u], ri);
+                }
         }
     }
-    double tot[2];
-    if (grid_reduce<K, 2>(acc, partial, counter, tot)) {
+    double av[2], tot[2];
+    acc.get(av);
+    if (grid_reduce<K, 2>(av, partial, counter, tot)) {
         Slot &S = sl[threadIdx.x];
         if (S.phase != PH_ITER) return;
         S.iters += 1;
@@ -406,8 +545,10 @@ __global__ void k_update_xr(int64_t D, Slot *sl, SolveParams P, const T *__restr
         const bool conv = !(S.rr > S.tol2);
         if (P.mixed) {
             S.rr_max = fmax(S.rr_max, S.rr);
-            // reliable update when the FP32 residual fell by delta or claims convergence
-            if (conv || S.rr <= P.delta * P.delta * S.rr_max || S.iters >= P.max_iters || !isfinite(S.rr)) {
+            // a slot whose FP32 residual claims convergence waits for the next
+            // reliable update; one whose residual merely fell by delta keeps
+            // iterating until then (k_refine_gate)
+            if (conv || S.iters >= P.max_iters || !isfinite(S.rr)) {
                 S.rho_old = S.rho;
                 S.phase = PH_REFINE;
                 return;
@@ -442,24 +583,33 @@ __global__ void k_update_xr(int64_t D, Slot *sl, SolveParams P, const T *__restr
 
 // plain-path restart: r = b - A x ; r0 = r ; rho = r0norm2 = ||r||^2
 template <class T, int K>
-__global__ void k_restart(OpView<T> op, Slot *sl, T m, T n, const double *__restrict__ b, const T *__restrict__ x,
-                          const T *__restrict__ te, T *__restrict__ r, T *__restrict__ r0, double *partial,
-                          unsigned int *counter) {
+__global__ void __launch_bounds__(BS, 4) k_restart(OpView<T> op, Slot *sl, T m, T n, const double *__restrict__ b,
+                                                const T *__restrict__ x, const T *__restrict__ te, T *__restrict__ r,
+                                                T *__restrict__ r0, double *partial, unsigned int *counter) {
     GRID_LOOP
     const bool act = sl[s].phase == PH_RESTART;
-    double acc[1] = {0.0};
-    if (run_rows<K>(act))
-        for (int64_t row = r0i; row < op.D; row += rstride) {
-            T ax = L_ROW<T, K>(op, row, s, m, n, x, te, act);
-            if (act) {
-                T ri = (T)b[row * K + s] - ax;
-                r[row * K + s] = ri;
-                r0[row * K + s] = ri;
-                acc[0] += (double)ri * (double)ri;
-            }
+    Dot<T, 1> acc;
+    if (act)
+        ROWS_UNR(op.D) {
+            ROWS_OF_TRIP(rr)
+            double bv[UNR];
+            T ax[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) bv[u] = rr[u] < op.D ? b[rr[u] * K + s] : 0.0;
+            l_rows<T, K, UNR>(op, rr, s, m, n, x, te, true, ax);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+                if (rr[u] < op.D) {
+                    const int64_t i = rr[u] * K + s;
+                    T ri = (T)bv[u] - ax[u];
+                    r[i] = ri;
+                    r0[i] = ri;
+                    acc.add(0, ri, ri);
+                }
         }
-    double tot[1];
-    if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
+    double av[1], tot[1];
+    acc.get(av);
+    if (grid_reduce<K, 1>(av, partial, counter, tot)) {
         Slot &S = sl[threadIdx.x];
         if (S.phase != PH_RESTART) return;
         S.rho = S.r0norm2 = tot[0];
@@ -467,6 +617,17 @@ __global__ void k_restart(OpView<T> op, Slot *sl, T m, T n, const double *__rest
         S.beta = (S.rho / S.rho_old) * (S.alpha / S.omega);
         S.phase = PH_ITER;
     }
+}
+
+// reliable updates run for all slots at once every few iterations, so one FP64
+// apply serves every slot that needs it: a slot joins when its FP32 residual has
+// fallen by delta since its last update (Sleijpen & van der Vorst's criterion)
+template <int K>
+__global__ void k_refine_gate(Slot *sl, SolveParams P) {
+    const int s = threadIdx.x;
+    if (s >= K) return;
+    Slot &S = sl[s];
+    if (S.phase == PH_ITER && S.rr <= P.delta * P.delta * S.rr_max) S.phase = PH_REFINE;
 }
 
 // reliable update, step 1: x64 += scale * u32, u32 = 0
@@ -482,20 +643,27 @@ __global__ void k_refine_accumulate(int64_t D, const Slot *__restrict__ sl, floa
 
 // step 2: r64 = b - A x64 (FP64) and ||r64||: done, or replace the FP32 residual
 template <int K>
-__global__ void k_refine_residual(OpView<double> op, Slot *sl, SolveParams P, double m, double n, const double *__restrict__ b,
-                                  const double *__restrict__ x64, const double *__restrict__ te, double *__restrict__ r64,
-                                  double *partial, unsigned int *counter) {
+__global__ void __launch_bounds__(BS, 4) k_refine_residual(OpView<double> op, Slot *sl, SolveParams P, double m, double n,
+                                                        const double *__restrict__ b, const double *__restrict__ x64,
+                                                        const double *__restrict__ te, double *__restrict__ r64,
+                                                        double *partial, unsigned int *counter) {
     GRID_LOOP
     const bool act = sl[s].phase == PH_REFINE;
     double acc[1] = {0.0};
-    if (run_rows<K>(act))
-        for (int64_t row = r0i; row < op.D; row += rstride) {
-            double ax = L_ROW<double, K>(op, row, s, m, n, x64, te, act);
-            if (act) {
-                double ri = b[row * K + s] - ax;
-                r64[row * K + s] = ri;
-                acc[0] += ri * ri;
-            }
+    if (act)
+        ROWS_UNR(op.D) {
+            ROWS_OF_TRIP(rr)
+            double bv[UNR], ax[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) bv[u] = rr[u] < op.D ? b[rr[u] * K + s] : 0.0;
+            l_rows<double, K, UNR>(op, rr, s, m, n, x64, te, true, ax);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+                if (rr[u] < op.D) {
+                    const double ri = bv[u] - ax[u];
+                    r64[rr[u] * K + s] = ri;
+                    acc[0] += ri * ri;
+                }
         }
     double tot[1];
     if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
@@ -518,29 +686,44 @@ __global__ void k_refine_residual(OpView<double> op, Slot *sl, SolveParams P, do
 // step 3: r32 = r64 / scale; keep p, v, r0 and the scalars, recompute rho = r0 . r
 // (after a rho breakdown the Krylov space restarts from the true residual instead)
 template <int K>
-__global__ void k_reliable(int64_t D, Slot *sl, const double *__restrict__ r64, float *__restrict__ r, float *__restrict__ r0,
-                           float *__restrict__ p, float *__restrict__ v, double *partial, unsigned int *counter) {
+__global__ void __launch_bounds__(BS, 4) k_reliable(int64_t D, Slot *sl, const double *__restrict__ r64, float *__restrict__ r,
+                                                 float *__restrict__ r0, float *__restrict__ p, float *__restrict__ v,
+                                                 double *partial, unsigned int *counter) {
     GRID_LOOP
     const bool act = sl[s].phase == PH_RELIABLE;
     const bool fresh = act && sl[s].krylov_restart;
-    double acc[2] = {0.0, 0.0};
+    Dot<float, 2> acc;
     if (act) {
         const double inv = 1.0 / sl[s].scale;
-        for (int64_t row = r0i; row < D; row += rstride) {
-            int64_t i = row * K + s;
-            float ri = (float)(r64[i] * inv);
-            r[i] = ri;
-            if (fresh) {
-                r0[i] = ri;
-                p[i] = 0.0f;
-                v[i] = 0.0f;
-            }
-            acc[0] += (double)ri * (double)ri;
-            acc[1] += (double)(fresh ? ri : r0[i]) * (double)ri;
+        ROWS_UNR(D) {
+            ROWS_OF_TRIP(rr)
+            double rv[UNR];
+            float r0v[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+                if (rr[u] < D) {
+                    rv[u] = r64[rr[u] * K + s];
+                    r0v[u] = fresh ? 0.0f : r0[rr[u] * K + s];
+                }
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+                if (rr[u] < D) {
+                    const int64_t i = rr[u] * K + s;
+                    float ri = (float)(rv[u] * inv);
+                    r[i] = ri;
+                    if (fresh) {
+                        r0[i] = ri;
+                        p[i] = 0.0f;
+                        v[i] = 0.0f;
+                    }
+                    acc.add(0, ri, ri);
+                    acc.add(1, fresh ? ri : r0v[u], ri);
+                }
         }
     }
-    double tot[2];
-    if (grid_reduce<K, 2>(acc, partial, counter, tot)) {
+    double av[2], tot[2];
+    acc.get(av);
+    if (grid_reduce<K, 2>(av, partial, counter, tot)) {
         Slot &S = sl[threadIdx.x];
         if (S.phase != PH_RELIABLE) return;
         S.rr = tot[0];
@@ -561,17 +744,26 @@ __global__ void k_reliable(int64_t D, Slot *sl, const double *__restrict__ r64, 
 
 // mixed-path start: x64 = 0, r64 = b, ||b||
 template <int K>
-__global__ void k_mixed_start(int64_t D, Slot *sl, SolveParams P, const double *__restrict__ b, double *__restrict__ x64,
-                              double *__restrict__ r64, double *partial, unsigned int *counter) {
+__global__ void __launch_bounds__(BS, 4) k_mixed_start(int64_t D, Slot *sl, SolveParams P, const double *__restrict__ b,
+                                                    double *__restrict__ x64, double *__restrict__ r64, double *partial,
+                                                    unsigned int *counter) {
     GRID_LOOP
     const bool act = sl[s].phase == PH_REFINE;
     double acc[1] = {0.0};
     if (act)
-        for (int64_t row = r0i; row < D; row += rstride) {
-            int64_t i = row * K + s;
-            x64[i] = 0.0;
-            r64[i] = b[i];
-            acc[0] += b[i] * b[i];
+        ROWS_UNR(D) {
+            ROWS_OF_TRIP(rr)
+            double bv[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) bv[u] = rr[u] < D ? b[rr[u] * K + s] : 0.0;
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+                if (rr[u] < D) {
+                    const int64_t i = rr[u] * K + s;
+                    x64[i] = 0.0;
+                    r64[i] = bv[u];
+                    acc[0] += bv[u] * bv[u];
+                }
         }
     double tot[1];
     if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
@@ -682,12 +874,12 @@ static void plain_iteration(cpm_solver_s *s, const SolveParams &P) {
     Slot *sl = s->slots.p;
     const double *pden = P.precond == 0 ? nullptr : s->pden64.p;
     const double ys = P.precond == 2 ? JACOBI_OMEGA : 1.0;
-    k_update_p<double, K><<<nblk(D * K), BS, 0, st>>>(D, sl, pden, ys, s->dr.p, s->dv.p, s->dp.p, s->dy.p);
+    k_update_p<double, K><<<s->G, BS, 0, st>>>(D, sl, pden, ys, s->dr.p, s->dv.p, s->dp.p, s->dy.p);
     if (P.precond == 2) jacobi_rest<K>(s, P, s->dp.p, s->dy.p);
     launch_epass<double, K>(op, sl, PH_ITER, s->dy.p, s->te64.p, st);
     k_apply_alpha<double, K><<<s->G, BS, 0, st>>>(op, sl, s->m, s->n, s->dy.p, s->te64.p, s->dr0.p, s->dv.p, s->partial.p,
                                                   s->counter.p);
-    k_update_s<double, K><<<nblk(D * K), BS, 0, st>>>(D, sl, pden, ys, s->dr.p, s->dv.p, s->ds.p, s->dz.p);
+    k_update_s<double, K><<<s->G, BS, 0, st>>>(D, sl, pden, ys, s->dr.p, s->dv.p, s->ds.p, s->dz.p);
     if (P.precond == 2) jacobi_rest<K>(s, P, s->ds.p, s->dz.p);
     launch_epass<double, K>(op, sl, PH_ITER, s->dz.p, s->te64.p, st);
     k_apply_omega<double, K><<<s->G, BS, 0, st>>>(op, sl, s->m, s->n, s->dz.p, s->te64.p, s->ds.p, s->dt.p, s->partial.p,
@@ -713,10 +905,10 @@ static void mixed_iteration(cpm_solver_s *s, const SolveParams &P) {
     Slot *sl = s->slots.p;
     const float m = (float)s->m, n = (float)s->n;
     const float *pden = P.precond == 0 ? nullptr : s->pden32.p;
-    k_update_p<float, K><<<nblk(D * K), BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fp.p, s->fy.p);
+    k_update_p<float, K><<<s->G, BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fp.p, s->fy.p);
     launch_epass<float, K>(op, sl, PH_ITER, s->fy.p, s->fte.p, st);
     k_apply_alpha<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p, s->counter.p);
-    k_update_s<float, K><<<nblk(D * K), BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fs.p, s->fz.p);
+    k_update_s<float, K><<<s->G, BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fs.p, s->fz.p);
     launch_epass<float, K>(op, sl, PH_ITER, s->fz.p, s->fte.p, st);
     k_apply_omega<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p, s->counter.p);
     k_update_xr<float, K><<<s->G, BS, 0, st>>>(D, sl, P, s->fy.p, s->fz.p, s->fs.p, s->ft.p, s->fr0.p, s->fx.p, s->fr.p,
@@ -730,6 +922,7 @@ static void mixed_refine(cpm_solver_s *s, const SolveParams &P) {
     const int64_t D = s->D;
     cudaStream_t st = stream();
     Slot *sl = s->slots.p;
+    k_refine_gate<K><<<1, 32, 0, st>>>(sl, P);
     k_refine_accumulate<K><<<nblk(D * K), BS, 0, st>>>(D, sl, s->fx.p, s->x64.p);
     launch_epass<double, K>(op64, sl, PH_REFINE, s->x64.p, s->te64.p, st);
     k_refine_residual<K><<<s->G, BS, 0, st>>>(op64, sl, P, s->m, s->n, s->b64.p, s->x64.p, s->te64.p, s->r64.p, s->partial.p,
@@ -755,11 +948,9 @@ static int alloc_vectors(cpm_solver_s *s, bool want64, bool want32) {
 
 static bool same_params(const SolveParams &a, const SolveParams &b) {
     return a.tol == b.tol && a.delta == b.delta && a.max_iters == b.max_iters && a.max_refine == b.max_refine &&
-           a.mixed == b.mixed && a.precond == b.precond && a.sweeps == b.sweeps;
+           a.mixed == b.mixed && a.precond == b.precond && a.sweeps == b.sweeps && a.refine_every == b.refine_every;
 }
 
-// mixed graphs interleave a reliable-update step every 2 iterations
-constexpr int REFINE_EVERY = 2;
 
 template <int K>
 static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_stats *stats) {
@@ -770,6 +961,9 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
     P.mixed = o->precision == 1;
     P.delta = o->inner_tol > 0 ? o->inner_tol : 0.2;
     P.max_refine = o->max_refine > 0 ? o->max_refine : 400;
+    P.refine_every = o->refine_every > 0 ? o->refine_every : 8;
+    if (P.refine_every > 16 || (P.refine_every & (P.refine_every - 1)))
+        return fail(CPM_ERR_INVALID_ARG, "refine_every must be 1, 2, 4, 8 or 16");
     P.precond = o->precond;
     P.sweeps = o->precond_iters;
     if (P.precond < 0 || P.precond > 2) return fail(CPM_ERR_INVALID_ARG, "precond must be 0 (identity), 1 (diagonal) or 2 (jacobi)");
@@ -810,7 +1004,7 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
         for (int it = 0; it < chunk; ++it) {
             if (P.mixed) {
                 mixed_iteration<K>(s, P);
-                if (it % REFINE_EVERY == REFINE_EVERY - 1) mixed_refine<K>(s, P);
+                if (it % P.refine_every == P.refine_every - 1) mixed_refine<K>(s, P);
             } else {
                 plain_iteration<K>(s, P);
             }
@@ -825,7 +1019,7 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
     const int chunk = (P.precond == 2) ? 1 : s->chunk;
     const int64_t max_chunks = (int64_t)P.max_iters / chunk + 2 * P.max_refine + 4;
     const long long per_graph = (7LL + (P.precond == 2 ? 4LL * (P.sweeps - 1) : 0)) * chunk +
-                                (P.mixed ? 4LL * (chunk / REFINE_EVERY) : 0);
+                                (P.mixed ? 5LL * (chunk / P.refine_every) : 0);
     count_launches(P.mixed ? 2 : 1);
     bool done = false;
     for (int64_t c = 0; c < max_chunks && !done; ++c) {
@@ -880,18 +1074,15 @@ extern "C" int cpm_solver_create(cpm_opset_t op, double m, double n, int32_t ksl
     s->n = n;
     s->K = (kslots == 1) ? 1 : 32;
     s->D = op->D;
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int64_t need = (s->D * s->K + BS - 1) / BS;
-    s->G = (int)std::max<int64_t>(1, std::min<int64_t>(need, 8LL * sms));
+    s->G = row_grid(s->D, s->K);
     s->h_slots.assign(s->K, Slot());
     auto bail = [&](int rc) {
         delete s;
         return rc;
     };
     int rc;
-    if ((rc = s->slots.alloc(s->K)) || (rc = s->partial.alloc((size_t)s->G * s->K * 2)) || (rc = s->counter.alloc(1)) ||
+    if ((rc = s->slots.alloc(s->K)) || (rc = s->partial.alloc((size_t)(s->G + reduce_groups(s->G)) * s->K * 2)) ||
+        (rc = s->counter.alloc((size_t)(1 + reduce_groups(s->G)))) ||
         (rc = s->counter.zero()) || (rc = s->b64.alloc((size_t)s->D * s->K)) || (rc = s->x64.alloc((size_t)s->D * s->K)) ||
         (rc = s->r64.alloc((size_t)s->D * s->K)) || (rc = s->te64.alloc((size_t)s->D * s->K)) || (rc = s->pden64.alloc(s->D)))
         return bail(rc);
@@ -946,7 +1137,7 @@ extern "C" int cpm_apply(cpm_opset_t op, double m, double n, int32_t k, const do
     for (int j = 0; j < k; ++j) {
         CPM_CUDA_TRY(cudaMemcpyAsync(dx.p, x + (size_t)j * D, D * 8, cudaMemcpyHostToDevice, stream()));
         launch_epass<double, 1>(v, nullptr, -1, dx.p, dt.p, stream());
-        k_lpass<double, 1><<<nblk(D), BS, 0, stream()>>>(v, m, n, dx.p, dt.p, dy.p);
+        k_lpass<double, 1><<<row_grid(D, 1), BS, 0, stream()>>>(v, m, n, dx.p, dt.p, dy.p);
         CPM_CUDA_TRY(cudaGetLastError());
         CPM_CUDA_TRY(cudaMemcpyAsync(y + (size_t)j * D, dy.p, D * 8, cudaMemcpyDeviceToHost, stream()));
     }
@@ -966,10 +1157,10 @@ extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslo
         float *t = (float *)t_dev, *y = (float *)y_dev;
         if (kslots == 1) {
             launch_epass<float, 1>(v, nullptr, -1, x, t, st);
-            k_lpass<float, 1><<<nblk(D), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
+            k_lpass<float, 1><<<row_grid(D, 1), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
         } else {
             launch_epass<float, 32>(v, nullptr, -1, x, t, st);
-            k_lpass<float, 32><<<nblk(D * 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
+            k_lpass<float, 32><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
         }
     } else {
         auto v = op->view<double>();
@@ -977,10 +1168,10 @@ extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslo
         double *t = (double *)t_dev, *y = (double *)y_dev;
         if (kslots == 1) {
             launch_epass<double, 1>(v, nullptr, -1, x, t, st);
-            k_lpass<double, 1><<<nblk(D), BS, 0, st>>>(v, m, n, x, t, y);
+            k_lpass<double, 1><<<row_grid(D, 1), BS, 0, st>>>(v, m, n, x, t, y);
         } else {
             launch_epass<double, 32>(v, nullptr, -1, x, t, st);
-            k_lpass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, m, n, x, t, y);
+            k_lpass<double, 32><<<row_grid(D, 32), BS, 0, st>>>(v, m, n, x, t, y);
         }
     }
     count_launches(2);
@@ -1035,10 +1226,10 @@ extern "C" int cpm_apply_device_noalloc(cpm_opset_t op, double m, double n, int3
         float *tt = (float *)t, *y = (float *)y_dev;
         if (kslots == 1) {
             launch_epass<float, 1>(v, nullptr, -1, x, tt, st);
-            k_lpass<float, 1><<<nblk(D), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
+            k_lpass<float, 1><<<row_grid(D, 1), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
         } else {
             launch_epass<float, 32>(v, nullptr, -1, x, tt, st);
-            k_lpass<float, 32><<<nblk(D * 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
+            k_lpass<float, 32><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
         }
     } else {
         auto v = op->view<double>();
@@ -1046,10 +1237,10 @@ extern "C" int cpm_apply_device_noalloc(cpm_opset_t op, double m, double n, int3
         double *tt = (double *)t, *y = (double *)y_dev;
         if (kslots == 1) {
             launch_epass<double, 1>(v, nullptr, -1, x, tt, st);
-            k_lpass<double, 1><<<nblk(D), BS, 0, st>>>(v, m, n, x, tt, y);
+            k_lpass<double, 1><<<row_grid(D, 1), BS, 0, st>>>(v, m, n, x, tt, y);
         } else {
             launch_epass<double, 32>(v, nullptr, -1, x, tt, st);
-            k_lpass<double, 32><<<nblk(D * 32), BS, 0, st>>>(v, m, n, x, tt, y);
+            k_lpass<double, 32><<<row_grid(D, 32), BS, 0, st>>>(v, m, n, x, tt, y);
         }
     }
     count_launches(2);

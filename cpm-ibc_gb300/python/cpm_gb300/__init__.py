@@ -58,7 +58,7 @@ class TubeInfo(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iters", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("precond", ctypes.c_int32), ("precond_iters", ctypes.c_int32), ("inner_tol", ctypes.c_double),
-                ("max_refine", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("max_refine", ctypes.c_int32), ("refine_every", ctypes.c_int32)]
 
 
 class SolveStats(ctypes.Structure):
@@ -329,12 +329,12 @@ class Solver:
             pass
 
     def solve(self, b, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.2, max_refine=400, raise_on_error=True,
-              precond=DIAGONAL, precond_iters=0):
+              precond=DIAGONAL, precond_iters=0, refine_every=0):
         b = np.ascontiguousarray(np.atleast_2d(b), np.float64)
         k = b.shape[0]
         x = np.zeros_like(b)
         o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=precond, precond_iters=precond_iters,
-                      inner_tol=inner_tol, max_refine=max_refine)
+                      inner_tol=inner_tol, max_refine=max_refine, refine_every=refine_every)
         st = (SolveStats * k)()
         rc = lib().cpm_solve(self.h, k, _p(b), _p(x), ctypes.byref(o), st)
         stats = [dict(iterations=s.iterations, refinements=s.refinements, restarts=s.restarts, status=s.status,
@@ -344,9 +344,9 @@ class Solver:
         return x, stats
 
     def solve_device(self, b_ptr, x_ptr, k, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.2, max_refine=400,
-                     precond=DIAGONAL, precond_iters=0):
+                     precond=DIAGONAL, precond_iters=0, refine_every=0):
         o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=precond, precond_iters=precond_iters,
-                      inner_tol=inner_tol, max_refine=max_refine)
+                      inner_tol=inner_tol, max_refine=max_refine, refine_every=refine_every)
         st = (SolveStats * k)()
         rc = lib().cpm_solve_device(self.h, k, b_ptr, x_ptr, ctypes.byref(o), st)
         stats = [dict(iterations=s.iterations, refinements=s.refinements, restarts=s.restarts, status=s.status,

@@ -192,7 +192,8 @@ typedef struct cpm_solve_opts {
     double inner_tol;       /* precision 1: the FP32 residual reduction (default 0.2) after which the
                                FP64 true residual replaces it (one refinement step) */
     int32_t max_refine;     /* FP64 refinement steps (default 400) */
-    int32_t pad;
+    int32_t refine_every;   /* precision 1: iterations between reliable-update points, one of
+                               1, 2, 4, 8, 16 (0: 8) */
 } cpm_solve_opts;
 
 typedef struct cpm_solve_stats {
