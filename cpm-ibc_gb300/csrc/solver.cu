@@ -20,7 +20,9 @@
 // Every slot is an independent state machine (idle / iterating / refine /
 // reliable-update / restart / done), so slots start and finish independently.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <deque>
 #include <cstring>
 #include <limits>
 #include <mutex>
@@ -30,7 +32,16 @@
 
 namespace cpm {
 
-enum Phase : int { PH_IDLE = 0, PH_ITER = 1, PH_REFINE = 2, PH_DONE = 3, PH_RESTART = 4, PH_INNER_INIT = 5, PH_RELIABLE = 6 };
+enum Phase : int {
+    PH_IDLE = 0,
+    PH_ITER = 1,
+    PH_REFINE = 2,
+    PH_DONE = 3,
+    PH_RESTART = 4,
+    PH_INNER_INIT = 5,
+    PH_RELIABLE = 6,
+    PH_START = 7  // mixed path: a new right-hand side waiting for k_mixed_start
+};
 
 struct Slot {
     double rho, rho_old, alpha, omega, beta;
@@ -742,13 +753,13 @@ __global__ void __launch_bounds__(BS, 4) k_reliable(int64_t D, Slot *sl, const d
     }
 }
 
-// mixed-path start: x64 = 0, r64 = b, ||b||
+// mixed-path start of the slots in PH_START: x64 = 0, r64 = b, ||b||
 template <int K>
 __global__ void __launch_bounds__(BS, 4) k_mixed_start(int64_t D, Slot *sl, SolveParams P, const double *__restrict__ b,
                                                     double *__restrict__ x64, double *__restrict__ r64, double *partial,
                                                     unsigned int *counter) {
     GRID_LOOP
-    const bool act = sl[s].phase == PH_REFINE;
+    const bool act = sl[s].phase == PH_START;
     double acc[1] = {0.0};
     if (act)
         ROWS_UNR(D) {
@@ -768,7 +779,7 @@ __global__ void __launch_bounds__(BS, 4) k_mixed_start(int64_t D, Slot *sl, Solv
     double tot[1];
     if (grid_reduce<K, 1>(acc, partial, counter, tot)) {
         Slot &S = sl[threadIdx.x];
-        if (S.phase != PH_REFINE) return;
+        if (S.phase != PH_START) return;
         S.b64norm2 = tot[0];
         S.outer_tol2 = P.tol * P.tol * tot[0];
         S.iters = 0;
@@ -796,6 +807,16 @@ __global__ void k_pden(OpView<T> op, double m, double n, T *__restrict__ pden) {
     }
     double ld = (r < op.N) ? (double)op.Ldiag : (double)op.ldiag[r - op.N];
     pden[r] = (T)(m + ld * n);
+}
+
+// one slot column of a [D][K] array from / to a contiguous vector
+__global__ void k_scatter_col(int64_t D, int K, int j, const double *__restrict__ src, double *__restrict__ dst) {
+    int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r < D) dst[r * K + j] = src[r];
+}
+__global__ void k_gather_col(int64_t D, int K, int j, const double *__restrict__ src, double *__restrict__ dst) {
+    int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r < D) dst[r] = src[r * K + j];
 }
 
 // layout transposes between RHS-major host arrays and [D][K] slot layout
@@ -952,9 +973,7 @@ static bool same_params(const SolveParams &a, const SolveParams &b) {
 }
 
 
-template <int K>
-static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_stats *stats) {
-    SolveParams P;
+static int parse_params(const cpm_solve_opts *o, SolveParams &P) {
     memset(&P, 0, sizeof(P));
     P.tol = o->tol > 0 ? o->tol : 1e-10;
     P.max_iters = o->max_iters > 0 ? o->max_iters : 100000;
@@ -974,23 +993,16 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
     // preconditioner is an FP64 solve
     if (P.precond == 2 && P.mixed)
         return fail(CPM_ERR_UNSUPPORTED, "the jacobi preconditioner runs in FP64 (precision 0) only");
-    CPM_TRY(alloc_vectors(s, !P.mixed, P.mixed));
+    return 0;
+}
+
+// iterations per captured graph
+static inline int graph_chunk(const cpm_solver_s *s, const SolveParams &P) { return (P.precond == 2) ? 1 : s->chunk; }
+
+// the captured iteration graph for P (reused while the parameters match)
+template <int K>
+static int prepare_graph(cpm_solver_s *s, const SolveParams &P, cudaGraphExec_t *out) {
     cudaStream_t st = stream();
-    for (int j = 0; j < K; ++j) {
-        memset(&s->h_slots[j], 0, sizeof(Slot));
-        s->h_slots[j].phase = (j < k) ? (P.mixed ? PH_REFINE : PH_ITER) : PH_IDLE;
-    }
-    CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p, s->h_slots.data(), sizeof(Slot) * K, cudaMemcpyHostToDevice, st));
-    CPM_CUDA_TRY(cudaEventRecord(s->e0, st));
-    if (!P.mixed) {
-        k_init<double, K><<<s->G, BS, 0, st>>>(s->op->view<double>(), s->slots.p, P, PH_ITER, s->b64.p, s->x64.p, s->dr.p,
-                                               s->dr0.p, s->dp.p, s->dv.p, s->partial.p, s->counter.p);
-    } else {
-        k_mixed_start<K><<<s->G, BS, 0, st>>>(s->D, s->slots.p, P, s->b64.p, s->x64.p, s->r64.p, s->partial.p, s->counter.p);
-        k_init<float, K><<<s->G, BS, 0, st>>>(s->op->view<float>(), s->slots.p, P, PH_INNER_INIT, s->r64.p, s->fx.p, s->fr.p,
-                                              s->fr0.p, s->fp.p, s->fv.p, s->partial.p, s->counter.p);
-    }
-    CPM_CUDA_TRY(cudaGetLastError());
     cudaGraphExec_t &gexec = P.mixed ? s->g_mixed : s->g_plain;
     SolveParams &gpar = P.mixed ? s->gp_mixed : s->gp_plain;
     if (gexec && !same_params(gpar, P)) {
@@ -1000,7 +1012,7 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
     if (!gexec) {
         cudaGraph_t graph;
         CPM_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        const int chunk = (P.precond == 2) ? 1 : s->chunk;
+        const int chunk = graph_chunk(s, P);
         for (int it = 0; it < chunk; ++it) {
             if (P.mixed) {
                 mixed_iteration<K>(s, P);
@@ -1016,11 +1028,62 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
         if (ce != cudaSuccess) return fail(CPM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
         gpar = P;
     }
-    const int chunk = (P.precond == 2) ? 1 : s->chunk;
+    *out = gexec;
+    return 0;
+}
+
+// kernels launched by one graph replay
+static inline long long graph_launches(const cpm_solver_s *s, const SolveParams &P) {
+    const int chunk = graph_chunk(s, P);
+    return (7LL + (P.precond == 2 ? 4LL * (P.sweeps - 1) : 0)) * chunk + (P.mixed ? 5LL * (chunk / P.refine_every) : 0);
+}
+
+// start the mixed-path slots in PH_START (FP64 residual, then the FP32 Krylov state)
+template <int K>
+static void mixed_start(cpm_solver_s *s, const SolveParams &P) {
+    cudaStream_t st = stream();
+    k_mixed_start<K><<<s->G, BS, 0, st>>>(s->D, s->slots.p, P, s->b64.p, s->x64.p, s->r64.p, s->partial.p, s->counter.p);
+    k_init<float, K><<<s->G, BS, 0, st>>>(s->op->view<float>(), s->slots.p, P, PH_INNER_INIT, s->r64.p, s->fx.p, s->fr.p,
+                                          s->fr0.p, s->fp.p, s->fv.p, s->partial.p, s->counter.p);
+    count_launches(2);
+}
+
+static void slot_stats(const Slot &S, bool mixed, float ms, cpm_solve_stats *st) {
+    const int status = (S.phase == PH_DONE) ? S.status : CPM_ERR_TIMEOUT;
+    st->iterations = S.iters;
+    st->refinements = S.refinements;
+    st->restarts = S.restarts;
+    st->status = status;
+    st->rel_residual = mixed ? (S.b64norm2 > 0 ? S.rnorm64 / std::sqrt(S.b64norm2) : 0.0)
+                             : (S.bnorm2 > 0 ? std::sqrt(S.rr / S.bnorm2) : 0.0);
+    st->seconds = ms * 1e-3;
+}
+
+template <int K>
+static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_stats *stats) {
+    SolveParams P;
+    CPM_TRY(parse_params(o, P));
+    CPM_TRY(alloc_vectors(s, !P.mixed, P.mixed));
+    cudaStream_t st = stream();
+    for (int j = 0; j < K; ++j) {
+        memset(&s->h_slots[j], 0, sizeof(Slot));
+        s->h_slots[j].phase = (j < k) ? (P.mixed ? PH_START : PH_ITER) : PH_IDLE;
+    }
+    CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p, s->h_slots.data(), sizeof(Slot) * K, cudaMemcpyHostToDevice, st));
+    CPM_CUDA_TRY(cudaEventRecord(s->e0, st));
+    if (!P.mixed) {
+        k_init<double, K><<<s->G, BS, 0, st>>>(s->op->view<double>(), s->slots.p, P, PH_ITER, s->b64.p, s->x64.p, s->dr.p,
+                                               s->dr0.p, s->dp.p, s->dv.p, s->partial.p, s->counter.p);
+        count_launches(1);
+    } else {
+        mixed_start<K>(s, P);
+    }
+    CPM_CUDA_TRY(cudaGetLastError());
+    cudaGraphExec_t gexec = nullptr;
+    CPM_TRY(prepare_graph<K>(s, P, &gexec));
+    const int chunk = graph_chunk(s, P);
     const int64_t max_chunks = (int64_t)P.max_iters / chunk + 2 * P.max_refine + 4;
-    const long long per_graph = (7LL + (P.precond == 2 ? 4LL * (P.sweeps - 1) : 0)) * chunk +
-                                (P.mixed ? 5LL * (chunk / P.refine_every) : 0);
-    count_launches(P.mixed ? 2 : 1);
+    const long long per_graph = graph_launches(s, P);
     bool done = false;
     for (int64_t c = 0; c < max_chunks && !done; ++c) {
         CPM_CUDA_TRY(cudaGraphLaunch(gexec, st));
@@ -1046,18 +1109,10 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
     cudaEventElapsedTime(&ms, s->e0, s->e1);
     int rc = 0;
     for (int j = 0; j < k; ++j) {
-        const Slot &S = s->h_slots[j];
-        int status = (S.phase == PH_DONE) ? S.status : CPM_ERR_TIMEOUT;
-        if (status != 0 && rc == 0) rc = status;
-        if (stats) {
-            stats[j].iterations = S.iters;
-            stats[j].refinements = S.refinements;
-            stats[j].restarts = S.restarts;
-            stats[j].status = status;
-            stats[j].rel_residual = P.mixed ? (S.b64norm2 > 0 ? S.rnorm64 / std::sqrt(S.b64norm2) : 0.0)
-                                            : (S.bnorm2 > 0 ? std::sqrt(S.rr / S.bnorm2) : 0.0);
-            stats[j].seconds = ms * 1e-3;
-        }
+        cpm_solve_stats sj;
+        slot_stats(s->h_slots[j], P.mixed, ms, &sj);
+        if (sj.status != 0 && rc == 0) rc = sj.status;
+        if (stats) stats[j] = sj;
     }
     if (rc) set_error("solve did not converge for every right-hand side (see per-RHS status)");
     return rc;
@@ -1122,6 +1177,204 @@ extern "C" int cpm_solve(cpm_solver_t s, int32_t k, const double *b, double *x, 
 extern "C" int cpm_solver_destroy(cpm_solver_t s) {
     delete s;
     return 0;
+}
+
+// ================================================================= serving
+// Continuous batching over the 32 slots of one mixed-precision solver: a
+// request is admitted into a free slot as soon as one frees up (its column of
+// b is written and the slot alone is started, the other slots keep their
+// state), iteration graphs run while any slot is busy, and finished slots are
+// harvested after every graph.
+
+struct cpm_server_s {
+    cpm_solver_s *solver = nullptr;
+    SolveParams P{};
+    struct Req {
+        int64_t tag;
+        std::vector<double> b;        // host right-hand side, or
+        const double *b_dev = nullptr;  // a device one
+        double *x_dev = nullptr;        // device destination of the solution (else host, via poll)
+        std::chrono::steady_clock::time_point t_submit;
+    };
+    struct Busy {
+        bool used = false;
+        int64_t tag = 0;
+        double *x_dev = nullptr;
+        std::chrono::steady_clock::time_point t_submit, t_admit;
+    };
+    struct Done {
+        int64_t tag;
+        std::vector<double> x;
+        cpm_solve_stats st;
+        double latency;
+    };
+    std::deque<Req> queue;
+    std::vector<Busy> busy;
+    std::deque<Done> done;
+    double *h_stage = nullptr;  // pinned, [32][D]: one staging column per slot
+    DBuf<double> d_stage;       // device, [32][D]
+    ~cpm_server_s() {
+        if (h_stage) cudaFreeHost(h_stage);
+        delete solver;
+    }
+};
+
+extern "C" int cpm_server_create(cpm_opset_t op, double m, double n, const cpm_solve_opts *opts, cpm_server_t *out) {
+    if (!op || !opts || !out) return fail(CPM_ERR_INVALID_ARG, "server_create: null argument");
+    *out = nullptr;
+    if (opts->precision != 1) return fail(CPM_ERR_UNSUPPORTED, "the server runs the mixed-precision path (precision 1)");
+    cpm_server_s *sv = new cpm_server_s();
+    auto bail = [&](int rc) {
+        delete sv;
+        return rc;
+    };
+    int rc = parse_params(opts, sv->P);
+    if (!rc) rc = cpm_solver_create(op, m, n, 32, &sv->solver);
+    if (!rc) rc = alloc_vectors(sv->solver, false, true);
+    if (rc) return bail(rc);
+    const int64_t D = sv->solver->D;
+    if (cudaMallocHost((void **)&sv->h_stage, sizeof(double) * 32 * (size_t)D) != cudaSuccess)
+        return bail(fail(CPM_ERR_OOM, "server_create: pinned staging"));
+    if ((rc = sv->d_stage.alloc(32 * (size_t)D))) return bail(rc);
+    sv->busy.assign(32, cpm_server_s::Busy());
+    for (int j = 0; j < 32; ++j) {
+        memset(&sv->solver->h_slots[j], 0, sizeof(Slot));
+        sv->solver->h_slots[j].phase = PH_IDLE;
+    }
+    CPM_CUDA_TRY(cudaMemcpyAsync(sv->solver->slots.p, sv->solver->h_slots.data(), sizeof(Slot) * 32, cudaMemcpyHostToDevice,
+                                 stream()));
+    cudaGraphExec_t g = nullptr;
+    if ((rc = prepare_graph<32>(sv->solver, sv->P, &g))) return bail(rc);
+    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
+    *out = sv;
+    return 0;
+}
+
+extern "C" int cpm_server_submit(cpm_server_t sv, const double *b, int64_t tag) {
+    if (!sv || !b) return fail(CPM_ERR_INVALID_ARG, "server_submit: null argument");
+    cpm_server_s::Req r;
+    r.tag = tag;
+    r.b.assign(b, b + sv->solver->D);
+    r.t_submit = std::chrono::steady_clock::now();
+    sv->queue.push_back(std::move(r));
+    return 0;
+}
+
+extern "C" int cpm_server_submit_device(cpm_server_t sv, const void *b_dev, void *x_dev, int64_t tag) {
+    if (!sv || !b_dev || !x_dev) return fail(CPM_ERR_INVALID_ARG, "server_submit_device: null argument");
+    cpm_server_s::Req r;
+    r.tag = tag;
+    r.b_dev = (const double *)b_dev;
+    r.x_dev = (double *)x_dev;
+    r.t_submit = std::chrono::steady_clock::now();
+    sv->queue.push_back(std::move(r));
+    return 0;
+}
+
+extern "C" int cpm_server_step(cpm_server_t sv, int32_t *active, int32_t *queued, int32_t *finished) {
+    if (!sv) return fail(CPM_ERR_INVALID_ARG, "server_step: null server");
+    cpm_solver_s *s = sv->solver;
+    const int64_t D = s->D;
+    cudaStream_t st = stream();
+    // admit queued requests into free slots
+    bool admitted = false;
+    for (int j = 0; j < 32 && !sv->queue.empty(); ++j) {
+        if (sv->busy[j].used) continue;
+        cpm_server_s::Req r = std::move(sv->queue.front());
+        sv->queue.pop_front();
+        double *hs = sv->h_stage + (size_t)j * D, *ds = sv->d_stage.p + (size_t)j * D;
+        const double *src = r.b_dev;
+        if (!src) {
+            memcpy(hs, r.b.data(), sizeof(double) * D);
+            CPM_CUDA_TRY(cudaMemcpyAsync(ds, hs, sizeof(double) * D, cudaMemcpyHostToDevice, st));
+            src = ds;
+        }
+        k_scatter_col<<<nblk(D), BS, 0, st>>>(D, 32, j, src, s->b64.p);
+        count_launches(1);
+        memset(&s->h_slots[j], 0, sizeof(Slot));
+        s->h_slots[j].phase = PH_START;
+        CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p + j, &s->h_slots[j], sizeof(Slot), cudaMemcpyHostToDevice, st));
+        sv->busy[j].used = true;
+        sv->busy[j].tag = r.tag;
+        sv->busy[j].x_dev = r.x_dev;
+        sv->busy[j].t_submit = r.t_submit;
+        sv->busy[j].t_admit = std::chrono::steady_clock::now();
+        admitted = true;
+    }
+    if (admitted) mixed_start<32>(s, sv->P);
+    int n_busy = 0;
+    for (int j = 0; j < 32; ++j) n_busy += sv->busy[j].used;
+    if (n_busy) {
+        cudaGraphExec_t g = nullptr;
+        CPM_TRY(prepare_graph<32>(s, sv->P, &g));
+        CPM_CUDA_TRY(cudaGraphLaunch(g, st));
+        count_launches(graph_launches(s, sv->P));
+    }
+    CPM_CUDA_TRY(cudaMemcpyAsync(s->h_slots.data(), s->slots.p, sizeof(Slot) * 32, cudaMemcpyDeviceToHost, st));
+    CPM_CUDA_TRY(cudaStreamSynchronize(st));
+    // harvest finished slots
+    int n_fin = 0;
+    std::vector<int> fin;
+    for (int j = 0; j < 32; ++j) {
+        const Slot &S = s->h_slots[j];
+        if (!sv->busy[j].used) continue;
+        const bool over = S.phase == PH_DONE || S.iters >= sv->P.max_iters || S.refinements >= sv->P.max_refine;
+        if (!over) continue;
+        double *ds = sv->busy[j].x_dev ? sv->busy[j].x_dev : sv->d_stage.p + (size_t)j * D;
+        k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->x64.p, ds);
+        count_launches(1);
+        if (!sv->busy[j].x_dev)
+            CPM_CUDA_TRY(cudaMemcpyAsync(sv->h_stage + (size_t)j * D, ds, sizeof(double) * D, cudaMemcpyDeviceToHost, st));
+        fin.push_back(j);
+    }
+    if (!fin.empty()) {
+        CPM_CUDA_TRY(cudaStreamSynchronize(st));
+        const auto now = std::chrono::steady_clock::now();
+        for (int j : fin) {
+            cpm_server_s::Done d;
+            d.tag = sv->busy[j].tag;
+            if (!sv->busy[j].x_dev) d.x.assign(sv->h_stage + (size_t)j * D, sv->h_stage + (size_t)(j + 1) * D);
+            slot_stats(s->h_slots[j], true, 0.0f, &d.st);
+            d.latency = std::chrono::duration<double>(now - sv->busy[j].t_submit).count();
+            d.st.seconds = std::chrono::duration<double>(now - sv->busy[j].t_admit).count();
+            sv->done.push_back(std::move(d));
+            sv->busy[j].used = false;
+            s->h_slots[j].phase = PH_IDLE;
+            CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p + j, &s->h_slots[j], sizeof(Slot), cudaMemcpyHostToDevice, st));
+            ++n_fin;
+        }
+    }
+    n_busy = 0;
+    for (int j = 0; j < 32; ++j) n_busy += sv->busy[j].used;
+    if (active) *active = n_busy;
+    if (queued) *queued = (int32_t)sv->queue.size();
+    if (finished) *finished = n_fin;
+    return 0;
+}
+
+extern "C" int cpm_server_poll(cpm_server_t sv, int64_t *tag, double *x, cpm_solve_stats *stats, double *latency) {
+    if (!sv) return fail(CPM_ERR_INVALID_ARG, "server_poll: null server");
+    if (sv->done.empty()) return 0;
+    cpm_server_s::Done &d = sv->done.front();
+    if (tag) *tag = d.tag;
+    if (x && !d.x.empty()) memcpy(x, d.x.data(), sizeof(double) * d.x.size());
+    if (stats) *stats = d.st;
+    if (latency) *latency = d.latency;
+    sv->done.pop_front();
+    return 1;
+}
+
+extern "C" int cpm_server_destroy(cpm_server_t sv) {
+    if (sv) cudaStreamSynchronize(stream());
+    delete sv;
+    return 0;
+}
+
+extern "C" int64_t cpm_server_device_bytes(cpm_opset_t op) {
+    if (!op) return -1;
+    const int64_t D = op->D;
+    // FP32 Krylov vectors (10), FP64 b, x, r, E~x (4), staging, reduction scratch
+    return D * 32 * (10 * 4 + 4 * 8 + 8) + D * (8 + 4) + (int64_t)(1 << 20);
 }
 
 // ================================================================= apply

@@ -127,6 +127,14 @@ def lib():
         L.cpm_solve.argtypes = [vp, ctypes.c_int32, vp, vp, P(SolveOpts), P(SolveStats)]
         L.cpm_solve_device.argtypes = [vp, ctypes.c_int32, vp, vp, P(SolveOpts), P(SolveStats)]
         L.cpm_solver_destroy.argtypes = [vp]
+        L.cpm_server_create.argtypes = [vp, ctypes.c_double, ctypes.c_double, P(SolveOpts), P(vp)]
+        L.cpm_server_submit.argtypes = [vp, vp, ctypes.c_int64]
+        L.cpm_server_submit_device.argtypes = [vp, vp, vp, ctypes.c_int64]
+        L.cpm_server_step.argtypes = [vp, vp, vp, vp]
+        L.cpm_server_poll.argtypes = [vp, vp, vp, P(SolveStats), vp]
+        L.cpm_server_destroy.argtypes = [vp]
+        L.cpm_server_device_bytes.argtypes = [vp]
+        L.cpm_server_device_bytes.restype = ctypes.c_int64
         _lib = L
     return _lib
 
@@ -354,3 +362,71 @@ class Solver:
         if rc != 0:
             raise CpmError(rc, lib().cpm_last_error().decode() + f" stats={stats}")
         return stats
+
+
+class Server:
+    """Continuous batching of right-hand sides on one operator (m, n): up to 32
+    in flight in the mixed-precision solver, admitted as slots free up."""
+
+    def __init__(self, opset, m, n, tol=1e-10, inner_tol=0.2, max_refine=400, refine_every=0, max_iters=100000):
+        self.opset, self.D = opset, opset.D
+        o = SolveOpts(tol=tol, max_iters=max_iters, precision=1, precond=DIAGONAL, precond_iters=0,
+                      inner_tol=inner_tol, max_refine=max_refine, refine_every=refine_every)
+        h = ctypes.c_void_p()
+        _check(lib().cpm_server_create(opset.h, m, n, ctypes.byref(o), ctypes.byref(h)))
+        self.h = h
+
+    @staticmethod
+    def device_bytes(opset):
+        return int(lib().cpm_server_device_bytes(opset.h))
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().cpm_server_destroy(self.h)
+        except Exception:
+            pass
+
+    def submit(self, b, tag):
+        b = np.ascontiguousarray(b, np.float64)
+        assert b.shape == (self.D,)
+        _check(lib().cpm_server_submit(self.h, _p(b), int(tag)))
+
+    def submit_device(self, b_ptr, x_ptr, tag):
+        """device right-hand side and solution destination (D doubles each)"""
+        _check(lib().cpm_server_submit_device(self.h, b_ptr, x_ptr, int(tag)))
+
+    def step(self):
+        """one admission + iteration-graph + harvest round: (active, queued, finished)"""
+        a, q, f = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().cpm_server_step(self.h, ctypes.byref(a), ctypes.byref(q), ctypes.byref(f)))
+        return a.value, q.value, f.value
+
+    def poll(self, want_x=True):
+        """pop one finished request: (tag, x or None, stats) or None"""
+        tag = ctypes.c_int64()
+        x = np.empty(self.D) if want_x else None
+        st = SolveStats()
+        lat = ctypes.c_double()
+        got = lib().cpm_server_poll(self.h, ctypes.byref(tag), _p(x) if want_x else None, ctypes.byref(st),
+                                    ctypes.byref(lat))
+        if got < 0:
+            _check(got)
+        if got == 0:
+            return None
+        return tag.value, x, dict(iterations=st.iterations, refinements=st.refinements, restarts=st.restarts,
+                                  status=st.status, rel_residual=st.rel_residual, service=st.seconds,
+                                  latency=lat.value)
+
+    def drain(self, want_x=True):
+        """step until every submitted request has finished; returns {tag: (x, stats)}"""
+        out = {}
+        while True:
+            a, q, _ = self.step()
+            while True:
+                r = self.poll(want_x)
+                if r is None:
+                    break
+                out[r[0]] = (r[1], r[2])
+            if a == 0 and q == 0:
+                return out

@@ -236,6 +236,30 @@ int cpm_geodesic_run(cpm_geodesic_t g, double dt, int32_t precision, double tol,
                      int32_t *iters_out);
 int cpm_geodesic_destroy(cpm_geodesic_t g);
 
+/* ---- Serving: continuous batching ------------------------------------------
+ * No counterpart in the reference (its Solve is one blocking call per RHS,
+ * src/Solver.cpp:104-113).  A server owns a 32-slot mixed-precision solver
+ * (opts->precision must be 1) on one operator (opset, m, n).  submit queues a
+ * right-hand side (D doubles, copied) with a caller tag; step admits queued
+ * requests into free slots (each slot starts alone; the others keep their
+ * state), runs one iteration graph if any slot is busy, and harvests finished
+ * slots; poll pops one finished request (returns 1, or 0 if none) with its
+ * solution (D doubles, caller buffer or NULL), stats (stats.seconds = time
+ * from admission into a slot to harvest) and latency (seconds from submit to
+ * harvest, queueing included).  submit_device takes a device right-hand side
+ * (D doubles, read when the request is admitted) and a device destination for
+ * its solution (written when it finishes; poll then returns no x).
+ * device_bytes estimates the device memory a server on `op` allocates, for
+ * admission by free HBM. */
+typedef struct cpm_server_s *cpm_server_t;
+int cpm_server_create(cpm_opset_t op, double m, double n, const cpm_solve_opts *opts, cpm_server_t *out);
+int cpm_server_submit(cpm_server_t s, const double *b, int64_t tag);
+int cpm_server_submit_device(cpm_server_t s, const void *b_dev, void *x_dev, int64_t tag);
+int cpm_server_step(cpm_server_t s, int32_t *active, int32_t *queued, int32_t *finished);
+int cpm_server_poll(cpm_server_t s, int64_t *tag, double *x, cpm_solve_stats *stats, double *latency);
+int cpm_server_destroy(cpm_server_t s);
+int64_t cpm_server_device_bytes(cpm_opset_t op);
+
 /* Synchronise the library stream. */
 int cpm_sync(void);
 
