@@ -47,7 +47,10 @@ struct Slot {
     double rho, rho_old, alpha, omega, beta;
     double bnorm2, r0norm2, rr, tol2, rr_max;
     double scale, rnorm64, outer_tol2, b64norm2;
-    int phase, iters, inner_iters, refinements, restarts, status, krylov_restart, pad1;
+    double rr_upd;  // mixed path: FP32 residual norm^2 right after the last reliable update
+    double rbest;   // mixed path: smallest FP64 true residual norm so far
+    int phase, iters, inner_iters, refinements, restarts, status, krylov_restart;
+    int stall;      // mixed path: reliable updates since rbest last improved by 10%
 };
 
 struct SolveParams {
@@ -318,6 +321,7 @@ __global__ void __launch_bounds__(BS, 4) k_init(OpView<T> op, Slot *sl, SolvePar
         S.r0norm2 = b2;
         S.rr = b2;
         S.rr_max = b2;
+        S.rr_upd = b2;
         S.rho_old = 1.0;
         S.alpha = 1.0;
         S.omega = 1.0;
@@ -332,12 +336,17 @@ __global__ void __launch_bounds__(BS, 4) k_init(OpView<T> op, Slot *sl, SolvePar
             S.restarts = 0;
             S.refinements = 0;
         }
+        if (!isfinite(b2)) {  // a non-finite right-hand side never counts as converged
+            S.phase = PH_DONE;
+            S.status = CPM_ERR_BREAKDOWN;
+            return;
+        }
         if (b2 == 0.0) {  // src/BiCGStab.h:53: x = 0, converged
             S.phase = (from_phase == PH_INNER_INIT) ? PH_REFINE : PH_DONE;
             S.status = 0;
             return;
         }
-        if (!(S.rr > S.tol2)) {
+        if (S.rr <= S.tol2) {
             S.phase = (from_phase == PH_INNER_INIT) ? PH_REFINE : PH_DONE;
             return;
         }
@@ -412,6 +421,15 @@ __global__ void __launch_bounds__(BS, 4) k_apply_alpha(OpView<T> op, Slot *sl, T
         Slot &S = sl[threadIdx.x];
         if (S.phase != PH_ITER) return;
         S.alpha = S.rho / tot[0];
+        if constexpr (sizeof(T) == 4) {
+            // FP32 inner iteration: r0 . v = 0 (or a non-finite value) ends this
+            // Krylov space; the FP64 reliable update restarts it from the true residual
+            if (!isfinite(S.alpha)) {
+                S.krylov_restart = 1;
+                S.rho_old = S.rho;
+                S.phase = PH_REFINE;
+            }
+        }
     }
 }
 
@@ -553,13 +571,23 @@ __global__ void __launch_bounds__(BS, 4) k_update_xr(int64_t D, Slot *sl, SolveP
         S.iters += 1;
         S.inner_iters += 1;
         S.rr = tot[0];
-        const bool conv = !(S.rr > S.tol2);
+        const bool conv = S.rr <= S.tol2;  // false for a non-finite residual
         if (P.mixed) {
             S.rr_max = fmax(S.rr_max, S.rr);
             // a slot whose FP32 residual claims convergence waits for the next
             // reliable update; one whose residual merely fell by delta keeps
             // iterating until then (k_refine_gate)
             if (conv || S.iters >= P.max_iters || !isfinite(S.rr)) {
+                S.rho_old = S.rho;
+                S.phase = PH_REFINE;
+                return;
+            }
+            // an FP32 residual 10^4 times larger than right after the last
+            // reliable update has diverged (BiCGStab residuals may spike by
+            // a few orders of magnitude and recover; this does not): restart
+            // the Krylov space from the FP64 true residual
+            if (S.rr > 1e8 * S.rr_upd) {
+                S.krylov_restart = 1;
                 S.rho_old = S.rho;
                 S.phase = PH_REFINE;
                 return;
@@ -682,10 +710,19 @@ __global__ void __launch_bounds__(BS, 4) k_refine_residual(OpView<double> op, Sl
         if (S.phase != PH_REFINE) return;
         S.refinements += 1;
         S.rnorm64 = sqrt(tot[0]);
-        if (!(tot[0] > S.outer_tol2)) {
+        if (S.rnorm64 < 0.9 * S.rbest) {
+            S.rbest = S.rnorm64;
+            S.stall = 0;
+        } else {
+            S.stall += 1;
+        }
+        if (tot[0] <= S.outer_tol2) {
             S.phase = PH_DONE;
             S.status = 0;
-        } else if (S.refinements >= P.max_refine || S.iters >= P.max_iters || !isfinite(tot[0])) {
+        } else if (S.refinements >= P.max_refine || S.iters >= P.max_iters || !isfinite(tot[0]) || S.stall >= 40 ||
+                   S.rnorm64 > 1e6 * sqrt(S.b64norm2)) {
+            // out of budget, non-finite, no 10% gain of the true residual in 40
+            // reliable updates, or diverged: the FP32 iteration cannot solve this system
             S.phase = PH_DONE;
             S.status = isfinite(tot[0]) ? CPM_ERR_NOT_CONVERGED : CPM_ERR_BREAKDOWN;
         } else {
@@ -739,6 +776,7 @@ __global__ void __launch_bounds__(BS, 4) k_reliable(int64_t D, Slot *sl, const d
         if (S.phase != PH_RELIABLE) return;
         S.rr = tot[0];
         S.rr_max = tot[0];
+        S.rr_upd = tot[0];
         if (S.krylov_restart) {
             S.krylov_restart = 0;
             S.restarts += 1;
@@ -786,12 +824,19 @@ __global__ void __launch_bounds__(BS, 4) k_mixed_start(int64_t D, Slot *sl, Solv
         S.refinements = 0;
         S.restarts = 0;
         S.rnorm64 = sqrt(tot[0]);
+        if (!isfinite(tot[0])) {
+            S.phase = PH_DONE;
+            S.status = CPM_ERR_BREAKDOWN;
+            return;
+        }
         if (tot[0] == 0.0) {
             S.phase = PH_DONE;
             S.status = 0;
             return;
         }
         S.scale = S.rnorm64;
+        S.rbest = S.rnorm64;
+        S.stall = 0;
         S.phase = PH_INNER_INIT;
     }
 }
@@ -1057,17 +1102,19 @@ static void slot_stats(const Slot &S, bool mixed, float ms, cpm_solve_stats *st)
     st->rel_residual = mixed ? (S.b64norm2 > 0 ? S.rnorm64 / std::sqrt(S.b64norm2) : 0.0)
                              : (S.bnorm2 > 0 ? std::sqrt(S.rr / S.bnorm2) : 0.0);
     st->seconds = ms * 1e-3;
+    st->fp64_fallback = 0;
+    st->pad = 0;
 }
 
+// One pass of the slot loop for the slots in `active` (others idle): the
+// start kernels, then iteration graphs until every active slot is done.
 template <int K>
-static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_stats *stats) {
-    SolveParams P;
-    CPM_TRY(parse_params(o, P));
+static int solve_pass(cpm_solver_s *s, const SolveParams &P, const std::vector<char> &active, float *ms) {
     CPM_TRY(alloc_vectors(s, !P.mixed, P.mixed));
     cudaStream_t st = stream();
     for (int j = 0; j < K; ++j) {
         memset(&s->h_slots[j], 0, sizeof(Slot));
-        s->h_slots[j].phase = (j < k) ? (P.mixed ? PH_START : PH_ITER) : PH_IDLE;
+        s->h_slots[j].phase = active[j] ? (P.mixed ? PH_START : PH_ITER) : PH_IDLE;
     }
     CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p, s->h_slots.data(), sizeof(Slot) * K, cudaMemcpyHostToDevice, st));
     CPM_CUDA_TRY(cudaEventRecord(s->e0, st));
@@ -1105,14 +1152,52 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
     }
     CPM_CUDA_TRY(cudaEventRecord(s->e1, st));
     CPM_CUDA_TRY(cudaEventSynchronize(s->e1));
+    *ms = 0;
+    cudaEventElapsedTime(ms, s->e0, s->e1);
+    return 0;
+}
+
+// Solve k right-hand sides.  A mixed-precision slot that does not converge
+// (an FP32 inner iteration that cannot follow an ill-conditioned system, where
+// cond * 2^-24 ~ 1) is solved again by the plain FP64 path from x = 0; its
+// stats then carry fp64_fallback = 1 and both passes' iterations.
+template <int K>
+static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_stats *stats) {
+    SolveParams P;
+    CPM_TRY(parse_params(o, P));
+    std::vector<char> active(K, 0);
+    for (int j = 0; j < k; ++j) active[j] = 1;
     float ms = 0;
-    cudaEventElapsedTime(&ms, s->e0, s->e1);
+    CPM_TRY(solve_pass<K>(s, P, active, &ms));
+    std::vector<cpm_solve_stats> st(K);
+    std::vector<char> redo(K, 0);
+    bool any_redo = false;
+    for (int j = 0; j < k; ++j) {
+        slot_stats(s->h_slots[j], P.mixed, ms, &st[j]);
+        if (P.mixed && st[j].status != 0) redo[j] = any_redo = true;
+    }
+    if (any_redo) {
+        SolveParams P64 = P;
+        P64.mixed = 0;
+        float ms64 = 0;
+        CPM_TRY(solve_pass<K>(s, P64, redo, &ms64));
+        for (int j = 0; j < k; ++j) {
+            if (!redo[j]) {
+                st[j].seconds += ms64 * 1e-3;
+                continue;
+            }
+            cpm_solve_stats s64;
+            slot_stats(s->h_slots[j], false, ms + ms64, &s64);
+            s64.iterations += st[j].iterations;
+            s64.refinements = st[j].refinements;
+            s64.fp64_fallback = 1;
+            st[j] = s64;
+        }
+    }
     int rc = 0;
     for (int j = 0; j < k; ++j) {
-        cpm_solve_stats sj;
-        slot_stats(s->h_slots[j], P.mixed, ms, &sj);
-        if (sj.status != 0 && rc == 0) rc = sj.status;
-        if (stats) stats[j] = sj;
+        if (st[j].status != 0 && rc == 0) rc = st[j].status;
+        if (stats) stats[j] = st[j];
     }
     if (rc) set_error("solve did not converge for every right-hand side (see per-RHS status)");
     return rc;
@@ -1188,7 +1273,9 @@ extern "C" int cpm_solver_destroy(cpm_solver_t s) {
 
 struct cpm_server_s {
     cpm_solver_s *solver = nullptr;
+    cpm_solver_s *fallback = nullptr;  // 1-slot solver for requests the mixed path cannot converge
     SolveParams P{};
+    cpm_solve_opts opts{};
     struct Req {
         int64_t tag;
         std::vector<double> b;        // host right-hand side, or
@@ -1216,6 +1303,7 @@ struct cpm_server_s {
     ~cpm_server_s() {
         if (h_stage) cudaFreeHost(h_stage);
         delete solver;
+        delete fallback;
     }
 };
 
@@ -1228,6 +1316,7 @@ extern "C" int cpm_server_create(cpm_opset_t op, double m, double n, const cpm_s
         delete sv;
         return rc;
     };
+    sv->opts = *opts;
     int rc = parse_params(opts, sv->P);
     if (!rc) rc = cpm_solver_create(op, m, n, 32, &sv->solver);
     if (!rc) rc = alloc_vectors(sv->solver, false, true);
@@ -1315,14 +1404,29 @@ extern "C" int cpm_server_step(cpm_server_t sv, int32_t *active, int32_t *queued
     // harvest finished slots
     int n_fin = 0;
     std::vector<int> fin;
+    std::vector<cpm_solve_stats> fb_st(32);
+    std::vector<char> fb(32, 0);
     for (int j = 0; j < 32; ++j) {
         const Slot &S = s->h_slots[j];
         if (!sv->busy[j].used) continue;
         const bool over = S.phase == PH_DONE || S.iters >= sv->P.max_iters || S.refinements >= sv->P.max_refine;
         if (!over) continue;
         double *ds = sv->busy[j].x_dev ? sv->busy[j].x_dev : sv->d_stage.p + (size_t)j * D;
-        k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->x64.p, ds);
-        count_launches(1);
+        if (S.phase == PH_DONE && S.status == 0) {
+            k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->x64.p, ds);
+            count_launches(1);
+        } else {
+            // the FP32 inner iteration could not solve this right-hand side:
+            // solve it again with the plain FP64 path (one slot, blocking)
+            if (!sv->fallback) CPM_TRY(cpm_solver_create(s->op, s->m, s->n, 1, &sv->fallback));
+            double *bj = sv->d_stage.p + (size_t)j * D;
+            k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->b64.p, bj);
+            count_launches(1);
+            cpm_solve_opts o64 = sv->opts;
+            o64.precision = 0;
+            CPM_TRY(cpm_solve_device(sv->fallback, 1, bj, ds, &o64, &fb_st[j]));
+            fb[j] = 1;
+        }
         if (!sv->busy[j].x_dev)
             CPM_CUDA_TRY(cudaMemcpyAsync(sv->h_stage + (size_t)j * D, ds, sizeof(double) * D, cudaMemcpyDeviceToHost, st));
         fin.push_back(j);
@@ -1335,6 +1439,13 @@ extern "C" int cpm_server_step(cpm_server_t sv, int32_t *active, int32_t *queued
             d.tag = sv->busy[j].tag;
             if (!sv->busy[j].x_dev) d.x.assign(sv->h_stage + (size_t)j * D, sv->h_stage + (size_t)(j + 1) * D);
             slot_stats(s->h_slots[j], true, 0.0f, &d.st);
+            if (fb[j]) {
+                const int it = d.st.iterations, rf = d.st.refinements;
+                d.st = fb_st[j];
+                d.st.iterations += it;
+                d.st.refinements = rf;
+                d.st.fp64_fallback = 1;
+            }
             d.latency = std::chrono::duration<double>(now - sv->busy[j].t_submit).count();
             d.st.seconds = std::chrono::duration<double>(now - sv->busy[j].t_admit).count();
             sv->done.push_back(std::move(d));

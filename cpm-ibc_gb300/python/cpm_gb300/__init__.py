@@ -63,7 +63,8 @@ class SolveOpts(ctypes.Structure):
 
 class SolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("refinements", ctypes.c_int32), ("restarts", ctypes.c_int32),
-                ("status", ctypes.c_int32), ("rel_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
+                ("status", ctypes.c_int32), ("rel_residual", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("fp64_fallback", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 def desc(kind, params=(), bbox=(-1.0, 1.0), boundary_order=1, on_ibc_tolerance=0.0, verts=None, prims=None,
@@ -346,7 +347,8 @@ class Solver:
         st = (SolveStats * k)()
         rc = lib().cpm_solve(self.h, k, _p(b), _p(x), ctypes.byref(o), st)
         stats = [dict(iterations=s.iterations, refinements=s.refinements, restarts=s.restarts, status=s.status,
-                      rel_residual=s.rel_residual, seconds=s.seconds) for s in st]
+                      rel_residual=s.rel_residual, seconds=s.seconds,
+                      fp64_fallback=s.fp64_fallback) for s in st]
         if rc != 0 and raise_on_error:
             raise CpmError(rc, lib().cpm_last_error().decode() + f" stats={stats}")
         return x, stats
@@ -358,7 +360,8 @@ class Solver:
         st = (SolveStats * k)()
         rc = lib().cpm_solve_device(self.h, k, b_ptr, x_ptr, ctypes.byref(o), st)
         stats = [dict(iterations=s.iterations, refinements=s.refinements, restarts=s.restarts, status=s.status,
-                      rel_residual=s.rel_residual, seconds=s.seconds) for s in st]
+                      rel_residual=s.rel_residual, seconds=s.seconds,
+                      fp64_fallback=s.fp64_fallback) for s in st]
         if rc != 0:
             raise CpmError(rc, lib().cpm_last_error().decode() + f" stats={stats}")
         return stats

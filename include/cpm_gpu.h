@@ -203,6 +203,9 @@ typedef struct cpm_solve_stats {
     int32_t status;          /* cpm_status of this right-hand side */
     double rel_residual;     /* final ||b - A x|| / ||b|| in FP64 */
     double seconds;          /* device time of the solve */
+    int32_t fp64_fallback;   /* precision 1: 1 if the mixed solve did not converge and the plain
+                                FP64 path solved this right-hand side again from x = 0 */
+    int32_t pad;
 } cpm_solve_stats;
 
 /* Solver::Init(m, n, L, E, precond, identity_rows) (src/Solver.cpp:8-68):
@@ -243,7 +246,8 @@ int cpm_geodesic_destroy(cpm_geodesic_t g);
  * right-hand side (D doubles, copied) with a caller tag; step admits queued
  * requests into free slots (each slot starts alone; the others keep their
  * state), runs one iteration graph if any slot is busy, and harvests finished
- * slots; poll pops one finished request (returns 1, or 0 if none) with its
+ * slots (a request the mixed path cannot converge is solved again by a 1-slot
+ * plain FP64 solver at harvest, stats.fp64_fallback = 1); poll pops one finished request (returns 1, or 0 if none) with its
  * solution (D doubles, caller buffer or NULL), stats (stats.seconds = time
  * from admission into a slot to harvest) and latency (seconds from submit to
  * harvest, queueing included).  submit_device takes a device right-hand side
