@@ -6,15 +6,22 @@ circles z = 0.3 and z = -0.5, dx = 0.025 (~166k tube nodes, 215,662 rows with
 the IBC DOF and Dirichlet value rows), tricubic extension, 2nd-order IBCs.
 Requests are right-hand sides with random circle values U[0,1] (seeded).
 
-A step solves one batch of 32 right-hand sides with the batched path: FP32
+A step is 32 requests served by the continuous-batching server: FP32
 BiCGStab inside FP64 iterative refinement to ||b - A x|| <= 1e-10 ||b||
-(the reference's relative residual).  `value` is solves/s of that path with
-inputs resident in HBM (device time, CUDA events on the library stream, L2
-flushed between steps).  Reported beside it: the plain FP64 one-request-at-a-
-time GPU path (the reference algorithm on the device), latencies, the error
-against the FP64 solutions, the L.E apply roofline and the CPU baseline (the
-oracle — the C++ restatement of the reference's custom solver — on the
-host's cores).  `--impl reference` times the CPU restatement alone.
+(the reference's relative residual), slots refilled as solves finish.
+`value` is solves/s with every right-hand side resident in HBM (CUDA events on
+the library stream).  Reported beside it: the plain FP64 one-request-at-a-time
+GPU path (the reference algorithm on the device), latencies, the error against
+the FP64 solutions, one static batch of 32, the end-to-end number through the
+C-ABI with host buffers, the L.E apply roofline and the CPU baseline (the
+oracle, the C++ restatement of the reference's custom solver, on the host's
+cores).  `--impl reference` times the CPU restatement alone.
+
+`--workload torus-geodesic | mesh-curves | serving-mix` prints one line for
+the other configurations instead: the heat-method geodesic on the torus
+R = 1, r = 0.4 at dx = 0.01; diffusion curves on the perturbed icosphere mesh
+(327,680 triangles, 16 polyline IBCs, 3 right-hand sides) at dx = 0.005; and
+a seeded Poisson stream of requests over the sphere, torus and mesh.
 """
 import argparse
 import json
@@ -225,6 +232,122 @@ def run_profile(what):
     torch.cuda.synchronize()
 
 
+def run_workload(args):
+    """One JSON line for a configuration other than the headline one."""
+    import build_ext
+
+    build_ext.build()
+    import cpm_gb300 as cg
+    from cpm_gb300 import serving as SV
+    from cpm_gb300 import workloads as W
+
+    cg.set_device(0)
+    line = {"workload": args.workload, "n_gpus": 1, "data": "synthetic"}
+    if args.workload == "torus-geodesic":
+        dx = 0.01
+        t = time.perf_counter()
+        T = cg.Tube(cg.desc(cg.TORUS, [1.0, 0.4], (-1.4, 1.4)), 3, dx)
+        cg.sync()
+        t_tube = time.perf_counter() - t
+        cp = T.export()["cp"]
+        src = cp[np.random.default_rng(12).integers(T.N)]
+        t = time.perf_counter()
+        G = cg.Geodesic(T, src)
+        t_setup = time.perf_counter() - t
+        res = {}
+        for prec in (0, 1):
+            G.run(dx * dx, precision=prec)  # warm-up (graph capture)
+            t = time.perf_counter()
+            phi, its = G.run(dx * dx, precision=prec)
+            res[prec] = (time.perf_counter() - t, phi, its)
+        line.update({
+            "config": {"surface": "torus R=1 r=0.4", "dx": dx, "tube_nodes": T.N, "rows": G.D,
+                       "source": "seeded random tube node's closest point", "dt": dx * dx,
+                       "heat_step": "FP64, 2000 damped Jacobi sweeps per preconditioner call"},
+            "tube_build_s": t_tube, "geodesic_setup_s": t_setup,
+            "fp64": {"seconds": res[0][0], "iterations": res[0][2]},
+            "mixed": {"seconds": res[1][0], "iterations": res[1][2]},
+            "mixed_rel_err_vs_fp64": float(np.max(np.abs(res[1][1] - res[0][1])) / np.max(np.abs(res[0][1]))),
+            "note": "Poisson steps whose FP32 inner iteration cannot converge are re-solved in FP64 (fp64_fallback)",
+        })
+    elif args.workload == "mesh-curves":
+        dx = 0.005
+        t = time.perf_counter()
+        v, f = W.perturbed_icosphere(7, seed=3)
+        bb = W.mesh_bbox(v)
+        T = cg.Tube(cg.desc(cg.TRIANGULATION, (), bb, verts=v, prims=f), 3, dx)
+        cg.sync()
+        t_tube = time.perf_counter() - t
+        curves, _ = W.parallel_plane_curves(v, f, 16, seed=4)
+        t = time.perf_counter()
+        O = cg.OpSet(T, [cg.desc(cg.POLYLINE, (), bb, boundary_order=2, on_ibc_tolerance=0.1 * dx * dx, verts=p,
+                                 prims=sg) for p, sg in curves])
+        cg.sync()
+        t_ops = time.perf_counter() - t
+        rows = O.rows()
+        rgb = np.random.default_rng(9).uniform(0, 1, (16, 3))
+        B = np.zeros((3, O.D))
+        d = rows["kind"] == 2
+        for ch in range(3):
+            B[ch][d] = rgb[rows["ibc"][d], ch]
+        S32 = cg.Solver(O, 0.0, -1.0, kslots=32)
+        S32.solve(B, tol=TOL, precision=1)
+        t = time.perf_counter()
+        X32, st32 = S32.solve(B, tol=TOL, precision=1)
+        t_mixed = time.perf_counter() - t
+        S1 = cg.Solver(O, 0.0, -1.0, kslots=1)
+        t = time.perf_counter()
+        X64, st64 = [], []
+        for ch in range(3):
+            x, st = S1.solve(B[ch], tol=TOL, precision=0)
+            X64.append(x[0])
+            st64.append(st[0])
+        t_fp64 = time.perf_counter() - t
+        line.update({
+            "config": {"surface": "perturbed icosphere level 7 (327,680 triangles), 8 real SH l<=6, amplitude 0.1",
+                       "dx": dx, "tube_nodes": T.N, "rows": O.D, "ibc_dofs": O.total_ibc_dofs, "curves": 16,
+                       "rhs": 3},
+            "tube_build_s": t_tube, "operator_build_s": t_ops,
+            "mixed_batched_3": {"seconds": t_mixed, "solves_per_s": 3 / t_mixed,
+                                "iterations": [s_["iterations"] for s_ in st32],
+                                "fp64_fallbacks": sum(s_["fp64_fallback"] for s_ in st32)},
+            "fp64_one_at_a_time": {"seconds": t_fp64, "solves_per_s": 3 / t_fp64,
+                                   "iterations": [s_["iterations"] for s_ in st64]},
+            "mixed_rel_err_vs_fp64": float(max(np.max(np.abs(X32[c] - X64[c])) / np.max(np.abs(X64[c]))
+                                               for c in range(3))),
+        })
+    else:  # serving-mix
+        t = time.perf_counter()
+        surfaces = W.serving_surfaces(cg)
+        t_setup = time.perf_counter() - t
+        loop = SV.ServingLoop(surfaces)
+        reqs = SV.poisson_stream(surfaces, args.requests, rate=args.rate, geodesic_every=32, seed=11)
+        warm = SV.poisson_stream(surfaces, 12, rate=0.0, geodesic_every=0, seed=12)
+        for r in warm:
+            r["id"] = -1 - r["id"]
+        loop.run(warm)
+        t = time.perf_counter()
+        out = loop.run(reqs)
+        span = time.perf_counter() - t
+        lat = {k: [o["latency"] for o in out.values() if o["kind"] == k] for k in ("laplace", "geodesic")}
+        fb = sum(1 for o in out.values() if o["kind"] == "laplace" and o["stats"].get("fp64_fallback"))
+        sample = [r for r in reqs if r["kind"] == "laplace"][:12]
+        t64 = SV.fp64_one_at_a_time(surfaces, sample)
+        line.update({
+            "config": {"surfaces": {s.name: {"tube_nodes": s.tube.N, "rows": s.opset.D, "curves": s.n_ibc,
+                                             "server_bytes": s.bytes} for s in surfaces},
+                       "requests": args.requests, "rate_per_s": args.rate, "geodesic_every": 32,
+                       "arrivals": "seeded Poisson process", "slots_per_surface": 32, "tol": TOL},
+            "setup_s": t_setup, "makespan_s": span, "solves_per_s": len(out) / span,
+            "latency_ms": {k: {"p50": float(np.percentile(v, 50) * 1e3), "p99": float(np.percentile(v, 99) * 1e3),
+                               "n": len(v)} for k, v in lat.items() if v},
+            "laplace_fp64_fallbacks": fb, "admissions": loop.admissions, "evictions": loop.evictions,
+            "fp64_one_at_a_time_laplace_solves_per_s": len(t64) / sum(t64),
+            "note": "geodesics run one at a time on their own point-IBC operator between server steps",
+        })
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -235,7 +358,13 @@ def main():
     ap.add_argument("--plain-solves", type=int, default=8)
     ap.add_argument("--profile", choices=["apply", "solve"], default=None,
                     help="run only a few applies (or one batched solve) of the workload, for ncu")
+    ap.add_argument("--workload", choices=["torus-geodesic", "mesh-curves", "serving-mix"], default=None,
+                    help="one line for another configuration instead of the headline benchmark")
+    ap.add_argument("--requests", type=int, default=256, help="serving-mix: requests in the stream")
+    ap.add_argument("--rate", type=float, default=40.0, help="serving-mix: mean arrivals per second")
     args = ap.parse_args()
+    if args.workload:
+        return run_workload(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.profile:

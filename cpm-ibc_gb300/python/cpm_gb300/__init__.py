@@ -419,7 +419,7 @@ class Server:
             return None
         return tag.value, x, dict(iterations=st.iterations, refinements=st.refinements, restarts=st.restarts,
                                   status=st.status, rel_residual=st.rel_residual, service=st.seconds,
-                                  latency=lat.value)
+                                  latency=lat.value, fp64_fallback=st.fp64_fallback)
 
     def drain(self, want_x=True):
         """step until every submitted request has finished; returns {tag: (x, stats)}"""

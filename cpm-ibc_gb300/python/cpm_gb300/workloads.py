@@ -187,3 +187,40 @@ def parallel_plane_curves(verts, faces, count, seed=0, spread=0.8):
         loops = plane_loops(verts, faces, n, off)
         curves.append(max(loops, key=lambda lp: len(lp[0])))
     return curves, n
+
+
+# ---------------------------------------------------------------- the serving mix
+
+
+def serving_surfaces(cg, dx_scale=1.0, mesh_level=7, n_curves=16, seed=3):
+    """The three surfaces of the serving stream, each with fixed Dirichlet IBC
+    curves (order 2, on_ibc_tolerance 0.1 dx^2):
+
+    * the unit sphere at dx = 0.025 with the circles z = 0.3 and z = -0.5;
+    * the torus R = 1, r = 0.4 at dx = 0.01 with its outer and inner equators;
+    * the perturbed icosphere (``perturbed_icosphere(mesh_level)``) at
+      dx = 0.005 with ``n_curves`` parallel plane cuts.
+
+    dx_scale multiplies every dx (smaller configurations for tests)."""
+    from .serving import ServedSurface
+
+    def circ(R, z, dx, bb):
+        return cg.desc(cg.CIRCLE3D, [R, 0, 0, z, 0, 0, 1], bb, boundary_order=2, on_ibc_tolerance=0.1 * dx * dx)
+
+    out = []
+    dx = 0.025 * dx_scale
+    T = cg.Tube(cg.desc(cg.SPHERE, [1.0]), 3, dx)
+    out.append(ServedSurface("sphere", T, [circ(math.sqrt(1 - 0.09), 0.3, dx, (-1.0, 1.0)),
+                                           circ(math.sqrt(1 - 0.25), -0.5, dx, (-1.0, 1.0))]))
+    dx = 0.01 * dx_scale
+    bb = (-1.4, 1.4)
+    T = cg.Tube(cg.desc(cg.TORUS, [1.0, 0.4], bb), 3, dx)
+    out.append(ServedSurface("torus", T, [circ(1.4, 0.0, dx, bb), circ(0.6, 0.0, dx, bb)]))
+    dx = 0.005 * dx_scale
+    v, f = perturbed_icosphere(mesh_level, seed=seed)
+    bb = mesh_bbox(v)
+    T = cg.Tube(cg.desc(cg.TRIANGULATION, (), bb, verts=v, prims=f), 3, dx)
+    curves, _ = parallel_plane_curves(v, f, n_curves, seed=seed + 1)
+    out.append(ServedSurface("mesh", T, [cg.desc(cg.POLYLINE, (), bb, boundary_order=2, on_ibc_tolerance=0.1 * dx * dx,
+                                                 verts=p, prims=s) for p, s in curves]))
+    return out

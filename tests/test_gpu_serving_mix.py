@@ -1,0 +1,38 @@
+"""The serving mix at reduced size: three device-resident surfaces with their
+IBC curves, a seeded Poisson stream of IBC-Laplace and geodesic requests, and
+an HBM budget that holds only two servers at a time (so servers are released
+and admitted while the stream runs).
+
+Tolerances: every Laplace result within 1e-8 relative l_inf of the plain FP64
+device solve of the same right-hand side; every geodesic within 1e-8 of the
+FP64 geodesic from the same source."""
+import numpy as np
+import pytest
+
+from cpm_gb300 import serving as SV
+from cpm_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def test_serving_mix_results_and_admission(gpu):
+    surfaces = W.serving_surfaces(gpu, dx_scale=5.0, mesh_level=3, n_curves=2)
+    by = {s.name: s for s in surfaces}
+    sizes = sorted(s.bytes for s in surfaces)
+    loop = SV.ServingLoop(surfaces, hbm_budget=sizes[-1] + sizes[-2])
+    reqs = SV.poisson_stream(surfaces, 48, rate=400.0, geodesic_every=16, seed=2)
+    out = loop.run(reqs, keep_solutions=True)
+    assert sorted(out) == [r["id"] for r in reqs]
+    assert loop.admissions >= 3
+    for r in reqs:
+        rec = out[r["id"]]
+        s = by[r["surface"]]
+        assert rec["latency"] >= 0
+        if r["kind"] == "laplace":
+            assert rec["stats"]["status"] == 0
+            x64, _ = gpu.Solver(s.opset, 0.0, -1.0).solve(s.rhs(r["values"]), tol=1e-12, precision=0)
+            assert np.max(np.abs(rec["x"] - x64[0])) / np.max(np.abs(x64[0])) <= 1e-8
+        else:
+            g = gpu.Geodesic(s.tube, r["source"])
+            p64, _ = g.run(s.tube.dx ** 2, precision=0)
+            assert np.max(np.abs(rec["x"] - p64)) / np.max(np.abs(p64)) <= 1e-8
