@@ -162,6 +162,7 @@ struct cpm_tube_s {
     cpm::DBuf<double> cp, dist;  // 3N, N
     cpm::DBuf<uint32_t> base;   // packed base triplet per node
     cpm::DBuf<double> w;        // 12 per node: [d][j]
+    int seed[3] = {0, 0, 0};    // grid triplet of the build's seed node
     cpm::BrickView view() const { return cpm::BrickView{bmap.p, bmask.p, bstart.p, g.NB, g.N1d}; }
 };
 

@@ -641,6 +641,7 @@ static int finish_build(cpm_tube_s *t, const std::vector<uint32_t> &cand_h, std:
     const GridParams &g = t->g;
     const int64_t nc = (int64_t)cand_h.size();
     const int bs = 256;
+    for (int d = 0; d < 3; ++d) t->seed[d] = seed[d];
     DBuf<int32_t> cmap, parent, err;
     CPM_TRY(cmap.upload(cmap_h));
     CPM_TRY(parent.alloc((size_t)nc * 64));
@@ -919,6 +920,41 @@ extern "C" int cpm_tube_export(cpm_tube_t t, int64_t *rec, double *x, double *cp
         CPM_TRY(d.download(h, 6 * N));
         std::copy(h.begin(), h.end(), nbr);
     }
+    return 0;
+}
+
+// The reference numbers tube nodes in the order its breadth-first flood
+// discovers them (Tube::BuildTube, src/Tube.cpp:321-454): the seed first, then
+// each dequeued node's in-band neighbours in the order +x,-x,+y,-y,+z,-z
+// (src/Tube.cpp:431-435).  The device tube is that flood's node set; a
+// breadth-first walk of its neighbour table from the seed gives the order.
+extern "C" int cpm_tube_reference_order(cpm_tube_t t, int64_t *order) {
+    if (!t || !order) return fail(CPM_ERR_INVALID_ARG, "tube_reference_order: null argument");
+    const int64_t N = t->N;
+    std::vector<uint32_t> key;
+    CPM_TRY(t->key.download(key, N));
+    const uint32_t sk = pack3(t->seed[0], t->seed[1], t->seed[2]);
+    int64_t s0 = -1;
+    for (int64_t q = 0; q < N && s0 < 0; ++q)
+        if (key[q] == sk) s0 = q;
+    if (s0 < 0) return fail(CPM_ERR_CUDA, "tube_reference_order: the seed node is not in the tube");
+    std::vector<int64_t> nbr((size_t)6 * N);
+    CPM_TRY(cpm_tube_export(t, nullptr, nullptr, nullptr, nullptr, nullptr, nbr.data(), nullptr));
+    std::vector<char> seen((size_t)N, 0);
+    int64_t head = 0, tail = 0;
+    order[tail++] = s0;
+    seen[s0] = 1;
+    while (head < tail) {
+        const int64_t q = order[head++];
+        for (int d = 0; d < 6; ++d) {
+            const int64_t m = nbr[6 * q + d];
+            if (m >= 0 && !seen[m]) {
+                seen[m] = 1;
+                order[tail++] = m;
+            }
+        }
+    }
+    if (tail != N) return fail(CPM_ERR_CUDA, "tube_reference_order: the tube is not connected");
     return 0;
 }
 

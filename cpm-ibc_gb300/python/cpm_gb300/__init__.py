@@ -110,6 +110,7 @@ def lib():
                                              P(vp)]
         L.cpm_tube_info_get.argtypes = [vp, P(TubeInfo)]
         L.cpm_tube_export.argtypes = [vp] * 8
+        L.cpm_tube_reference_order.argtypes = [vp, vp]
         L.cpm_interp_query.argtypes = [vp, ctypes.c_int64, vp, vp, vp]
         L.cpm_tube_destroy.argtypes = [vp]
         L.cpm_opset_create.argtypes = [vp, ctypes.c_int32, P(SurfaceDesc), P(vp)]
@@ -196,6 +197,12 @@ class Tube:
         _check(lib().cpm_tube_export(self.h, _p(out["rec"]), _p(out["x"]), _p(out["cp"]), _p(out["dist"]),
                                      _p(out["bpt"]), _p(out["nbr"]), _p(out["w"])))
         return out
+
+    def reference_order(self):
+        """Device index of each node in the reference's tube numbering (its BFS flood order)."""
+        order = np.zeros(self.N, np.int64)
+        _check(lib().cpm_tube_reference_order(self.h, _p(order)))
+        return order
 
     def interp_query(self, xq):
         """Interpolation(Tube&, xq) rows: 64 (column, value) per query point."""

@@ -117,6 +117,12 @@ int cpm_tube_info_get(cpm_tube_t t, cpm_tube_info *info);
 int cpm_tube_export(cpm_tube_t t, int64_t *rec, double *x, double *cp, double *dist, int64_t *bpt_rec, int64_t *nbr,
                     double *w);
 
+/* Tube node numbering of the reference: order[i] is the device index of the
+ * node the reference's breadth-first flood numbers i (Tube::BuildTube,
+ * src/Tube.cpp:321-454; seed first, neighbours +x,-x,+y,-y,+z,-z), so that
+ * device-ordered exports can be permuted into reference-shaped vectors. */
+int cpm_tube_reference_order(cpm_tube_t t, int64_t *order);
+
 /* Interpolation(Tube&, xq) + BuildInterpolationMatrix (src/Interpolation.cpp:23-36,52-121):
  * per query point the 64 column indices (device tube order) and E entries
  * (w2[k]*w1[j]*w0[i], walk +x outer, +y, +z inner).  Returns

@@ -1,0 +1,375 @@
+// C++ classes with the reference's names over the C-ABI of cpm_gpu.h, so that
+// code written against cpm-ibc's custom-solver path (Tube, Solver,
+// PoissonWithIBC, HeatWithIBC, GeodesicDistance) can call the GB300 path.
+//
+// Differences a caller sees:
+//   * vectors are std::vector<double> (the reference uses Eigen::VectorX);
+//     they are in the reference's row layout: tube rows in the reference's
+//     breadth-first node numbering (src/Tube.cpp:321-454), then the IBC DOF
+//     rows and Dirichlet value rows (src/IBCSubsets.cpp:74-116);
+//   * errors throw std::runtime_error with the library's message where the
+//     reference throws, and also where it would return silently (a solve
+//     that does not converge, src/BiCGStab.h:107);
+//   * a Solver can run the reference's FP64 BiCGStab (precision 0) or FP32
+//     BiCGStab with FP64 reliable updates (precision 1).
+// Header-only; link against libcpmgpu.so.
+#pragma once
+
+#include <algorithm>
+#include <array>
+#include <cstdint>
+#include <functional>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "cpm_gpu.h"
+
+namespace cpm_gb300 {
+
+using Scalar = double;
+using VectorX = std::vector<Scalar>;
+using Point3 = std::array<Scalar, 3>;
+
+// src/Defines.h:13-18
+enum class Preconditioner { identity = 0, diagonal = 1, jacobi = 2 };
+
+inline void check(int rc) {
+    if (rc != CPM_OK) throw std::runtime_error(std::string("cpm_gb300: ") + cpm_last_error());
+}
+
+// SurfaceSpecifier (src/SurfaceSpecifier.h:198-216) with the IBCMetaData
+// fields (src/IBCMetaData.h:9-24) an IBC curve carries.
+class SurfaceSpecifier {
+  public:
+    static SurfaceSpecifier Sphere(Scalar R = 1.0, std::array<Scalar, 2> bbox = {-1.0, 1.0}) {
+        return analytic(CPM_SPHERE, {R}, bbox);
+    }
+    static SurfaceSpecifier Torus(Scalar R, Scalar r, std::array<Scalar, 2> bbox) { return analytic(CPM_TORUS, {R, r}, bbox); }
+    static SurfaceSpecifier Circle3D(Scalar R, Point3 centre, Point3 normal, std::array<Scalar, 2> bbox) {
+        return analytic(CPM_CIRCLE3D, {R, centre[0], centre[1], centre[2], normal[0], normal[1], normal[2]}, bbox);
+    }
+    static SurfaceSpecifier Point(Point3 p, std::array<Scalar, 2> bbox) { return analytic(CPM_POINT, {p[0], p[1], p[2]}, bbox); }
+    // a triangle mesh: 3 coordinates per vertex, 3 vertex indices per face; the
+    // bounding interval is derived as SurfaceSpecifier::SetSurface does
+    // (src/SurfaceSpecifier.cpp:346-361)
+    static SurfaceSpecifier Triangulation(std::vector<Scalar> verts, std::vector<int64_t> faces) {
+        Scalar lo = 0.0, hi = 0.0;
+        for (Scalar v : verts) {
+            lo = std::min(lo, v);
+            hi = std::max(hi, v);
+        }
+        SurfaceSpecifier s = analytic(CPM_TRIANGULATION, {}, {lo, hi});
+        s.verts_ = std::move(verts);
+        s.prims_ = std::move(faces);
+        return s;
+    }
+    // a polyline on a surface: 3 coordinates per vertex, 2 vertex indices per segment
+    static SurfaceSpecifier Polyline(std::vector<Scalar> verts, std::vector<int64_t> segments, std::array<Scalar, 2> bbox) {
+        SurfaceSpecifier s = analytic(CPM_POLYLINE, {}, bbox);
+        s.verts_ = std::move(verts);
+        s.prims_ = std::move(segments);
+        return s;
+    }
+
+    // IBCMetaData fields
+    SurfaceSpecifier &boundary_order(int order) { d_.boundary_order = order; return *this; }
+    SurfaceSpecifier &boundary_type(int side1, int side2) { d_.boundary_type[0] = side1; d_.boundary_type[1] = side2; return *this; }
+    SurfaceSpecifier &on_ibc_tolerance(Scalar tol) { d_.on_ibc_tolerance = tol; return *this; }
+    SurfaceSpecifier &is_oriented(bool o) { d_.is_oriented = o; return *this; }
+
+    // the descriptor, with its array pointers bound to this object's storage
+    const cpm_surface_desc &desc() const {
+        d_.nverts = (int64_t)(verts_.size() / 3);
+        d_.verts = verts_.empty() ? nullptr : verts_.data();
+        const int per = d_.kind == CPM_POLYLINE ? 2 : 3;
+        d_.nprims = (int64_t)(prims_.size() / per);
+        d_.prims = prims_.empty() ? nullptr : prims_.data();
+        return d_;
+    }
+
+  private:
+    static SurfaceSpecifier analytic(int kind, std::vector<Scalar> params, std::array<Scalar, 2> bbox) {
+        SurfaceSpecifier s;
+        s.d_ = cpm_surface_desc{};
+        s.d_.kind = kind;
+        s.d_.nparams = (int32_t)params.size();
+        for (size_t i = 0; i < params.size() && i < 8; ++i) s.d_.params[i] = params[i];
+        s.d_.bbox[0] = bbox[0];
+        s.d_.bbox[1] = bbox[1];
+        s.d_.boundary_order = 1;
+        s.d_.use_Jcp_surface_normals = 1;
+        s.d_.dof_radius_scale = 1.0;
+        return s;
+    }
+    mutable cpm_surface_desc d_{};
+    std::vector<Scalar> verts_;
+    std::vector<int64_t> prims_;
+};
+
+// Tube(SurfaceSpecifier&, size_t p, Scalar dx) (src/Tube.h:45) on the device.
+class Tube {
+  public:
+    Tube(const SurfaceSpecifier &surface, size_t p, Scalar dx) {
+        cpm_tube_t t = nullptr;
+        check(cpm_tube_build(&surface.desc(), (int32_t)p, dx, &t));
+        h_.reset(t);
+        check(cpm_tube_info_get(t, &info_));
+        order_.resize((size_t)info_.n_nodes);
+        check(cpm_tube_reference_order(t, order_.data()));
+    }
+    size_t nNodes() const { return (size_t)info_.n_nodes; }
+    size_t N1d() const { return (size_t)info_.n1d; }
+    Scalar dx() const { return info_.dx; }
+    Scalar xstart() const { return info_.xstart; }
+    Scalar TubeRadius() const { return info_.radius; }
+    // grid coordinates and closest points in the reference's node numbering
+    std::vector<Point3> x() const { return points(true); }
+    std::vector<Point3> cpx() const { return points(false); }
+    // device index of reference node i (cpm_tube_reference_order)
+    const std::vector<int64_t> &device_index() const { return order_; }
+    cpm_tube_t handle() const { return h_.get(); }
+
+  private:
+    std::vector<Point3> points(bool grid) const {
+        const size_t N = nNodes();
+        std::vector<Scalar> a(3 * N);
+        check(cpm_tube_export(h_.get(), nullptr, grid ? a.data() : nullptr, grid ? nullptr : a.data(), nullptr, nullptr,
+                              nullptr, nullptr));
+        std::vector<Point3> out(N);
+        for (size_t i = 0; i < N; ++i) {
+            const size_t q = (size_t)order_[i];
+            out[i] = {a[3 * q], a[3 * q + 1], a[3 * q + 2]};
+        }
+        return out;
+    }
+    struct Del {
+        void operator()(cpm_tube_t t) const { cpm_tube_destroy(t); }
+    };
+    std::unique_ptr<cpm_tube_s, Del> h_;
+    cpm_tube_info info_{};
+    std::vector<int64_t> order_;
+};
+
+// Lfull, Efull and the identity rows of a tube with IBC curves
+// (Helpers::SetupMatrices, IBCSubsets::Initialize, IBCMatrixManipulations
+// AddIBCFiniteDifference / AddIBCExtension) kept on the device.
+class SystemOperator {
+  public:
+    SystemOperator(const Tube &tube, const std::vector<SurfaceSpecifier> &ibcs) : tube_(&tube) {
+        std::vector<cpm_surface_desc> d;
+        for (const auto &s : ibcs) d.push_back(s.desc());
+        cpm_opset_t o = nullptr;
+        check(cpm_opset_create(tube.handle(), (int32_t)d.size(), d.empty() ? nullptr : d.data(), &o));
+        h_.reset(o);
+        int64_t sz[7];
+        check(cpm_opset_sizes(o, sz));
+        D_ = sz[0];
+        N_ = sz[1];
+        total_ibc_dofs_ = sz[2];
+        n_ibc_ = sz[4];
+        const size_t D = (size_t)D_;
+        std::vector<uint8_t> ident(D);
+        kind_.resize(D);
+        ibc_.resize(D);
+        std::vector<Scalar> pt(3 * D);
+        check(cpm_opset_rows(o, ident.data(), kind_.data(), ibc_.data(), pt.data()));
+        // reference row r -> device row
+        dev_.resize(D);
+        for (size_t r = 0; r < D; ++r) dev_[r] = r < (size_t)N_ ? tube.device_index()[r] : (int64_t)r;
+        point_.resize(D);
+        identity_.resize(D);
+        for (size_t r = 0; r < D; ++r) {
+            const size_t q = (size_t)dev_[r];
+            point_[r] = {pt[3 * q], pt[3 * q + 1], pt[3 * q + 2]};
+            identity_[r] = ident[q] != 0;
+        }
+    }
+    size_t rows() const { return (size_t)D_; }
+    size_t nNodes() const { return (size_t)N_; }
+    size_t TotalIBCDOFs() const { return (size_t)total_ibc_dofs_; }
+    size_t NumIBCs() const { return (size_t)n_ibc_; }
+    const std::vector<bool> &identity_rows() const { return identity_; }
+    // per reference row: 0 tube row, 1 IBC DOF row, 2 Dirichlet value row; its
+    // IBC; the point its right-hand side is evaluated at
+    int kind(size_t r) const { return kind_[(size_t)dev_[r]]; }
+    int ibc(size_t r) const { return ibc_[(size_t)dev_[r]]; }
+    const Point3 &point(size_t r) const { return point_[r]; }
+    VectorX to_device(const VectorX &ref) const {
+        VectorX d(ref.size());
+        for (size_t r = 0; r < ref.size(); ++r) d[(size_t)dev_[r]] = ref[r];
+        return d;
+    }
+    VectorX from_device(const VectorX &dev) const {
+        VectorX ref(dev.size());
+        for (size_t r = 0; r < dev.size(); ++r) ref[r] = dev[(size_t)dev_[r]];
+        return ref;
+    }
+    cpm_opset_t handle() const { return h_.get(); }
+    const Tube &tube() const { return *tube_; }
+
+  private:
+    struct Del {
+        void operator()(cpm_opset_t o) const { cpm_opset_destroy(o); }
+    };
+    const Tube *tube_;
+    std::unique_ptr<cpm_opset_s, Del> h_;
+    int64_t D_ = 0, N_ = 0, total_ibc_dofs_ = 0, n_ibc_ = 0;
+    std::vector<int64_t> dev_;
+    std::vector<int32_t> kind_, ibc_;
+    std::vector<Point3> point_;
+    std::vector<bool> identity_;
+};
+
+// Solver (src/Solver.h:22-26): Init(m, n, ...), SetPrecond, Solve, Multiply.
+class Solver {
+  public:
+    void Init(Scalar m, Scalar n, const SystemOperator &op, Preconditioner p = Preconditioner::diagonal) {
+        op_ = &op;
+        m_ = m;
+        n_ = n;
+        precond_ = p;
+        cpm_solver_t s = nullptr;
+        check(cpm_solver_create(op.handle(), m, n, 1, &s));
+        h_.reset(s);
+    }
+    void SetPrecond(int precond_iters) { precond_iters_ = precond_iters; }
+    // 0: the reference's FP64 BiCGStab; 1: FP32 BiCGStab with FP64 reliable updates
+    void SetPrecision(int precision) { precision_ = precision; }
+    void SetTolerance(Scalar tol) { tol_ = tol; }
+    VectorX Solve(const VectorX &rhs) {
+        require();
+        VectorX b = op_->to_device(rhs), x(b.size());
+        cpm_solve_opts o{};
+        o.tol = tol_;
+        o.max_iters = 100000;
+        o.precision = precision_;
+        o.precond = (int32_t)precond_;
+        o.precond_iters = precond_iters_;
+        check(cpm_solve(h_.get(), 1, b.data(), x.data(), &o, &stats_));
+        return op_->from_device(x);
+    }
+    // b = m x + n (diag(L) x + offdiag(L) E~ x), identity rows b = x
+    void Multiply(const VectorX &x, VectorX &b, Scalar m, Scalar n) const {
+        require();
+        VectorX xd = op_->to_device(x), yd(xd.size());
+        check(cpm_apply(op_->handle(), m, n, 1, xd.data(), yd.data()));
+        b = op_->from_device(yd);
+    }
+    const cpm_solve_stats &stats() const { return stats_; }
+
+  private:
+    void require() const {
+        if (!op_ || !h_) throw std::runtime_error("cpm_gb300: Solver::Init was not called");
+    }
+    struct Del {
+        void operator()(cpm_solver_t s) const { cpm_solver_destroy(s); }
+    };
+    const SystemOperator *op_ = nullptr;
+    std::unique_ptr<cpm_solver_s, Del> h_;
+    Scalar m_ = 0, n_ = 0, tol_ = 1e-10;
+    Preconditioner precond_ = Preconditioner::diagonal;
+    int precond_iters_ = 0, precision_ = 0;
+    cpm_solve_stats stats_{};
+};
+
+using SourceFn = std::function<Scalar(const Point3 &)>;
+// Dirichlet value on IBC c at its closest point (side is 0 for non-oriented curves)
+using IBCFn = std::function<Scalar(size_t c, size_t side, const Point3 &)>;
+
+// PoissonWithIBC (problems/PoissonWithIBC.h:17-117): -Delta_S u = f with
+// Dirichlet values on IBC curves, solved with Init(0, -1, diagonal).
+class PoissonWithIBC {
+  public:
+    PoissonWithIBC(const SurfaceSpecifier &surface, const std::vector<SurfaceSpecifier> &ibcs, Scalar dx,
+                   size_t interp_deg = 3, int precision = 0)
+        : tube_(surface, interp_deg, dx), op_(tube_, ibcs) {
+        sv_.Init(0.0, -1.0, op_);
+        sv_.SetPrecision(precision);
+    }
+    // PoissonWithIBC::GetRHS (problems/PoissonWithIBC.cpp:162-192)
+    VectorX GetRHS(const SourceFn &f, const IBCFn &ibc_exact) const {
+        VectorX b(op_.rows(), 0.0);
+        for (size_t r = 0; r < b.size(); ++r)
+            b[r] = op_.kind(r) == 2 ? ibc_exact((size_t)op_.ibc(r), 0, op_.point(r)) : f(op_.point(r));
+        return b;
+    }
+    VectorX Solve(const VectorX &rhs) { return sv_.Solve(rhs); }
+    const Tube &tube() const { return tube_; }
+    const SystemOperator &system() const { return op_; }
+    Solver &solver() { return sv_; }
+
+  private:
+    Tube tube_;
+    SystemOperator op_;
+    Solver sv_;
+};
+
+// HeatWithIBC (problems/HeatWithIBC.h:17-60): implicit time steps of
+// u_t = Delta_S u with Dirichlet IBC values; time_stepping_method 1 is
+// backward Euler (Init(1, -dt)), 2 Crank-Nicolson (Init(1, -dt/2) with the
+// right-hand side Multiply(u, 1, dt/2)), as problems/HeatWithIBC.cpp:115-128.
+class HeatWithIBC {
+  public:
+    HeatWithIBC(const SurfaceSpecifier &surface, const std::vector<SurfaceSpecifier> &ibcs, Scalar dx, Scalar dt,
+                size_t time_stepping_method, size_t interp_deg = 3, int precision = 0)
+        : tube_(surface, interp_deg, dx), op_(tube_, ibcs), dt_(dt), method_(time_stepping_method) {
+        if (method_ != 1 && method_ != 2)
+            throw std::runtime_error("cpm_gb300: HeatWithIBC supports the implicit methods 1 and 2");
+        const Scalar r = method_ == 1 ? 1.0 : 0.5;
+        sv_.Init(1.0, -r * dt_, op_);
+        sv_.SetPrecision(precision);
+    }
+    // HeatWithIBC::TimeStep (problems/HeatWithIBC.cpp:104-128): returns u at the next time
+    VectorX TimeStep(VectorX &ufull, const IBCFn &ibc_exact) {
+        if (method_ == 2) {
+            VectorX tmp;
+            sv_.Multiply(ufull, tmp, 1.0, 0.5 * dt_);
+            ufull = tmp;
+        }
+        // SetDirichletValue (problems/HeatWithIBC.cpp:62-85)
+        for (size_t r = 0; r < ufull.size(); ++r)
+            if (op_.kind(r) == 2) ufull[r] = ibc_exact((size_t)op_.ibc(r), 0, op_.point(r));
+        return sv_.Solve(ufull);
+    }
+    const Tube &tube() const { return tube_; }
+    const SystemOperator &system() const { return op_; }
+
+  private:
+    Tube tube_;
+    SystemOperator op_;
+    Scalar dt_;
+    size_t method_;
+    Solver sv_;
+};
+
+// GeodesicDistance::ComputeDistance (problems/GeodesicDistance.cpp:11-69) from
+// a point source: returns phi on the tube rows (reference numbering) and the
+// point IBC's DOF rows.
+class GeodesicDistance {
+  public:
+    explicit GeodesicDistance(int precision = 0) : precision_(precision) {}
+    VectorX ComputeDistance(const Tube &tube, const Point3 &source, Scalar dt) {
+        cpm_geodesic_t g = nullptr;
+        int64_t D = 0;
+        check(cpm_geodesic_create(tube.handle(), source.data(), &g, &D));
+        std::unique_ptr<cpm_geodesic_s, Del> hold(g);
+        VectorX phi((size_t)D);
+        check(cpm_geodesic_run(g, dt, precision_, 1e-10, 2000, phi.data(), iterations_.data()));
+        VectorX out(phi);
+        for (size_t i = 0; i < tube.nNodes(); ++i) out[i] = phi[(size_t)tube.device_index()[i]];
+        return out;
+    }
+    const std::array<int32_t, 4> &iterations() const { return iterations_; }
+
+  private:
+    struct Del {
+        void operator()(cpm_geodesic_t g) const { cpm_geodesic_destroy(g); }
+    };
+    int precision_;
+    std::array<int32_t, 4> iterations_{};
+};
+
+}  // namespace cpm_gb300

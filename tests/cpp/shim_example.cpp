@@ -1,0 +1,62 @@
+// Drives the C++ classes of include/cpm_ibc.hpp the way the reference's
+// convergence studies drive cpm-ibc (Tube, Solver::Init/Solve,
+// PoissonWithIBC::GetRHS/Solve, GeodesicDistance::ComputeDistance) and writes
+// the solutions, in the reference's row layout, to a binary file:
+//   int64 n, then n doubles, for each of: C1 solution, C2 FP64 solution,
+//   C2 mixed solution, geodesic distance.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "cpm_ibc.hpp"
+
+using namespace cpm_gb300;
+
+static void put(FILE *f, const VectorX &v) {
+    int64_t n = (int64_t)v.size();
+    fwrite(&n, sizeof(n), 1, f);
+    fwrite(v.data(), sizeof(double), v.size(), f);
+}
+
+int main(int argc, char **argv) {
+    if (argc < 2) {
+        fprintf(stderr, "usage: %s out.bin\n", argv[0]);
+        return 2;
+    }
+    FILE *f = fopen(argv[1], "wb");
+    if (!f) return 2;
+    try {
+        // screened Poisson -Delta_S u + u = 3z on the unit sphere, dx = 0.1 (exact u = z)
+        SurfaceSpecifier sphere = SurfaceSpecifier::Sphere();
+        Tube tube(sphere, 3, 0.1);
+        SystemOperator op(tube, {});
+        Solver sv;
+        sv.Init(1.0, -1.0, op);
+        VectorX b(op.rows());
+        for (size_t r = 0; r < b.size(); ++r) b[r] = 3.0 * op.point(r)[2];
+        VectorX u = sv.Solve(b);
+        put(f, u);
+        // Laplace with Dirichlet circles z = 0.3 (u = 1) and z = -0.5 (u = 0), dx = 0.05
+        const double dx = 0.05;
+        std::vector<SurfaceSpecifier> ibcs = {
+            SurfaceSpecifier::Circle3D(std::sqrt(1 - 0.09), {0, 0, 0.3}, {0, 0, 1}, {-1, 1}).boundary_order(2).on_ibc_tolerance(0.1 * dx * dx),
+            SurfaceSpecifier::Circle3D(std::sqrt(1 - 0.25), {0, 0, -0.5}, {0, 0, 1}, {-1, 1}).boundary_order(2).on_ibc_tolerance(0.1 * dx * dx)};
+        PoissonWithIBC p(sphere, ibcs, dx);
+        VectorX rhs = p.GetRHS([](const Point3 &) { return 0.0; },
+                               [](size_t c, size_t, const Point3 &) { return c == 0 ? 1.0 : 0.0; });
+        put(f, p.Solve(rhs));
+        p.solver().SetPrecision(1);
+        put(f, p.Solve(rhs));
+        // heat-method geodesic distance from (0.36, 0.48, 0.8) on the sphere, dx = 0.1
+        GeodesicDistance gd;
+        put(f, gd.ComputeDistance(tube, {0.36, 0.48, 0.8}, 0.01));
+        printf("nodes %zu rows %zu ibc_dofs %zu iterations %d\n", tube.nNodes(), p.system().rows(),
+               p.system().TotalIBCDOFs(), p.solver().stats().iterations);
+    } catch (const std::exception &e) {
+        fprintf(stderr, "error: %s\n", e.what());
+        fclose(f);
+        return 1;
+    }
+    fclose(f);
+    return 0;
+}

@@ -52,6 +52,18 @@ def test_tube_bit_exact_given_same_closest_points(gpu, oracle, kind, dx):
     assert np.array_equal(gn_ref, ref["nbr"])
 
 
+@pytest.mark.parametrize("kind,dx", [("sphere", 0.1), ("sphere", 0.05), ("torus", 0.05)])
+def test_reference_node_order(gpu, oracle, kind, dx):
+    """cpm_tube_reference_order reproduces the reference's BFS tube numbering."""
+    if kind == "sphere":
+        od, gd = oracle.sphere_desc(), gpu.desc(gpu.SPHERE, [1.0], (-1.0, 1.0))
+    else:
+        od, gd = oracle.torus_desc(1.0, 0.4, (-1.4, 1.4)), gpu.desc(gpu.TORUS, [1.0, 0.4], (-1.4, 1.4))
+    P = oracle.RefProblem(od, [], 3, dx, record_visited=True)
+    T = gpu.Tube.from_closest_points(gd, 3, dx, *P.visited())
+    assert np.array_equal(T.export()["rec"][T.reference_order()], P.tube()["rec"])
+
+
 @pytest.mark.parametrize("kind,dx", [("sphere", 0.1), ("torus", 0.05)])
 def test_device_closest_points_match_oracle(gpu, oracle, kind, dx):
     if kind == "sphere":
