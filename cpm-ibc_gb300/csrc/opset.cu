@@ -23,7 +23,8 @@
 namespace cpm {
 
 template <class T>
-static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, const T *lval, const T *ldiag, const T *w_ord) {
+static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, const T *lval, const T *ldiag, const T *w_ord,
+                           const T *pl_xval, const T *pe_w) {
     OpView<T> v;
     v.bv = o->tube->view();
     v.N = o->N;
@@ -57,6 +58,15 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
     v.n_ord = o->n_ord;
     v.n_grp = o->n_grp;
     v.n_ident = o->n_ident;
+    v.pl_row = o->pl_row.p;
+    v.pl_off = o->pl_off.p;
+    v.pl_xcol = o->pl_xcol.p;
+    v.pl_neg = o->pl_neg.p;
+    v.pl_xval = pl_xval;
+    v.pe_new = o->pe_new.p;
+    v.pe_old = o->pe_old.p;
+    v.pe_w = pe_w;
+    v.n_pl = o->n_pl;
     return v;
 }
 
@@ -64,11 +74,11 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
 
 template <>
 cpm::OpView<double> cpm_opset_s::view<double>() const {
-    return cpm::make_view<double>(this, w.p, p_xval.p, lval.p, ldiag.p, w_ord.p);
+    return cpm::make_view<double>(this, w.p, p_xval.p, lval.p, ldiag.p, w_ord.p, pl_xval.p, pe_w.p);
 }
 template <>
 cpm::OpView<float> cpm_opset_s::view<float>() const {
-    return cpm::make_view<float>(this, w32.p, p_xval32.p, lval32.p, ldiag32.p, w_ord32.p);
+    return cpm::make_view<float>(this, w32.p, p_xval32.p, lval32.p, ldiag32.p, w_ord32.p, pl_xval32.p, pe_w32.p);
 }
 
 namespace cpm {
@@ -547,6 +557,8 @@ static int make_float_copies(cpm_opset_s *o) {
     CPM_TRY(conv(o->p_xval, o->p_xval32));
     CPM_TRY(conv(o->lval, o->lval32));
     CPM_TRY(conv(o->ldiag, o->ldiag32));
+    CPM_TRY(conv(o->pl_xval, o->pl_xval32));
+    CPM_TRY(conv(o->pe_w, o->pe_w32));
     return 0;
 }
 
@@ -905,6 +917,91 @@ __global__ void k_sorted_rows(OpView<double> op, int64_t n_ord, double *__restri
     if (a == 0) fl_ord[p] = op.flags[r];
 }
 
+// entries of the patch list: one thread per patched row, moved points in
+// increasing stencil order s = 16 i + 4 j + k
+__global__ void k_patch_entries(OpView<double> op, int64_t n_pl, int32_t *__restrict__ pe_new, int32_t *__restrict__ pe_old,
+                                double *__restrict__ pe_w, int *__restrict__ err) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n_pl) return;
+    const int r = op.pl_row[q];
+    const int pi = op.patch[r];
+    uint64_t em = (op.flags[r] & F_EMOVE) ? op.p_emask[pi] : 0ull;
+    int mo = op.p_eoff[pi];
+    const uint32_t b = op.base[r];
+    const int bi = unpack_i(b), bj = unpack_j(b), bk = unpack_k(b);
+    const double *w = op.w + 12 * (int64_t)r;
+    int e = op.pl_off[q];
+    while (em) {
+        const int s = __ffsll((long long)em) - 1;
+        em &= em - 1;
+        const int i = s >> 4, j = (s >> 2) & 3, k = s & 3;
+        const int old = node_at(op.bv, bi + i, bj + j, bk + k);
+        if (old < 0) atomicOr(err, 1);
+        pe_new[e] = op.moved[mo++];
+        pe_old[e] = old < 0 ? 0 : old;
+        pe_w[e] = (w[i] * w[4 + j]) * w[8 + k];
+        ++e;
+    }
+}
+
+// The patch list: rows whose E row is not the plain bulk stencil (moved
+// columns, negation, an extra entry), so the 32-slot E passes can evaluate
+// every row as bulk and correct these rows in a separate, parallel pass.
+static int build_patch_list(cpm_opset_s *o, const std::vector<uint8_t> &flags) {
+    const int64_t D = o->D;
+    std::vector<int32_t> patch, p_xcol;
+    std::vector<uint64_t> p_emask;
+    std::vector<double> p_xval;
+    std::vector<int32_t> rows, off{0}, xcol;
+    std::vector<uint8_t> neg;
+    std::vector<double> xval;
+    if (o->patch.n >= (size_t)D) {
+        CPM_TRY(o->patch.download(patch, D));
+        CPM_TRY(o->p_emask.download(p_emask, o->p_emask.n));
+        CPM_TRY(o->p_xcol.download(p_xcol, o->p_xcol.n));
+        CPM_TRY(o->p_xval.download(p_xval, o->p_xval.n));
+        for (int64_t r = 0; r < D; ++r) {
+            const uint8_t f = flags[r];
+            if ((f & F_IDENT) || !(f & (F_EMOVE | F_EXTRA | F_ENEG))) continue;
+            const int pi = patch[r];
+            if (pi < 0 || (size_t)pi >= p_emask.size()) return fail(CPM_ERR_CUDA, "internal: patched row without a patch record");
+            rows.push_back((int32_t)r);
+            off.push_back(off.back() + ((f & F_EMOVE) ? __builtin_popcountll(p_emask[pi]) : 0));
+            neg.push_back((f & F_ENEG) ? 1 : 0);
+            xcol.push_back((f & F_EXTRA) ? p_xcol[pi] : -1);
+            xval.push_back((f & F_EXTRA) ? p_xval[pi] : 0.0);
+        }
+    }
+    o->n_pl = (int64_t)rows.size();
+    const int64_t ne = off.back();
+    if (rows.empty()) {
+        rows.push_back(0);
+        neg.push_back(0);
+        xcol.push_back(-1);
+        xval.push_back(0.0);
+    }
+    CPM_TRY(o->pl_row.upload(rows));
+    CPM_TRY(o->pl_off.upload(off));
+    CPM_TRY(o->pl_neg.upload(neg));
+    CPM_TRY(o->pl_xcol.upload(xcol));
+    CPM_TRY(o->pl_xval.upload(xval));
+    CPM_TRY(o->pe_new.alloc(std::max<int64_t>(1, ne)));
+    CPM_TRY(o->pe_old.alloc(std::max<int64_t>(1, ne)));
+    CPM_TRY(o->pe_w.alloc(std::max<int64_t>(1, ne)));
+    if (o->n_pl > 0) {
+        DBuf<int> err;
+        CPM_TRY(err.alloc(1));
+        CPM_TRY(err.zero());
+        k_patch_entries<<<(unsigned)((o->n_pl + 255) / 256), 256, 0, stream()>>>(o->view<double>(), o->n_pl, o->pe_new.p,
+                                                                                 o->pe_old.p, o->pe_w.p, err.p);
+        CPM_CUDA_TRY(cudaGetLastError());
+        std::vector<int> he;
+        CPM_TRY(err.download(he, 1));
+        if (he[0]) return fail(CPM_ERR_CUDA, "internal: a moved stencil point has no tube node");
+    }
+    return 0;
+}
+
 // Apply schedule: neighbour table, rows sorted by base point with their groups,
 // identity rows.  Rows sharing a base point read the same 64 values of x.
 static int build_schedule(cpm_opset_s *o) {
@@ -960,7 +1057,7 @@ static int build_schedule(cpm_opset_s *o) {
                                                                                     o->fl_ord.p);
         CPM_CUDA_TRY(cudaGetLastError());
     }
-    return 0;
+    return build_patch_list(o, flags);
 }
 
 }  // namespace cpm

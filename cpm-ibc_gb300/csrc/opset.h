@@ -45,7 +45,14 @@ struct OpView {
     const T *w_ord;         // weights of ord[p] at 12 p (sorted copy: coalesced per group)
     const uint8_t *fl_ord;  // flags of ord[p]
     const int32_t *ident;   // identity rows
-    int64_t n_ord, n_grp, n_ident;
+    // IBC patch list of the rows whose E row differs from the bulk stencil:
+    // t_r = sign (bulk + sum_e w_e (x[new_e] - x[old_e])) + xval x[xcol]
+    const int32_t *pl_row, *pl_off, *pl_xcol;  // n_pl rows; entries pl_off[i] .. pl_off[i+1]
+    const uint8_t *pl_neg;                    // 1: negated (2nd-order Dirichlet DOF rows)
+    const T *pl_xval;
+    const int32_t *pe_new, *pe_old;           // moved column and the bulk column it replaces
+    const T *pe_w;                            // stencil weight (wx_i wy_j) wz_k of the moved point
+    int64_t n_ord, n_grp, n_ident, n_pl;
 };
 
 // ---------------------------------------------------------------------------
@@ -228,6 +235,8 @@ __device__ __forceinline__ void load_w12(const double *w, double (&o)[12]) {
 // slot), evaluates wx_w * sum_j wy_j sum_k wz_k x for every row of the group,
 // and the four planes are summed through shared memory.  16 registers per
 // plane instead of 64 keep ~4x more warps resident to hide gather latency.
+// Every row gets the bulk stencil; rows on the IBC patch list are corrected
+// afterwards (k_epatch32).
 constexpr int EG_ROWS = 32;  // rows per shared-memory chunk of a group
 template <class T>
 struct EGShared {
@@ -285,33 +294,7 @@ __device__ __forceinline__ void e_group_split(const OpView<T> &op, int64_t g, in
         __syncthreads();
         for (int q = warp; q < nr; q += 4) {
             const int r = sh.rows[q];
-            T acc = ((sh.part[0][q][lane] + sh.part[1][q][lane]) + sh.part[2][q][lane]) + sh.part[3][q][lane];
-            const uint8_t fl = sh.fl[q];
-            if (fl & (F_EMOVE | F_EXTRA | F_ENEG)) {
-                if (fl & (F_EMOVE | F_EXTRA)) {
-                    const int pi = op.patch[r];
-                    uint64_t em = op.p_emask[pi];
-                    int mo = op.p_eoff[pi];
-                    if (em) {
-                        T w[12];
-#pragma unroll
-                        for (int a = 0; a < 12; ++a) w[a] = sh.w[12 * q + a];
-                        const T wx[4] = {w[0], w[1], w[2], w[3]}, wy[4] = {w[4], w[5], w[6], w[7]},
-                                wz[4] = {w[8], w[9], w[10], w[11]};
-                        while (em) {  // warp-uniform: one row per warp
-                            const int s = __ffsll((long long)em) - 1;
-                            em &= em - 1;
-                            const int nc = op.moved[mo++];
-                            const T ws = pick4(wx, s >> 4) * pick4(wy, (s >> 2) & 3) * pick4(wz, s & 3);
-                            acc += ws * (x[(uint32_t)nc * 32u + lane] - x[(uint32_t)sh.cols[s] * 32u + lane]);
-                        }
-                    }
-                    if (fl & F_ENEG) acc = -acc;
-                    if (fl & F_EXTRA) acc += op.p_xval[pi] * x[(uint32_t)op.p_xcol[pi] * 32u + lane];
-                } else {
-                    acc = -acc;
-                }
-            }
+            const T acc = ((sh.part[0][q][lane] + sh.part[1][q][lane]) + sh.part[2][q][lane]) + sh.part[3][q][lane];
             if (act) t[(uint32_t)r * 32u + lane] = acc;
         }
         __syncthreads();
@@ -393,6 +376,11 @@ struct cpm_opset_s {
     cpm::DBuf<double> p_xval, lval, ldiag;
     cpm::DBuf<float> p_xval32, lval32, ldiag32;
     cpm::DBuf<int32_t> nbr6, ord, grp, ident, gcols;
+    cpm::DBuf<int32_t> pl_row, pl_off, pl_xcol, pe_new, pe_old;
+    cpm::DBuf<uint8_t> pl_neg;
+    cpm::DBuf<double> pl_xval, pe_w;
+    cpm::DBuf<float> pl_xval32, pe_w32;
+    int64_t n_pl = 0;
     cpm::DBuf<double> w_ord;
     cpm::DBuf<float> w_ord32;
     cpm::DBuf<uint8_t> fl_ord;

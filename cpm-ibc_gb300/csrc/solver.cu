@@ -238,6 +238,62 @@ __global__ void k_epass1(OpView<T> op, const Slot *__restrict__ sl, int ph, cons
     }
 }
 
+// IBC patch of the 32-slot E passes: for each row on the patch list (warp per
+// row, lane = slot), t_r = sign (bulk t_r + sum_e w_e (x[new_e] - x[old_e]))
+// + xval x[xcol]: moved stencil points read the IBC DOF column instead of the
+// tube node (IBCMatrixManipulations::AddIBCExtension's column moves,
+// src/IBCMatrixManipulations.cpp:118-186).  The lanes load 32 entries at once
+// and broadcast them, so a row's x loads are all in flight together.
+template <class T>
+__global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x,
+                                                  T *__restrict__ t) {
+    const int lane = threadIdx.x & 31;
+    const bool act = (ph < 0) || sl[lane].phase == ph;
+    if (!__any_sync(FULL, act)) return;  // the same slots in every warp: block-uniform
+    const int64_t warps = (int64_t)gridDim.x * 4;
+    for (int64_t q = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5); q < op.n_pl; q += warps) {
+        const uint32_t r = (uint32_t)op.pl_row[q];
+        const int e0 = op.pl_off[q], e1 = op.pl_off[q + 1];
+        const int xc = op.pl_xcol[q];
+        T acc = act ? t[r * 32u + lane] : T(0);
+        const T xe = (act && xc >= 0) ? x[(uint32_t)xc * 32u + lane] : T(0);
+        for (int base = e0; base < e1; base += 32) {
+            const int cnt = min(32, e1 - base);
+            int nc = 0, oc = 0;
+            T w = 0;
+            if (lane < cnt) {
+                nc = op.pe_new[base + lane];
+                oc = op.pe_old[base + lane];
+                w = op.pe_w[base + lane];
+            }
+            for (int u0 = 0; u0 < cnt; u0 += 8) {
+                T xn[8], xo[8], ww[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int k = u0 + u;
+                    const uint32_t ncu = (uint32_t)__shfl_sync(FULL, nc, k & 31), ocu = (uint32_t)__shfl_sync(FULL, oc, k & 31);
+                    ww[u] = __shfl_sync(FULL, w, k & 31);
+                    const bool ok = act && k < cnt;
+                    xn[u] = ok ? x[ncu * 32u + lane] : T(0);
+                    xo[u] = ok ? x[ocu * 32u + lane] : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (u0 + u < cnt) acc += ww[u] * (xn[u] - xo[u]);
+            }
+        }
+        if (op.pl_neg[q]) acc = -acc;
+        if (xc >= 0) acc += op.pl_xval[q] * xe;
+        if (act) t[r * 32u + lane] = acc;
+    }
+}
+
+// kernels one E pass launches
+template <class T, int K>
+static inline int epass_kernels(const OpView<T> &op) {
+    return (K == 32 && op.n_pl > 0) ? 2 : 1;
+}
+
 template <class T, int K>
 static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x, T *t, cudaStream_t st) {
     static_assert(K == 1 || K == 32, "slot widths 1 and 32");
@@ -247,6 +303,10 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
     } else {
         const int64_t threads = op.n_ord + op.n_ident;
         k_epass1<T><<<(unsigned)((threads + BS - 1) / BS), BS, 0, st>>>(op, sl, ph, x, t);
+    }
+    if (epass_kernels<T, K>(op) == 2) {
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_pl + 3) / 4, 16LL * sm_count()));
+        k_epatch32<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
     }
 }
 
@@ -1025,7 +1085,7 @@ static int parse_params(const cpm_solve_opts *o, SolveParams &P) {
     P.mixed = o->precision == 1;
     P.delta = o->inner_tol > 0 ? o->inner_tol : 0.2;
     P.max_refine = o->max_refine > 0 ? o->max_refine : 400;
-    P.refine_every = o->refine_every > 0 ? o->refine_every : 8;
+    P.refine_every = o->refine_every > 0 ? o->refine_every : 16;
     if (P.refine_every > 16 || (P.refine_every & (P.refine_every - 1)))
         return fail(CPM_ERR_INVALID_ARG, "refine_every must be 1, 2, 4, 8 or 16");
     P.precond = o->precond;
@@ -1080,7 +1140,13 @@ static int prepare_graph(cpm_solver_s *s, const SolveParams &P, cudaGraphExec_t 
 // kernels launched by one graph replay
 static inline long long graph_launches(const cpm_solver_s *s, const SolveParams &P) {
     const int chunk = graph_chunk(s, P);
-    return (7LL + (P.precond == 2 ? 4LL * (P.sweeps - 1) : 0)) * chunk + (P.mixed ? 5LL * (chunk / P.refine_every) : 0);
+    // an iteration: 5 vector / L-pass kernels and two E passes; a Jacobi sweep: an E
+    // pass and the sweep; a reliable update: 4 kernels and an FP64 E pass
+    const long long e32 = s->K == 32 ? epass_kernels<float, 32>(s->op->view<float>()) : 1;
+    const long long e64 = s->K == 32 ? epass_kernels<double, 32>(s->op->view<double>()) : 1;
+    const long long eit = P.mixed ? e32 : e64;
+    return (5LL + 2 * eit + (P.precond == 2 ? 2LL * (P.sweeps - 1) * (e64 + 1) : 0)) * chunk +
+           (P.mixed ? (4LL + e64) * (chunk / P.refine_every) : 0);
 }
 
 // start the mixed-path slots in PH_START (FP64 residual, then the FP32 Krylov state)
@@ -1538,7 +1604,7 @@ extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslo
             k_lpass<double, 32><<<row_grid(D, 32), BS, 0, st>>>(v, m, n, x, t, y);
         }
     }
-    count_launches(2);
+    count_launches((kslots == 32 && op->n_pl > 0) ? 3 : 2);
     CPM_CUDA_TRY(cudaGetLastError());
     return 0;
 }
@@ -1607,7 +1673,7 @@ extern "C" int cpm_apply_device_noalloc(cpm_opset_t op, double m, double n, int3
             k_lpass<double, 32><<<row_grid(D, 32), BS, 0, st>>>(v, m, n, x, tt, y);
         }
     }
-    count_launches(2);
+    count_launches((kslots == 32 && op->n_pl > 0) ? 3 : 2);
     CPM_CUDA_TRY(cudaGetLastError());
     return 0;
 }
