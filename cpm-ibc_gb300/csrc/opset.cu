@@ -974,6 +974,7 @@ static int build_patch_list(cpm_opset_s *o, const std::vector<uint8_t> &flags) {
     }
     o->n_pl = (int64_t)rows.size();
     const int64_t ne = off.back();
+    o->n_pe = ne;
     if (rows.empty()) {
         rows.push_back(0);
         neg.push_back(0);
@@ -1094,6 +1095,8 @@ extern "C" int cpm_opset_sizes(cpm_opset_t o, int64_t *s) {
     s[4] = o->n_ibc;
     s[5] = o->n_patched;
     s[6] = o->n_moved;
+    s[7] = o->n_pl;
+    s[8] = o->n_pe;
     return 0;
 }
 

@@ -380,7 +380,7 @@ struct cpm_opset_s {
     cpm::DBuf<uint8_t> pl_neg;
     cpm::DBuf<double> pl_xval, pe_w;
     cpm::DBuf<float> pl_xval32, pe_w32;
-    int64_t n_pl = 0;
+    int64_t n_pl = 0, n_pe = 0;
     cpm::DBuf<double> w_ord;
     cpm::DBuf<float> w_ord32;
     cpm::DBuf<uint8_t> fl_ord;

@@ -1086,8 +1086,8 @@ static int parse_params(const cpm_solve_opts *o, SolveParams &P) {
     P.delta = o->inner_tol > 0 ? o->inner_tol : 0.2;
     P.max_refine = o->max_refine > 0 ? o->max_refine : 400;
     P.refine_every = o->refine_every > 0 ? o->refine_every : 16;
-    if (P.refine_every > 16 || (P.refine_every & (P.refine_every - 1)))
-        return fail(CPM_ERR_INVALID_ARG, "refine_every must be 1, 2, 4, 8 or 16");
+    if (P.refine_every > 32 || (P.refine_every & (P.refine_every - 1)))
+        return fail(CPM_ERR_INVALID_ARG, "refine_every must be 1, 2, 4, 8, 16 or 32");
     P.precond = o->precond;
     P.sweeps = o->precond_iters;
     if (P.precond < 0 || P.precond > 2) return fail(CPM_ERR_INVALID_ARG, "precond must be 0 (identity), 1 (diagonal) or 2 (jacobi)");
@@ -1102,7 +1102,11 @@ static int parse_params(const cpm_solve_opts *o, SolveParams &P) {
 }
 
 // iterations per captured graph
-static inline int graph_chunk(const cpm_solver_s *s, const SolveParams &P) { return (P.precond == 2) ? 1 : s->chunk; }
+// (Jacobi-preconditioned solves: one iteration, already thousands of launches;
+// mixed: 32 iterations, so that the reliable-update period can reach 32)
+static inline int graph_chunk(const cpm_solver_s *s, const SolveParams &P) {
+    return (P.precond == 2) ? 1 : (P.mixed ? 2 * s->chunk : s->chunk);
+}
 
 // the captured iteration graph for P (reused while the parameters match)
 template <int K>

@@ -224,9 +224,10 @@ class OpSet:
         arr = (SurfaceDesc * max(1, len(ibcs)))(*ibcs) if ibcs else None
         _check(lib().cpm_opset_create(tube.h, len(ibcs), arr, ctypes.byref(h)))
         self.h = h
-        s = np.zeros(7, np.int64)
+        s = np.zeros(9, np.int64)
         _check(lib().cpm_opset_sizes(self.h, _p(s)))
-        self.D, self.N, self.total_ibc_dofs, self.num2, self.n_ibc, self.n_patched, self.n_moved = [int(v) for v in s]
+        (self.D, self.N, self.total_ibc_dofs, self.num2, self.n_ibc, self.n_patched, self.n_moved, self.n_patch_rows,
+         self.n_patch_entries) = [int(v) for v in s]
 
     def __del__(self):
         try:

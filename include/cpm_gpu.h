@@ -139,7 +139,8 @@ int cpm_tube_destroy(cpm_tube_t t);
  * rows in the reference's column layout (src/IBCSubsets.cpp:74-116). */
 int cpm_opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, cpm_opset_t *out);
 
-/* sizes: [D, N, total_ibc_dofs, num_2nd_order_rows, n_ibc, n_patched_rows, n_moved_entries] */
+/* sizes (9 entries): [D, N, total_ibc_dofs, num_2nd_order_rows, n_ibc, n_patched_rows,
+ * n_moved_entries, rows whose E row is patched, moved E stencil points] */
 int cpm_opset_sizes(cpm_opset_t op, int64_t *sizes);
 
 /* Row layout for right-hand sides (PoissonWithIBC::GetRHS, problems/PoissonWithIBC.cpp:92-133):
@@ -199,7 +200,7 @@ typedef struct cpm_solve_opts {
                                FP64 true residual replaces it (one refinement step) */
     int32_t max_refine;     /* FP64 refinement steps (default 400) */
     int32_t refine_every;   /* precision 1: iterations between reliable-update points, one of
-                               1, 2, 4, 8, 16 (0: 8) */
+                               1, 2, 4, 8, 16, 32 (0: 16) */
 } cpm_solve_opts;
 
 typedef struct cpm_solve_stats {

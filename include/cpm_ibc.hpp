@@ -164,7 +164,7 @@ class SystemOperator {
         cpm_opset_t o = nullptr;
         check(cpm_opset_create(tube.handle(), (int32_t)d.size(), d.empty() ? nullptr : d.data(), &o));
         h_.reset(o);
-        int64_t sz[7];
+        int64_t sz[9];
         check(cpm_opset_sizes(o, sz));
         D_ = sz[0];
         N_ = sz[1];
