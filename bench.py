@@ -342,6 +342,8 @@ def run_workload(args):
             "latency_ms": {k: {"p50": float(np.percentile(v, 50) * 1e3), "p99": float(np.percentile(v, 99) * 1e3),
                                "n": len(v)} for k, v in lat.items() if v},
             "laplace_fp64_fallbacks": fb, "admissions": loop.admissions, "evictions": loop.evictions,
+            "precision_switches": loop.precision_switches,
+            "final_precision": {s.name: ("mixed" if s.precision else "fp64") for s in surfaces},
             "fp64_one_at_a_time_laplace_solves_per_s": len(t64) / sum(t64),
             "note": "geodesics run one at a time on their own point-IBC operator between server steps",
         })
@@ -360,8 +362,8 @@ def main():
                     help="run only a few applies (or one batched solve) of the workload, for ncu")
     ap.add_argument("--workload", choices=["torus-geodesic", "mesh-curves", "serving-mix"], default=None,
                     help="one line for another configuration instead of the headline benchmark")
-    ap.add_argument("--requests", type=int, default=256, help="serving-mix: requests in the stream")
-    ap.add_argument("--rate", type=float, default=40.0, help="serving-mix: mean arrivals per second")
+    ap.add_argument("--requests", type=int, default=96, help="serving-mix: requests in the stream")
+    ap.add_argument("--rate", type=float, default=2.0, help="serving-mix: mean arrivals per second")
     args = ap.parse_args()
     if args.workload:
         return run_workload(args)

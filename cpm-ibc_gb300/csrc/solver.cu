@@ -1380,7 +1380,8 @@ struct cpm_server_s {
 extern "C" int cpm_server_create(cpm_opset_t op, double m, double n, const cpm_solve_opts *opts, cpm_server_t *out) {
     if (!op || !opts || !out) return fail(CPM_ERR_INVALID_ARG, "server_create: null argument");
     *out = nullptr;
-    if (opts->precision != 1) return fail(CPM_ERR_UNSUPPORTED, "the server runs the mixed-precision path (precision 1)");
+    if (opts->precision != 0 && opts->precision != 1) return fail(CPM_ERR_INVALID_ARG, "precision must be 0 or 1");
+    if (opts->precond != 1) return fail(CPM_ERR_UNSUPPORTED, "the server runs the diagonal preconditioner");
     cpm_server_s *sv = new cpm_server_s();
     auto bail = [&](int rc) {
         delete sv;
@@ -1389,7 +1390,7 @@ extern "C" int cpm_server_create(cpm_opset_t op, double m, double n, const cpm_s
     sv->opts = *opts;
     int rc = parse_params(opts, sv->P);
     if (!rc) rc = cpm_solver_create(op, m, n, 32, &sv->solver);
-    if (!rc) rc = alloc_vectors(sv->solver, false, true);
+    if (!rc) rc = alloc_vectors(sv->solver, !sv->P.mixed, sv->P.mixed);
     if (rc) return bail(rc);
     const int64_t D = sv->solver->D;
     if (cudaMallocHost((void **)&sv->h_stage, sizeof(double) * 32 * (size_t)D) != cudaSuccess)
@@ -1460,7 +1461,15 @@ extern "C" int cpm_server_step(cpm_server_t sv, int32_t *active, int32_t *queued
         sv->busy[j].t_admit = std::chrono::steady_clock::now();
         admitted = true;
     }
-    if (admitted) mixed_start<32>(s, sv->P);
+    if (admitted) {
+        if (sv->P.mixed) {
+            mixed_start<32>(s, sv->P);
+        } else {
+            k_init<double, 32><<<s->G, BS, 0, st>>>(s->op->view<double>(), s->slots.p, sv->P, PH_START, s->b64.p, s->x64.p,
+                                                    s->dr.p, s->dr0.p, s->dp.p, s->dv.p, s->partial.p, s->counter.p);
+            count_launches(1);
+        }
+    }
     int n_busy = 0;
     for (int j = 0; j < 32; ++j) n_busy += sv->busy[j].used;
     if (n_busy) {
@@ -1471,6 +1480,15 @@ extern "C" int cpm_server_step(cpm_server_t sv, int32_t *active, int32_t *queued
     }
     CPM_CUDA_TRY(cudaMemcpyAsync(s->h_slots.data(), s->slots.p, sizeof(Slot) * 32, cudaMemcpyDeviceToHost, st));
     CPM_CUDA_TRY(cudaStreamSynchronize(st));
+    if (!sv->P.mixed) {  // the plain path's restarts run between graphs (as in run_solve)
+        bool restart = false;
+        for (int j = 0; j < 32; ++j) restart = restart || s->h_slots[j].phase == PH_RESTART;
+        if (restart) {
+            plain_restart<32>(s);
+            count_launches(2);
+            CPM_CUDA_TRY(cudaGetLastError());
+        }
+    }
     // harvest finished slots
     int n_fin = 0;
     std::vector<int> fin;
@@ -1482,7 +1500,7 @@ extern "C" int cpm_server_step(cpm_server_t sv, int32_t *active, int32_t *queued
         const bool over = S.phase == PH_DONE || S.iters >= sv->P.max_iters || S.refinements >= sv->P.max_refine;
         if (!over) continue;
         double *ds = sv->busy[j].x_dev ? sv->busy[j].x_dev : sv->d_stage.p + (size_t)j * D;
-        if (S.phase == PH_DONE && S.status == 0) {
+        if (S.phase == PH_DONE && (S.status == 0 || !sv->P.mixed)) {
             k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->x64.p, ds);
             count_launches(1);
         } else {
@@ -1508,7 +1526,7 @@ extern "C" int cpm_server_step(cpm_server_t sv, int32_t *active, int32_t *queued
             cpm_server_s::Done d;
             d.tag = sv->busy[j].tag;
             if (!sv->busy[j].x_dev) d.x.assign(sv->h_stage + (size_t)j * D, sv->h_stage + (size_t)(j + 1) * D);
-            slot_stats(s->h_slots[j], true, 0.0f, &d.st);
+            slot_stats(s->h_slots[j], sv->P.mixed != 0, 0.0f, &d.st);
             if (fb[j]) {
                 const int it = d.st.iterations, rf = d.st.refinements;
                 d.st = fb_st[j];
@@ -1555,7 +1573,9 @@ extern "C" int64_t cpm_server_device_bytes(cpm_opset_t op) {
     if (!op) return -1;
     const int64_t D = op->D;
     // FP32 Krylov vectors (10), FP64 b, x, r, E~x (4), staging, reduction scratch
-    return D * 32 * (10 * 4 + 4 * 8 + 8) + D * (8 + 4) + (int64_t)(1 << 20);
+    // the larger of the two precisions: FP32 Krylov vectors (10) + FP64 b, x, r, E~x
+    // (4), or FP64 Krylov vectors (8) + the same 4; staging; reduction scratch
+    return D * 32 * (12 * 8 + 8) + D * (8 + 4) + (int64_t)(1 << 20);
 }
 
 // ================================================================= apply

@@ -377,11 +377,13 @@ class Solver:
 
 class Server:
     """Continuous batching of right-hand sides on one operator (m, n): up to 32
-    in flight in the mixed-precision solver, admitted as slots free up."""
+    in flight in a 32-slot solver (precision 1: FP32 with FP64 reliable
+    updates; 0: plain FP64), admitted as slots free up."""
 
-    def __init__(self, opset, m, n, tol=1e-10, inner_tol=0.2, max_refine=400, refine_every=0, max_iters=100000):
-        self.opset, self.D = opset, opset.D
-        o = SolveOpts(tol=tol, max_iters=max_iters, precision=1, precond=DIAGONAL, precond_iters=0,
+    def __init__(self, opset, m, n, tol=1e-10, inner_tol=0.2, max_refine=400, refine_every=0, max_iters=100000,
+                 precision=1):
+        self.opset, self.D, self.precision = opset, opset.D, precision
+        o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=DIAGONAL, precond_iters=0,
                       inner_tol=inner_tol, max_refine=max_refine, refine_every=refine_every)
         h = ctypes.c_void_p()
         _check(lib().cpm_server_create(opset.h, m, n, ctypes.byref(o), ctypes.byref(h)))

@@ -14,8 +14,10 @@ fixed IBC curves) on the device.  Requests arrive over time:
 
 A surface's server is admitted only while the device has room for it (its
 estimated bytes within the HBM budget); an idle server is released to make
-room for another surface's.  Latency is measured from a request's arrival to
-the harvest of its result.
+room for another surface's.  A surface starts on the mixed-precision server;
+once a quarter of its finished requests (at least 8 finished) needed the FP64
+re-solve, it drains that server and continues on a plain FP64 32-slot server.
+Latency is measured from a request's arrival to the harvest of its result.
 """
 import heapq
 import time
@@ -23,6 +25,8 @@ import time
 import numpy as np
 
 from . import DIAGONAL, Geodesic, OpSet, Server, Solver, device_info
+
+MAX_SLOTS = 32
 
 
 class ServedSurface:
@@ -39,6 +43,11 @@ class ServedSurface:
         self.bytes = Server.device_bytes(self.opset)
         self.waiting = []  # (request id, rhs, arrival time) not yet submitted
         self.active = False  # requests in the server's slots or queue
+        self.precision = 1  # the server's precision: 1 mixed, 0 plain FP64
+        self.finished = 0
+        self.fallbacks = 0
+        self.switch_pending = False
+        self.inflight = 0  # submitted to the server and not yet harvested
         self._cp = None
 
     def rhs(self, values):
@@ -69,6 +78,7 @@ class ServingLoop:
         self.dt_scale = dt_scale
         self.admissions = 0
         self.evictions = 0
+        self.precision_switches = 0
 
     def _held(self):
         return sum(s.bytes for s in self.surfaces.values() if s.server is not None)
@@ -88,7 +98,7 @@ class ServingLoop:
                         break
         if self._held() + s.bytes > self.budget:
             return False
-        s.server = Server(s.opset, s.m, s.n, tol=s.tol)
+        s.server = Server(s.opset, s.m, s.n, tol=s.tol, precision=s.precision)
         self.admissions += 1
         return True
 
@@ -116,11 +126,20 @@ class ServingLoop:
                     geo_wait.append(r)
             progressed = False
             for s in self.surfaces.values():
-                if s.waiting and self._admit(s):
-                    for rid, b, _ in s.waiting:
+                if s.switch_pending and s.server is not None and not s.active:
+                    s.server = None
+                    s.precision = 0
+                    s.switch_pending = False
+                    self.precision_switches += 1
+                if s.waiting and not s.switch_pending and self._admit(s):
+                    # at most two batches in the server, so a precision switch takes
+                    # effect within two batches
+                    take = max(0, min(len(s.waiting), 2 * MAX_SLOTS - s.inflight))
+                    for rid, b, _ in s.waiting[:take]:
                         s.server.submit(b, rid)
-                    s.waiting = []
-                    s.active = True
+                    s.waiting = s.waiting[take:]
+                    s.inflight += take
+                    s.active = s.active or take > 0
                 if s.server is not None and s.active:
                     a, q, _ = s.server.step()
                     s.active = (a + q) > 0
@@ -132,7 +151,12 @@ class ServingLoop:
                         rid, x, st = res
                         done = time.perf_counter() - t0
                         rec = dict(kind="laplace", surface=s.name, arrival=arrival[rid], completion=done,
-                                   latency=done - arrival[rid], stats=st)
+                                   latency=done - arrival[rid], stats=st, precision=s.precision)
+                        s.finished += 1
+                        s.inflight -= 1
+                        s.fallbacks += int(st.get("fp64_fallback", 0))
+                        if s.precision == 1 and s.finished >= 8 and 4 * s.fallbacks >= s.finished:
+                            s.switch_pending = True
                         if keep_solutions:
                             rec["x"] = x
                         out[rid] = rec
@@ -141,7 +165,9 @@ class ServingLoop:
                 s = self.surfaces[r["surface"]]
                 g = Geodesic(s.tube, r["source"])
                 dx = s.tube.dx
-                phi, its = g.run(self.dt_scale * dx * dx, precision=self.geodesic_precision, tol=s.tol)
+                # a surface whose Laplace solves left mixed precision runs its geodesics in FP64 too
+                prec = min(self.geodesic_precision, s.precision)
+                phi, its = g.run(self.dt_scale * dx * dx, precision=prec, tol=s.tol)
                 done = time.perf_counter() - t0
                 rec = dict(kind="geodesic", surface=s.name, arrival=r["t"], completion=done, latency=done - r["t"],
                            stats=dict(iterations=its))

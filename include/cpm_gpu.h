@@ -248,8 +248,9 @@ int cpm_geodesic_destroy(cpm_geodesic_t g);
 
 /* ---- Serving: continuous batching ------------------------------------------
  * No counterpart in the reference (its Solve is one blocking call per RHS,
- * src/Solver.cpp:104-113).  A server owns a 32-slot mixed-precision solver
- * (opts->precision must be 1) on one operator (opset, m, n).  submit queues a
+ * src/Solver.cpp:104-113).  A server owns a 32-slot solver on one operator
+ * (opset, m, n), mixed precision (opts->precision 1) or plain FP64 (0), with
+ * the diagonal preconditioner.  submit queues a
  * right-hand side (D doubles, copied) with a caller tag; step admits queued
  * requests into free slots (each slot starts alone; the others keep their
  * state), runs one iteration graph if any slot is busy, and harvests finished

@@ -71,3 +71,20 @@ def test_server_interleaved_submission(gpu):
     got.update({k: v[1] for k, v in srv.drain().items()})
     assert sorted(got) == list(range(20))
     assert all(v["status"] == 0 and v["latency"] > 0 for v in got.values())
+
+
+def test_server_plain_fp64_mode(gpu):
+    """A server on the plain FP64 path (precision 0) returns the FP64 solve's results."""
+    T, O, rows = _setup(gpu, dx=0.1)
+    rng = np.random.default_rng(9)
+    B = [_rhs(rows, rng.uniform(0, 1, 2)) for _ in range(40)]
+    srv = gpu.Server(O, 0.0, -1.0, precision=0)
+    for k, b in enumerate(B):
+        srv.submit(b, k)
+    out = srv.drain()
+    ref = gpu.Solver(O, 0.0, -1.0, kslots=1)
+    for k in (0, 17, 39):
+        x, st = out[k]
+        assert st["status"] == 0 and st["fp64_fallback"] == 0
+        x64, _ = ref.solve(B[k], tol=1e-12, precision=0)
+        assert _rel(x, x64[0]) <= 1e-9
