@@ -241,46 +241,117 @@ constexpr int EG_ROWS = 32;  // rows per shared-memory chunk of a group
 template <class T>
 struct EGShared {
     T part[4][EG_ROWS][32];
-    T w[EG_ROWS * 12];
-    int cols[64];
+    alignas(16) T w[EG_ROWS * 12];
     int rows[EG_ROWS];
-    uint8_t fl[EG_ROWS];
 };
 
-template <class T>
-__device__ __forceinline__ void e_group_split(const OpView<T> &op, int64_t g, int warp, int lane, bool act, EGShared<T> &sh,
-                                              const T *__restrict__ x, T *__restrict__ t) {
-    const unsigned FULL = 0xffffffffu;
-    const int tid = warp * 32 + lane;
-    const int p0 = op.grp[g], p1 = op.grp[g + 1];
-    // the 16 columns of this warp's plane (lanes 16..31 duplicate lanes 0..15)
-    const int sidx = 16 * warp + (lane & 15);
-    const int mycol = __ldg(op.gcols + 64 * g + sidx);
-    if (lane < 16) sh.cols[sidx] = mycol;
-    T xb[16];
+// packed FP32 pairs (f32x2 arithmetic, one instruction for two rows)
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// four consecutive values from 16-byte aligned shared memory, as vector loads
+__device__ __forceinline__ void lds4(const float *p, float (&o)[4]) {
+    const float4 v = *(const float4 *)p;
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+    o[3] = v.w;
+}
+__device__ __forceinline__ void lds4(const double *p, double (&o)[4]) {
+    const double2 a = *(const double2 *)p, b = *(const double2 *)(p + 2);
+    o[0] = a.x;
+    o[1] = a.y;
+    o[2] = b.x;
+    o[3] = b.y;
+}
+
+// the 16 columns of plane `warp` of group g: four 16-byte loads every lane makes alike
+__device__ __forceinline__ void e_group_cols(const int32_t *gcols, int64_t g, int warp, int (&col)[16]) {
+    const int4 *gc = (const int4 *)(gcols + 64 * g + 16 * warp);
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-        const uint32_t cq = (uint32_t)__shfl_sync(FULL, mycol, q);
-        xb[q] = act ? x[cq * 32u + lane] : T(0);  // inactive slots issue no memory requests
+    for (int v = 0; v < 4; ++v) {
+        const int4 c = __ldg(gc + v);
+        col[4 * v] = c.x;
+        col[4 * v + 1] = c.y;
+        col[4 * v + 2] = c.z;
+        col[4 * v + 3] = c.w;
     }
+}
+// the plane's 16 x values of this lane's slot (inactive slots issue no memory requests)
+template <class T>
+__device__ __forceinline__ void e_group_x(const T *__restrict__ x, const int (&col)[16], int lane, bool act, T (&xb)[16]) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) xb[q] = act ? x[(uint32_t)col[q] * 32u + lane] : T(0);
+}
+
+// rows ord[p0 .. p1) of group g from the plane's x values xb
+template <class T>
+__device__ __forceinline__ void e_group_split(const OpView<T> &op, int p0, int p1, int warp, int lane, bool act, EGShared<T> &sh,
+                                              const T (&xb)[16], T *__restrict__ t) {
+    const int tid = warp * 32 + lane;
     for (int c0 = p0; c0 < p1; c0 += EG_ROWS) {
         const int nr = min(p1 - c0, EG_ROWS);
+        if constexpr (sizeof(T) == 4) {
+            // FP32: rows in pairs with packed f32x2 arithmetic.  The chunk's weights
+            // are staged pair-interleaved (component c of rows 2p, 2p+1 at
+            // 24 p + 2 c, 24 p + 2 c + 1), zero for the odd row of a last pair.
+            const int nr2 = nr + (nr & 1);
+            for (int e = tid; e < nr2 * 12; e += 128) {
+                const int q = e / 12, c = e - 12 * q;
+                sh.w[24 * (q >> 1) + 2 * c + (q & 1)] = q < nr ? op.w_ord[12 * (size_t)(c0 + q) + c] : T(0);
+            }
+            if (tid < nr) sh.rows[tid] = op.ord[c0 + tid];
+            __syncthreads();
+            uint64_t x2[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) x2[q] = f2_pack((float)xb[q], (float)xb[q]);
+            for (int q = 0; q < nr; q += 2) {
+                const float *w = (const float *)sh.w + 12 * q;
+                const uint64_t wx2 = *(const uint64_t *)(w + 2 * warp);
+                const ulonglong2 y01 = *(const ulonglong2 *)(w + 8), y23 = *(const ulonglong2 *)(w + 12);
+                const ulonglong2 z01 = *(const ulonglong2 *)(w + 16), z23 = *(const ulonglong2 *)(w + 20);
+                const uint64_t wy2[4] = {y01.x, y01.y, y23.x, y23.y}, wz2[4] = {z01.x, z01.y, z23.x, z23.y};
+                uint64_t ay2 = 0ull;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    uint64_t az2 = f2_mul(wz2[0], x2[4 * j]);
+                    az2 = f2_fma(wz2[1], x2[4 * j + 1], az2);
+                    az2 = f2_fma(wz2[2], x2[4 * j + 2], az2);
+                    az2 = f2_fma(wz2[3], x2[4 * j + 3], az2);
+                    ay2 = j == 0 ? f2_mul(wy2[0], az2) : f2_fma(wy2[j], az2, ay2);
+                }
+                float lo, hi;
+                f2_unpack(f2_mul(wx2, ay2), lo, hi);
+                sh.part[warp][q][lane] = (T)lo;
+                if (q + 1 < nr) sh.part[warp][q + 1][lane] = (T)hi;
+            }
+        } else {
         // stage the chunk's sorted weights, row ids and flags (coalesced, independent loads)
         for (int e = tid; e < nr * 12; e += 128) sh.w[e] = op.w_ord[12 * (size_t)c0 + e];
-        if (tid < nr) {
-            sh.rows[tid] = op.ord[c0 + tid];
-            sh.fl[tid] = op.fl_ord[c0 + tid];
-        }
+        if (tid < nr) sh.rows[tid] = op.ord[c0 + tid];
         __syncthreads();
         for (int q = 0; q < nr; ++q) {
             const T *w = sh.w + 12 * q;
             const T wxi = w[warp];
             T wy[4], wz[4];
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                wy[a] = w[4 + a];
-                wz[a] = w[8 + a];
-            }
+            lds4(w + 4, wy);
+            lds4(w + 8, wz);
             T ay = 0;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
@@ -290,6 +361,7 @@ __device__ __forceinline__ void e_group_split(const OpView<T> &op, int64_t g, in
                 ay += wy[j] * az;
             }
             sh.part[warp][q][lane] = wxi * ay;
+        }
         }
         __syncthreads();
         for (int q = warp; q < nr; q += 4) {

@@ -212,7 +212,13 @@ __global__ void __launch_bounds__(128) k_epass32s(OpView<T> op, const Slot *__re
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool act = (ph < 0) || sl[lane].phase == ph;
     if (!__any_sync(FULL, act)) return;  // the same 32 slots in every warp: block-uniform
-    for (int64_t g = blockIdx.x; g < op.n_grp; g += gridDim.x) e_group_split<T>(op, g, warp, lane, act, sh, x, t);
+    for (int64_t g = blockIdx.x; g < op.n_grp; g += gridDim.x) {
+        int col[16];
+        T xb[16];
+        e_group_cols(op.gcols, g, warp, col);
+        e_group_x(x, col, lane, act, xb);
+        e_group_split<T>(op, op.grp[g], op.grp[g + 1], warp, lane, act, sh, xb, t);
+    }
     if (act)
         for (int64_t q = (int64_t)blockIdx.x * 4 + warp; q < op.n_ident; q += (int64_t)gridDim.x * 4) {
             const uint32_t r = (uint32_t)op.ident[q];
