@@ -265,6 +265,17 @@ __device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
     return d;
 }
 
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 // four consecutive values from 16-byte aligned shared memory, as vector loads
 __device__ __forceinline__ void lds4(const float *p, float (&o)[4]) {
     const float4 v = *(const float4 *)p;
@@ -428,6 +439,60 @@ __device__ __forceinline__ void l_rows(const OpView<T> &op, const int64_t (&r)[U
                 }
             off += (T)(k - 6) * xr[u];
             y[u] = (fl[u] & F_IDENT) ? xr[u] : m * xr[u] + n * (op.Loff * off);
+        }
+    }
+}
+
+// l_rows for 32 FP32 slots, four per thread: slots 4q .. 4q+3 of U rows, as
+// two f32x2 pairs (slots 4q, 4q+1 in .x; 4q+2, 4q+3 in .y).  One 16-byte load
+// per vector and row, the neighbour columns shared by the four slots, and the
+// difference form of the FP32 row on slot pairs.  Rows >= D produce nothing.
+template <int U>
+__device__ __forceinline__ void l_rows4(const OpView<float> &op, const int64_t (&r)[U], int q, float m, float n,
+                                        const float *__restrict__ x, const float *__restrict__ t, ulonglong2 (&y)[U]) {
+    uint8_t fl[U];
+    ulonglong2 xr[U];
+    int c[U][6];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const bool ok = r[u] < op.D;
+        fl[u] = ok ? __ldg(op.flags + r[u]) : (uint8_t)F_IDENT;
+        xr[u] = ok ? *(const ulonglong2 *)(x + (uint32_t)r[u] * 32u + 4 * q) : make_ulonglong2(0ull, 0ull);
+        int2 a = make_int2(-1, -1), b = a, e = a;
+        if (!(fl[u] & F_IDENT)) {
+            a = __ldg((const int2 *)(op.nbr6 + 6 * r[u]));
+            b = __ldg((const int2 *)(op.nbr6 + 6 * r[u] + 2));
+            e = __ldg((const int2 *)(op.nbr6 + 6 * r[u] + 4));
+        }
+        c[u][0] = a.x;
+        c[u][1] = a.y;
+        c[u][2] = b.x;
+        c[u][3] = b.y;
+        c[u][4] = e.x;
+        c[u][5] = e.y;
+    }
+    const uint64_t m2 = f2_pack(m, m), n2 = f2_pack(n, n), l2 = f2_pack(op.Loff, op.Loff);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        uint64_t o0 = 0ull, o1 = 0ull;  // +0.0f pairs
+        int k = 0;
+#pragma unroll
+        for (int d = 0; d < 6; ++d)
+            if (c[u][d] >= 0) {
+                const ulonglong2 tv = *(const ulonglong2 *)(t + (uint32_t)c[u][d] * 32u + 4 * q);
+                o0 = f2_add(o0, f2_sub(tv.x, xr[u].x));
+                o1 = f2_add(o1, f2_sub(tv.y, xr[u].y));
+                ++k;
+            }
+        const float km = (float)(k - 6);
+        const uint64_t k2 = f2_pack(km, km);
+        o0 = f2_fma(k2, xr[u].x, o0);
+        o1 = f2_fma(k2, xr[u].y, o1);
+        if (fl[u] & F_IDENT) {
+            y[u] = xr[u];
+        } else {
+            y[u].x = f2_fma(n2, f2_mul(l2, o0), f2_mul(m2, xr[u].x));
+            y[u].y = f2_fma(n2, f2_mul(l2, o1), f2_mul(m2, xr[u].y));
         }
     }
 }

@@ -51,6 +51,7 @@ struct Slot {
     double rbest;   // mixed path: smallest FP64 true residual norm so far
     int phase, iters, inner_iters, refinements, restarts, status, krylov_restart;
     int stall;      // mixed path: reliable updates since rbest last improved by 10%
+    int fresh;      // mixed path: Krylov space restarted from the FP32 residual, p = r0 = r pending
 };
 
 struct SolveParams {
@@ -132,7 +133,9 @@ struct Dot<float, N> {
 // the group's last block, and the groups in group order by the last group: the
 // result depends only on the grid size, never on timing or on other slots.
 // partial holds (G + groups) * K * NDOT doubles, counter 1 + groups zeros.
-template <int K, int NDOT>
+// SUMMED: the block's per-slot sums are already in v of threads tid < K (the
+// other threads' v are not read), and the block tree is skipped.
+template <int K, int NDOT, bool SUMMED = false>
 __device__ __forceinline__ bool grid_reduce(double (&v)[NDOT], double *partial, unsigned int *counter, double (&out)[NDOT]) {
     __shared__ double sh[NDOT][BS];
     __shared__ bool last;
@@ -148,9 +151,16 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NDOT], double *partial, 
             __syncthreads();
         }
     };
+    if (SUMMED) {
+        if (tid < K)
 #pragma unroll
-    for (int d = 0; d < NDOT; ++d) sh[d][tid] = v[d];
-    tree();
+            for (int d = 0; d < NDOT; ++d) sh[d][tid] = v[d];
+        __syncthreads();
+    } else {
+#pragma unroll
+        for (int d = 0; d < NDOT; ++d) sh[d][tid] = v[d];
+        tree();
+    }
     const unsigned G = gridDim.x, grp = blockIdx.x / RGROUP, ngrp = (G + RGROUP - 1) / RGROUP;
     double *gpart = partial + (size_t)G * K * NDOT;
     if (tid < K)
@@ -199,6 +209,94 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NDOT], double *partial, 
         for (int d = 0; d < NDOT; ++d) out[d] = sh[d][tid];
     if (tid == 0) *counter = 0u;
     return tid < K;
+}
+
+// ---- per-slot scalar updates at the end of a reduction (one thread per slot)
+
+// alpha = rho / (r0 . v)   (src/BiCGStab.h:79-80)
+template <class T>
+__device__ __forceinline__ void alpha_update(Slot &S, double r0v) {
+    if (S.phase != PH_ITER) return;
+    S.fresh = 0;  // k_update_p has consumed it
+    S.alpha = S.rho / r0v;
+    if constexpr (sizeof(T) == 4) {
+        // FP32 inner iteration: r0 . v = 0 (or a non-finite value) ends this
+        // Krylov space; the FP64 reliable update restarts it from the true residual
+        if (!isfinite(S.alpha)) {
+            S.krylov_restart = 1;
+            S.rho_old = S.rho;
+            S.phase = PH_REFINE;
+        }
+    }
+}
+
+// omega = (t . s) / (t . t)   (src/BiCGStab.h:85-95)
+__device__ __forceinline__ void omega_update(Slot &S, double tt, double ts) {
+    if (S.phase != PH_ITER) return;
+    S.omega = (tt > 0.0) ? ts / tt : 0.0;
+}
+
+// r . r and r0 . r: convergence test, rho, beta   (src/BiCGStab.h:97-103, :59-73)
+__device__ __forceinline__ void xr_update(Slot &S, const SolveParams &P, double rr, double r0r) {
+    if (S.phase != PH_ITER) return;
+    S.iters += 1;
+    S.inner_iters += 1;
+    S.rr = rr;
+    const bool conv = S.rr <= S.tol2;  // false for a non-finite residual
+    if (P.mixed) {
+        S.rr_max = fmax(S.rr_max, S.rr);
+        // a slot whose FP32 residual claims convergence waits for the next
+        // reliable update; one whose residual merely fell by delta keeps
+        // iterating until then (k_refine_gate)
+        if (conv || S.iters >= P.max_iters || !isfinite(S.rr)) {
+            S.rho_old = S.rho;
+            S.phase = PH_REFINE;
+            return;
+        }
+        // an FP32 residual 10^4 times larger than right after the last
+        // reliable update has diverged (BiCGStab residuals may spike by
+        // a few orders of magnitude and recover; this does not): restart
+        // the Krylov space from the FP64 true residual
+        if (S.rr > 1e8 * S.rr_upd) {
+            S.krylov_restart = 1;
+            S.rho_old = S.rho;
+            S.phase = PH_REFINE;
+            return;
+        }
+    } else {
+        if (conv) {
+            S.phase = PH_DONE;
+            S.status = 0;
+            return;
+        }
+        if (S.iters >= P.max_iters || !isfinite(S.rr)) {
+            S.phase = PH_DONE;
+            S.status = isfinite(S.rr) ? CPM_ERR_NOT_CONVERGED : CPM_ERR_BREAKDOWN;
+            return;
+        }
+    }
+    S.rho_old = S.rho;
+    S.rho = r0r;
+    const double eps = 2.220446049250313e-16;
+    if (fabs(S.rho) < eps * eps * S.r0norm2) {  // restart on rho breakdown (src/BiCGStab.h:62-71)
+        if (P.mixed) {
+            // FP32 iteration: restart in place from the recurrence residual
+            // (r0 = p = r in k_update_p, rho = r . r) rather than idle until the
+            // next reliable update
+            S.fresh = 1;
+            S.restarts += 1;
+            S.r0norm2 = S.rr;
+            S.rho = S.rr;
+            S.rho_old = 1.0;
+            S.alpha = 1.0;
+            S.omega = 1.0;
+            S.beta = S.rr;
+        } else {
+            S.phase = PH_RESTART;
+        }
+        return;
+    }
+    S.beta = (S.rho / S.rho_old) * (S.alpha / S.omega);
 }
 
 // ================================================================= kernels
@@ -429,11 +527,12 @@ __global__ void __launch_bounds__(BS, 4) k_init(OpView<T> op, Slot *sl, SolvePar
 template <class T, int K>
 __global__ void __launch_bounds__(BS, 4) k_update_p(int64_t D, const Slot *__restrict__ sl, const T *__restrict__ pden, T ys,
                                                  const T *__restrict__ r, const T *__restrict__ v, T *__restrict__ p,
-                                                 T *__restrict__ y) {
+                                                 T *__restrict__ y, T *__restrict__ r0) {
     GRID_LOOP
     constexpr int UN = unr_stream6<T>();
     if (sl[s].phase != PH_ITER) return;
     const T w = (T)sl[s].omega, beta = (T)sl[s].beta;
+    const bool fresh = sl[s].fresh;  // restarted Krylov space: p = r0 = r
     ROWS_UNR_N(D, UN) {
         ROWS_OF_TRIP_N(rr, UN)
         T pv[UN], vv[UN], rv[UN], dv[UN];
@@ -453,6 +552,10 @@ __global__ void __launch_bounds__(BS, 4) k_update_p(int64_t D, const Slot *__res
                 T pi = -w * vv[u] + pv[u];
                 pi *= beta;
                 pi = pi + rv[u];
+                if (fresh) {
+                    pi = rv[u];
+                    r0[i] = pi;
+                }
                 p[i] = pi;
                 y[i] = pden ? ys * (pi / dv[u]) : pi;
             }
@@ -483,20 +586,7 @@ __global__ void __launch_bounds__(BS, 4) k_apply_alpha(OpView<T> op, Slot *sl, T
         }
     double av[1], tot[1];
     acc.get(av);
-    if (grid_reduce<K, 1>(av, partial, counter, tot)) {
-        Slot &S = sl[threadIdx.x];
-        if (S.phase != PH_ITER) return;
-        S.alpha = S.rho / tot[0];
-        if constexpr (sizeof(T) == 4) {
-            // FP32 inner iteration: r0 . v = 0 (or a non-finite value) ends this
-            // Krylov space; the FP64 reliable update restarts it from the true residual
-            if (!isfinite(S.alpha)) {
-                S.krylov_restart = 1;
-                S.rho_old = S.rho;
-                S.phase = PH_REFINE;
-            }
-        }
-    }
+    if (grid_reduce<K, 1>(av, partial, counter, tot)) alpha_update<T>(sl[threadIdx.x], tot[0]);
 }
 
 // s = r - alpha v ; z = M^-1 s   (src/BiCGStab.h:82-84), M^-1 as in k_update_p
@@ -582,11 +672,7 @@ __global__ void __launch_bounds__(BS, 4) k_apply_omega(OpView<T> op, Slot *sl, T
         }
     double av[2], tot[2];
     acc.get(av);
-    if (grid_reduce<K, 2>(av, partial, counter, tot)) {
-        Slot &S = sl[threadIdx.x];
-        if (S.phase != PH_ITER) return;
-        S.omega = (tot[0] > 0.0) ? tot[1] / tot[0] : 0.0;
-    }
+    if (grid_reduce<K, 2>(av, partial, counter, tot)) omega_update(sl[threadIdx.x], tot[0], tot[1]);
 }
 
 // x += alpha y + w z ; r = s - w t ; r.r and r0.r -> convergence test, rho, beta
@@ -631,59 +717,242 @@ __global__ void __launch_bounds__(BS, 4) k_update_xr(int64_t D, Slot *sl, SolveP
     }
     double av[2], tot[2];
     acc.get(av);
-    if (grid_reduce<K, 2>(av, partial, counter, tot)) {
-        Slot &S = sl[threadIdx.x];
-        if (S.phase != PH_ITER) return;
-        S.iters += 1;
-        S.inner_iters += 1;
-        S.rr = tot[0];
-        const bool conv = S.rr <= S.tol2;  // false for a non-finite residual
-        if (P.mixed) {
-            S.rr_max = fmax(S.rr_max, S.rr);
-            // a slot whose FP32 residual claims convergence waits for the next
-            // reliable update; one whose residual merely fell by delta keeps
-            // iterating until then (k_refine_gate)
-            if (conv || S.iters >= P.max_iters || !isfinite(S.rr)) {
-                S.rho_old = S.rho;
-                S.phase = PH_REFINE;
-                return;
-            }
-            // an FP32 residual 10^4 times larger than right after the last
-            // reliable update has diverged (BiCGStab residuals may spike by
-            // a few orders of magnitude and recover; this does not): restart
-            // the Krylov space from the FP64 true residual
-            if (S.rr > 1e8 * S.rr_upd) {
-                S.krylov_restart = 1;
-                S.rho_old = S.rho;
-                S.phase = PH_REFINE;
-                return;
-            }
-        } else {
-            if (conv) {
-                S.phase = PH_DONE;
-                S.status = 0;
-                return;
-            }
-            if (S.iters >= P.max_iters || !isfinite(S.rr)) {
-                S.phase = PH_DONE;
-                S.status = isfinite(S.rr) ? CPM_ERR_NOT_CONVERGED : CPM_ERR_BREAKDOWN;
-                return;
-            }
-        }
-        S.rho_old = S.rho;
-        S.rho = tot[1];
-        const double eps = 2.220446049250313e-16;
-        if (fabs(S.rho) < eps * eps * S.r0norm2) {  // restart on rho breakdown (src/BiCGStab.h:62-71)
-            if (P.mixed) {
-                S.krylov_restart = 1;
-                S.phase = PH_REFINE;
-            } else {
-                S.phase = PH_RESTART;
-            }
-            return;
-        }
-        S.beta = (S.rho / S.rho_old) * (S.alpha / S.omega);
+    if (grid_reduce<K, 2>(av, partial, counter, tot)) xr_update(sl[threadIdx.x], P, tot[0], tot[1]);
+}
+
+// ---- 32-slot FP32 row kernels, four slots per thread.  Thread tid owns slots
+// 4q .. 4q+3 (q = tid & 7) of rows tid / 8 + 32 b + ..., so a row of a [D][32]
+// vector is one 128-byte request of eight threads and each thread issues one
+// 16-byte load per vector and row: a quarter of the load and index
+// instructions of one slot per thread, and the arithmetic on f32x2 pairs.  The
+// grid is the one-slot kernels' (row_grid), so the reduction tree is the same.
+constexpr int V4_RPB = BS / 8;  // rows per block and step
+constexpr int V4_UN = 2;        // rows in flight per thread (L passes; one for six-vector streams)
+
+#define GRID_LOOP4                                                              \
+    const int q = threadIdx.x & 7;                                              \
+    const int64_t r0i = (int64_t)blockIdx.x * V4_RPB + (threadIdx.x >> 3);      \
+    const int64_t rstride = (int64_t)gridDim.x * V4_RPB;
+#define ROWS4(Dn, UN) for (int64_t rb = r0i; rb < (Dn); rb += (int64_t)(UN) * rstride)
+#define ROWS4_OF_TRIP(rr, UN)                                                   \
+    int64_t rr[UN];                                                             \
+    _Pragma("unroll") for (int u = 0; u < (UN); ++u) rr[u] = rb + (int64_t)u * rstride;
+
+// bit j set: slot 4q + j is in phase ph
+__device__ __forceinline__ unsigned act4(const Slot *sl, int q, int ph) {
+    unsigned a = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) a |= (sl[4 * q + j].phase == ph ? 1u : 0u) << j;
+    return a;
+}
+// all-ones lanes of the active slots, per f32x2 pair
+__device__ __forceinline__ void mask4(unsigned a, uint64_t &m0, uint64_t &m1) {
+    m0 = ((a & 1u) ? 0xffffffffull : 0ull) | ((a & 2u) ? 0xffffffff00000000ull : 0ull);
+    m1 = ((a & 4u) ? 0xffffffffull : 0ull) | ((a & 8u) ? 0xffffffff00000000ull : 0ull);
+}
+__device__ __forceinline__ ulonglong2 ld4(const float *__restrict__ v, int64_t row, int q) {
+    return *(const ulonglong2 *)(v + (uint32_t)row * 32u + 4 * q);
+}
+// the active slots' values of a row (one 16-byte store when all four are)
+__device__ __forceinline__ void st4(float *v, int64_t row, int q, ulonglong2 a, unsigned act) {
+    float *p = v + (uint32_t)row * 32u + 4 * q;
+    if (act == 15u) {
+        *(ulonglong2 *)p = a;
+        return;
     }
+    float e[4];
+    f2_unpack(a.x, e[0], e[1]);
+    f2_unpack(a.y, e[2], e[3]);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (act & (1u << j)) p[j] = e[j];
+}
+// per-slot f32x2 pairs of four slots' scalars
+__device__ __forceinline__ void slot_pairs(const Slot *sl, int q, double Slot::*f, uint64_t &a0, uint64_t &a1) {
+    a0 = f2_pack((float)(sl[4 * q].*f), (float)(sl[4 * q + 1].*f));
+    a1 = f2_pack((float)(sl[4 * q + 2].*f), (float)(sl[4 * q + 3].*f));
+}
+
+// Dot<float, N> for four slots on f32x2 pairs: exact products p + e, p added
+// by TwoSum, errors collected in the low words.  Inactive slots' products are
+// masked to zero (their operands are not read for them, and may be anything).
+template <int N>
+struct Dot4 {
+    uint64_t hi[N][2], lo[N][2];
+    __device__ __forceinline__ Dot4() {
+#pragma unroll
+        for (int d = 0; d < N; ++d) hi[d][0] = hi[d][1] = lo[d][0] = lo[d][1] = 0ull;
+    }
+    __device__ __forceinline__ static void add2(uint64_t &h, uint64_t &l, uint64_t x, uint64_t y, uint64_t msk) {
+        const uint64_t p0 = f2_mul(x, y);
+        const uint64_t e = f2_fma(x, y, p0 ^ 0x8000000080000000ull) & msk;  // x*y - p0, exactly
+        const uint64_t p = p0 & msk;
+        const uint64_t s = f2_add(h, p);
+        const uint64_t bp = f2_sub(s, h);
+        const uint64_t err = f2_add(f2_sub(h, f2_sub(s, bp)), f2_sub(p, bp));
+        h = s;
+        l = f2_add(l, f2_add(err, e));
+    }
+    __device__ __forceinline__ void add(int d, ulonglong2 x, ulonglong2 y, uint64_t m0, uint64_t m1) {
+        add2(hi[d][0], lo[d][0], x.x, y.x, m0);
+        add2(hi[d][1], lo[d][1], x.y, y.y, m1);
+    }
+};
+
+// double-float sum (a + b): TwoSum of the high words, low words added
+__device__ __forceinline__ void df_add(float &h, float &l, float bh, float bl) {
+    const float sum = __fadd_rn(h, bh);
+    const float bp = __fsub_rn(sum, h);
+    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(sum, bp)), __fsub_rn(bh, bp));
+    h = sum;
+    l = __fadd_rn(l, __fadd_rn(bl, err));
+}
+
+// the block's per-slot sums in double-float on the FP32 pipes (lanes with
+// equal q by shuffles, then the eight warps by the first 32 threads), one
+// conversion to FP64 per slot and dot, then the grid reduction
+template <int N>
+__device__ __forceinline__ bool grid_reduce4(const Dot4<N> &acc, double *partial, unsigned int *counter, double (&out)[N]) {
+    __shared__ float red[N][2][BS / 32][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float h[N][4], l[N][4];
+#pragma unroll
+    for (int d = 0; d < N; ++d)
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            f2_unpack(acc.hi[d][p], h[d][2 * p], h[d][2 * p + 1]);
+            f2_unpack(acc.lo[d][p], l[d][2 * p], l[d][2 * p + 1]);
+        }
+#pragma unroll
+    for (int o = 8; o <= 16; o <<= 1)
+#pragma unroll
+        for (int d = 0; d < N; ++d)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float bh = __shfl_xor_sync(FULL, h[d][j], o), bl = __shfl_xor_sync(FULL, l[d][j], o);
+                df_add(h[d][j], l[d][j], bh, bl);
+            }
+    if (lane < 8)
+#pragma unroll
+        for (int d = 0; d < N; ++d)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                red[d][0][warp][4 * lane + j] = h[d][j];
+                red[d][1][warp][4 * lane + j] = l[d][j];
+            }
+    __syncthreads();
+    double v[N];
+    if (threadIdx.x < 32)
+#pragma unroll
+        for (int d = 0; d < N; ++d) {
+            float sh = red[d][0][0][lane], sl = red[d][1][0][lane];
+#pragma unroll
+            for (int w = 1; w < BS / 32; ++w) df_add(sh, sl, red[d][0][w][lane], red[d][1][w][lane]);
+            v[d] = (double)sh + (double)sl;
+        }
+    return grid_reduce<32, N, true>(v, partial, counter, out);
+}
+
+// k_apply_alpha for 32 FP32 slots
+__global__ void __launch_bounds__(BS, 4) k_apply_alpha4(OpView<float> op, Slot *sl, float m, float n, const float *__restrict__ y,
+                                                     const float *__restrict__ te, const float *__restrict__ r0,
+                                                     float *__restrict__ v, double *partial, unsigned int *counter) {
+    GRID_LOOP4
+    const unsigned act = act4(sl, q, PH_ITER);
+    uint64_t m0, m1;
+    mask4(act, m0, m1);
+    Dot4<1> acc;
+    if (act)
+        ROWS4(op.D, V4_UN) {
+            ROWS4_OF_TRIP(rr, V4_UN)
+            ulonglong2 r0v[V4_UN], vv[V4_UN];
+#pragma unroll
+            for (int u = 0; u < V4_UN; ++u) r0v[u] = rr[u] < op.D ? ld4(r0, rr[u], q) : make_ulonglong2(0ull, 0ull);
+            l_rows4<V4_UN>(op, rr, q, m, n, y, te, vv);
+#pragma unroll
+            for (int u = 0; u < V4_UN; ++u)
+                if (rr[u] < op.D) {
+                    st4(v, rr[u], q, vv[u], act);
+                    acc.add(0, r0v[u], vv[u], m0, m1);
+                }
+        }
+    double tot[1];
+    if (grid_reduce4<1>(acc, partial, counter, tot)) alpha_update<float>(sl[threadIdx.x], tot[0]);
+}
+
+// k_apply_omega for 32 FP32 slots
+__global__ void __launch_bounds__(BS, 4) k_apply_omega4(OpView<float> op, Slot *sl, float m, float n, const float *__restrict__ z,
+                                                     const float *__restrict__ te, const float *__restrict__ sv,
+                                                     float *__restrict__ tv, double *partial, unsigned int *counter) {
+    GRID_LOOP4
+    const unsigned act = act4(sl, q, PH_ITER);
+    uint64_t m0, m1;
+    mask4(act, m0, m1);
+    Dot4<2> acc;
+    if (act)
+        ROWS4(op.D, V4_UN) {
+            ROWS4_OF_TRIP(rr, V4_UN)
+            ulonglong2 svv[V4_UN], tt[V4_UN];
+#pragma unroll
+            for (int u = 0; u < V4_UN; ++u) svv[u] = rr[u] < op.D ? ld4(sv, rr[u], q) : make_ulonglong2(0ull, 0ull);
+            l_rows4<V4_UN>(op, rr, q, m, n, z, te, tt);
+#pragma unroll
+            for (int u = 0; u < V4_UN; ++u)
+                if (rr[u] < op.D) {
+                    st4(tv, rr[u], q, tt[u], act);
+                    acc.add(0, tt[u], tt[u], m0, m1);
+                    acc.add(1, tt[u], svv[u], m0, m1);
+                }
+        }
+    double tot[2];
+    if (grid_reduce4<2>(acc, partial, counter, tot)) omega_update(sl[threadIdx.x], tot[0], tot[1]);
+}
+
+// k_update_xr for 32 FP32 slots
+__global__ void __launch_bounds__(BS, 4) k_update_xr4(int64_t D, Slot *sl, SolveParams P, const float *__restrict__ y,
+                                                   const float *__restrict__ z, const float *__restrict__ sv,
+                                                   const float *__restrict__ tv, const float *__restrict__ r0, float *x,
+                                                   float *__restrict__ r, double *partial, unsigned int *counter) {
+    GRID_LOOP4
+    const unsigned act = act4(sl, q, PH_ITER);
+    uint64_t m0, m1;
+    mask4(act, m0, m1);
+    Dot4<2> acc;
+    if (act) {
+        uint64_t a0, a1, w0, w1;
+        slot_pairs(sl, q, &Slot::alpha, a0, a1);
+        slot_pairs(sl, q, &Slot::omega, w0, w1);
+        const uint64_t nw0 = w0 ^ 0x8000000080000000ull, nw1 = w1 ^ 0x8000000080000000ull;
+        ROWS4(D, 1) {
+            ROWS4_OF_TRIP(rr, 1)
+            ulonglong2 yv[1], zv[1], xv[1], tw[1], sw[1], r0v[1];
+#pragma unroll
+            for (int u = 0; u < 1; ++u)
+                if (rr[u] < D) {
+                    yv[u] = ld4(y, rr[u], q);
+                    zv[u] = ld4(z, rr[u], q);
+                    xv[u] = *(const ulonglong2 *)(x + (uint32_t)rr[u] * 32u + 4 * q);
+                    tw[u] = ld4(tv, rr[u], q);
+                    sw[u] = ld4(sv, rr[u], q);
+                    r0v[u] = ld4(r0, rr[u], q);
+                }
+#pragma unroll
+            for (int u = 0; u < 1; ++u)
+                if (rr[u] < D) {
+                    ulonglong2 xn, rn;
+                    xn.x = f2_fma(w0, zv[u].x, f2_fma(a0, yv[u].x, xv[u].x));
+                    xn.y = f2_fma(w1, zv[u].y, f2_fma(a1, yv[u].y, xv[u].y));
+                    rn.x = f2_fma(nw0, tw[u].x, sw[u].x);
+                    rn.y = f2_fma(nw1, tw[u].y, sw[u].y);
+                    st4(x, rr[u], q, xn, act);
+                    st4(r, rr[u], q, rn, act);
+                    acc.add(0, rn, rn, m0, m1);
+                    acc.add(1, r0v[u], rn, m0, m1);
+                }
+        }
+    }
+    double tot[2];
+    if (grid_reduce4<2>(acc, partial, counter, tot)) xr_update(sl[threadIdx.x], P, tot[0], tot[1]);
 }
 
 // plain-path restart: r = b - A x ; r0 = r ; rho = r0norm2 = ||r||^2
@@ -1006,7 +1275,7 @@ static void plain_iteration(cpm_solver_s *s, const SolveParams &P) {
     Slot *sl = s->slots.p;
     const double *pden = P.precond == 0 ? nullptr : s->pden64.p;
     const double ys = P.precond == 2 ? JACOBI_OMEGA : 1.0;
-    k_update_p<double, K><<<s->G, BS, 0, st>>>(D, sl, pden, ys, s->dr.p, s->dv.p, s->dp.p, s->dy.p);
+    k_update_p<double, K><<<s->G, BS, 0, st>>>(D, sl, pden, ys, s->dr.p, s->dv.p, s->dp.p, s->dy.p, s->dr0.p);
     if (P.precond == 2) jacobi_rest<K>(s, P, s->dp.p, s->dy.p);
     launch_epass<double, K>(op, sl, PH_ITER, s->dy.p, s->te64.p, st);
     k_apply_alpha<double, K><<<s->G, BS, 0, st>>>(op, sl, s->m, s->n, s->dy.p, s->te64.p, s->dr0.p, s->dv.p, s->partial.p,
@@ -1037,14 +1306,27 @@ static void mixed_iteration(cpm_solver_s *s, const SolveParams &P) {
     Slot *sl = s->slots.p;
     const float m = (float)s->m, n = (float)s->n;
     const float *pden = P.precond == 0 ? nullptr : s->pden32.p;
-    k_update_p<float, K><<<s->G, BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fp.p, s->fy.p);
+    // four slots per thread: 32 slots, and row offsets D * 32 within 32 bits
+    const bool v4 = (K == 32) && D * 32 <= (int64_t)UINT32_MAX;
+    k_update_p<float, K><<<s->G, BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fp.p, s->fy.p, s->fr0.p);
     launch_epass<float, K>(op, sl, PH_ITER, s->fy.p, s->fte.p, st);
-    k_apply_alpha<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p, s->counter.p);
+    if (v4)
+        k_apply_alpha4<<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p, s->counter.p);
+    else
+        k_apply_alpha<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p,
+                                                     s->counter.p);
     k_update_s<float, K><<<s->G, BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fs.p, s->fz.p);
     launch_epass<float, K>(op, sl, PH_ITER, s->fz.p, s->fte.p, st);
-    k_apply_omega<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p, s->counter.p);
-    k_update_xr<float, K><<<s->G, BS, 0, st>>>(D, sl, P, s->fy.p, s->fz.p, s->fs.p, s->ft.p, s->fr0.p, s->fx.p, s->fr.p,
-                                               s->partial.p, s->counter.p);
+    if (v4) {
+        k_apply_omega4<<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p, s->counter.p);
+        k_update_xr4<<<s->G, BS, 0, st>>>(D, sl, P, s->fy.p, s->fz.p, s->fs.p, s->ft.p, s->fr0.p, s->fx.p, s->fr.p,
+                                          s->partial.p, s->counter.p);
+    } else {
+        k_apply_omega<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p,
+                                                     s->counter.p);
+        k_update_xr<float, K><<<s->G, BS, 0, st>>>(D, sl, P, s->fy.p, s->fz.p, s->fs.p, s->ft.p, s->fr0.p, s->fx.p, s->fr.p,
+                                                   s->partial.p, s->counter.p);
+    }
 }
 
 // reliable update (FP64) for slots that asked for one
