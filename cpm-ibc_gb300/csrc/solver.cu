@@ -324,6 +324,85 @@ __global__ void __launch_bounds__(128) k_epass32s(OpView<T> op, const Slot *__re
         }
 }
 
+// 32 FP32 slots, warp per base group: the warp gathers the group's 64 x
+// values plane by plane (16 columns each) and keeps each pair of rows' sum in
+// registers (f32x2): plane i adds wx_i (sum_j wy_j sum_k wz_k x_ijk) in the
+// plane order of k_epass32s's combine, so the results are the same bit for
+// bit, with no block-level synchronisation and no shared partial sums.  Rows
+// EW_ROWS at a time; weights staged pair-interleaved in the warp's shared
+// memory.  Identity rows copied warp per row.  ph < 0: every slot.
+constexpr int EW_ROWS = 8;
+__global__ void __launch_bounds__(128) k_epass32w(OpView<float> op, const Slot *__restrict__ sl, int ph,
+                                                  const float *__restrict__ x, float *__restrict__ t) {
+    __shared__ __align__(16) float sw[4][EW_ROWS * 12];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool act = (ph < 0) || sl[lane].phase == ph;
+    if (!__any_sync(FULL, act)) return;  // the same 32 slots in every warp: block-uniform
+    float *w = sw[warp];
+    const int64_t W = (int64_t)gridDim.x * 4;
+    for (int64_t g = (int64_t)blockIdx.x * 4 + warp; g < op.n_grp; g += W) {
+        const int p0 = op.grp[g], p1 = op.grp[g + 1];
+        for (int c0 = p0; c0 < p1; c0 += EW_ROWS) {
+            // rows in pairs, the odd row of a last pair with zero weights
+            const int nr = min(p1 - c0, EW_ROWS), np = (nr + 1) >> 1;
+            __syncwarp();
+            for (int e = lane; e < 24 * np; e += 32) {
+                const int q = e / 12, c = e - 12 * q;
+                w[24 * (q >> 1) + 2 * c + (q & 1)] = q < nr ? op.w_ord[12 * (size_t)(c0 + q) + c] : 0.f;
+            }
+            const int row = lane < nr ? op.ord[c0 + lane] : 0;  // lane q: row q of the chunk
+            __syncwarp();
+            uint64_t acc[EW_ROWS / 2];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                int col[16];
+                float xb[16];
+                e_group_cols(op.gcols, g, i, col);
+                e_group_x(x, col, lane, act, xb);
+                uint64_t x2[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) x2[q] = f2_pack(xb[q], xb[q]);
+#pragma unroll
+                for (int p = 0; p < EW_ROWS / 2; ++p)
+                    if (p < np) {
+                        const float *wp = w + 24 * p;
+                        const uint64_t wx2 = *(const uint64_t *)(wp + 2 * i);
+                        const ulonglong2 y01 = *(const ulonglong2 *)(wp + 8), y23 = *(const ulonglong2 *)(wp + 12);
+                        const ulonglong2 z01 = *(const ulonglong2 *)(wp + 16), z23 = *(const ulonglong2 *)(wp + 20);
+                        const uint64_t wy2[4] = {y01.x, y01.y, y23.x, y23.y}, wz2[4] = {z01.x, z01.y, z23.x, z23.y};
+                        uint64_t ay2 = 0ull;
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            uint64_t az2 = f2_mul(wz2[0], x2[4 * j]);
+                            az2 = f2_fma(wz2[1], x2[4 * j + 1], az2);
+                            az2 = f2_fma(wz2[2], x2[4 * j + 2], az2);
+                            az2 = f2_fma(wz2[3], x2[4 * j + 3], az2);
+                            ay2 = j == 0 ? f2_mul(wy2[0], az2) : f2_fma(wy2[j], az2, ay2);
+                        }
+                        const uint64_t part = f2_mul(wx2, ay2);
+                        acc[p] = i == 0 ? part : f2_add(acc[p], part);
+                    }
+            }
+#pragma unroll
+            for (int p = 0; p < EW_ROWS / 2; ++p)
+                if (2 * p < nr) {
+                    float lo, hi;
+                    f2_unpack(acc[p], lo, hi);
+                    const int r0 = __shfl_sync(FULL, row, 2 * p), r1 = __shfl_sync(FULL, row, 2 * p + 1);
+                    if (act) {
+                        t[(uint32_t)r0 * 32u + lane] = lo;
+                        if (2 * p + 1 < nr) t[(uint32_t)r1 * 32u + lane] = hi;
+                    }
+                }
+        }
+    }
+    if (act)
+        for (int64_t q = (int64_t)blockIdx.x * 4 + warp; q < op.n_ident; q += W) {
+            const uint32_t r = (uint32_t)op.ident[q];
+            t[r * 32u + lane] = x[r * 32u + lane];
+        }
+}
+
 // 1 slot: one thread per row, rows visited in base-point order so that the
 // threads of a warp that share a base read the same cache lines.
 template <class T>
@@ -402,8 +481,13 @@ template <class T, int K>
 static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x, T *t, cudaStream_t st) {
     static_assert(K == 1 || K == 32, "slot widths 1 and 32");
     if constexpr (K == 32) {
-        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(op.n_grp, 16LL * sm_count()));
-        k_epass32s<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
+        if constexpr (sizeof(T) == 4) {
+            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_grp + 3) / 4, 32LL * sm_count()));
+            k_epass32w<<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
+        } else {
+            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(op.n_grp, 16LL * sm_count()));
+            k_epass32s<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
+        }
     } else {
         const int64_t threads = op.n_ord + op.n_ident;
         k_epass1<T><<<(unsigned)((threads + BS - 1) / BS), BS, 0, st>>>(op, sl, ph, x, t);
