@@ -366,6 +366,8 @@ def main():
     ap.add_argument("--rate", type=float, default=2.0, help="serving-mix: mean arrivals per second")
     ap.add_argument("--refine-every", type=int, default=0,
                     help="mixed precision: reliable-update period in iterations (0: the library default)")
+    ap.add_argument("--inner-tol", type=float, default=0.0,
+                    help="mixed precision: residual drop that asks for a reliable update (0: the library default)")
     args = ap.parse_args()
     if args.workload:
         return run_workload(args)
@@ -402,7 +404,7 @@ def main():
     B = np.stack([rhs_from_rows(rows, v) for v in vals])  # [requests][D]
     b_dev = torch.from_numpy(B).to(dev)  # every request's right-hand side resident in HBM
     x_dev = torch.zeros_like(b_dev)
-    srv = cg.Server(O, 0.0, -1.0, tol=TOL, refine_every=args.refine_every)
+    srv = cg.Server(O, 0.0, -1.0, tol=TOL, refine_every=args.refine_every, inner_tol=args.inner_tol or 0.2)
 
     def stream(lo, hi):
         """submit requests lo..hi-1 at once and serve them to completion (continuous batching)"""
@@ -536,7 +538,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-inner/f64-refine", "data": "synthetic",
             "config": {"workload": WORKLOAD, "rows": D, "tube_nodes": O.N, "ibc_dofs": O.total_ibc_dofs,
                        "slots": KSLOTS, "requests_per_step": KSLOTS, "tol": TOL,
-                       "refine_every": args.refine_every or 16,
+                       "refine_every": args.refine_every or 16, "inner_tol": args.inner_tol or 0.2,
                        "serving": "continuous batching: every step's 32 requests submitted at t=0 with RHS resident "
                                   "in HBM; slots refill as solves finish",
                        "l2": "no flush: the served working set (10 FP32 + 4 FP64 [D][32] arrays, "

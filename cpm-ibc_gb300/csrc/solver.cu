@@ -434,10 +434,24 @@ __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__re
     const bool act = (ph < 0) || sl[lane].phase == ph;
     if (!__any_sync(FULL, act)) return;  // the same slots in every warp: block-uniform
     const int64_t warps = (int64_t)gridDim.x * 4;
-    for (int64_t q = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5); q < op.n_pl; q += warps) {
-        const uint32_t r = (uint32_t)op.pl_row[q];
-        const int e0 = op.pl_off[q], e1 = op.pl_off[q + 1];
-        const int xc = op.pl_xcol[q];
+    int64_t q = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (q >= op.n_pl) return;
+    // the row's list record, loaded one row ahead
+    uint32_t r_n = (uint32_t)op.pl_row[q];
+    int e0_n = op.pl_off[q], e1_n = op.pl_off[q + 1], xc_n = op.pl_xcol[q], neg_n = op.pl_neg[q];
+    T xv_n = op.pl_xval[q];
+    for (; q < op.n_pl; q += warps) {
+        const uint32_t r = r_n;
+        const int e0 = e0_n, e1 = e1_n, xc = xc_n, neg = neg_n;
+        const T xv = xv_n;
+        if (q + warps < op.n_pl) {
+            r_n = (uint32_t)op.pl_row[q + warps];
+            e0_n = op.pl_off[q + warps];
+            e1_n = op.pl_off[q + warps + 1];
+            xc_n = op.pl_xcol[q + warps];
+            neg_n = op.pl_neg[q + warps];
+            xv_n = op.pl_xval[q + warps];
+        }
         T acc = act ? t[r * 32u + lane] : T(0);
         const T xe = (act && xc >= 0) ? x[(uint32_t)xc * 32u + lane] : T(0);
         for (int base = e0; base < e1; base += 32) {
@@ -465,8 +479,8 @@ __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__re
                     if (u0 + u < cnt) acc += ww[u] * (xn[u] - xo[u]);
             }
         }
-        if (op.pl_neg[q]) acc = -acc;
-        if (xc >= 0) acc += op.pl_xval[q] * xe;
+        if (neg) acc = -acc;
+        if (xc >= 0) acc += xv * xe;
         if (act) t[r * 32u + lane] = acc;
     }
 }
