@@ -331,20 +331,28 @@ def run_workload(args):
         span = time.perf_counter() - t
         lat = {k: [o["latency"] for o in out.values() if o["kind"] == k] for k in ("laplace", "geodesic")}
         fb = sum(1 for o in out.values() if o["kind"] == "laplace" and o["stats"].get("fp64_fallback"))
-        sample = [r for r in reqs if r["kind"] == "laplace"][:12]
-        t64 = SV.fp64_one_at_a_time(surfaces, sample)
+        t = time.perf_counter()
+        out64 = SV.serve_fp64_one_at_a_time(surfaces, reqs)
+        span64 = time.perf_counter() - t
+        lat64 = {k: [o["latency"] for o in out64.values() if o["kind"] == k] for k in ("laplace", "geodesic")}
+
+        def pct(v):
+            return {k: {"p50": float(np.percentile(x, 50) * 1e3), "p99": float(np.percentile(x, 99) * 1e3), "n": len(x)}
+                    for k, x in v.items() if x}
+
         line.update({
             "config": {"surfaces": {s.name: {"tube_nodes": s.tube.N, "rows": s.opset.D, "curves": s.n_ibc,
                                              "server_bytes": s.bytes} for s in surfaces},
                        "requests": args.requests, "rate_per_s": args.rate, "geodesic_every": 32,
                        "arrivals": "seeded Poisson process", "slots_per_surface": 32, "tol": TOL},
             "setup_s": t_setup, "makespan_s": span, "solves_per_s": len(out) / span,
-            "latency_ms": {k: {"p50": float(np.percentile(v, 50) * 1e3), "p99": float(np.percentile(v, 99) * 1e3),
-                               "n": len(v)} for k, v in lat.items() if v},
+            "latency_ms": pct(lat),
             "laplace_fp64_fallbacks": fb, "admissions": loop.admissions, "evictions": loop.evictions,
             "precision_switches": loop.precision_switches,
             "final_precision": {s.name: ("mixed" if s.precision else "fp64") for s in surfaces},
-            "fp64_one_at_a_time_laplace_solves_per_s": len(t64) / sum(t64),
+            "solo_fp64_solves": loop.solo_solves,
+            "fp64_one_at_a_time": {"makespan_s": span64, "solves_per_s": len(out64) / span64, "latency_ms": pct(lat64),
+                                   "path": "the same stream and arrival times, each request solved alone in FP64"},
             "note": "geodesics run one at a time on their own point-IBC operator between server steps",
         })
     print(json.dumps(line), flush=True)
@@ -404,7 +412,7 @@ def main():
     B = np.stack([rhs_from_rows(rows, v) for v in vals])  # [requests][D]
     b_dev = torch.from_numpy(B).to(dev)  # every request's right-hand side resident in HBM
     x_dev = torch.zeros_like(b_dev)
-    srv = cg.Server(O, 0.0, -1.0, tol=TOL, refine_every=args.refine_every, inner_tol=args.inner_tol or 0.2)
+    srv = cg.Server(O, 0.0, -1.0, tol=TOL, refine_every=args.refine_every, inner_tol=args.inner_tol)
 
     def stream(lo, hi):
         """submit requests lo..hi-1 at once and serve them to completion (continuous batching)"""
@@ -491,7 +499,7 @@ def main():
     assert all(got[k][1]["status"] == 0 for k in he)
     e2e_value = world * n_e2e / e2e_s
 
-    # ---- roofline of the L.E apply (FP32, 32 RHS): E pass + L pass on the library stream
+    # ---- roofline of the L.E apply (FP32, 32 RHS): E pass, IBC patch rows and L pass on the library stream
     xf = torch.randn((D, KSLOTS), dtype=torch.float32, device=dev)
     tf = torch.empty_like(xf)
     yf = torch.empty_like(xf)
@@ -538,7 +546,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-inner/f64-refine", "data": "synthetic",
             "config": {"workload": WORKLOAD, "rows": D, "tube_nodes": O.N, "ibc_dofs": O.total_ibc_dofs,
                        "slots": KSLOTS, "requests_per_step": KSLOTS, "tol": TOL,
-                       "refine_every": args.refine_every or 16, "inner_tol": args.inner_tol or 0.2,
+                       "refine_every": args.refine_every or 32, "inner_tol": args.inner_tol or 0.1,
                        "serving": "continuous batching: every step's 32 requests submitted at t=0 with RHS resident "
                                   "in HBM; slots refill as solves finish",
                        "l2": "no flush: the served working set (10 FP32 + 4 FP64 [D][32] arrays, "
@@ -558,11 +566,12 @@ def main():
             "rel_err_vs_fp64": rel_err,
             "iterations_p50": float(np.median(iters)), "iterations_max": int(max(iters)),
             "refinements_p50": float(np.median(refs)),
+            "fp64_fallbacks": int(sum(int(x.get("fp64_fallback", 0)) for x in st_timed)),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(D * KSLOTS * 8),
                     "d2h_bytes_per_step": int(D * KSLOTS * 8),
                     "path": "cpm_server_submit / cpm_server_step / cpm_server_poll with host arrays, 64 requests"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "kernel": "L.E apply (E pass + L pass), FP32, 32 RHS",
+                         "traffic": traffic, "kernel": "L.E apply (E pass + IBC patch rows + L pass), FP32, 32 RHS",
                          "apply_us": apply_s * 1e6, "alg_bytes_per_apply": alg_bytes, "peak_source": peak_src},
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),

@@ -52,6 +52,7 @@ struct Slot {
     int phase, iters, inner_iters, refinements, restarts, status, krylov_restart;
     int stall;      // mixed path: reliable updates since rbest last improved by 10%
     int fresh;      // mixed path: Krylov space restarted from the FP32 residual, p = r0 = r pending
+    int upd_iters;  // mixed path: FP32 iterations since the last reliable update
 };
 
 struct SolveParams {
@@ -241,6 +242,7 @@ __device__ __forceinline__ void xr_update(Slot &S, const SolveParams &P, double 
     if (S.phase != PH_ITER) return;
     S.iters += 1;
     S.inner_iters += 1;
+    S.upd_iters += 1;
     S.rr = rr;
     const bool conv = S.rr <= S.tol2;  // false for a non-finite residual
     if (P.mixed) {
@@ -588,6 +590,7 @@ __global__ void __launch_bounds__(BS, 4) k_init(OpView<T> op, Slot *sl, SolvePar
         S.alpha = 1.0;
         S.omega = 1.0;
         S.inner_iters = 0;
+        S.upd_iters = 0;
         S.krylov_restart = 0;
         if (from_phase == PH_INNER_INIT) {
             // claimed convergence of the FP32 residual, in the scaled system
@@ -951,6 +954,26 @@ __device__ __forceinline__ bool grid_reduce4(const Dot4<N> &acc, double *partial
     return grid_reduce<32, N, true>(v, partial, counter, out);
 }
 
+// k_lpass for 32 FP32 slots (every slot)
+__global__ void __launch_bounds__(BS, 4) k_lpass4(OpView<float> op, float m, float n, const float *__restrict__ x,
+                                               const float *__restrict__ t, float *__restrict__ y) {
+    GRID_LOOP4
+    ROWS4(op.D, V4_UN) {
+        ROWS4_OF_TRIP(rr, V4_UN)
+        ulonglong2 v[V4_UN];
+        l_rows4<V4_UN>(op, rr, q, m, n, x, t, v);
+#pragma unroll
+        for (int u = 0; u < V4_UN; ++u)
+            if (rr[u] < op.D) st4(y, rr[u], q, v[u], 15u);
+    }
+}
+
+// the four-slot row kernels read and write 16-byte vectors: caller-owned
+// arrays must be 16-byte aligned, and row offsets D * 32 must fit 32 bits
+static inline bool lpass4_ok(int64_t D, const void *a, const void *b, const void *c) {
+    return D * 32 <= (int64_t)UINT32_MAX && ((uintptr_t)a % 16) == 0 && ((uintptr_t)b % 16) == 0 && ((uintptr_t)c % 16) == 0;
+}
+
 // k_apply_alpha for 32 FP32 slots
 __global__ void __launch_bounds__(BS, 4) k_apply_alpha4(OpView<float> op, Slot *sl, float m, float n, const float *__restrict__ y,
                                                      const float *__restrict__ te, const float *__restrict__ r0,
@@ -1093,13 +1116,16 @@ __global__ void __launch_bounds__(BS, 4) k_restart(OpView<T> op, Slot *sl, T m, 
 
 // reliable updates run for all slots at once every few iterations, so one FP64
 // apply serves every slot that needs it: a slot joins when its FP32 residual has
-// fallen by delta since its last update (Sleijpen & van der Vorst's criterion)
+// fallen by delta since its last update (Sleijpen & van der Vorst's criterion),
+// or after four periods without one (an FP32 residual stuck above delta would
+// otherwise never meet the true residual, nor the stagnation exit)
 template <int K>
 __global__ void k_refine_gate(Slot *sl, SolveParams P) {
     const int s = threadIdx.x;
     if (s >= K) return;
     Slot &S = sl[s];
-    if (S.phase == PH_ITER && S.rr <= P.delta * P.delta * S.rr_max) S.phase = PH_REFINE;
+    if (S.phase == PH_ITER && (S.rr <= P.delta * P.delta * S.rr_max || S.upd_iters >= 4 * P.refine_every))
+        S.phase = PH_REFINE;
 }
 
 // reliable update, step 1: x64 += scale * u32, u32 = 0
@@ -1152,9 +1178,9 @@ __global__ void __launch_bounds__(BS, 4) k_refine_residual(OpView<double> op, Sl
         if (tot[0] <= S.outer_tol2) {
             S.phase = PH_DONE;
             S.status = 0;
-        } else if (S.refinements >= P.max_refine || S.iters >= P.max_iters || !isfinite(tot[0]) || S.stall >= 40 ||
+        } else if (S.refinements >= P.max_refine || S.iters >= P.max_iters || !isfinite(tot[0]) || S.stall >= 16 ||
                    S.rnorm64 > 1e6 * sqrt(S.b64norm2)) {
-            // out of budget, non-finite, no 10% gain of the true residual in 40
+            // out of budget, non-finite, no 10% gain of the true residual in 16
             // reliable updates, or diverged: the FP32 iteration cannot solve this system
             S.phase = PH_DONE;
             S.status = isfinite(tot[0]) ? CPM_ERR_NOT_CONVERGED : CPM_ERR_BREAKDOWN;
@@ -1210,6 +1236,7 @@ __global__ void __launch_bounds__(BS, 4) k_reliable(int64_t D, Slot *sl, const d
         S.rr = tot[0];
         S.rr_max = tot[0];
         S.rr_upd = tot[0];
+        S.upd_iters = 0;
         if (S.krylov_restart) {
             S.krylov_restart = 0;
             S.restarts += 1;
@@ -1469,9 +1496,9 @@ static int parse_params(const cpm_solve_opts *o, SolveParams &P) {
     P.tol = o->tol > 0 ? o->tol : 1e-10;
     P.max_iters = o->max_iters > 0 ? o->max_iters : 100000;
     P.mixed = o->precision == 1;
-    P.delta = o->inner_tol > 0 ? o->inner_tol : 0.2;
+    P.delta = o->inner_tol > 0 ? o->inner_tol : 0.1;
     P.max_refine = o->max_refine > 0 ? o->max_refine : 400;
-    P.refine_every = o->refine_every > 0 ? o->refine_every : 16;
+    P.refine_every = o->refine_every > 0 ? o->refine_every : 32;
     if (P.refine_every > 32 || (P.refine_every & (P.refine_every - 1)))
         return fail(CPM_ERR_INVALID_ARG, "refine_every must be 1, 2, 4, 8, 16 or 32");
     P.precond = o->precond;
@@ -2000,7 +2027,10 @@ extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslo
             k_lpass<float, 1><<<row_grid(D, 1), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
         } else {
             launch_epass<float, 32>(v, nullptr, -1, x, t, st);
-            k_lpass<float, 32><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
+            if (lpass4_ok(D, x, t, y))
+                k_lpass4<<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
+            else
+                k_lpass<float, 32><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
         }
     } else {
         auto v = op->view<double>();
@@ -2069,7 +2099,10 @@ extern "C" int cpm_apply_device_noalloc(cpm_opset_t op, double m, double n, int3
             k_lpass<float, 1><<<row_grid(D, 1), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
         } else {
             launch_epass<float, 32>(v, nullptr, -1, x, tt, st);
-            k_lpass<float, 32><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
+            if (lpass4_ok(D, x, tt, y))
+                k_lpass4<<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
+            else
+                k_lpass<float, 32><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
         }
     } else {
         auto v = op->view<double>();

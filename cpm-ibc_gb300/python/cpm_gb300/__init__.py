@@ -345,7 +345,7 @@ class Solver:
         except Exception:
             pass
 
-    def solve(self, b, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.2, max_refine=400, raise_on_error=True,
+    def solve(self, b, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.0, max_refine=400, raise_on_error=True,
               precond=DIAGONAL, precond_iters=0, refine_every=0):
         b = np.ascontiguousarray(np.atleast_2d(b), np.float64)
         k = b.shape[0]
@@ -361,7 +361,7 @@ class Solver:
             raise CpmError(rc, lib().cpm_last_error().decode() + f" stats={stats}")
         return x, stats
 
-    def solve_device(self, b_ptr, x_ptr, k, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.2, max_refine=400,
+    def solve_device(self, b_ptr, x_ptr, k, tol=1e-10, precision=0, max_iters=100000, inner_tol=0.0, max_refine=400,
                      precond=DIAGONAL, precond_iters=0, refine_every=0):
         o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=precond, precond_iters=precond_iters,
                       inner_tol=inner_tol, max_refine=max_refine, refine_every=refine_every)
@@ -380,7 +380,7 @@ class Server:
     in flight in a 32-slot solver (precision 1: FP32 with FP64 reliable
     updates; 0: plain FP64), admitted as slots free up."""
 
-    def __init__(self, opset, m, n, tol=1e-10, inner_tol=0.2, max_refine=400, refine_every=0, max_iters=100000,
+    def __init__(self, opset, m, n, tol=1e-10, inner_tol=0.0, max_refine=400, refine_every=0, max_iters=100000,
                  precision=1):
         self.opset, self.D, self.precision = opset, opset.D, precision
         o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=DIAGONAL, precond_iters=0,

@@ -14,9 +14,21 @@ fixed IBC curves) on the device.  Requests arrive over time:
 
 A surface's server is admitted only while the device has room for it (its
 estimated bytes within the HBM budget); an idle server is released to make
-room for another surface's.  A surface starts on the mixed-precision server;
-once a quarter of its finished requests (at least 8 finished) needed the FP64
-re-solve, it drains that server and continues on a plain FP64 32-slot server.
+room for another surface's.
+
+A 32-slot batch costs about the same whether it holds one request or 32, so
+requests are solved alone by the plain FP64 path (the reference's algorithm,
+one right-hand side) while a surface's server is idle and fewer of them wait
+than the break-even count: a 32-slot iteration costs about K32_MIXED (FP32
+with FP64 reliable updates) or K32_FP64 one-RHS FP64 iterations, times the
+surface's measured ratio of mixed to FP64 iteration counts.  A surface's first
+request is always solved alone, which measures its FP64 iteration count; its
+mixed-precision server then stops a solve after 6x that many iterations (and
+re-solves it in FP64).  The first mixed batch is a probe of PROBE requests
+(others are served alone meanwhile); once a quarter of a surface's finished
+batched requests (at least two of at least two) needed the FP64 re-solve, it
+stops feeding that server, serves its requests alone while it drains, and
+continues on a plain FP64 32-slot server.
 Latency is measured from a request's arrival to the harvest of its result.
 """
 import heapq
@@ -27,6 +39,9 @@ import numpy as np
 from . import DIAGONAL, Geodesic, OpSet, Server, Solver, device_info
 
 MAX_SLOTS = 32
+PROBE = 2  # requests in a surface's first mixed-precision batch
+K32_MIXED = 2.3  # 32-slot FP32 iteration (reliable updates amortised) / one-RHS FP64 iteration
+K32_FP64 = 14.0  # 32-slot FP64 iteration / one-RHS FP64 iteration
 
 
 class ServedSurface:
@@ -47,8 +62,22 @@ class ServedSurface:
         self.finished = 0
         self.fallbacks = 0
         self.switch_pending = False
-        self.inflight = 0  # submitted to the server and not yet harvested
+        self.inflight_arrival = {}  # submitted to the server, not yet harvested: id -> arrival
+        self.submitted = 0  # requests ever submitted to a mixed-precision server
+        self.solo = None  # one-RHS FP64 solver for requests served alone
+        self.fp64_iters = None  # running mean iterations of a solo FP64 solve
+        self.mixed_iters = None  # running mean iterations of a batched mixed solve
         self._cp = None
+
+    def break_even(self):
+        """requests waiting from which a 32-slot batch beats solving them one by one
+        (None until the surface's FP64 iteration count is measured)"""
+        if self.fp64_iters is None:
+            return None
+        if self.precision == 0:
+            return max(2, int(np.ceil(K32_FP64)))
+        ratio = self.mixed_iters / self.fp64_iters if self.mixed_iters else 2.0
+        return max(2, int(np.ceil(K32_MIXED * ratio)))
 
     def rhs(self, values):
         """PoissonWithIBC::GetRHS with f = 0: Dirichlet value values[c] on curve c."""
@@ -79,6 +108,7 @@ class ServingLoop:
         self.admissions = 0
         self.evictions = 0
         self.precision_switches = 0
+        self.solo_solves = 0
 
     def _held(self):
         return sum(s.bytes for s in self.surfaces.values() if s.server is not None)
@@ -98,85 +128,141 @@ class ServingLoop:
                         break
         if self._held() + s.bytes > self.budget:
             return False
-        s.server = Server(s.opset, s.m, s.n, tol=s.tol, precision=s.precision)
+        cap = max(200, int(6 * s.fp64_iters)) if (s.precision == 1 and s.fp64_iters) else 100000
+        s.server = Server(s.opset, s.m, s.n, tol=s.tol, precision=s.precision, max_iters=cap)
         self.admissions += 1
         return True
+
+    def _solo(self, s, keep_solutions, t0, out):
+        """the oldest waiting request of s alone, plain FP64"""
+        rid, b, arr = s.waiting.pop(0)
+        if s.solo is None:
+            s.solo = Solver(s.opset, s.m, s.n, kslots=1)
+        t = time.perf_counter()
+        x, st = s.solo.solve(b, tol=s.tol, precision=0, precond=DIAGONAL)
+        dt = time.perf_counter() - t
+        it = float(st[0]["iterations"])
+        s.fp64_iters = it if s.fp64_iters is None else 0.7 * s.fp64_iters + 0.3 * it
+        self.solo_solves += 1
+        done = time.perf_counter() - t0
+        rec = dict(kind="laplace", surface=s.name, arrival=arr, completion=done, latency=done - arr,
+                   stats=dict(st[0], service=dt), precision=0, mode="solo")
+        if keep_solutions:
+            rec["x"] = x[0]
+        out[rid] = rec
+
+    def _step(self, s, keep_solutions, t0, out):
+        """one iteration graph of s's server, then its finished requests"""
+        a, q, _ = s.server.step()
+        s.active = (a + q) > 0
+        while True:
+            res = s.server.poll(want_x=keep_solutions)
+            if res is None:
+                break
+            rid, x, st = res
+            done = time.perf_counter() - t0
+            arr = s.inflight_arrival.pop(rid)
+            rec = dict(kind="laplace", surface=s.name, arrival=arr, completion=done, latency=done - arr, stats=st,
+                       precision=s.precision, mode="batched")
+            if s.precision == 1 and not st.get("fp64_fallback"):
+                it = float(st["iterations"])
+                s.mixed_iters = it if s.mixed_iters is None else 0.7 * s.mixed_iters + 0.3 * it
+            s.finished += 1
+            s.fallbacks += int(st.get("fp64_fallback", 0))
+            if s.precision == 1 and s.fallbacks >= 2 and 4 * s.fallbacks >= s.finished:
+                s.switch_pending = True
+            if keep_solutions:
+                rec["x"] = x
+            out[rid] = rec
 
     def run(self, requests, keep_solutions=False):
         """requests: list of dicts {id, t (arrival, seconds from start), surface,
         kind ('laplace' | 'geodesic'), values | source}.  Returns {id: record}
-        with arrival, completion, latency, kind, surface, stats (and x if kept)."""
+        with arrival, completion, latency, kind, surface, stats (and x if kept).
+
+        Earliest arrival first: each pass runs the one unit of work (an
+        iteration graph of a server, a request solved alone, a batch submitted
+        to a server, or a geodesic) whose oldest request arrived first."""
         order = sorted(requests, key=lambda r: r["t"])
         heap = [(r["t"], i, r) for i, r in enumerate(order)]
         heapq.heapify(heap)
         geo_wait = []
         out = {}
-        arrival = {}
         t0 = time.perf_counter()
         total = len(order)
+        for s in self.surfaces.values():
+            s.inflight_arrival = {}
         while len(out) < total:
             now = time.perf_counter() - t0
             while heap and heap[0][0] <= now:
                 _, _, r = heapq.heappop(heap)
-                arrival[r["id"]] = r["t"]
                 s = self.surfaces[r["surface"]]
                 if r["kind"] == "laplace":
                     s.waiting.append((r["id"], s.rhs(r["values"]), r["t"]))
                 else:
                     geo_wait.append(r)
-            progressed = False
             for s in self.surfaces.values():
                 if s.switch_pending and s.server is not None and not s.active:
                     s.server = None
                     s.precision = 0
                     s.switch_pending = False
                     self.precision_switches += 1
-                if s.waiting and not s.switch_pending and self._admit(s):
-                    # at most two batches in the server, so a precision switch takes
-                    # effect within two batches
-                    take = max(0, min(len(s.waiting), 2 * MAX_SLOTS - s.inflight))
-                    for rid, b, _ in s.waiting[:take]:
-                        s.server.submit(b, rid)
-                    s.waiting = s.waiting[take:]
-                    s.inflight += take
-                    s.active = s.active or take > 0
+            # candidate units of work, keyed by the arrival of their oldest request
+            cands = []
+            for s in self.surfaces.values():
                 if s.server is not None and s.active:
-                    a, q, _ = s.server.step()
-                    s.active = (a + q) > 0
-                    progressed = True
-                    while True:
-                        res = s.server.poll(want_x=keep_solutions)
-                        if res is None:
-                            break
-                        rid, x, st = res
-                        done = time.perf_counter() - t0
-                        rec = dict(kind="laplace", surface=s.name, arrival=arrival[rid], completion=done,
-                                   latency=done - arrival[rid], stats=st, precision=s.precision)
-                        s.finished += 1
-                        s.inflight -= 1
-                        s.fallbacks += int(st.get("fp64_fallback", 0))
-                        if s.precision == 1 and s.finished >= 8 and 4 * s.fallbacks >= s.finished:
-                            s.switch_pending = True
-                        if keep_solutions:
-                            rec["x"] = x
-                        out[rid] = rec
+                    cands.append((min(s.inflight_arrival.values(), default=now), 0, s.name, "step"))
+                if not s.waiting:
+                    continue
+                idle = s.server is None or not s.active
+                probing = s.precision == 1 and s.finished < PROBE and s.submitted >= PROBE
+                be = s.break_even()
+                if be is None or s.switch_pending or probing or (idle and len(s.waiting) < be):
+                    cands.append((s.waiting[0][2], 1, s.name, "solo"))
+                elif len(s.inflight_arrival) < 2 * MAX_SLOTS:
+                    cands.append((s.waiting[0][2], 1, s.name, "submit"))
             if geo_wait:
+                cands.append((geo_wait[0]["t"], 2, None, "geodesic"))
+            if not cands:
+                if heap:
+                    time.sleep(max(0.0, min(0.002, heap[0][0] - (time.perf_counter() - t0))))
+                continue
+            _, _, name, what = min(cands)
+            if what == "geodesic":
                 r = geo_wait.pop(0)
                 s = self.surfaces[r["surface"]]
-                g = Geodesic(s.tube, r["source"])
-                dx = s.tube.dx
                 # a surface whose Laplace solves left mixed precision runs its geodesics in FP64 too
                 prec = min(self.geodesic_precision, s.precision)
-                phi, its = g.run(self.dt_scale * dx * dx, precision=prec, tol=s.tol)
+                phi, its = Geodesic(s.tube, r["source"]).run(self.dt_scale * s.tube.dx ** 2, precision=prec, tol=s.tol)
                 done = time.perf_counter() - t0
                 rec = dict(kind="geodesic", surface=s.name, arrival=r["t"], completion=done, latency=done - r["t"],
                            stats=dict(iterations=its))
                 if keep_solutions:
                     rec["x"] = phi
                 out[r["id"]] = rec
-                progressed = True
-            if not progressed and heap:
-                time.sleep(max(0.0, min(0.002, heap[0][0] - (time.perf_counter() - t0))))
+                continue
+            s = self.surfaces[name]
+            if what == "solo":
+                self._solo(s, keep_solutions, t0, out)
+            elif what == "step":
+                self._step(s, keep_solutions, t0, out)
+            elif self._admit(s):
+                # at most two batches in the server, so a precision switch takes effect within two batches
+                take = max(0, min(len(s.waiting), 2 * MAX_SLOTS - len(s.inflight_arrival)))
+                if s.precision == 1 and s.finished < PROBE:
+                    take = min(take, max(0, PROBE - s.submitted))
+                if s.precision == 1:
+                    s.submitted += take
+                for rid, b, arr in s.waiting[:take]:
+                    s.server.submit(b, rid)
+                    s.inflight_arrival[rid] = arr
+                s.waiting = s.waiting[take:]
+                s.active = s.active or take > 0
+                if s.active:
+                    self._step(s, keep_solutions, t0, out)
+            else:
+                # no room on the device for this surface's server: serve the request alone
+                self._solo(s, keep_solutions, t0, out)
         return out
 
 
@@ -200,6 +286,35 @@ def poisson_stream(surfaces, count, rate, geodesic_every=32, seed=0):
             reqs.append(dict(id=i, t=float(t[i]), surface=s.name, kind="laplace",
                              values=rng.uniform(0, 1, size=s.n_ibc)))
     return reqs
+
+
+def serve_fp64_one_at_a_time(surfaces, requests, dt_scale=1.0, keep_solutions=False):
+    """The plain FP64 path serving the same stream: requests in arrival order,
+    each solved alone once it has arrived (one right-hand side, the reference's
+    algorithm; geodesics in FP64).  Returns {id: record} like ServingLoop.run."""
+    by = {s.name: s for s in surfaces}
+    solvers = {}
+    out = {}
+    t0 = time.perf_counter()
+    for r in sorted(requests, key=lambda q: q["t"]):
+        wait = r["t"] - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        s = by[r["surface"]]
+        if r["kind"] == "laplace":
+            if s.name not in solvers:
+                solvers[s.name] = Solver(s.opset, s.m, s.n, kslots=1)
+            x, st = solvers[s.name].solve(s.rhs(r["values"]), tol=s.tol, precision=0, precond=DIAGONAL)
+            x, stats = x[0], st[0]
+        else:
+            x, its = Geodesic(s.tube, r["source"]).run(dt_scale * s.tube.dx ** 2, precision=0, tol=s.tol)
+            stats = dict(iterations=its)
+        done = time.perf_counter() - t0
+        rec = dict(kind=r["kind"], surface=s.name, arrival=r["t"], completion=done, latency=done - r["t"], stats=stats)
+        if keep_solutions:
+            rec["x"] = x
+        out[r["id"]] = rec
+    return out
 
 
 def fp64_one_at_a_time(surfaces, requests, geodesic_precision=0, dt_scale=1.0):

@@ -36,3 +36,24 @@ def test_serving_mix_results_and_admission(gpu):
             g = gpu.Geodesic(s.tube, r["source"])
             p64, _ = g.run(s.tube.dx ** 2, precision=0)
             assert np.max(np.abs(rec["x"] - p64)) / np.max(np.abs(p64)) <= 1e-8
+
+
+def test_sparse_stream_solves_alone_in_fp64(gpu):
+    """A stream slow enough that requests arrive one by one: each is solved
+    alone by the plain FP64 path (a 32-slot batch of one costs a full batch),
+    with the same results as the FP64 device solve."""
+    surfaces = W.serving_surfaces(gpu, dx_scale=5.0, mesh_level=3, n_curves=2)
+    by = {s.name: s for s in surfaces}
+    loop = SV.ServingLoop(surfaces)
+    reqs = SV.poisson_stream(surfaces, 12, rate=8.0, geodesic_every=0, seed=4)
+    out = loop.run(reqs, keep_solutions=True)
+    assert sorted(out) == [r["id"] for r in reqs]
+    assert loop.solo_solves >= 1
+    assert any(o["mode"] == "solo" for o in out.values())
+    for r in reqs:
+        rec = out[r["id"]]
+        s = by[r["surface"]]
+        x64, _ = gpu.Solver(s.opset, 0.0, -1.0).solve(s.rhs(r["values"]), tol=1e-12, precision=0)
+        assert np.max(np.abs(rec["x"] - x64[0])) / np.max(np.abs(x64[0])) <= 1e-8
+    base = SV.serve_fp64_one_at_a_time(surfaces, reqs)
+    assert sorted(base) == sorted(out)

@@ -43,3 +43,23 @@ def test_plane_loops_closed_on_plane():
         assert np.ptp(h) < 1e-12  # on one plane
         assert np.array_equal(segs[:, 1], np.roll(segs[:, 0], -1))  # closed chain
         assert len(np.unique(np.round(pts, 14), axis=0)) == len(pts)
+
+
+def test_break_even_count():
+    """Requests waiting from which a 32-slot batch beats one-by-one FP64 solves:
+    unknown until the surface's FP64 iteration count is measured; then the
+    32-slot iteration cost (in one-RHS FP64 iterations) times the ratio of
+    mixed to FP64 iterations (2 until measured), at least 2."""
+    from cpm_gb300 import serving as SV
+
+    s = object.__new__(SV.ServedSurface)
+    s.precision, s.fp64_iters, s.mixed_iters = 1, None, None
+    assert s.break_even() is None
+    s.fp64_iters = 247.0
+    assert s.break_even() == int(np.ceil(SV.K32_MIXED * 2.0))
+    s.mixed_iters = 466.0
+    assert s.break_even() == int(np.ceil(SV.K32_MIXED * 466.0 / 247.0))
+    s.mixed_iters = 100.0
+    assert s.break_even() == 2
+    s.precision = 0
+    assert s.break_even() == int(np.ceil(SV.K32_FP64))
