@@ -370,8 +370,8 @@ def main():
                     help="run only a few applies (or one batched solve) of the workload, for ncu")
     ap.add_argument("--workload", choices=["torus-geodesic", "mesh-curves", "serving-mix"], default=None,
                     help="one line for another configuration instead of the headline benchmark")
-    ap.add_argument("--requests", type=int, default=96, help="serving-mix: requests in the stream")
-    ap.add_argument("--rate", type=float, default=2.0, help="serving-mix: mean arrivals per second")
+    ap.add_argument("--requests", type=int, default=160, help="serving-mix: requests in the stream")
+    ap.add_argument("--rate", type=float, default=8.0, help="serving-mix: mean arrivals per second")
     ap.add_argument("--refine-every", type=int, default=0,
                     help="mixed precision: reliable-update period in iterations (0: the library default)")
     ap.add_argument("--inner-tol", type=float, default=0.0,
