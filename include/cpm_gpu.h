@@ -196,11 +196,11 @@ typedef struct cpm_solve_opts {
     int32_t precision;      /* 0 plain FP64 BiCGStab, 1 FP32 BiCGStab refined in FP64 (reliable updates) */
     int32_t precond;        /* 0 identity, 1 diagonal, 2 jacobi (Defines.h:13-18) */
     int32_t precond_iters;  /* jacobi sweeps (Solver::SetPrecond, src/Solver.cpp:115-120) */
-    double inner_tol;       /* precision 1: the FP32 residual reduction (default 0.2) after which the
+    double inner_tol;       /* precision 1: the FP32 residual reduction (0: 0.1) after which the
                                FP64 true residual replaces it (one refinement step) */
     int32_t max_refine;     /* FP64 refinement steps (default 400) */
     int32_t refine_every;   /* precision 1: iterations between reliable-update points, one of
-                               1, 2, 4, 8, 16, 32 (0: 16) */
+                               1, 2, 4, 8, 16, 32 (0: 32) */
 } cpm_solve_opts;
 
 typedef struct cpm_solve_stats {
