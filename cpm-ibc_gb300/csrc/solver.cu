@@ -341,6 +341,7 @@ __global__ void __launch_bounds__(128) k_epass32w(OpView<float> op, const Slot *
     const bool act = (ph < 0) || sl[lane].phase == ph;
     if (!__any_sync(FULL, act)) return;  // the same 32 slots in every warp: block-uniform
     float *w = sw[warp];
+    const float *__restrict__ xl = x + lane;
     const int64_t W = (int64_t)gridDim.x * 4;
     for (int64_t g = (int64_t)blockIdx.x * 4 + warp; g < op.n_grp; g += W) {
         const int p0 = op.grp[g], p1 = op.grp[g + 1];
@@ -360,7 +361,10 @@ __global__ void __launch_bounds__(128) k_epass32w(OpView<float> op, const Slot *
                 int col[16];
                 float xb[16];
                 e_group_cols(op.gcols, g, i, col);
-                e_group_x(x, col, lane, act, xb);
+                // every lane loads (inactive slots' values are computed and not stored);
+                // the rows are whole 128-byte lines either way
+#pragma unroll
+                for (int q = 0; q < 16; ++q) xb[q] = xl[(uint32_t)col[q] * 32u];
                 uint64_t x2[16];
 #pragma unroll
                 for (int q = 0; q < 16; ++q) x2[q] = f2_pack(xb[q], xb[q]);
@@ -1368,11 +1372,13 @@ struct cpm_solver_s {
     SolveParams gp_plain{}, gp_mixed{};
     int chunk = 16;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cpm_solver_s *fb1 = nullptr;  // 32 slots: one-slot FP64 solver for a few mixed solves to redo
     ~cpm_solver_s() {
         if (g_plain) cudaGraphExecDestroy(g_plain);
         if (g_mixed) cudaGraphExecDestroy(g_mixed);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
+        delete fb1;
     }
 };
 
@@ -1658,6 +1664,32 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
     for (int j = 0; j < k; ++j) {
         slot_stats(s->h_slots[j], P.mixed, ms, &st[j]);
         if (P.mixed && st[j].status != 0) redo[j] = any_redo = true;
+    }
+    int n_redo = 0;
+    for (int j = 0; j < k; ++j) n_redo += redo[j];
+    // a 32-slot FP64 iteration costs about 14 one-slot ones: a few right-hand sides
+    // are solved again one at a time
+    if (K == 32 && n_redo > 0 && n_redo < 14) {
+        if (!s->fb1) CPM_TRY(cpm_solver_create(s->op, s->m, s->n, 1, &s->fb1));
+        cpm_solve_opts o64 = *o;
+        o64.precision = 0;
+        const int64_t D = s->D;
+        for (int j = 0; j < k; ++j) {
+            if (!redo[j]) continue;
+            k_gather_col<<<nblk(D), BS, 0, stream()>>>(D, 32, j, s->b64.p, s->fb1->b64.p);
+            CPM_CUDA_TRY(cudaGetLastError());
+            cpm_solve_stats s64;
+            const int rc64 = cpm_solve_device(s->fb1, 1, s->fb1->b64.p, nullptr, &o64, &s64);
+            if (rc64 != 0 && rc64 != CPM_ERR_NOT_CONVERGED && rc64 != CPM_ERR_BREAKDOWN) return rc64;
+            k_scatter_col<<<nblk(D), BS, 0, stream()>>>(D, 32, j, s->fb1->x64.p, s->x64.p);
+            CPM_CUDA_TRY(cudaGetLastError());
+            s64.iterations += st[j].iterations;
+            s64.refinements = st[j].refinements;
+            s64.seconds += st[j].seconds;
+            s64.fp64_fallback = 1;
+            st[j] = s64;
+        }
+        any_redo = false;
     }
     if (any_redo) {
         SolveParams P64 = P;
