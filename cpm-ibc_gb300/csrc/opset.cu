@@ -597,6 +597,19 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs) {
     CPM_CUDA_TRY(cudaGetLastError());
     std::vector<IBCData> ibs(n_ibc);
     for (int c = 0; c < n_ibc; ++c) CPM_TRY(build_ibc_data(t, ht, descs[c], normals, xdev, ibs[c]));
+    o->ibc_desc.assign(descs, descs + n_ibc);
+    o->ibc_verts.assign(n_ibc, {});
+    o->ibc_prims.assign(n_ibc, {});
+    for (int c = 0; c < n_ibc; ++c) {
+        const cpm_surface_desc &d = descs[c];
+        if (d.verts && d.nverts > 0) o->ibc_verts[c].assign(d.verts, d.verts + 3 * d.nverts);
+        if (d.prims && d.nprims > 0) {
+            const int64_t per = (d.kind == CPM_TRIANGULATION) ? 3 : 2;
+            o->ibc_prims[c].assign(d.prims, d.prims + per * d.nprims);
+        }
+        o->ibc_desc[c].verts = o->ibc_verts[c].empty() ? nullptr : o->ibc_verts[c].data();
+        o->ibc_desc[c].prims = o->ibc_prims[c].empty() ? nullptr : o->ibc_prims[c].data();
+    }
 
     // column layout: IBCStartingColumns / TotalDOFs (src/IBCSubsets.cpp:74-116)
     o->n_ibc = n_ibc;
@@ -1208,5 +1221,105 @@ extern "C" int cpm_opset_export_csr(cpm_opset_t o, int32_t which, int64_t *nnz, 
 
 extern "C" int cpm_opset_destroy(cpm_opset_t o) {
     delete o;
+    return 0;
+}
+
+// GetPlotInterpMatrix + AddIBCPlotInterpolation (src/Helpers.cpp:97-103;
+// src/IBCMatrixManipulations.cpp:84-106 with PlotPointsCPDiff :254-416, the
+// non-oriented branch): each evaluation point's 64 interpolation entries, with
+// the stencil nodes that lie across an IBC from the point moved to that IBC's
+// DOF columns, as the operator's E rows are.  The IBC subsets are derived again
+// from the stored descriptions (this is a post-processing query, not a solve).
+extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp, int64_t *cols, double *vals) {
+    if (!op || n < 0 || (n > 0 && (!xp || !cols || !vals))) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
+    if (n == 0) return 0;
+    CPM_TRY(cpm_interp_query(op->tube, n, xp, cols, vals));
+    for (int64_t e = 0; e < 64 * n; ++e)
+        if (cols[e] < 0) return fail(CPM_ERR_BASEPOINT_OUTSIDE_TUBE, "plot interpolation stencil leaves the tube");
+    const int n_ibc = (int)op->n_ibc;
+    if (n_ibc == 0) return 0;
+    cpm_tube_s *t = op->tube;
+    HostTube ht;
+    CPM_TRY(ht.load(t));
+    const int64_t N = ht.N;
+    const double r = ht.radius;
+    std::vector<double> normals;
+    bool need_normals = false;
+    for (int c = 0; c < n_ibc; ++c)
+        if (!op->ibc_desc[c].use_cp_diff_directions) need_normals = true;
+    if (need_normals) {
+        if (op->normals.n >= (size_t)(3 * N))
+            CPM_TRY(op->normals.download(normals, 3 * N));
+        else
+            CPM_TRY(tube_normals(op, normals));
+    }
+    DBuf<double> xdev;
+    CPM_TRY(xdev.alloc(3 * N));
+    k_node_coords<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, t->key.p, t->g.xstart, t->g.dx, xdev.p);
+    CPM_CUDA_TRY(cudaGetLastError());
+    std::vector<IBCData> ibs(n_ibc);
+    for (int c = 0; c < n_ibc; ++c) CPM_TRY(build_ibc_data(t, ht, op->ibc_desc[c], normals, xdev, ibs[c]));
+    std::vector<double> hx(xp, xp + 3 * n);
+    DBuf<double> dxp;
+    CPM_TRY(dxp.upload(hx));
+    // per IBC: the points within 2r of it and their tagging directions
+    std::vector<std::vector<int64_t>> sub(n_ibc, std::vector<int64_t>(n, -1));
+    std::vector<std::vector<double>> dirs(n_ibc);
+    for (int c = 0; c < n_ibc; ++c) {
+        const cpm_surface_desc &desc = op->ibc_desc[c];
+        SurfaceObj s;
+        CPM_TRY(surface_init(s, &desc, r));
+        DBuf<double> dcp, dd;
+        CPM_TRY(dcp.alloc(3 * n));
+        CPM_TRY(dd.alloc(n));
+        CPM_TRY(closest_points_dev(s.params(), n, dxp.p, dcp.p, dd.p, 2.0 * r * (1.0 + 1e-12)));
+        std::vector<double> cpc, dist;
+        CPM_TRY(dcp.download(cpc, 3 * n));
+        CPM_TRY(dd.download(dist, n));
+        std::vector<double> scp, sdiff;
+        int64_t count = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            double cd[3];
+            for (int k = 0; k < 3; ++k) cd[k] = hx[3 * i + k] - cpc[3 * i + k];
+            if (!(std::sqrt(hdot(cd, cd)) < 2.0 * r)) continue;
+            sub[c][i] = count++;
+            for (int k = 0; k < 3; ++k) {
+                scp.push_back(cpc[3 * i + k]);
+                sdiff.push_back(cd[k]);
+            }
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t si = sub[c][i];
+            if (si < 0 || !(std::sqrt(hdot(&sdiff[3 * si], &sdiff[3 * si])) < desc.on_ibc_tolerance)) continue;
+            const int64_t nearest = ht.nearest(&hx[3 * i]);
+            if (nearest >= 0 && ibs[c].tag_sub[nearest] >= 0)
+                for (int k = 0; k < 3; ++k) sdiff[3 * si + k] = ibs[c].tag_cpdiff[3 * ibs[c].tag_sub[nearest] + k];
+        }
+        QueryRows qs;
+        CPM_TRY(query_weights(t, scp, qs));
+        const std::vector<double> bn = interp_unoriented(ht, qs, ibs[c].tag_binormal, &ibs[c].tag_sub);
+        dirs[c].assign(3 * count, 0.0);
+        for (int64_t si = 0; si < count; ++si) {
+            const double b = hdot(&bn[3 * si], &sdiff[3 * si]);
+            for (int k = 0; k < 3; ++k) dirs[c][3 * si + k] = b * bn[3 * si + k];
+        }
+    }
+    // TagStencils + MoveToIBCColumns on the evaluation rows
+    for (int64_t i = 0; i < n; ++i)
+        for (int e = 0; e < 64; ++e) {
+            const int col = (int)cols[64 * i + e];
+            int hits = 0;
+            int64_t tgt = -1;
+            for (int c = 0; c < n_ibc; ++c) {
+                const int64_t si = sub[c][i];
+                if (si < 0) continue;
+                if (tagged(ibs[c], &dirs[c][3 * si], col, 1.0) && ibs[c].dof_sub[col] >= 0) {
+                    ++hits;
+                    tgt = op->col_start[c] + ibs[c].dof_sub[col];
+                }
+            }
+            if (hits > 1) return fail(CPM_ERR_UNSUPPORTED, "IBCs too close together: a stencil entry moves to two IBCs");
+            if (hits == 1) cols[64 * i + e] = tgt;
+        }
     return 0;
 }

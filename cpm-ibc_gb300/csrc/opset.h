@@ -532,6 +532,10 @@ struct cpm_opset_s {
     // unoriented surface normals of the tube nodes (eigenvector 0 of the
     // symmetrised closest-point Jacobian), kept when IBC frames needed them
     cpm::DBuf<double> normals;
+    // the IBC descriptions (vertex and segment arrays owned here), for evaluation-point queries
+    std::vector<cpm_surface_desc> ibc_desc;
+    std::vector<std::vector<double>> ibc_verts;
+    std::vector<std::vector<int64_t>> ibc_prims;
     std::vector<int64_t> col_start, dcol_start;
     int64_t identity_rows_start = 0;
 

@@ -119,6 +119,7 @@ def lib():
         L.cpm_opset_ibc_sizes.argtypes = [vp, ctypes.c_int32, vp]
         L.cpm_opset_ibc_export.argtypes = [vp, ctypes.c_int32, vp, vp, vp]
         L.cpm_opset_export_csr.argtypes = [vp, ctypes.c_int32, vp, vp, vp, vp]
+        L.cpm_opset_plot_interp.argtypes = [vp, ctypes.c_int64, vp, vp, vp]
         L.cpm_opset_destroy.argtypes = [vp]
         L.cpm_apply.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, vp, vp]
         L.cpm_apply_device.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, vp, vp]
@@ -263,6 +264,21 @@ class OpSet:
         val = np.zeros(nnz.value)
         _check(lib().cpm_opset_export_csr(self.h, which, ctypes.byref(nnz), _p(ptr), _p(idx), _p(val)))
         return ptr, idx, val
+
+    def plot_interp(self, xp):
+        """GetPlotInterpMatrix + AddIBCPlotInterpolation: per evaluation point 64
+        (column, value) entries in the operator's column layout."""
+        xp = np.ascontiguousarray(xp, np.float64)
+        n = xp.shape[0]
+        cols = np.zeros((n, 64), np.int64)
+        vals = np.zeros((n, 64))
+        _check(lib().cpm_opset_plot_interp(self.h, n, _p(xp), _p(cols), _p(vals)))
+        return cols, vals
+
+    def evaluate(self, x, xp):
+        """u at evaluation points xp from a solution x on the operator's rows"""
+        cols, vals = self.plot_interp(xp)
+        return np.einsum("pe,pe->p", vals, np.asarray(x, np.float64)[cols])
 
     def apply(self, m, n, x):
         """Solver::Multiply (src/Solver.cpp:122-138); x: (D,) or (k, D)."""

@@ -158,6 +158,15 @@ int cpm_opset_ibc_export(cpm_opset_t op, int32_t c, int64_t *tag_set, int64_t *d
  * for oracle comparison (columns sorted ascending). nnz query with ptr = NULL. */
 int cpm_opset_export_csr(cpm_opset_t op, int32_t which, int64_t *nnz, int64_t *ptr, int64_t *idx, double *val);
 
+/* Evaluation of a solution at surface points (replaces Helpers::GetPlotInterpMatrix
+ * + IBCMatrixManipulations::AddIBCPlotInterpolation, src/Helpers.cpp:97-103,
+ * src/IBCMatrixManipulations.cpp:84-106 and PlotPointsCPDiff :254-416): per point
+ * xp[3i..3i+2] its 64 interpolation entries cols[64i..], vals[64i..] in the
+ * operator's column layout, the stencil nodes that lie across an IBC from the
+ * point moved to that IBC's DOF columns.  u(xp_i) = sum_e vals[64i+e] x[cols[64i+e]].
+ * CPM_ERR_BASEPOINT_OUTSIDE_TUBE if a stencil leaves the tube. */
+int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp, int64_t *cols, double *vals);
+
 int cpm_opset_destroy(cpm_opset_t op);
 
 /* ---- Operator apply and solve --------------------------------------------

@@ -209,6 +209,23 @@ class SystemOperator {
     }
     cpm_opset_t handle() const { return h_.get(); }
     const Tube &tube() const { return *tube_; }
+    // a solution (reference row order) at surface points, through the interpolation
+    // with IBC columns (Helpers::GetPlotInterpMatrix + AddIBCPlotInterpolation,
+    // src/Helpers.cpp:97-103, src/IBCMatrixManipulations.cpp:84-106)
+    VectorX Evaluate(const VectorX &u, const std::vector<Point3> &xp) const {
+        const int64_t n = (int64_t)xp.size();
+        std::vector<Scalar> pts(3 * (size_t)n);
+        for (size_t i = 0; i < xp.size(); ++i)
+            for (int k = 0; k < 3; ++k) pts[3 * i + (size_t)k] = xp[i][(size_t)k];
+        std::vector<int64_t> cols(64 * (size_t)n);
+        std::vector<Scalar> vals(64 * (size_t)n);
+        check(cpm_opset_plot_interp(h_.get(), n, pts.data(), cols.data(), vals.data()));
+        const VectorX ud = to_device(u);
+        VectorX out((size_t)n, 0.0);
+        for (size_t i = 0; i < (size_t)n; ++i)
+            for (size_t e = 0; e < 64; ++e) out[i] += vals[64 * i + e] * ud[(size_t)cols[64 * i + e]];
+        return out;
+    }
 
   private:
     struct Del {

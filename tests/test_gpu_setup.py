@@ -179,3 +179,32 @@ def test_ibc_operator_rows_match_oracle(gpu, oracle, which):
         for k in a:
             assert abs(a[k] - b[k]) <= tol * max(1.0, abs(a[k])), (r, k, a[k], b[k])
     assert on_plane <= 8
+
+
+@pytest.mark.parametrize("dx", [0.1, 0.05])
+def test_plot_interpolation_with_ibc_columns_matches_oracle(gpu, oracle, dx):
+    """Evaluation-point rows (GetPlotInterpMatrix + AddIBCPlotInterpolation) equal the
+    oracle's: the same columns, moved to IBC DOF columns across the curves, and the
+    same values."""
+    P = oracle.RefProblem(oracle.sphere_desc(), c2_ibcs(oracle, dx), 3, dx, record_visited=True)
+    T = gpu.Tube.from_closest_points(gpu.desc(gpu.SPHERE, [1.0]), 3, dx, *P.visited())
+    O = gpu.OpSet(T, c2_ibcs(gpu, dx))
+    ref, g = P.tube(), T.export()
+    m = ref_to_gpu_index(ref["rec"], g["rec"])
+    full = np.arange(O.D)
+    full[m] = np.arange(P.N)  # gpu tube column -> reference column; IBC columns unchanged
+    xp = P.xp()
+    rp, ri, rv = P.csr(4)
+    cols, vals = O.plot_interp(xp)
+    moved = 0
+    for i in range(len(xp)):
+        a = {k: v for k, v in zip(ri[rp[i]:rp[i + 1]].tolist(), rv[rp[i]:rp[i + 1]].tolist()) if v != 0.0}
+        b = {}
+        for c, v in zip(full[cols[i]].tolist(), vals[i].tolist()):
+            if v != 0.0:
+                b[c] = b.get(c, 0.0) + v
+        assert a.keys() == b.keys(), (i, sorted(set(a) ^ set(b)))
+        for k in a:
+            assert abs(a[k] - b[k]) <= 1e-14 * max(1.0, abs(a[k])), (i, k, a[k], b[k])
+        moved += sum(1 for k in b if k >= P.N)
+    assert moved > 0
