@@ -2044,6 +2044,38 @@ extern "C" int cpm_apply(cpm_opset_t op, double m, double n, int32_t k, const do
     return 0;
 }
 
+// identity rows of Lfull hold 1 on the diagonal (SetIdentityRows): u + dt Lfull u
+// is (1 + dt) u there
+__global__ void k_scale_ident(const int32_t *__restrict__ ident, int64_t n_ident, double f, const double *__restrict__ u,
+                              double *__restrict__ v) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q < n_ident) v[ident[q]] = f * u[ident[q]];
+}
+
+// explicit heat step u <- Efull (u + dt Lfull u) (HeatWithIBC::TimeStep, method 0,
+// problems/HeatWithIBC.cpp:129-132): the L pass with the row's own vector as its
+// neighbour input, the identity rows scaled by 1 + dt, then the E pass (identity
+// rows copy, as Efull's unit diagonal there)
+extern "C" int cpm_explicit_step(cpm_opset_t op, double dt, int32_t k, const double *u, double *u_out) {
+    if (!op || !u || !u_out || k < 1) return fail(CPM_ERR_INVALID_ARG, "invalid explicit step arguments");
+    const int64_t D = op->D;
+    DBuf<double> du, dv;
+    CPM_TRY(du.alloc(D));
+    CPM_TRY(dv.alloc(D));
+    auto v = op->view<double>();
+    for (int j = 0; j < k; ++j) {
+        CPM_CUDA_TRY(cudaMemcpyAsync(du.p, u + (size_t)j * D, D * 8, cudaMemcpyHostToDevice, stream()));
+        k_lpass<double, 1><<<row_grid(D, 1), BS, 0, stream()>>>(v, 1.0, dt, du.p, du.p, dv.p);
+        if (v.n_ident > 0) k_scale_ident<<<nblk(v.n_ident), BS, 0, stream()>>>(v.ident, v.n_ident, 1.0 + dt, du.p, dv.p);
+        CPM_CUDA_TRY(cudaGetLastError());
+        launch_epass<double, 1>(v, nullptr, -1, dv.p, du.p, stream());
+        CPM_CUDA_TRY(cudaGetLastError());
+        CPM_CUDA_TRY(cudaMemcpyAsync(u_out + (size_t)j * D, du.p, D * 8, cudaMemcpyDeviceToHost, stream()));
+    }
+    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
+    return 0;
+}
+
 extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslots, int32_t fp32, const void *x_dev, void *t_dev,
                                 void *y_dev) {
     if (!op || !x_dev || !t_dev || !y_dev || (kslots != 1 && kslots != 32))

@@ -120,6 +120,7 @@ def lib():
         L.cpm_opset_ibc_export.argtypes = [vp, ctypes.c_int32, vp, vp, vp]
         L.cpm_opset_export_csr.argtypes = [vp, ctypes.c_int32, vp, vp, vp, vp]
         L.cpm_opset_plot_interp.argtypes = [vp, ctypes.c_int64, vp, vp, vp]
+        L.cpm_explicit_step.argtypes = [vp, ctypes.c_double, ctypes.c_int32, vp, vp]
         L.cpm_opset_destroy.argtypes = [vp]
         L.cpm_apply.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, vp, vp]
         L.cpm_apply_device.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, vp, vp]
@@ -274,6 +275,13 @@ class OpSet:
         vals = np.zeros((n, 64))
         _check(lib().cpm_opset_plot_interp(self.h, n, _p(xp), _p(cols), _p(vals)))
         return cols, vals
+
+    def explicit_step(self, dt, u):
+        """HeatWithIBC explicit step: Efull (u + dt Lfull u); u: (D,) or (k, D)."""
+        u = np.ascontiguousarray(np.atleast_2d(u), np.float64)
+        out = np.zeros_like(u)
+        _check(lib().cpm_explicit_step(self.h, dt, u.shape[0], _p(u), _p(out)))
+        return out
 
     def evaluate(self, x, xp):
         """u at evaluation points xp from a solution x on the operator's rows"""

@@ -175,6 +175,11 @@ int cpm_opset_destroy(cpm_opset_t op);
  *   y = x on identity rows, else m x + n (L_qq x_q + sum_{c!=q} L_qc (E~x)_c).
  * x, y: host arrays of D*k doubles, RHS-major (x[j*D + r] is row r of RHS j). */
 int cpm_apply(cpm_opset_t op, double m, double n, int32_t k, const double *x, double *y);
+
+/* Explicit heat step (HeatWithIBC::TimeStep with time_stepping_method 0,
+ * problems/HeatWithIBC.cpp:129-132): u_out = Efull (u + dt Lfull u), FP64, k
+ * right-hand sides RHS-major; the caller sets the Dirichlet value rows after it. */
+int cpm_explicit_step(cpm_opset_t op, double dt, int32_t k, const double *u, double *u_out);
 /* Same with device pointers: row-major [D][kslots] arrays (kslots 1 or 32),
  * FP64 or FP32 (fp32 = 1), t_dev a caller-owned scratch array of the same
  * shape for E~x.  Enqueued on the library stream, asynchronous (cpm_sync). */

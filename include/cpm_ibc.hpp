@@ -324,37 +324,49 @@ class PoissonWithIBC {
     Solver sv_;
 };
 
-// HeatWithIBC (problems/HeatWithIBC.h:17-60): implicit time steps of
-// u_t = Delta_S u with Dirichlet IBC values; time_stepping_method 1 is
-// backward Euler (Init(1, -dt)), 2 Crank-Nicolson (Init(1, -dt/2) with the
-// right-hand side Multiply(u, 1, dt/2)), as problems/HeatWithIBC.cpp:115-128.
+// HeatWithIBC (problems/HeatWithIBC.h:17-60): time steps of u_t = Delta_S u
+// with Dirichlet IBC values; time_stepping_method 0 is explicit (u <- Efull
+// (u + dt Lfull u)), 1 backward Euler (Init(1, -dt)), 2 Crank-Nicolson
+// (Init(1, -dt/2) with the right-hand side Multiply(u, 1, dt/2)), as
+// problems/HeatWithIBC.cpp:115-132.
 class HeatWithIBC {
   public:
     HeatWithIBC(const SurfaceSpecifier &surface, const std::vector<SurfaceSpecifier> &ibcs, Scalar dx, Scalar dt,
                 size_t time_stepping_method, size_t interp_deg = 3, int precision = 0)
         : tube_(surface, interp_deg, dx), op_(tube_, ibcs), dt_(dt), method_(time_stepping_method) {
-        if (method_ != 1 && method_ != 2)
-            throw std::runtime_error("cpm_gb300: HeatWithIBC supports the implicit methods 1 and 2");
-        const Scalar r = method_ == 1 ? 1.0 : 0.5;
-        sv_.Init(1.0, -r * dt_, op_);
-        sv_.SetPrecision(precision);
+        if (method_ > 2) throw std::runtime_error("cpm_gb300: HeatWithIBC time_stepping_method is 0, 1 or 2");
+        if (method_ > 0) {
+            const Scalar r = method_ == 1 ? 1.0 : 0.5;
+            sv_.Init(1.0, -r * dt_, op_);
+            sv_.SetPrecision(precision);
+        }
     }
-    // HeatWithIBC::TimeStep (problems/HeatWithIBC.cpp:104-128): returns u at the next time
+    // HeatWithIBC::TimeStep (problems/HeatWithIBC.cpp:104-132): returns u at the next time
     VectorX TimeStep(VectorX &ufull, const IBCFn &ibc_exact) {
+        if (method_ == 0) {
+            VectorX dev = op_.to_device(ufull), out(dev.size());
+            check(cpm_explicit_step(op_.handle(), dt_, 1, dev.data(), out.data()));
+            ufull = op_.from_device(out);
+            set_dirichlet(ufull, ibc_exact);
+            return ufull;
+        }
         if (method_ == 2) {
             VectorX tmp;
             sv_.Multiply(ufull, tmp, 1.0, 0.5 * dt_);
             ufull = tmp;
         }
-        // SetDirichletValue (problems/HeatWithIBC.cpp:62-85)
-        for (size_t r = 0; r < ufull.size(); ++r)
-            if (op_.kind(r) == 2) ufull[r] = ibc_exact((size_t)op_.ibc(r), 0, op_.point(r));
+        set_dirichlet(ufull, ibc_exact);
         return sv_.Solve(ufull);
     }
     const Tube &tube() const { return tube_; }
     const SystemOperator &system() const { return op_; }
 
   private:
+    // SetDirichletValue (problems/HeatWithIBC.cpp:62-85)
+    void set_dirichlet(VectorX &ufull, const IBCFn &ibc_exact) const {
+        for (size_t r = 0; r < ufull.size(); ++r)
+            if (op_.kind(r) == 2) ufull[r] = ibc_exact((size_t)op_.ibc(r), 0, op_.point(r));
+    }
     Tube tube_;
     SystemOperator op_;
     Scalar dt_;

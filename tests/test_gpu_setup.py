@@ -208,3 +208,21 @@ def test_plot_interpolation_with_ibc_columns_matches_oracle(gpu, oracle, dx):
             assert abs(a[k] - b[k]) <= 1e-14 * max(1.0, abs(a[k])), (i, k, a[k], b[k])
         moved += sum(1 for k in b if k >= P.N)
     assert moved > 0
+
+
+def test_explicit_heat_step_matches_lfull_efull(gpu, oracle):
+    """HeatWithIBC's explicit step u <- Efull (u + dt Lfull u) on the device equals the
+    same products of the exported Lfull / Efull (whose rows match the oracle's),
+    identity rows included (Lfull and Efull hold 1 on their diagonal there)."""
+    dx = 0.1
+    dt = 0.1 * dx * dx
+    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), c2_ibcs(gpu, dx))
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal((2, O.D))
+    got = O.explicit_step(dt, u)
+    Lp, Li, Lv = O.csr(0)
+    Ep, Ei, Ev = O.csr(1)
+    for j in range(2):
+        v = u[j] + dt * oracle.csr_matvec(Lp, Li, Lv, u[j])
+        want = oracle.csr_matvec(Ep, Ei, Ev, v)
+        assert np.max(np.abs(got[j] - want)) <= 1e-13 * np.max(np.abs(want))
