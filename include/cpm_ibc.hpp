@@ -17,9 +17,12 @@
 
 #include <algorithm>
 #include <array>
+#include <cctype>
 #include <cstdint>
+#include <fstream>
 #include <functional>
 #include <memory>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -39,6 +42,110 @@ enum class Preconditioner { identity = 0, diagonal = 1, jacobi = 2 };
 inline void check(int rc) {
     if (rc != CPM_OK) throw std::runtime_error(std::string("cpm_gb300: ") + cpm_last_error());
 }
+
+// SimplePolygonMesh (src/SimplePolygonMesh.h): a polygon mesh or polyline read
+// from an OBJ file (SimplePolygonMesh::readMeshFromFile / readMeshFromObjFile,
+// src/SimplePolygonMesh.cpp:103-222): "v" records are vertices, "f" records
+// faces whose tokens are "v", "v/vt", "v//vn" or "v/vt/vn" (1-based; a "\"
+// token continues the face on the next line), "l" records polylines, kept as
+// their consecutive segments; other records are skipped.
+class SimplePolygonMesh {
+  public:
+    std::vector<std::vector<Scalar>> vertices;
+    std::vector<std::vector<size_t>> faces;
+
+    SimplePolygonMesh() = default;
+    explicit SimplePolygonMesh(const std::string &filename) { readMeshFromFile(filename); }
+    size_t nVertices() const { return vertices.size(); }
+    size_t nFaces() const { return faces.size(); }
+
+    void readMeshFromFile(const std::string &filename) {
+        const std::string::size_type dot = filename.rfind('.');
+        std::string ext = dot == std::string::npos ? "" : filename.substr(dot + 1);
+        for (char &c : ext) c = (char)std::tolower((unsigned char)c);
+        if (ext != "obj") throw std::runtime_error("Did not recognize mesh file type " + ext);
+        std::ifstream in(filename, std::ios::binary);
+        if (!in) throw std::runtime_error("couldn't open file " + filename);
+        readMeshFromObjFile(in);
+    }
+
+    void readMeshFromObjFile(std::istream &in) {
+        vertices.clear();
+        faces.clear();
+        std::string line;
+        while (std::getline(in, line)) {
+            std::istringstream ss(line);
+            std::string rec;
+            if (!(ss >> rec)) continue;
+            if (rec == "v") {
+                std::vector<Scalar> p;
+                Scalar v;
+                while (ss >> v) p.push_back(v);
+                vertices.push_back(p);
+            } else if (rec == "f") {
+                std::vector<size_t> f;
+                std::string tok;
+                for (;;) {
+                    if (!(ss >> tok)) break;
+                    if (tok == "\\") {  // continued on the next line
+                        if (!std::getline(in, line)) break;
+                        ss.clear();
+                        ss.str(line);
+                        continue;
+                    }
+                    f.push_back(index_of(tok.substr(0, tok.find('/'))));
+                }
+                faces.push_back(f);
+            } else if (rec == "l") {
+                std::vector<size_t> ids;
+                std::string tok;
+                while (ss >> tok) ids.push_back(index_of(tok));
+                for (size_t i = 0; i + 1 < ids.size(); ++i) faces.push_back({ids[i], ids[i + 1]});
+            }
+        }
+    }
+
+  private:
+    static size_t index_of(const std::string &tok) {
+        const long long i = std::stoll(tok);
+        if (i < 1) throw std::runtime_error("OBJ index " + tok + " is not a 1-based vertex index");
+        return (size_t)(i - 1);
+    }
+};
+
+// Helpers::WriteCSV / ReadCSV (src/Helpers.cpp:11-82): one vector as one line of
+// comma-separated values, or a table as one line per row; values written with
+// the stream's default formatting, read with std::stod.
+struct Helpers {
+    template <class V>
+    static void WriteCSV(const V &data, const std::string &filename) {
+        std::ofstream f(filename);
+        for (size_t i = 0; i < data.size(); ++i) f << data[i] << (i + 1 < data.size() ? "," : "\n");
+    }
+    static void WriteCSV(const std::vector<std::vector<Scalar>> &data, const std::string &filename) {
+        std::ofstream f(filename);
+        for (const auto &row : data)
+            for (size_t i = 0; i < row.size(); ++i) f << row[i] << (i + 1 < row.size() ? "," : "\n");
+    }
+    static void ReadCSV(const std::string &filename, std::vector<std::vector<Scalar>> &data) {
+        std::ifstream in(filename);
+        std::string line;
+        while (std::getline(in, line)) {
+            std::istringstream ss(line);
+            std::string tok;
+            std::vector<Scalar> row;
+            while (std::getline(ss, tok, ',')) row.push_back(std::stod(tok));
+            data.push_back(row);
+        }
+    }
+    static void ReadCSV(const std::string &filename, VectorX &data) {
+        std::vector<std::vector<Scalar>> t;
+        ReadCSV(filename, t);
+        if (t.size() != 1)
+            throw std::runtime_error("In Helpers::ReadCSV(), " + filename + " does not contain one line of comma separated values");
+        data = t[0];
+    }
+};
 
 // SurfaceSpecifier (src/SurfaceSpecifier.h:198-216) with the IBCMetaData
 // fields (src/IBCMetaData.h:9-24) an IBC curve carries.
@@ -72,6 +179,31 @@ class SurfaceSpecifier {
         s.verts_ = std::move(verts);
         s.prims_ = std::move(segments);
         return s;
+    }
+
+    // SurfaceSpecifier(SimplePolygonMesh) (src/SurfaceSpecifier.cpp:299-361): a
+    // triangulation when the first face has 3 vertices, a polyline when it has 2;
+    // the bounding interval spans the vertex coordinates and 0
+    static SurfaceSpecifier FromMesh(const SimplePolygonMesh &mesh) {
+        if (mesh.faces.empty() || mesh.vertices.empty()) throw std::runtime_error("cpm_gb300: empty mesh");
+        std::vector<Scalar> v;
+        Scalar lo = 0.0, hi = 0.0;
+        for (const auto &p : mesh.vertices) {
+            if (p.size() != 3) throw std::runtime_error("cpm_gb300: mesh vertices need 3 coordinates");
+            for (Scalar c : p) {
+                v.push_back(c);
+                lo = std::min(lo, c);
+                hi = std::max(hi, c);
+            }
+        }
+        const size_t per = mesh.faces[0].size();
+        if (per != 3 && per != 2) throw std::runtime_error("cpm_gb300: faces of 3 (triangulation) or 2 (polyline) vertices");
+        std::vector<int64_t> prims;
+        for (const auto &f : mesh.faces) {
+            if (f.size() != per) throw std::runtime_error("cpm_gb300: faces of mixed sizes");
+            for (size_t i : f) prims.push_back((int64_t)i);
+        }
+        return per == 3 ? Triangulation(std::move(v), std::move(prims)) : Polyline(std::move(v), std::move(prims), {lo, hi});
     }
 
     // IBCMetaData fields
