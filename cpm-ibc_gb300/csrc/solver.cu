@@ -2076,6 +2076,47 @@ extern "C" int cpm_explicit_step(cpm_opset_t op, double dt, int32_t k, const dou
     return 0;
 }
 
+// Gray-Scott reaction terms from the old u, v: un += dt (-u v^2 + F (1 - u)),
+// vn += dt (u v^2 - (F + k) v)   (problems/ReactionDiffusionWithIBC.cpp:104-110)
+__global__ void k_gray_scott(int64_t D, double dt, double F, double k, const double *__restrict__ u, const double *__restrict__ v,
+                             double *__restrict__ un, double *__restrict__ vn) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= D) return;
+    const double uv2 = u[i] * v[i] * v[i];
+    un[i] += dt * (-uv2 + F * (1.0 - u[i]));
+    vn[i] += dt * (uv2 - (F + k) * v[i]);
+}
+
+// ReactionDiffusionWithIBC::TimeStep (problems/ReactionDiffusionWithIBC.cpp:93-117)
+// before its Dirichlet values: u <- Efull (u + nu_u dt Lfull u + dt R_u(u, v)),
+// v <- Efull (v + nu_v dt Lfull v + dt R_v(u, v)), nu_u = (dx / 3)^2, nu_v = nu_u / 3
+extern "C" int cpm_gray_scott_step(cpm_opset_t op, double dt, double F, double k, double *u, double *v) {
+    if (!op || !u || !v) return fail(CPM_ERR_INVALID_ARG, "invalid reaction-diffusion step arguments");
+    const int64_t D = op->D;
+    const double nu_u = 1.0 / ((3.0 / op->dx) * (3.0 / op->dx)), nu_v = nu_u / 3.0;
+    DBuf<double> du, dv, dun, dvn;
+    CPM_TRY(du.upload(u, D));
+    CPM_TRY(dv.upload(v, D));
+    CPM_TRY(dun.alloc(D));
+    CPM_TRY(dvn.alloc(D));
+    auto w = op->view<double>();
+    k_lpass<double, 1><<<row_grid(D, 1), BS, 0, stream()>>>(w, 1.0, nu_u * dt, du.p, du.p, dun.p);
+    k_lpass<double, 1><<<row_grid(D, 1), BS, 0, stream()>>>(w, 1.0, nu_v * dt, dv.p, dv.p, dvn.p);
+    if (w.n_ident > 0) {
+        k_scale_ident<<<nblk(w.n_ident), BS, 0, stream()>>>(w.ident, w.n_ident, 1.0 + nu_u * dt, du.p, dun.p);
+        k_scale_ident<<<nblk(w.n_ident), BS, 0, stream()>>>(w.ident, w.n_ident, 1.0 + nu_v * dt, dv.p, dvn.p);
+    }
+    k_gray_scott<<<nblk(D), BS, 0, stream()>>>(D, dt, F, k, du.p, dv.p, dun.p, dvn.p);
+    CPM_CUDA_TRY(cudaGetLastError());
+    launch_epass<double, 1>(w, nullptr, -1, dun.p, du.p, stream());
+    launch_epass<double, 1>(w, nullptr, -1, dvn.p, dv.p, stream());
+    CPM_CUDA_TRY(cudaGetLastError());
+    CPM_CUDA_TRY(cudaMemcpyAsync(u, du.p, D * 8, cudaMemcpyDeviceToHost, stream()));
+    CPM_CUDA_TRY(cudaMemcpyAsync(v, dv.p, D * 8, cudaMemcpyDeviceToHost, stream()));
+    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
+    return 0;
+}
+
 extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslots, int32_t fp32, const void *x_dev, void *t_dev,
                                 void *y_dev) {
     if (!op || !x_dev || !t_dev || !y_dev || (kslots != 1 && kslots != 32))

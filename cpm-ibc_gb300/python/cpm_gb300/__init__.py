@@ -121,6 +121,7 @@ def lib():
         L.cpm_opset_export_csr.argtypes = [vp, ctypes.c_int32, vp, vp, vp, vp]
         L.cpm_opset_plot_interp.argtypes = [vp, ctypes.c_int64, vp, vp, vp]
         L.cpm_explicit_step.argtypes = [vp, ctypes.c_double, ctypes.c_int32, vp, vp]
+        L.cpm_gray_scott_step.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp, vp]
         L.cpm_opset_destroy.argtypes = [vp]
         L.cpm_apply.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, vp, vp]
         L.cpm_apply_device.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, vp, vp]
@@ -282,6 +283,13 @@ class OpSet:
         out = np.zeros_like(u)
         _check(lib().cpm_explicit_step(self.h, dt, u.shape[0], _p(u), _p(out)))
         return out
+
+    def gray_scott_step(self, dt, u, v, F=0.054, k=0.063):
+        """ReactionDiffusionWithIBC step (before the Dirichlet values): new (u, v)."""
+        u = np.array(u, np.float64)
+        v = np.array(v, np.float64)
+        _check(lib().cpm_gray_scott_step(self.h, dt, F, k, _p(u), _p(v)))
+        return u, v
 
     def evaluate(self, x, xp):
         """u at evaluation points xp from a solution x on the operator's rows"""

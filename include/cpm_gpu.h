@@ -180,6 +180,13 @@ int cpm_apply(cpm_opset_t op, double m, double n, int32_t k, const double *x, do
  * problems/HeatWithIBC.cpp:129-132): u_out = Efull (u + dt Lfull u), FP64, k
  * right-hand sides RHS-major; the caller sets the Dirichlet value rows after it. */
 int cpm_explicit_step(cpm_opset_t op, double dt, int32_t k, const double *u, double *u_out);
+
+/* Gray-Scott step of ReactionDiffusionWithIBC::TimeStep (problems/ReactionDiffusionWithIBC.cpp:93-117),
+ * in place on host arrays of D doubles: u <- Efull (u + nu_u dt Lfull u + dt (-u v^2 + F (1 - u))),
+ * v <- Efull (v + nu_v dt Lfull v + dt (u v^2 - (F + k) v)), the reaction terms from the old u, v,
+ * nu_u = (dx / 3)^2, nu_v = nu_u / 3 (the reference uses F = 0.054, k = 0.063); the caller sets
+ * the Dirichlet value rows afterwards. */
+int cpm_gray_scott_step(cpm_opset_t op, double dt, double F, double k, double *u, double *v);
 /* Same with device pointers: row-major [D][kslots] arrays (kslots 1 or 32),
  * FP64 or FP32 (fp32 = 1), t_dev a caller-owned scratch array of the same
  * shape for E~x.  Enqueued on the library stream, asynchronous (cpm_sync). */

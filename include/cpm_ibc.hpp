@@ -506,6 +506,36 @@ class HeatWithIBC {
     Solver sv_;
 };
 
+// ReactionDiffusionWithIBC (problems/ReactionDiffusionWithIBC.h): explicit
+// Gray-Scott steps (F = 0.054, k = 0.063, nu_u = (dx / 3)^2, nu_v = nu_u / 3)
+// of u and v with Dirichlet IBC values, as problems/ReactionDiffusionWithIBC.cpp:93-117.
+class ReactionDiffusionWithIBC {
+  public:
+    ReactionDiffusionWithIBC(const SurfaceSpecifier &surface, const std::vector<SurfaceSpecifier> &ibcs, Scalar dx, Scalar dt,
+                             size_t interp_deg = 3)
+        : tube_(surface, interp_deg, dx), op_(tube_, ibcs), dt_(dt) {}
+    void TimeStep(VectorX &ufull, VectorX &vfull, const IBCFn &ibc_exact_u, const IBCFn &ibc_exact_v) {
+        VectorX u = op_.to_device(ufull), v = op_.to_device(vfull);
+        check(cpm_gray_scott_step(op_.handle(), dt_, 0.054, 0.063, u.data(), v.data()));
+        ufull = op_.from_device(u);
+        vfull = op_.from_device(v);
+        set_dirichlet(ufull, ibc_exact_u);
+        set_dirichlet(vfull, ibc_exact_v);
+    }
+    const Tube &tube() const { return tube_; }
+    const SystemOperator &system() const { return op_; }
+
+  private:
+    // SetDirichletValue (problems/ReactionDiffusionWithIBC.cpp:60-90)
+    void set_dirichlet(VectorX &ufull, const IBCFn &ibc_exact) const {
+        for (size_t r = 0; r < ufull.size(); ++r)
+            if (op_.kind(r) == 2) ufull[r] = ibc_exact((size_t)op_.ibc(r), 0, op_.point(r));
+    }
+    Tube tube_;
+    SystemOperator op_;
+    Scalar dt_;
+};
+
 // GeodesicDistance::ComputeDistance (problems/GeodesicDistance.cpp:11-69) from
 // a point source: returns phi on the tube rows (reference numbering) and the
 // point IBC's DOF rows.

@@ -226,3 +226,25 @@ def test_explicit_heat_step_matches_lfull_efull(gpu, oracle):
         v = u[j] + dt * oracle.csr_matvec(Lp, Li, Lv, u[j])
         want = oracle.csr_matvec(Ep, Ei, Ev, v)
         assert np.max(np.abs(got[j] - want)) <= 1e-13 * np.max(np.abs(want))
+
+
+def test_gray_scott_step_matches_lfull_efull(gpu, oracle):
+    """ReactionDiffusionWithIBC's Gray-Scott step on the device equals
+    Efull (u + nu_u dt Lfull u + dt R_u), Efull (v + nu_v dt Lfull v + dt R_v) from the
+    exported Lfull / Efull, the reaction terms from the old u, v."""
+    dx = 0.1
+    dt = 0.2
+    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), c2_ibcs(gpu, dx))
+    rng = np.random.default_rng(4)
+    u, v = rng.uniform(0, 1, O.D), rng.uniform(0, 0.5, O.D)
+    gu, gv = O.gray_scott_step(dt, u, v)
+    Lp, Li, Lv = O.csr(0)
+    Ep, Ei, Ev = O.csr(1)
+    nu_u = (dx / 3.0) ** 2
+    nu_v = nu_u / 3.0
+    F, k = 0.054, 0.063
+    un = u + nu_u * dt * oracle.csr_matvec(Lp, Li, Lv, u) + dt * (-u * v * v + F * (1 - u))
+    vn = v + nu_v * dt * oracle.csr_matvec(Lp, Li, Lv, v) + dt * (u * v * v - (F + k) * v)
+    wu, wv = oracle.csr_matvec(Ep, Ei, Ev, un), oracle.csr_matvec(Ep, Ei, Ev, vn)
+    assert np.max(np.abs(gu - wu)) <= 1e-13 * np.max(np.abs(wu))
+    assert np.max(np.abs(gv - wv)) <= 1e-13 * np.max(np.abs(wv))
