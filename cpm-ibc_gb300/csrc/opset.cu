@@ -1099,6 +1099,43 @@ extern "C" int cpm_opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_d
     return 0;
 }
 
+// the operator of the nearest-node baselines (PoissonWithIBCNearest::Initialize,
+// problems/PoissonWithIBCNearest.cpp:73-89): plain L and E of the tube (no IBC
+// columns) with identity rows at the given tube rows (device indices), which
+// hold Dirichlet values
+extern "C" int cpm_opset_create_identity(cpm_tube_t t, int64_t n_rows, const int64_t *rows, cpm_opset_t *out) {
+    if (!t || !out || n_rows < 0 || (n_rows > 0 && !rows)) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
+    *out = nullptr;
+    cpm_opset_s *o = new cpm_opset_s();
+    o->tube = t;
+    int rc = build_base(o);
+    if (!rc) {
+        std::vector<uint8_t> fl(o->D, 0);
+        for (int64_t i = 0; i < n_rows && !rc; ++i) {
+            if (rows[i] < 0 || rows[i] >= o->D) {
+                rc = fail(CPM_ERR_INVALID_ARG, "identity row outside the tube");
+                break;
+            }
+            fl[rows[i]] = F_IDENT;
+            o->h_identity[rows[i]] = 1;
+            o->h_kind[rows[i]] = 2;
+        }
+        if (!rc) rc = o->flags.upload(fl);
+    }
+    if (!rc) rc = build_schedule(o);
+    if (!rc) rc = make_float_copies(o);
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(stream());
+        if (e != cudaSuccess) rc = fail(CPM_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (rc) {
+        delete o;
+        return rc;
+    }
+    *out = o;
+    return 0;
+}
+
 extern "C" int cpm_opset_sizes(cpm_opset_t o, int64_t *s) {
     if (!o || !s) return fail(CPM_ERR_INVALID_ARG, "null argument");
     s[0] = o->D;

@@ -114,6 +114,7 @@ def lib():
         L.cpm_interp_query.argtypes = [vp, ctypes.c_int64, vp, vp, vp]
         L.cpm_tube_destroy.argtypes = [vp]
         L.cpm_opset_create.argtypes = [vp, ctypes.c_int32, P(SurfaceDesc), P(vp)]
+        L.cpm_opset_create_identity.argtypes = [vp, ctypes.c_int64, vp, P(vp)]
         L.cpm_opset_sizes.argtypes = [vp, vp]
         L.cpm_opset_rows.argtypes = [vp] * 5
         L.cpm_opset_ibc_sizes.argtypes = [vp, ctypes.c_int32, vp]
@@ -220,12 +221,20 @@ class Tube:
 class OpSet:
     """Lfull / Efull / identity rows (Helpers::SetupMatrices + IBCMatrixManipulations) on the device."""
 
-    def __init__(self, tube, ibcs=()):
+    def __init__(self, tube, ibcs=(), identity_rows=None):
+        """identity_rows (device tube indices): the nearest-node baselines' operator,
+        plain L and E with Dirichlet rows there (no IBC columns; ibcs must be empty)"""
         self.tube = tube
         self.ibcs = list(ibcs)
         h = ctypes.c_void_p()
-        arr = (SurfaceDesc * max(1, len(ibcs)))(*ibcs) if ibcs else None
-        _check(lib().cpm_opset_create(tube.h, len(ibcs), arr, ctypes.byref(h)))
+        if identity_rows is not None:
+            if ibcs:
+                raise ValueError("identity_rows and IBC curves are exclusive")
+            rows = np.ascontiguousarray(identity_rows, np.int64)
+            _check(lib().cpm_opset_create_identity(tube.h, len(rows), _p(rows), ctypes.byref(h)))
+        else:
+            arr = (SurfaceDesc * max(1, len(ibcs)))(*ibcs) if ibcs else None
+            _check(lib().cpm_opset_create(tube.h, len(ibcs), arr, ctypes.byref(h)))
         self.h = h
         s = np.zeros(9, np.int64)
         _check(lib().cpm_opset_sizes(self.h, _p(s)))

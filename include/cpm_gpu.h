@@ -167,6 +167,12 @@ int cpm_opset_export_csr(cpm_opset_t op, int32_t which, int64_t *nnz, int64_t *p
  * CPM_ERR_BASEPOINT_OUTSIDE_TUBE if a stencil leaves the tube. */
 int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp, int64_t *cols, double *vals);
 
+/* The operator of the nearest-node baselines (PoissonWithIBCNearest,
+ * problems/PoissonWithIBCNearest.cpp:73-89): the tube's plain L and E with
+ * identity rows (Dirichlet values) at the n_rows given tube rows (device
+ * indices). */
+int cpm_opset_create_identity(cpm_tube_t t, int64_t n_rows, const int64_t *rows, cpm_opset_t *out);
+
 int cpm_opset_destroy(cpm_opset_t op);
 
 /* ---- Operator apply and solve --------------------------------------------

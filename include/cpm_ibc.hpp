@@ -295,6 +295,24 @@ class SystemOperator {
         for (const auto &s : ibcs) d.push_back(s.desc());
         cpm_opset_t o = nullptr;
         check(cpm_opset_create(tube.handle(), (int32_t)d.size(), d.empty() ? nullptr : d.data(), &o));
+        init(tube, o);
+    }
+    // the nearest-node baselines' operator: plain L and E with identity rows at the
+    // given tube rows (reference numbering)
+    struct IdentityRows {
+        explicit IdentityRows(std::vector<size_t> r) : rows(std::move(r)) {}
+        std::vector<size_t> rows;
+    };
+    SystemOperator(const Tube &tube, const IdentityRows &identity) : tube_(&tube) {
+        std::vector<int64_t> rows;
+        for (size_t r : identity.rows) rows.push_back(tube.device_index()[r]);
+        cpm_opset_t o = nullptr;
+        check(cpm_opset_create_identity(tube.handle(), (int64_t)rows.size(), rows.empty() ? nullptr : rows.data(), &o));
+        init(tube, o);
+    }
+
+  private:
+    void init(const Tube &tube, cpm_opset_t o) {
         h_.reset(o);
         int64_t sz[9];
         check(cpm_opset_sizes(o, sz));
@@ -319,6 +337,8 @@ class SystemOperator {
             identity_[r] = ident[q] != 0;
         }
     }
+
+  public:
     size_t rows() const { return (size_t)D_; }
     size_t nNodes() const { return (size_t)N_; }
     size_t TotalIBCDOFs() const { return (size_t)total_ibc_dofs_; }
@@ -452,6 +472,60 @@ class PoissonWithIBC {
 
   private:
     Tube tube_;
+    SystemOperator op_;
+    Solver sv_;
+};
+
+// PoissonWithIBCNearest (problems/PoissonWithIBCNearest.cpp:5-89): the
+// nearest-node baseline.  No IBC columns: the tube rows of each IBC's DOF subset
+// become identity rows holding the exact surface value at their IBC closest
+// point (freeze_nearest = false); the plain L and E elsewhere, solved with
+// Init(0, -1).  freeze_nearest (the rows nearest to the IBC curves' own plot
+// points) is not offered.
+class PoissonWithIBCNearest {
+  public:
+    PoissonWithIBCNearest(const SurfaceSpecifier &surface, const std::vector<SurfaceSpecifier> &ibcs, Scalar dx,
+                          bool freeze_nearest = false, size_t interp_deg = 3, int precision = 0)
+        : tube_(surface, interp_deg, dx),
+          op_(tube_, SystemOperator::IdentityRows{nearest_rows(tube_, ibcs, freeze_nearest, rows_, cp_)}) {
+        sv_.Init(0.0, -1.0, op_);
+        sv_.SetPrecision(precision);
+    }
+    // PoissonWithIBCNearest::GetRHS (problems/PoissonWithIBCNearest.cpp:36-60)
+    VectorX GetRHS(const SourceFn &f, const SourceFn &surface_exact) const {
+        VectorX b(op_.rows(), 0.0);
+        for (size_t r = 0; r < b.size(); ++r) b[r] = f(op_.point(r));
+        for (size_t i = 0; i < rows_.size(); ++i) b[rows_[i]] = surface_exact(cp_[i]);
+        return b;
+    }
+    VectorX Solve(const VectorX &rhs) { return sv_.Solve(rhs); }
+    const Tube &tube() const { return tube_; }
+    const SystemOperator &system() const { return op_; }
+    const std::vector<bool> &GetIdentityRows() const { return op_.identity_rows(); }
+
+  private:
+    static const std::vector<size_t> &nearest_rows(const Tube &tube, const std::vector<SurfaceSpecifier> &ibcs, bool freeze,
+                                                   std::vector<size_t> &rows, std::vector<Point3> &cp) {
+        if (freeze) throw std::runtime_error("cpm_gb300: PoissonWithIBCNearest with freeze_nearest is not offered");
+        SystemOperator with_ibc(tube, ibcs);
+        std::vector<size_t> ref_of(tube.nNodes());
+        for (size_t r = 0; r < ref_of.size(); ++r) ref_of[(size_t)tube.device_index()[r]] = r;
+        for (size_t c = 0; c < ibcs.size(); ++c) {
+            int64_t sz[5];
+            check(cpm_opset_ibc_sizes(with_ibc.handle(), (int32_t)c, sz));
+            std::vector<int64_t> tag((size_t)sz[0]), dof((size_t)sz[1]);
+            std::vector<Scalar> dcp(3 * (size_t)sz[1]);
+            check(cpm_opset_ibc_export(with_ibc.handle(), (int32_t)c, tag.data(), dof.data(), dcp.data()));
+            for (size_t i = 0; i < dof.size(); ++i) {
+                rows.push_back(ref_of[(size_t)dof[i]]);
+                cp.push_back({dcp[3 * i], dcp[3 * i + 1], dcp[3 * i + 2]});
+            }
+        }
+        return rows;
+    }
+    Tube tube_;
+    std::vector<size_t> rows_;
+    std::vector<Point3> cp_;
     SystemOperator op_;
     Solver sv_;
 };

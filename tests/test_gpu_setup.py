@@ -248,3 +248,45 @@ def test_gray_scott_step_matches_lfull_efull(gpu, oracle):
     wu, wv = oracle.csr_matvec(Ep, Ei, Ev, un), oracle.csr_matvec(Ep, Ei, Ev, vn)
     assert np.max(np.abs(gu - wu)) <= 1e-13 * np.max(np.abs(wu))
     assert np.max(np.abs(gv - wv)) <= 1e-13 * np.max(np.abs(wv))
+
+
+def test_nearest_baseline_operator_matches_oracle(gpu, oracle):
+    """PoissonWithIBCNearest's operator (plain L and E, identity rows at the IBC DOF
+    subsets' tube nodes): the device apply equals the reference Multiply assembled
+    from the oracle's L and E with the same identity rows, and its FP64 solve
+    reaches the tolerance on that operator."""
+    dx = 0.1
+    P0 = oracle.RefProblem(oracle.sphere_desc(), [], 3, dx, record_visited=True)
+    PI = oracle.RefProblem(oracle.sphere_desc(), c2_ibcs(oracle, dx), 3, dx)
+    T = gpu.Tube.from_closest_points(gpu.desc(gpu.SPHERE, [1.0]), 3, dx, *P0.visited())
+    ref, g = P0.tube(), T.export()
+    m = ref_to_gpu_index(ref["rec"], g["rec"])  # reference tube row -> device row
+    N = P0.N
+    ident_ref = np.zeros(N, bool)
+    for c in range(2):
+        ident_ref[PI.ibc_subsets(c)["dof_set"]] = True
+    O = gpu.OpSet(T, identity_rows=np.sort(m[np.nonzero(ident_ref)[0]]))
+    assert O.D == N and int(O.rows()["identity"].sum()) == int(ident_ref.sum())
+    Lp, Li, Lv = P0.csr(0)
+    Ep, Ei, Ev = P0.csr(1)
+    diag = np.zeros(N)
+    for r in range(N):
+        for e in range(Lp[r], Lp[r + 1]):
+            if Li[e] == r:
+                diag[r] = Lv[e]
+    rng = np.random.default_rng(6)
+    x_ref = rng.standard_normal(N)
+    t = np.where(ident_ref, x_ref, oracle.csr_matvec(Ep, Ei, Ev, x_ref))
+    off = oracle.csr_matvec(Lp, Li, Lv, t) - diag * t
+    want = np.where(ident_ref, x_ref, 0.0 * x_ref - (diag * x_ref + off))
+    x_dev = np.empty(N)
+    x_dev[m] = x_ref
+    got = O.apply(0.0, -1.0, x_dev)[0][m]
+    assert np.max(np.abs(got - want)) <= 1e-12 * np.max(np.abs(want))
+    # solve: Dirichlet values at the identity rows, f = 0
+    b_ref = np.where(ident_ref, rng.uniform(0, 1, N), 0.0)
+    b_dev = np.empty(N)
+    b_dev[m] = b_ref
+    x, st = gpu.Solver(O, 0.0, -1.0).solve(b_dev, tol=1e-10, precision=0)
+    r = O.apply(0.0, -1.0, x[0])[0] - b_dev
+    assert st[0]["status"] == 0 and np.linalg.norm(r) <= 1e-9 * np.linalg.norm(b_dev)
