@@ -242,6 +242,9 @@ extern "C" int cpm_geodesic_run(cpm_geodesic_t g, double dt, int32_t precision, 
         // Step3: Poisson solve, then phi -= min phi
         if ((rc = cpm_solve_device(pois, 1, b.p, x.p, &o, &ss))) return cleanup(rc);
         if (iters_out) iters_out[1 + round] = ss.iterations;
+        // the rounds solve with the same operator: once its FP32 iteration has had to
+        // fall back to FP64, the later rounds go to FP64 directly
+        if (ss.fp64_fallback) o.precision = 0;
         k_block_min<<<nparts, 256, 0, st>>>(D, x.p, part.p);
         k_sub_min<<<bD, 256, 0, st>>>(D, nparts, part.p, x.p);
         count_launches(2);
