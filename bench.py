@@ -487,8 +487,9 @@ def main():
         plain_iters.append(stp[0]["iterations"])
     plain_sps = 1.0 / float(np.mean(plain_t))
 
-    # ---- end to end through the C-ABI server with host buffers (H2D of b and D2H of x per request)
-    n_e2e = 2 * KSLOTS
+    # ---- end to end through the C-ABI server with host buffers (H2D of b and D2H of x per request),
+    # the same requests as the timed device-resident stream
+    n_e2e = n_timed
     he = list(range(n_warm, n_warm + n_e2e))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -569,7 +570,7 @@ def main():
             "fp64_fallbacks": int(sum(int(x.get("fp64_fallback", 0)) for x in st_timed)),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(D * KSLOTS * 8),
                     "d2h_bytes_per_step": int(D * KSLOTS * 8),
-                    "path": "cpm_server_submit / cpm_server_step / cpm_server_poll with host arrays, 64 requests"},
+                    "path": f"cpm_server_submit / cpm_server_step / cpm_server_poll with host arrays, {n_e2e} requests"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "kernel": "L.E apply (E pass + IBC patch rows + L pass), FP32, 32 RHS",
                          "apply_us": apply_s * 1e6, "alg_bytes_per_apply": alg_bytes, "peak_source": peak_src},
