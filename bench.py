@@ -121,18 +121,42 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+def ranks():
+    """(world, rank, local rank) from the launcher's environment"""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def dist_setup(backend=None):
+    """one replica per GPU: the process group over the launcher's ranks (NCCL on the
+    rank's GPU by default), or None for a single process"""
+    world, rank, local = ranks()
     if world > 1:
         import torch
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend is None:
+            torch.cuda.set_device(local)
+            backend = "nccl"
+        dist.init_process_group(backend)
         return world, rank, local, dist
     return 1, 0, local, None
+
+
+def max_over_ranks(t, dist, device="cpu"):
+    """the slowest replica's time (the job ends when every replica has)"""
+    if dist is None:
+        return float(t)
+    import torch
+
+    tt = torch.tensor([float(t)], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replicas_value(world, n_per_rank, t_max):
+    """whole-job solves/s: every replica serves n_per_rank requests, no data-path collective"""
+    return world * n_per_rank / t_max
 
 
 def cpu_baseline_sample(threads, tubes=None, iters_per_solve=None, x_check=None, vals=None):
@@ -157,7 +181,8 @@ def cpu_baseline_sample(threads, tubes=None, iters_per_solve=None, x_check=None,
 
 
 def run_reference(args):
-    world, rank, local, dist = dist_setup()
+    # the host reference: rank 0 alone runs it (no process group needed); other ranks exit
+    world, rank, _ = ranks()
     if rank != 0:
         return
     import oracle_lib as ol
@@ -434,12 +459,8 @@ def main():
         e1.synchronize()
         torch.cuda.synchronize()
     launches = cg.launch_count() - launches0
-    t_total = e0.elapsed_time(e1) * 1e-3
-    if dist:
-        tt = torch.tensor([t_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt.item())
-    value = world * n_timed / t_total
+    t_total = max_over_ranks(e0.elapsed_time(e1) * 1e-3, dist, dev)
+    value = replicas_value(world, n_timed, t_total)
     st_timed = [served[k][1] for k in range(n_warm, n_warm + n_timed)]
     assert all(x["status"] == 0 for x in st_timed), "a served request did not converge"
     iters = [x["iterations"] for x in st_timed]
@@ -496,9 +517,9 @@ def main():
     for k in he:
         srv.submit(B[k], k)
     got = srv.drain(want_x=True)
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
     assert all(got[k][1]["status"] == 0 for k in he)
-    e2e_value = world * n_e2e / e2e_s
+    e2e_value = replicas_value(world, n_e2e, e2e_s)
 
     # ---- roofline of the L.E apply (FP32, 32 RHS): E pass, IBC patch rows and L pass on the library stream
     xf = torch.randn((D, KSLOTS), dtype=torch.float32, device=dev)
