@@ -581,8 +581,11 @@ def main():
                                    "into a slot to result"},
             "fp64_plain": {"solves_per_s": plain_sps, "p50_ms": float(np.percentile(plain_t, 50) * 1e3),
                            "p99_ms": float(np.percentile(plain_t, 99) * 1e3),
-                           "iterations": int(np.median(plain_iters))},
+                           "iterations": int(np.median(plain_iters)),
+                           "tube_node_iterations_per_s": float(O.N * np.sum(plain_iters) / np.sum(plain_t))},
             "speedup_vs_fp64_plain": value / world / plain_sps,
+            # tube nodes x BiCGStab iterations (per right-hand side) per second, the whole job
+            "tube_node_iterations_per_s": float(world * O.N * np.sum(iters) / t_total),
             "static_batch_32": {"solves_per_s": KSLOTS / static_s, "ms": static_s * 1e3,
                                 "iterations_max": int(max(x["iterations"] for x in sst))},
             "rel_err_vs_fp64": rel_err,
