@@ -341,25 +341,38 @@ static std::vector<Eig3> subset_jcp(const HostTube &ht, const IBCData &ib, const
 
 // First parameterisation point of an IBC (IBCSubset::FindStartingPoint uses xp()[0]):
 // paramCircle3D vertex 0 (src/Surface.cpp:1883-1904), the point itself, or vertex 0.
+// the unit basis t1, t2 of a circle's plane (ComputeOrthogonalBasis + Normalize)
+static void circle_basis(const double *p, double t1[3], double t2[3]) {
+    double n[3] = {p[4], p[5], p[6]};
+    if (std::fabs(n[0]) > std::fabs(n[1])) {
+        t1[0] = -n[2]; t1[1] = 0; t1[2] = n[0];
+    } else {
+        t1[0] = 0; t1[1] = n[2]; t1[2] = -n[1];
+    }
+    t2[0] = n[1] * t1[2] - n[2] * t1[1];
+    t2[1] = n[2] * t1[0] - n[0] * t1[2];
+    t2[2] = n[0] * t1[1] - n[1] * t1[0];
+    double n1 = std::sqrt(hdot(t1, t1)), n2 = std::sqrt(hdot(t2, t2));
+    for (int k = 0; k < 3; ++k) {
+        t1[k] = n1 > 0 ? t1[k] / n1 : 0;
+        t2[k] = n2 > 0 ? t2[k] / n2 : 0;
+    }
+}
+
+// plot point i of a Circle3D (Surface::paramCircle3D, src/Surface.cpp:1883-1904):
+// theta_i = i 2 pi / (Np - 1), Np = 100
+constexpr int64_t CIRCLE_NP = 100;
+static void circle_point(const double *p, int64_t i, double out[3]) {
+    double t1[3], t2[3];
+    circle_basis(p, t1, t2);
+    const double th = (double)i * (2.0 * M_PI / (double)(CIRCLE_NP - 1));
+    const double c = std::cos(th), sn = std::sin(th);
+    for (int k = 0; k < 3; ++k) out[k] = p[1 + k] + p[0] * (c * t1[k] + sn * t2[k]);
+}
+
 static void ibc_xp0(const cpm_surface_desc &d, const std::vector<double> &verts, double out[3]) {
     if (d.kind == CPM_CIRCLE3D) {
-        const double *p = d.params;
-        double n[3] = {p[4], p[5], p[6]}, t1[3], t2[3];
-        if (std::fabs(n[0]) > std::fabs(n[1])) {
-            t1[0] = -n[2]; t1[1] = 0; t1[2] = n[0];
-        } else {
-            t1[0] = 0; t1[1] = n[2]; t1[2] = -n[1];
-        }
-        t2[0] = n[1] * t1[2] - n[2] * t1[1];
-        t2[1] = n[2] * t1[0] - n[0] * t1[2];
-        t2[2] = n[0] * t1[1] - n[1] * t1[0];
-        double n1 = std::sqrt(hdot(t1, t1)), n2 = std::sqrt(hdot(t2, t2));
-        for (int k = 0; k < 3; ++k) {
-            t1[k] = n1 > 0 ? t1[k] / n1 : 0;
-            t2[k] = n2 > 0 ? t2[k] / n2 : 0;
-        }
-        double c0 = std::cos(0.0), s0 = std::sin(0.0);
-        for (int k = 0; k < 3; ++k) out[k] = p[1 + k] + p[0] * (c0 * t1[k] + s0 * t2[k]);
+        circle_point(d.params, 0, out);
     } else if (d.kind == CPM_POINT) {
         for (int k = 0; k < 3; ++k) out[k] = d.params[k];
     } else {
@@ -1358,5 +1371,47 @@ extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp
             if (hits > 1) return fail(CPM_ERR_UNSUPPORTED, "IBCs too close together: a stencil entry moves to two IBCs");
             if (hits == 1) cols[64 * i + e] = tgt;
         }
+    return 0;
+}
+
+// Surface::xp() of an IBC curve (Surface::GetSurfaceParameterization,
+// src/Surface.cpp:194-216): a Circle3D's 100 parameter points, a Point, or a
+// polyline's vertices.  n in, the count out; xp NULL queries the count.
+extern "C" int cpm_ibc_plot_points(const cpm_surface_desc *ibc, int64_t *n, double *xp) {
+    if (!ibc || !n) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
+    int64_t cnt = 0;
+    if (ibc->kind == CPM_CIRCLE3D)
+        cnt = CIRCLE_NP;
+    else if (ibc->kind == CPM_POINT)
+        cnt = 1;
+    else if (ibc->kind == CPM_POLYLINE || ibc->kind == CPM_TRIANGULATION)
+        cnt = ibc->nverts;
+    else
+        return fail(CPM_ERR_UNSUPPORTED, "plot points of this IBC kind are not offered");
+    if (!xp) {
+        *n = cnt;
+        return 0;
+    }
+    if (*n < cnt) return fail(CPM_ERR_INVALID_ARG, "xp holds fewer points than the curve has");
+    for (int64_t i = 0; i < cnt; ++i) {
+        if (ibc->kind == CPM_CIRCLE3D)
+            circle_point(ibc->params, i, xp + 3 * i);
+        else if (ibc->kind == CPM_POINT)
+            for (int k = 0; k < 3; ++k) xp[3 * i + k] = ibc->params[k];
+        else
+            for (int k = 0; k < 3; ++k) xp[3 * i + k] = ibc->verts[3 * i + k];
+    }
+    *n = cnt;
+    return 0;
+}
+
+// Tube::NearestTubeIndex (src/Tube.h:116-121): the tube node at the grid point
+// nearest each x (device index), or -1 where that grid point is not in the tube
+extern "C" int cpm_tube_nearest(cpm_tube_t t, int64_t n, const double *x, int64_t *idx) {
+    if (!t || n < 0 || (n > 0 && (!x || !idx))) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
+    if (n == 0) return 0;
+    HostTube ht;
+    CPM_TRY(ht.load(t));
+    for (int64_t i = 0; i < n; ++i) idx[i] = ht.nearest(x + 3 * i);
     return 0;
 }

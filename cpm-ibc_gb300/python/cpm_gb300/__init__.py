@@ -67,6 +67,15 @@ class SolveStats(ctypes.Structure):
                 ("fp64_fallback", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
+def ibc_plot_points(d):
+    """Surface::xp() of an IBC curve: a Circle3D's 100 parameter points, a Point, or a polyline's vertices"""
+    n = ctypes.c_int64()
+    _check(lib().cpm_ibc_plot_points(ctypes.byref(d), ctypes.byref(n), None))
+    xp = np.zeros((n.value, 3))
+    _check(lib().cpm_ibc_plot_points(ctypes.byref(d), ctypes.byref(n), _p(xp)))
+    return xp
+
+
 def desc(kind, params=(), bbox=(-1.0, 1.0), boundary_order=1, on_ibc_tolerance=0.0, verts=None, prims=None,
          boundary_type=(0, 0)):
     d = SurfaceDesc()
@@ -115,6 +124,8 @@ def lib():
         L.cpm_tube_destroy.argtypes = [vp]
         L.cpm_opset_create.argtypes = [vp, ctypes.c_int32, P(SurfaceDesc), P(vp)]
         L.cpm_opset_create_identity.argtypes = [vp, ctypes.c_int64, vp, P(vp)]
+        L.cpm_tube_nearest.argtypes = [vp, ctypes.c_int64, vp, vp]
+        L.cpm_ibc_plot_points.argtypes = [P(SurfaceDesc), vp, vp]
         L.cpm_opset_sizes.argtypes = [vp, vp]
         L.cpm_opset_rows.argtypes = [vp] * 5
         L.cpm_opset_ibc_sizes.argtypes = [vp, ctypes.c_int32, vp]
@@ -207,6 +218,13 @@ class Tube:
         order = np.zeros(self.N, np.int64)
         _check(lib().cpm_tube_reference_order(self.h, _p(order)))
         return order
+
+    def nearest(self, x):
+        """Tube::NearestTubeIndex: device index of the node at each point's nearest grid point, or -1"""
+        x = np.ascontiguousarray(np.atleast_2d(x), np.float64)
+        idx = np.zeros(x.shape[0], np.int64)
+        _check(lib().cpm_tube_nearest(self.h, x.shape[0], _p(x), _p(idx)))
+        return idx
 
     def interp_query(self, xq):
         """Interpolation(Tube&, xq) rows: 64 (column, value) per query point."""

@@ -129,6 +129,17 @@ int cpm_tube_reference_order(cpm_tube_t t, int64_t *order);
  * CPM_ERR_BASEPOINT_OUTSIDE_TUBE like Tube::ComputeBasePoints. */
 int cpm_interp_query(cpm_tube_t t, int64_t n, const double *xq, int64_t *cols, double *vals);
 
+/* Tube::NearestTubeIndex (src/Tube.h:116-121): per point x[3i..3i+2] the device
+ * index of the tube node at the nearest grid point, or -1 where that grid point
+ * is not in the tube. */
+int cpm_tube_nearest(cpm_tube_t t, int64_t n, const double *x, int64_t *idx);
+
+/* Surface::xp() of an IBC curve (Surface::GetSurfaceParameterization,
+ * src/Surface.cpp:194-216, paramCircle3D :1883-1904): a Circle3D's 100 points at
+ * theta_i = i 2 pi / 99, a Point, or a polyline's vertices.  *n is the capacity
+ * of xp on input and the count on output; xp = NULL queries the count. */
+int cpm_ibc_plot_points(const cpm_surface_desc *ibc, int64_t *n, double *xp);
+
 int cpm_tube_destroy(cpm_tube_t t);
 
 /* ---- Operator set (Lfull, Efull, identity rows) -------------------------

@@ -477,11 +477,11 @@ class PoissonWithIBC {
 };
 
 // PoissonWithIBCNearest (problems/PoissonWithIBCNearest.cpp:5-89): the
-// nearest-node baseline.  No IBC columns: the tube rows of each IBC's DOF subset
-// become identity rows holding the exact surface value at their IBC closest
-// point (freeze_nearest = false); the plain L and E elsewhere, solved with
-// Init(0, -1).  freeze_nearest (the rows nearest to the IBC curves' own plot
-// points) is not offered.
+// nearest-node baseline.  No IBC columns: identity rows hold exact surface
+// values, at the tube rows of each IBC's DOF subset with the value at their IBC
+// closest point (freeze_nearest false), or at the tube rows nearest to each
+// IBC curve's own plot points with the value there (freeze_nearest true); the
+// plain L and E elsewhere, solved with Init(0, -1).
 class PoissonWithIBCNearest {
   public:
     PoissonWithIBCNearest(const SurfaceSpecifier &surface, const std::vector<SurfaceSpecifier> &ibcs, Scalar dx,
@@ -506,10 +506,25 @@ class PoissonWithIBCNearest {
   private:
     static const std::vector<size_t> &nearest_rows(const Tube &tube, const std::vector<SurfaceSpecifier> &ibcs, bool freeze,
                                                    std::vector<size_t> &rows, std::vector<Point3> &cp) {
-        if (freeze) throw std::runtime_error("cpm_gb300: PoissonWithIBCNearest with freeze_nearest is not offered");
-        SystemOperator with_ibc(tube, ibcs);
         std::vector<size_t> ref_of(tube.nNodes());
         for (size_t r = 0; r < ref_of.size(); ++r) ref_of[(size_t)tube.device_index()[r]] = r;
+        if (freeze) {
+            for (const auto &ibc : ibcs) {
+                int64_t n = 0;
+                check(cpm_ibc_plot_points(&ibc.desc(), &n, nullptr));
+                std::vector<Scalar> xp(3 * (size_t)n);
+                check(cpm_ibc_plot_points(&ibc.desc(), &n, xp.data()));
+                std::vector<int64_t> idx((size_t)n);
+                check(cpm_tube_nearest(tube.handle(), n, xp.data(), idx.data()));
+                for (size_t i = 0; i < (size_t)n; ++i) {
+                    if (idx[i] < 0) throw std::runtime_error("cpm_gb300: an IBC plot point has no tube node nearby");
+                    rows.push_back(ref_of[(size_t)idx[i]]);
+                    cp.push_back({xp[3 * i], xp[3 * i + 1], xp[3 * i + 2]});
+                }
+            }
+            return rows;
+        }
+        SystemOperator with_ibc(tube, ibcs);
         for (size_t c = 0; c < ibcs.size(); ++c) {
             int64_t sz[5];
             check(cpm_opset_ibc_sizes(with_ibc.handle(), (int32_t)c, sz));

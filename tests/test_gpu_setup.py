@@ -290,3 +290,19 @@ def test_nearest_baseline_operator_matches_oracle(gpu, oracle):
     x, st = gpu.Solver(O, 0.0, -1.0).solve(b_dev, tol=1e-10, precision=0)
     r = O.apply(0.0, -1.0, x[0])[0] - b_dev
     assert st[0]["status"] == 0 and np.linalg.norm(r) <= 1e-9 * np.linalg.norm(b_dev)
+
+
+def test_tube_nearest_is_grid_rounding(gpu):
+    """Tube::NearestTubeIndex: the tube node at each point's rounded grid point, -1 off the tube."""
+    dx = 0.1
+    T = gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx)
+    g = T.export()
+    rng = np.random.default_rng(8)
+    x = rng.uniform(-1.3, 1.3, (2000, 3))
+    idx = T.nearest(x)
+    ijk = np.rint((x - T.xstart) / dx).astype(np.int64)
+    n1 = T.N1d
+    key = (ijk[:, 0] * n1 + ijk[:, 1]) * n1 + ijk[:, 2]
+    of_key = {int(k): i for i, k in enumerate(g["rec"])}
+    want = np.array([of_key.get(int(k), -1) for k in key])
+    assert np.array_equal(idx, want) and (want >= 0).sum() > 100 and (want < 0).sum() > 100
