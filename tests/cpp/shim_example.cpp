@@ -50,6 +50,16 @@ int main(int argc, char **argv) {
         // heat-method geodesic distance from (0.36, 0.48, 0.8) on the sphere, dx = 0.1
         GeodesicDistance gd;
         put(f, gd.ComputeDistance(tube, {0.36, 0.48, 0.8}, 0.01));
+        // nearest-node baselines on the same circles: solution, identity rows, right-hand side
+        for (bool freeze : {false, true}) {
+            PoissonWithIBCNearest pn(sphere, ibcs, dx, freeze);
+            VectorX rn = pn.GetRHS([](const Point3 &) { return 0.0; }, [](const Point3 &x) { return x[2]; });
+            put(f, pn.Solve(rn));
+            VectorX id(rn.size());
+            for (size_t r = 0; r < id.size(); ++r) id[r] = pn.GetIdentityRows()[r] ? 1.0 : 0.0;
+            put(f, id);
+            put(f, rn);
+        }
         printf("nodes %zu rows %zu ibc_dofs %zu iterations %d\n", tube.nNodes(), p.system().rows(),
                p.system().TotalIBCDOFs(), p.solver().stats().iterations);
     } catch (const std::exception &e) {

@@ -51,7 +51,7 @@ def test_shim_example_matches_oracle(gpu, oracle, tmp_path):
                     f"-Wl,-rpath,{libdir}", "-o", exe], check=True)
     out = str(tmp_path / "out.bin")
     subprocess.run([exe, out], check=True)
-    c1, c2, c2m, geo = _read(out)
+    c1, c2, c2m, geo, n_u, n_id, n_b, f_u, f_id, f_b = _read(out)
     # C1
     P1 = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1)
     b1 = 3.0 * P1.rows()["point"][:, 2]
@@ -70,3 +70,11 @@ def test_shim_example_matches_oracle(gpu, oracle, tmp_path):
     pg, _ = Pg.geodesic(0.01, 2000)
     assert len(geo) == Pg.D
     assert np.max(np.abs(geo - pg)) / np.max(np.abs(pg)) <= 1e-6
+    # nearest-node baselines: identity rows at the DOF subsets' nodes (as many as the IBC
+    # DOFs) or at the nodes nearest the circles' 100 plot points each, holding their values
+    assert len(n_u) == P2.N and int(n_id.sum()) == P2.total_ibc_dofs
+    assert 0 < int(f_id.sum()) <= 200
+    for u, ident, b in ((n_u, n_id, n_b), (f_u, f_id, f_b)):
+        m = ident > 0
+        assert np.max(np.abs(u[m] - b[m])) <= 1e-12
+        assert np.all(np.abs(b[m]) <= 1.0) and np.all(b[~m] == 0.0)
