@@ -120,6 +120,137 @@ __global__ void k_sub_min(int64_t n, int nparts, const double *__restrict__ part
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] -= mn;
 }
 
+
+// ---------------------------------------------------------------------------
+// GeodesicDistanceNearest (problems/GeodesicDistanceNearest.cpp:11-345): the
+// plain tube operator with identity rows at the constraint nodes.  Its heat
+// step solves the TRANSPOSE of the implicit-Euler matrix
+// I - dt (diag(L) + (L - diag(L)) E) (Helpers::ImplicitEulerMatrix,
+// src/Helpers.cpp:292-299; the reference factorises Afull.transpose() with a
+// sparse LU, :103-133) whose constraint rows are then identity rows.  L is
+// symmetric (the 7-point stencil over tube neighbours), so row k of that
+// matrix applied to v is
+//   v_k - dt (L_kk v_k + sum_q E_qk w_q),   w_q = sum_{c != q} L_qc v_c,
+// and the E^T gather runs over the base groups: column k lies in the 4^3
+// stencil of group g at offset (i, j, l) exactly when g's base node is
+// k - (i, j, l).  The sums run in a fixed order (deterministic).
+
+// grp_of[node] = the base group whose base point is that tube node
+__global__ void k_group_of_base(OpView<double> op, int32_t *__restrict__ grp_of, int32_t *__restrict__ err) {
+    const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= op.n_grp) return;
+    const uint32_t b = op.base[op.ord[op.grp[g]]];
+    const int nd = node_at(op.bv, unpack_i(b), unpack_j(b), unpack_k(b));
+    if (nd < 0) {
+        atomicExch(err, 1);
+        return;
+    }
+    grp_of[nd] = (int32_t)g;
+}
+
+// w_q = sum over q's tube neighbours c of L_qc v_c
+__global__ void k_loff_sum(int64_t N, const int32_t *__restrict__ nbr6, double Loff, const double *__restrict__ v,
+                           double *__restrict__ w) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    double s = 0.0;
+    for (int e = 0; e < 6; ++e) {
+        const int c = nbr6[6 * q + e];
+        if (c >= 0) s += Loff * v[c];
+    }
+    w[q] = s;
+}
+
+// y = A^T v (in == nullptr), or one damped Jacobi sweep y = v + omega (in - A^T v) / d
+// with the matrix-free diagonal d = 1 - dt L_kk (1 on identity rows), as the
+// reference's Jacobi preconditioner forms it (src/GeneralizedBiCGStabSystem.h:281-385)
+__global__ void k_heat_transposed(OpView<double> op, const int32_t *__restrict__ grp_of, const uint8_t *__restrict__ ident,
+                                  double dt, const double *__restrict__ v, const double *__restrict__ w,
+                                  const double *__restrict__ in, double omega, double *__restrict__ y) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= op.N) return;
+    const double vk = v[k];
+    double ak, d = 1.0;
+    if (ident[k] & F_IDENT) {
+        ak = vk;
+    } else {
+        const uint32_t key = op.key[k];
+        const int ci = unpack_i(key), cj = unpack_j(key), ck = unpack_k(key);
+        double z = 0.0;
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j)
+                for (int l = 0; l < 4; ++l) {
+                    const int nd = node_at(op.bv, ci - i, cj - j, ck - l);
+                    if (nd < 0) continue;
+                    const int g = grp_of[nd];
+                    if (g < 0) continue;
+                    const int p1 = op.grp[g + 1];
+                    for (int p = op.grp[g]; p < p1; ++p) {
+                        const double *wp = op.w_ord + 12 * (int64_t)p;
+                        z += ((wp[8 + l] * wp[4 + j]) * wp[i]) * w[op.ord[p]];
+                    }
+                }
+        ak = vk - dt * (op.Ldiag * vk + z);
+        d = 1.0 + op.Ldiag * (-dt);
+    }
+    y[k] = in ? vk + omega * ((in[k] - ak) / d) : ak;
+}
+
+// deterministic dot product: fixed grid of block partials, summed in order by one thread
+constexpr int NEAREST_DOT_BLOCKS = 304;
+// the Jacobi-preconditioned heat step converges in a few iterations; each costs
+// 4 x (sweeps) launches, so the cap bounds a non-converging run to seconds
+constexpr int NEAREST_HEAT_MAX_ITERS = 1000;
+__global__ void k_dot_parts(int64_t n, const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ part) {
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += a[i] * b[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+__global__ void k_sum_parts(int nparts, const double *__restrict__ part, double *__restrict__ out) {
+    double s = 0.0;
+    for (int p = 0; p < nparts; ++p) s += part[p];
+    *out = s;
+}
+
+// BiCGStab vector steps in the reference's operation order (src/BiCGStab.h:64-100)
+__global__ void k_bicg_p(int64_t n, double beta, double w, const double *__restrict__ r, const double *__restrict__ v,
+                         double *__restrict__ p) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double pi = -w * v[i] + p[i];
+    pi *= beta;
+    p[i] = pi + r[i];
+}
+__global__ void k_bicg_s(int64_t n, double alpha, const double *__restrict__ r, const double *__restrict__ v,
+                         double *__restrict__ s) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) s[i] = -alpha * v[i] + r[i];
+}
+__global__ void k_bicg_xr(int64_t n, double alpha, double w, const double *__restrict__ y, const double *__restrict__ z,
+                          const double *__restrict__ s, const double *__restrict__ t, double *__restrict__ x,
+                          double *__restrict__ r) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double xi = alpha * y[i] + x[i];
+    x[i] = w * z[i] + xi;
+    r[i] = -w * t[i] + s[i];
+}
+__global__ void k_sub(int64_t n, const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ c) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) c[i] = a[i] - b[i];
+}
+__global__ void k_zero_rows(int64_t n, const int32_t *__restrict__ rows, double *__restrict__ b) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[rows[i]] = 0.0;
+}
 }  // namespace cpm
 
 using namespace cpm;
@@ -255,6 +386,235 @@ extern "C" int cpm_geodesic_run(cpm_geodesic_t g, double dt, int32_t precision, 
 }
 
 extern "C" int cpm_geodesic_destroy(cpm_geodesic_t g) {
+    delete g;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// GeodesicDistanceNearest::ComputeDistance (problems/GeodesicDistanceNearest.cpp:11-53)
+struct cpm_geodesic_nearest_s {
+    cpm_tube_s *tube = nullptr;
+    cpm_opset_t op_plain = nullptr, op_id = nullptr;
+    int64_t N = 0;
+    DBuf<int32_t> grp_of;
+    std::vector<double> rhs_heat;  // Step1 right-hand side (:62-90)
+    ~cpm_geodesic_nearest_s() {
+        if (op_id) cpm_opset_destroy(op_id);
+        if (op_plain) cpm_opset_destroy(op_plain);
+    }
+};
+
+extern "C" int cpm_geodesic_nearest_create(cpm_tube_t t, int64_t n_ibc, const int64_t *ibc_rows, int64_t n_inside,
+                                           const int64_t *inside_rows, const double *inside_dist,
+                                           cpm_geodesic_nearest_t *out) {
+    if (!t || !out || n_ibc < 0 || n_inside < 0 || (n_ibc > 0 && !ibc_rows) || (n_inside > 0 && (!inside_rows || !inside_dist)))
+        return fail(CPM_ERR_INVALID_ARG, "geodesic_nearest_create: invalid arguments");
+    *out = nullptr;
+    const int64_t N = t->N;
+    for (int64_t i = 0; i < n_ibc; ++i)
+        if (ibc_rows[i] < 0 || ibc_rows[i] >= N) return fail(CPM_ERR_INVALID_ARG, "geodesic_nearest_create: constraint row outside the tube");
+    for (int64_t i = 0; i < n_inside; ++i)
+        if (inside_rows[i] < 0 || inside_rows[i] >= N)
+            return fail(CPM_ERR_INVALID_ARG, "geodesic_nearest_create: inside row outside the tube");
+    cpm_geodesic_nearest_s *g = new cpm_geodesic_nearest_s();
+    g->tube = t;
+    g->N = N;
+    auto bail = [&](int rc) {
+        delete g;
+        return rc;
+    };
+    int rc = cpm_opset_create(t, 0, nullptr, &g->op_plain);
+    if (!rc) rc = opset_tube_normals(g->op_plain);  // ComputeSurfaceNormals (:311-345)
+    if (!rc) rc = cpm_opset_create_identity(t, n_ibc, ibc_rows, &g->op_id);
+    if (!rc) rc = g->grp_of.alloc(N);
+    if (rc) return bail(rc);
+    cudaStream_t st = stream();
+    DBuf<int32_t> err;
+    if ((rc = err.alloc(1)) || (rc = err.zero())) return bail(rc);
+    if (cudaMemsetAsync(g->grp_of.p, 0xff, N * sizeof(int32_t), st) != cudaSuccess)
+        return bail(fail(CPM_ERR_CUDA, "geodesic_nearest_create: memset"));
+    const cpm_opset_s *op = g->op_plain;
+    if (op->n_grp > 0) {
+        k_group_of_base<<<(unsigned)((op->n_grp + 255) / 256), 256, 0, st>>>(op->view<double>(), g->grp_of.p, err.p);
+        count_launches(1);
+    }
+    std::vector<int32_t> he;
+    if ((rc = err.download(he, 1))) return bail(rc);
+    if (he[0]) return bail(fail(CPM_ERR_BASEPOINT_OUTSIDE_TUBE, "geodesic_nearest_create: a base point is not a tube node"));
+    // Step1 right-hand side: SmoothH(t) = 0.5 tanh(-scale t) + 0.5, scale = atanh(1 - dx) / r;
+    // constraint rows t = -|x - cp|, inside rows t = -dist (later entries win, as in the reference)
+    std::vector<uint32_t> key;
+    std::vector<double> cp;
+    if ((rc = t->key.download(key, N)) || (rc = t->cp.download(cp, 3 * N))) return bail(rc);
+    const double scale = std::atanh(1 - t->g.dx) / t->g.radius;
+    auto smooth = [scale](double x) { return 0.5 * std::tanh(-scale * x) + 0.5; };
+    g->rhs_heat.assign(N, 0.0);
+    for (int64_t i = 0; i < n_ibc; ++i) {
+        const int64_t r = ibc_rows[i];
+        const int ijk[3] = {unpack_i(key[r]), unpack_j(key[r]), unpack_k(key[r])};
+        double s = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            const double e = (t->g.xstart + (double)ijk[d] * t->g.dx) - cp[3 * r + d];
+            s += e * e;
+        }
+        g->rhs_heat[r] = smooth(-std::sqrt(s));
+    }
+    for (int64_t i = 0; i < n_inside; ++i) g->rhs_heat[inside_rows[i]] = smooth(-inside_dist[i]);
+    *out = g;
+    return 0;
+}
+
+extern "C" int cpm_geodesic_nearest_run(cpm_geodesic_nearest_t g, double dt, int32_t precision, double tol, int32_t heat_sweeps,
+                                        double *phi_out, int32_t *iters_out) {
+    if (!g || !phi_out || dt <= 0) return fail(CPM_ERR_INVALID_ARG, "geodesic_nearest_run: invalid arguments");
+    const int64_t N = g->N;
+    const double dx = g->tube->g.dx;
+    const cpm_opset_s *pl = g->op_plain;
+    auto plain = pl->view<double>();
+    const int32_t *nbr6 = pl->nbr6.p;
+    const uint8_t *ident = g->op_id->flags.p;
+    const double Loff = plain.Loff, omega = 2.0 / 3.0;
+    const int sweeps = heat_sweeps > 0 ? heat_sweeps : 2000;
+    const double rtol = tol > 0 ? tol : 1e-10;
+    DBuf<double> b, x, r, r0, p, v, s, tt, y, z, w, jac, part, dsc;
+    for (DBuf<double> *q : {&b, &x, &r, &r0, &p, &v, &s, &tt, &y, &z, &w, &jac}) CPM_TRY(q->alloc(N));
+    CPM_TRY(part.alloc(NEAREST_DOT_BLOCKS));
+    CPM_TRY(dsc.alloc(1));
+    cudaStream_t st = stream();
+    const unsigned bN = (unsigned)((N + 255) / 256);
+    auto dot = [&](const double *a, const double *c, double &out) -> int {
+        k_dot_parts<<<NEAREST_DOT_BLOCKS, 256, 0, st>>>(N, a, c, part.p);
+        k_sum_parts<<<1, 1, 0, st>>>(NEAREST_DOT_BLOCKS, part.p, dsc.p);
+        count_launches(2);
+        CPM_CUDA_TRY(cudaMemcpyAsync(&out, dsc.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CPM_CUDA_TRY(cudaStreamSynchronize(st));
+        return 0;
+    };
+    // A^T v -> o
+    auto multiply = [&](const double *in_v, double *o) {
+        k_loff_sum<<<bN, 256, 0, st>>>(N, nbr6, Loff, in_v, w.p);
+        k_heat_transposed<<<bN, 256, 0, st>>>(plain, g->grp_of.p, ident, dt, in_v, w.p, nullptr, 0.0, o);
+        count_launches(2);
+    };
+    // damped Jacobi sweeps from o = 0 (src/GeneralizedBiCGStabSystem.h:350-385)
+    auto precondition = [&](const double *in, double *o) -> int {
+        CPM_CUDA_TRY(cudaMemsetAsync(o, 0, N * sizeof(double), st));
+        double *cur = o, *nxt = jac.p;
+        for (int it = 0; it < sweeps; ++it) {
+            k_loff_sum<<<bN, 256, 0, st>>>(N, nbr6, Loff, cur, w.p);
+            k_heat_transposed<<<bN, 256, 0, st>>>(plain, g->grp_of.p, ident, dt, cur, w.p, in, omega, nxt);
+            std::swap(cur, nxt);
+        }
+        count_launches(2LL * sweeps);
+        if (cur != o) CPM_CUDA_TRY(cudaMemcpyAsync(o, cur, N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        CPM_CUDA_TRY(cudaGetLastError());
+        return 0;
+    };
+    // Step1: BiCGStab (src/BiCGStab.h:30-108) on the transposed heat matrix, x0 = 0
+    CPM_CUDA_TRY(cudaMemcpyAsync(b.p, g->rhs_heat.data(), N * 8, cudaMemcpyHostToDevice, st));
+    CPM_TRY(x.zero());
+    CPM_TRY(v.zero());
+    CPM_TRY(p.zero());
+    CPM_CUDA_TRY(cudaMemcpyAsync(r.p, b.p, N * 8, cudaMemcpyDeviceToDevice, st));
+    CPM_CUDA_TRY(cudaMemcpyAsync(r0.p, b.p, N * 8, cudaMemcpyDeviceToDevice, st));
+    double r0_sq = 0, rhs_sq = 0, rr = 0;
+    CPM_TRY(dot(r0.p, r0.p, r0_sq));
+    CPM_TRY(dot(b.p, b.p, rhs_sq));
+    int iters = 0, restarts = 0;
+    if (rhs_sq > 0.0) {
+        double rho = 1.0, alpha = 1.0, om = 1.0;
+        const double tol2 = rtol * rtol * rhs_sq, eps = 2.220446049250313e-16, eps2 = eps * eps;
+        rr = r0_sq;
+        while (rr > tol2 && iters < NEAREST_HEAT_MAX_ITERS) {
+            const double rho_old = rho;
+            CPM_TRY(dot(r0.p, r.p, rho));
+            if (std::abs(rho) < eps2 * r0_sq) {  // restart from the true residual
+                multiply(x.p, r0.p);
+                k_sub<<<bN, 256, 0, st>>>(N, b.p, r0.p, r.p);
+                count_launches(1);
+                CPM_CUDA_TRY(cudaMemcpyAsync(r0.p, r.p, N * 8, cudaMemcpyDeviceToDevice, st));
+                CPM_TRY(dot(r.p, r.p, r0_sq));
+                rho = r0_sq;
+                if (restarts++ == 0) iters = 0;
+            }
+            const double beta = (rho / rho_old) * (alpha / om);
+            k_bicg_p<<<bN, 256, 0, st>>>(N, beta, om, r.p, v.p, p.p);
+            count_launches(1);
+            CPM_TRY(precondition(p.p, y.p));
+            multiply(y.p, v.p);
+            double r0v = 0;
+            CPM_TRY(dot(r0.p, v.p, r0v));
+            alpha = rho / r0v;
+            k_bicg_s<<<bN, 256, 0, st>>>(N, alpha, r.p, v.p, s.p);
+            count_launches(1);
+            CPM_TRY(precondition(s.p, z.p));
+            multiply(z.p, tt.p);
+            double t2 = 0, ts = 0;
+            CPM_TRY(dot(tt.p, tt.p, t2));
+            if (t2 > 0.0) CPM_TRY(dot(tt.p, s.p, ts));
+            om = t2 > 0.0 ? ts / t2 : 0.0;
+            k_bicg_xr<<<bN, 256, 0, st>>>(N, alpha, om, y.p, z.p, s.p, tt.p, x.p, r.p);
+            count_launches(1);
+            ++iters;
+            CPM_TRY(dot(r.p, r.p, rr));
+        }
+        if (!(rr <= tol2)) return fail(CPM_ERR_NOT_CONVERGED, "geodesic_nearest_run: heat step did not converge");
+    }
+    if (iters_out) iters_out[0] = iters;
+    // u = -(E u) (:136 and :25)
+    k_extend1<<<bN, 256, 0, st>>>(plain, x.p, y.p);
+    k_negate<<<bN, 256, 0, st>>>(N, y.p, z.p);
+    count_launches(2);
+    double *u = z.p;
+    // Steps 2 and 3 with the Poisson solve (m = 0, n = 1, diagonal preconditioner, :244-293)
+    cpm_solve_opts o;
+    memset(&o, 0, sizeof(o));
+    o.tol = rtol;
+    o.max_iters = 100000;
+    o.precision = precision;
+    o.precond = 1;
+    cpm_solve_stats ss;
+    cpm_solver_t pois = nullptr;
+    CPM_TRY(cpm_solver_create(g->op_id, 0.0, 1.0, 1, &pois));
+    auto done = [&](int rc2) {
+        cpm_solver_destroy(pois);
+        return rc2;
+    };
+    DBuf<double> gr, eg;
+    int rc = gr.alloc(3 * N);
+    if (!rc) rc = eg.alloc(3 * N);
+    if (rc) return done(rc);
+    const int nparts = 256;
+    const int64_t n_id = g->op_id->n_ident;
+    for (int round = 0; round < 3; ++round) {
+        if (round > 0) {  // u = E phi (:36-41)
+            k_extend1<<<bN, 256, 0, st>>>(plain, x.p, z.p);
+            count_launches(1);
+        }
+        k_grad3<<<bN, 256, 0, st>>>(N, nbr6, dx, u, gr.p);
+        k_extend3<<<(unsigned)((3 * N + 255) / 256), 256, 0, st>>>(plain, gr.p, eg.p);
+        k_project_normalise<<<bN, 256, 0, st>>>(N, pl->normals.p, eg.p);
+        k_divergence<<<bN, 256, 0, st>>>(N, N, nbr6, dx, eg.p, b.p);
+        count_launches(4);
+        if (n_id > 0) {
+            k_zero_rows<<<(unsigned)((n_id + 255) / 256), 256, 0, st>>>(n_id, g->op_id->ident.p, b.p);
+            count_launches(1);
+        }
+        if (cudaGetLastError() != cudaSuccess) return done(fail(CPM_ERR_CUDA, "geodesic_nearest_run: launch failed"));
+        if ((rc = cpm_solve_device(pois, 1, b.p, x.p, &o, &ss))) return done(rc);
+        if (iters_out) iters_out[1 + round] = ss.iterations;
+        if (ss.fp64_fallback) o.precision = 0;
+        k_block_min<<<nparts, 256, 0, st>>>(N, x.p, part.p);
+        k_sub_min<<<bN, 256, 0, st>>>(N, nparts, part.p, x.p);
+        count_launches(2);
+    }
+    if (cudaMemcpyAsync(phi_out, x.p, N * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return done(fail(CPM_ERR_CUDA, "geodesic_nearest_run: copy-out failed"));
+    return done(0);
+}
+
+extern "C" int cpm_geodesic_nearest_destroy(cpm_geodesic_nearest_t g) {
     delete g;
     return 0;
 }

@@ -591,6 +591,12 @@ static int tube_normals(cpm_opset_s *base, std::vector<double> &normals) {
     return 0;
 }
 
+int opset_tube_normals(cpm_opset_s *o) {
+    std::vector<double> normals;
+    CPM_TRY(tube_normals(o, normals));
+    return o->normals.upload(normals);
+}
+
 static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs) {
     cpm_tube_s *t = o->tube;
     HostTube ht;

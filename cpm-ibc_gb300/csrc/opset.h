@@ -542,3 +542,8 @@ struct cpm_opset_s {
     template <class T>
     cpm::OpView<T> view() const;
 };
+
+namespace cpm {
+// whole-tube Jcp surface normals (eigenvector 0) of the operator's tube, uploaded to o->normals
+int opset_tube_normals(cpm_opset_s *o);
+}  // namespace cpm

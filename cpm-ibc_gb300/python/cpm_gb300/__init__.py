@@ -365,6 +365,43 @@ class Geodesic:
         return phi, its.tolist()
 
 
+class GeodesicNearest:
+    """GeodesicDistanceNearest::ComputeDistance (problems/GeodesicDistanceNearest.cpp:11-53):
+    identity rows at the constraint nodes `ibc_rows`, smoothed heat sources at
+    `inside_rows` (distances `inside_dist`), all device row indices."""
+
+    def __init__(self, tube, ibc_rows, inside_rows=(), inside_dist=()):
+        L = lib()
+        L.cpm_geodesic_nearest_create.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+        L.cpm_geodesic_nearest_run.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_double,
+                                               ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+        L.cpm_geodesic_nearest_destroy.argtypes = [ctypes.c_void_p]
+        self.tube = tube
+        a = np.ascontiguousarray(ibc_rows, np.int64)
+        b = np.ascontiguousarray(inside_rows, np.int64)
+        d = np.ascontiguousarray(inside_dist, np.float64)
+        if len(b) != len(d):
+            raise ValueError("inside_rows and inside_dist differ in length")
+        h = ctypes.c_void_p()
+        _check(L.cpm_geodesic_nearest_create(tube.h, len(a), _p(a), len(b), _p(b), _p(d), ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().cpm_geodesic_nearest_destroy(self.h)
+        except Exception:
+            pass
+
+    def run(self, dt, precision=0, tol=1e-10, heat_sweeps=2000):
+        """phi on the tube rows (device order) and the 4 iteration counts."""
+        phi = np.zeros(self.tube.N)
+        its = np.zeros(4, np.int32)
+        _check(lib().cpm_geodesic_nearest_run(self.h, dt, precision, tol, heat_sweeps, _p(phi), _p(its)))
+        return phi, its.tolist()
+
+
 def set_device(dev):
     lib().cpm_set_device.argtypes = [ctypes.c_int32]
     _check(lib().cpm_set_device(int(dev)))

@@ -284,6 +284,27 @@ int cpm_geodesic_run(cpm_geodesic_t g, double dt, int32_t precision, double tol,
                      int32_t *iters_out);
 int cpm_geodesic_destroy(cpm_geodesic_t g);
 
+/* GeodesicDistanceNearest::ComputeDistance(Tube&, ibc_idx, inside_ibc_idx,
+ * inside_ibc_idx_dist, dt) (problems/GeodesicDistanceNearest.cpp:11-53): the
+ * plain tube operator with identity rows at the constraint nodes `ibc_rows`
+ * (every curve's list, concatenated in order; device row indices), and
+ * smoothed heat sources SmoothH(-dist) at `inside_rows`.  The heat step
+ * solves, as the reference does, the TRANSPOSE of I - dt (diag(L) + (L -
+ * diag(L)) E) with the constraint rows set to identity rows; the reference
+ * factorises it with a sparse LU (:103-133), run solves it in FP64 by
+ * BiCGStab with `heat_sweeps` damped Jacobi sweeps per preconditioner call
+ * (<= 0: 2000) to relative residual `tol`.  The three Poisson steps (m = 0,
+ * n = 1, diagonal preconditioner) run in `precision` 0 or 1.  run writes phi on
+ * the N tube rows (device order; the reference returns plotE * phi, which
+ * cpm_opset_plot_interp of a plain operator set gives) and the 4 iteration
+ * counts. */
+typedef struct cpm_geodesic_nearest_s *cpm_geodesic_nearest_t;
+int cpm_geodesic_nearest_create(cpm_tube_t t, int64_t n_ibc, const int64_t *ibc_rows, int64_t n_inside,
+                                const int64_t *inside_rows, const double *inside_dist, cpm_geodesic_nearest_t *out);
+int cpm_geodesic_nearest_run(cpm_geodesic_nearest_t g, double dt, int32_t precision, double tol, int32_t heat_sweeps,
+                             double *phi_out, int32_t *iters_out);
+int cpm_geodesic_nearest_destroy(cpm_geodesic_nearest_t g);
+
 /* ---- Serving: continuous batching ------------------------------------------
  * No counterpart in the reference (its Solve is one blocking call per RHS,
  * src/Solver.cpp:104-113).  A server owns a 32-slot solver on one operator

@@ -652,4 +652,60 @@ class GeodesicDistance {
     std::array<int32_t, 4> iterations_{};
 };
 
+// GeodesicDistanceNearest (problems/GeodesicDistanceNearest.h:21-49): the heat
+// method on the plain tube operator with identity rows at each curve's
+// constraint nodes and smoothed heat sources at the nodes inside the curves'
+// tubes (the caller's lists, reference row order, as
+// examples/GeodesicDistanceBeetle/GeodesicDistanceBeetle.cpp:36-52 builds
+// them).  ComputeDistance returns phi on the tube rows (reference order); Plot
+// gives plotE * phi at surface points (the reference's return value, :48-52).
+class GeodesicDistanceNearest {
+  public:
+    explicit GeodesicDistanceNearest(bool visualize = false, int precision = 0) : precision_(precision) { (void)visualize; }
+    VectorX ComputeDistance(const Tube &tube, const std::vector<std::vector<size_t>> &ibc_idx,
+                            const std::vector<std::vector<size_t>> &inside_ibc_idx,
+                            const std::vector<std::vector<Scalar>> &inside_ibc_idx_dist, Scalar dt) {
+        const size_t N = tube.nNodes();
+        auto dev = [&](size_t r) {
+            if (r >= N) throw std::runtime_error("cpm_gb300: GeodesicDistanceNearest row outside the tube");
+            return tube.device_index()[r];
+        };
+        std::vector<int64_t> a, b;
+        std::vector<Scalar> d;
+        for (const auto &c : ibc_idx)
+            for (size_t r : c) a.push_back(dev(r));
+        if (inside_ibc_idx.size() != inside_ibc_idx_dist.size())
+            throw std::runtime_error("cpm_gb300: inside_ibc_idx and inside_ibc_idx_dist differ in size");
+        for (size_t c = 0; c < inside_ibc_idx.size(); ++c) {
+            if (inside_ibc_idx[c].size() != inside_ibc_idx_dist[c].size())
+                throw std::runtime_error("cpm_gb300: inside_ibc_idx and inside_ibc_idx_dist differ in size");
+            for (size_t i = 0; i < inside_ibc_idx[c].size(); ++i) {
+                b.push_back(dev(inside_ibc_idx[c][i]));
+                d.push_back(inside_ibc_idx_dist[c][i]);
+            }
+        }
+        cpm_geodesic_nearest_t g = nullptr;
+        check(cpm_geodesic_nearest_create(tube.handle(), (int64_t)a.size(), a.data(), (int64_t)b.size(), b.data(), d.data(), &g));
+        std::unique_ptr<cpm_geodesic_nearest_s, Del> hold(g);
+        VectorX phi(N);
+        check(cpm_geodesic_nearest_run(g, dt, precision_, 1e-10, 2000, phi.data(), iterations_.data()));
+        VectorX out(N);
+        for (size_t i = 0; i < N; ++i) out[i] = phi[(size_t)tube.device_index()[i]];
+        return out;
+    }
+    // plotE * phi (Helpers::GetPlotInterpMatrix, src/Helpers.cpp:97-103) at the points xp
+    static VectorX Plot(const Tube &tube, const VectorX &phi, const std::vector<Point3> &xp) {
+        SystemOperator plain(tube, std::vector<SurfaceSpecifier>{});
+        return plain.Evaluate(phi, xp);
+    }
+    const std::array<int32_t, 4> &iterations() const { return iterations_; }
+
+  private:
+    struct Del {
+        void operator()(cpm_geodesic_nearest_t g) const { cpm_geodesic_nearest_destroy(g); }
+    };
+    int precision_;
+    std::array<int32_t, 4> iterations_{};
+};
+
 }  // namespace cpm_gb300

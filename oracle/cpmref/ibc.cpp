@@ -146,7 +146,7 @@ std::vector<V3> InterpolateUnorientedVectors(const Tube &t, const std::vector<in
 
 // Whole-tube surface normals: eigenvector 0 of the symmetrised Jcp
 // (src/IBCSubset.cpp:192-228, use_Jcp_surface_normals branch).
-static std::vector<V3> NormalsFromJcp(const Tube &t) {
+std::vector<V3> NormalsFromJcp(const Tube &t) {
     std::vector<size_t> s2(t.nNodes());
     std::vector<int64_t> s1(t.nNodes());
     for (size_t i = 0; i < t.nNodes(); ++i) {

@@ -125,6 +125,10 @@ void InterpolateUnorientedVectorFromNeighbours(const Tube &t, std::vector<V3> &v
 std::vector<V3> InterpolateUnorientedVectors(const Tube &t, const std::vector<int64_t> &subset_from_set, size_t subset_size,
                                              const std::vector<V3> &vecs, const std::vector<V3> &xq, bool normalize = true);
 
+// Whole-tube surface normals: eigenvector 0 of the symmetrised Jcp
+// (GeodesicDistanceNearest::ComputeSurfaceNormals, problems/GeodesicDistanceNearest.cpp:311-345).
+std::vector<V3> NormalsFromJcp(const Tube &t);
+
 // Identity-row vector shared by PoissonWithIBC / GeodesicDistance (problems/PoissonWithIBC.cpp:173-191).
 std::vector<bool> IBCIdentityRows(const Tube &t, const IBCSubsets &ibc);
 // Row index holding the Dirichlet value of DOF i of IBC c.

@@ -5,6 +5,7 @@
 //   PoissonWithIBC          problems/PoissonWithIBC.cpp:8-47, 50-133, 162-192
 //   HeatWithIBC             problems/HeatWithIBC.cpp:50-103, 135-169
 //   GeodesicDistance        problems/GeodesicDistance.cpp:11-413
+//   GeodesicDistanceNearest problems/GeodesicDistanceNearest.cpp:11-345
 #pragma once
 
 #include <functional>
@@ -49,6 +50,17 @@ class Problem {
     // GeodesicDistance::ComputeDistance; returns phi on the system rows (not plotted).
     // step1_jacobi_iters = 0 selects the diagonal preconditioner for the heat solve.
     std::vector<double> GeodesicDistance(double dt, int step1_jacobi_iters, std::vector<int> *iters = nullptr) const;
+
+    // GeodesicDistanceNearest::ComputeDistance (problems/GeodesicDistanceNearest.cpp:11-53) on a
+    // problem without IBCs: identity rows at ibc_idx (the constraint rows of every curve, in
+    // order), smoothed heat sources at inside_idx with distances inside_dist.  Returns phi on
+    // the tube rows (the reference returns plotE * phi).  The heat step solves the transposed
+    // implicit-Euler matrix (:103-133); step1_jacobi_iters = 0 solves it directly (dense LU with
+    // partial pivoting, standing in for the reference's SparseLU, small tubes only), > 0 by
+    // BiCGStab with that many damped Jacobi sweeps per preconditioner call.
+    std::vector<double> GeodesicDistanceNearest(const std::vector<size_t> &ibc_idx, const std::vector<size_t> &inside_idx,
+                                                const std::vector<double> &inside_dist, double dt, int step1_jacobi_iters,
+                                                std::vector<int> *iters = nullptr) const;
 
     // (Re)assemble L, E and, with IBCs, the rewritten Lfull/Efull on the current tube.
     void Assemble(const std::vector<SurfaceSpec> &ibcs);

@@ -118,11 +118,18 @@ void GeneralizedSystem::Precondition(const std::vector<double> &x, std::vector<d
 // BiCGStab::Solve (src/BiCGStab.h:30-108).
 SolveStats BiCGStabSolve(const GeneralizedSystem &sys, std::vector<double> &x, const std::vector<double> &b,
                          double tolerance, int max_iterations) {
+    return BiCGStabSolveOp([&](const std::vector<double> &a, std::vector<double> &o) { sys.Multiply(a, o); },
+                           [&](const std::vector<double> &a, std::vector<double> &o) { sys.Precondition(a, o); }, x, b,
+                           tolerance, max_iterations);
+}
+
+SolveStats BiCGStabSolveOp(const LinOp &multiply, const LinOp &precondition, std::vector<double> &x,
+                           const std::vector<double> &b, double tolerance, int max_iterations) {
     SolveStats st;
     const size_t N = b.size();
     std::vector<double> r(N), r0(N, 0.0), v(N, 0.0), p(N, 0.0), s(N), t(N), y(N), z(N);
     r = b;
-    sys.Multiply(x, r0);
+    multiply(x, r0);
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < (long long)N; ++i) r[i] -= r0[i];
     r0 = r;
@@ -144,7 +151,7 @@ SolveStats BiCGStabSolve(const GeneralizedSystem &sys, std::vector<double> &x, c
         rho = DotSerial(r0, r);
         if (std::abs(rho) < eps2 * r0_sqnorm) {
             r = b;
-            sys.Multiply(x, r0);
+            multiply(x, r0);
 #pragma omp parallel for schedule(static)
             for (long long i = 0; i < (long long)N; ++i) r[i] -= r0[i];
             r0 = r;
@@ -158,13 +165,13 @@ SolveStats BiCGStabSolve(const GeneralizedSystem &sys, std::vector<double> &x, c
             pi *= beta;
             p[i] = pi + r[i];
         }
-        sys.Precondition(p, y);
-        sys.Multiply(y, v);
+        precondition(p, y);
+        multiply(y, v);
         alpha = rho / DotSerial(r0, v);
 #pragma omp parallel for schedule(static)
         for (long long i = 0; i < (long long)N; ++i) s[i] = -alpha * v[i] + r[i];
-        sys.Precondition(s, z);
-        sys.Multiply(z, t);
+        precondition(s, z);
+        multiply(z, t);
         double val = DotSerial(t, t);
         w = (val > 0.0) ? DotSerial(t, s) / val : 0.0;
 #pragma omp parallel for schedule(static)

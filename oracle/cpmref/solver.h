@@ -11,6 +11,7 @@
 // pinned by any version in the reference tree).
 #pragma once
 
+#include <functional>
 #include <vector>
 
 #include "sparse.h"
@@ -46,6 +47,12 @@ struct SolveStats {
     double final_rel_residual2 = 0;  // ||r||^2 / ||b||^2 on the recursive residual
     bool converged = false;
 };
+
+// BiCGStab::Solve (src/BiCGStab.h:30-108) over any operator and preconditioner
+// (the algorithm is a template over the system in the reference).
+using LinOp = std::function<void(const std::vector<double> &, std::vector<double> &)>;
+SolveStats BiCGStabSolveOp(const LinOp &multiply, const LinOp &precondition, std::vector<double> &x,
+                           const std::vector<double> &b, double tolerance, int max_iterations);
 
 // BiCGStab::Solve (src/BiCGStab.h:30-108) with x0 = 0 as Solver::Solve uses it.
 SolveStats BiCGStabSolve(const GeneralizedSystem &sys, std::vector<double> &x, const std::vector<double> &b,

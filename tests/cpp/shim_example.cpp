@@ -3,7 +3,8 @@
 // PoissonWithIBC::GetRHS/Solve, GeodesicDistance::ComputeDistance) and writes
 // the solutions, in the reference's row layout, to a binary file:
 //   int64 n, then n doubles, for each of: C1 solution, C2 FP64 solution,
-//   C2 mixed solution, geodesic distance.
+//   C2 mixed solution, geodesic distance, the nearest-node Poisson baselines,
+//   the nearest-node geodesic distance and three plotted values of it.
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -59,6 +60,31 @@ int main(int argc, char **argv) {
             for (size_t r = 0; r < id.size(); ++r) id[r] = pn.GetIdentityRows()[r] ? 1.0 : 0.0;
             put(f, id);
             put(f, rn);
+        }
+        // GeodesicDistanceNearest from the closest point of reference row 100 (a point curve),
+        // constraints built as examples/GeodesicDistanceBeetle/GeodesicDistanceBeetle.cpp:36-52
+        {
+            const std::vector<Point3> xs = tube.x(), cps = tube.cpx();
+            const Point3 src = cps[100];
+            auto dist = [](const Point3 &u, const Point3 &v) {
+                double s = 0.0;
+                for (size_t k = 0; k < 3; ++k) s += (u[k] - v[k]) * (u[k] - v[k]);
+                return std::sqrt(s);
+            };
+            std::vector<std::vector<size_t>> con(1), ins(1);
+            std::vector<std::vector<Scalar>> insd(1);
+            for (size_t i = 0; i < tube.nNodes(); ++i) {
+                if (dist(src, cps[i]) < 1e-6) {
+                    con[0].push_back(i);
+                } else if (dist(xs[i], src) < tube.TubeRadius()) {
+                    ins[0].push_back(i);
+                    insd[0].push_back(dist(xs[i], src));
+                }
+            }
+            GeodesicDistanceNearest gn;
+            VectorX phin = gn.ComputeDistance(tube, con, ins, insd, 0.01);
+            put(f, phin);
+            put(f, GeodesicDistanceNearest::Plot(tube, phin, {Point3{0, 0, 1}, Point3{0.6, 0, 0.8}, Point3{-1, 0, 0}}));
         }
         printf("nodes %zu rows %zu ibc_dofs %zu iterations %d\n", tube.nNodes(), p.system().rows(),
                p.system().TotalIBCDOFs(), p.solver().stats().iterations);

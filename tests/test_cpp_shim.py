@@ -6,7 +6,7 @@ numbering), equal the oracle's vectors entry by entry, with no permutation:
 screened Poisson on the sphere and the two-circle IBC Laplace (FP64) within
 1e-8 relative l_inf (the device computes its own closest points, which differ
 from glibc's by ulps), mixed precision within 1e-8 of the FP64 run, and the
-geodesic within 1e-6 of the oracle's."""
+geodesic and the nearest-node geodesic within 1e-6 of the oracle's."""
 import os
 import shutil
 import subprocess
@@ -51,7 +51,7 @@ def test_shim_example_matches_oracle(gpu, oracle, tmp_path):
                     f"-Wl,-rpath,{libdir}", "-o", exe], check=True)
     out = str(tmp_path / "out.bin")
     subprocess.run([exe, out], check=True)
-    c1, c2, c2m, geo, n_u, n_id, n_b, f_u, f_id, f_b = _read(out)
+    c1, c2, c2m, geo, n_u, n_id, n_b, f_u, f_id, f_b, gn, gn_plot = _read(out)
     # C1
     P1 = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1)
     b1 = 3.0 * P1.rows()["point"][:, 2]
@@ -78,3 +78,15 @@ def test_shim_example_matches_oracle(gpu, oracle, tmp_path):
         m = ident > 0
         assert np.max(np.abs(u[m] - b[m])) <= 1e-12
         assert np.all(np.abs(b[m]) <= 1.0) and np.all(b[~m] == 0.0)
+    # nearest-node geodesic from the closest point of row 100, same constraint rule as the example
+    P1n = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1)
+    t1 = P1n.tube()
+    src = t1["cp"][100]
+    dcp = np.linalg.norm(t1["cp"] - src, axis=1)
+    dxs = np.linalg.norm(t1["x"] - src, axis=1)
+    con = np.nonzero(dcp < 1e-6)[0]
+    ins = np.nonzero((dcp >= 1e-6) & (dxs < P1n.radius))[0]
+    ref, _ = P1n.geodesic_nearest(con, ins, dxs[ins], 0.01, 2000)
+    assert len(gn) == P1n.N
+    assert np.max(np.abs(gn - ref)) / np.max(np.abs(ref)) <= 1e-6
+    assert len(gn_plot) == 3 and np.all(np.isfinite(gn_plot)) and np.all(gn_plot >= -0.1)
