@@ -48,6 +48,29 @@ def test_apply_matches_oracle(gpu, oracle, ibc, mn):
     assert _rel_inf(y_gpu[gr], y_ref) <= 1e-14
 
 
+def test_fp32_batched_apply_matches_fp64(gpu):
+    """The FP32 32-RHS apply (E pass, IBC patch pass, L pass) against the
+    FP64 apply of the same inputs: relative l_inf <= 1e-5 per batch (FP32
+    rounding of 84 FMAs per row and the 1/dx^2 Laplacian)."""
+    import torch
+
+    dx = 0.05
+    T = gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx)
+    O = gpu.OpSet(T, c2_ibcs(gpu, dx))
+    gen = torch.Generator().manual_seed(4)
+    x = (torch.rand((O.D, 32), generator=gen, dtype=torch.float32) * 2 - 1).cuda()
+    x64 = x.double()
+    t, y = torch.empty_like(x), torch.empty_like(x)
+    t64, y64 = torch.empty_like(x64), torch.empty_like(x64)
+    torch.cuda.synchronize()
+    O.apply_device(0.0, -1.0, 32, True, x.data_ptr(), t.data_ptr(), y.data_ptr())
+    O.apply_device(0.0, -1.0, 32, False, x64.data_ptr(), t64.data_ptr(), y64.data_ptr())
+    gpu.sync()
+    a, b = y.cpu().double().numpy(), y64.cpu().numpy()
+    assert _rel_inf(a, b) <= 1e-5
+    assert _rel_inf(t.cpu().double().numpy(), t64.cpu().numpy()) <= 1e-5
+
+
 def test_plain_fp64_solve_matches_oracle_c1(gpu, oracle):
     """Config C1: -Delta_S u + u = f on the unit sphere, f = 3z (exact u = z), dx = 0.1."""
     dx = 0.1
