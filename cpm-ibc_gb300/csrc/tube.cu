@@ -1010,3 +1010,23 @@ extern "C" int cpm_tube_destroy(cpm_tube_t t) {
     delete t;
     return 0;
 }
+
+// Surface::ClosestPoint (src/Surface.cpp:61-190) for n points of any surface kind
+extern "C" int cpm_closest_points(const cpm_surface_desc *surface, int64_t n, const double *x, double max_dist, double *cp,
+                                  double *dist) {
+    if (!surface || n < 0 || (n > 0 && (!x || !cp || !dist))) return fail(CPM_ERR_INVALID_ARG, "closest_points: invalid arguments");
+    if (n == 0) return 0;
+    SurfaceObj s;
+    CPM_TRY(surface_init(s, surface, max_dist > 0 ? max_dist : 0.0));
+    DBuf<double> dx, dcp, dd;
+    CPM_TRY(dx.upload(x, 3 * (size_t)n));
+    CPM_TRY(dcp.alloc(3 * (size_t)n));
+    CPM_TRY(dd.alloc((size_t)n));
+    CPM_TRY(closest_points_dev(s.params(), n, dx.p, dcp.p, dd.p, max_dist > 0 ? max_dist : (double)INFINITY));
+    std::vector<double> hc, hd;
+    CPM_TRY(dcp.download(hc, 3 * (size_t)n));
+    CPM_TRY(dd.download(hd, (size_t)n));
+    std::copy(hc.begin(), hc.end(), cp);
+    std::copy(hd.begin(), hd.end(), dist);
+    return 0;
+}

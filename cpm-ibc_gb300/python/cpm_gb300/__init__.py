@@ -76,6 +76,19 @@ def ibc_plot_points(d):
     return xp
 
 
+def closest_points(d, x, max_dist=0.0):
+    """Surface::ClosestPoint (src/Surface.cpp:61-190) on the device for the points x (n, 3):
+    (cp (n, 3), dist (n,)).  max_dist > 0 bounds mesh and polyline searches."""
+    x = np.ascontiguousarray(np.atleast_2d(x), np.float64)
+    L = lib()
+    L.cpm_closest_points.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
+                                     ctypes.c_void_p]
+    cp = np.zeros_like(x)
+    dist = np.zeros(len(x))
+    _check(L.cpm_closest_points(ctypes.byref(d), len(x), _p(x), float(max_dist), _p(cp), _p(dist)))
+    return cp, dist
+
+
 def desc(kind, params=(), bbox=(-1.0, 1.0), boundary_order=1, on_ibc_tolerance=0.0, verts=None, prims=None,
          boundary_type=(0, 0)):
     d = SurfaceDesc()

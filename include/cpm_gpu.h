@@ -140,6 +140,16 @@ int cpm_tube_nearest(cpm_tube_t t, int64_t n, const double *x, int64_t *idx);
  * of xp on input and the count on output; xp = NULL queries the count. */
 int cpm_ibc_plot_points(const cpm_surface_desc *ibc, int64_t *n, double *xp);
 
+/* Surface::ClosestPoint(x, cpx, dist, bdy) (src/Surface.h:33-34, src/Surface.cpp:61-190) for
+ * n points x (3n doubles) of any surface kind: cp (3n) and dist (n) as the reference's
+ * closest-point functions give them.  max_dist > 0 bounds the triangle-mesh and polyline
+ * searches: a point farther than max_dist from every primitive reports dist > max_dist and an
+ * unspecified cp; max_dist <= 0 searches every primitive.  bdy is not reported.  This is the
+ * query the reference's callers use to pick constraint nodes against curves
+ * (examples/GeodesicDistanceBeetle/GeodesicDistanceBeetle.cpp:36-52). */
+int cpm_closest_points(const cpm_surface_desc *surface, int64_t n, const double *x, double max_dist, double *cp,
+                       double *dist);
+
 int cpm_tube_destroy(cpm_tube_t t);
 
 /* ---- Operator set (Lfull, Efull, identity rows) -------------------------

@@ -241,6 +241,32 @@ class SurfaceSpecifier {
     std::vector<int64_t> prims_;
 };
 
+// Surface (src/Surface.h:23-45): ClosestPoint of any surface kind, evaluated on
+// the device.  bdy is not reported.  ClosestPoints answers many points in one
+// call; max_dist > 0 bounds mesh and polyline searches, and points farther than
+// max_dist then report dist > max_dist.
+class Surface {
+  public:
+    explicit Surface(const SurfaceSpecifier &spec) : spec_(spec) {}
+    void ClosestPoint(const Point3 &x, Point3 &cpx) const {
+        Scalar d = 0;
+        ClosestPoint(x, cpx, d);
+    }
+    void ClosestPoint(const Point3 &x, Point3 &cpx, Scalar &dist) const {
+        check(cpm_closest_points(&spec_.desc(), 1, x.data(), 0.0, cpx.data(), &dist));
+    }
+    void ClosestPoints(const std::vector<Point3> &x, std::vector<Point3> &cpx, std::vector<Scalar> &dist,
+                       Scalar max_dist = 0.0) const {
+        cpx.resize(x.size());
+        dist.resize(x.size());
+        if (x.empty()) return;
+        check(cpm_closest_points(&spec_.desc(), (int64_t)x.size(), x[0].data(), max_dist, cpx[0].data(), dist.data()));
+    }
+
+  private:
+    SurfaceSpecifier spec_;
+};
+
 // Tube(SurfaceSpecifier&, size_t p, Scalar dx) (src/Tube.h:45) on the device.
 class Tube {
   public:

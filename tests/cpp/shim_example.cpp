@@ -73,12 +73,16 @@ int main(int argc, char **argv) {
             };
             std::vector<std::vector<size_t>> con(1), ins(1);
             std::vector<std::vector<Scalar>> insd(1);
+            Surface bc(SurfaceSpecifier::Point(src, {-1.0, 1.0}));
+            std::vector<Point3> cpc;
+            std::vector<Scalar> dc;
+            bc.ClosestPoints(xs, cpc, dc);
             for (size_t i = 0; i < tube.nNodes(); ++i) {
-                if (dist(src, cps[i]) < 1e-6) {
+                if (dist(cpc[i], cps[i]) < 1e-6) {
                     con[0].push_back(i);
-                } else if (dist(xs[i], src) < tube.TubeRadius()) {
+                } else if (dist(xs[i], cpc[i]) < tube.TubeRadius()) {
                     ins[0].push_back(i);
-                    insd[0].push_back(dist(xs[i], src));
+                    insd[0].push_back(dist(xs[i], cpc[i]));
                 }
             }
             GeodesicDistanceNearest gn;

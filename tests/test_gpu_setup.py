@@ -87,6 +87,41 @@ def test_device_closest_points_match_oracle(gpu, oracle, kind, dx):
     assert np.max(np.abs(g["w"][m][w_ok] - P.weights()[w_ok])) < 1e-12
 
 
+def test_closest_point_query_matches_oracle(gpu, oracle):
+    """cpm_closest_points (Surface::ClosestPoint) for every surface kind at random points
+    near the surface: cp and dist within 1e-12 of the oracle's; a mesh search bounded by
+    max_dist agrees with the unbounded one for points within max_dist."""
+    from cpm_gb300 import workloads as W
+
+    rng = np.random.default_rng(17)
+    v, f = W.perturbed_icosphere(3, seed=2)
+    bb = W.mesh_bbox(v)
+    curves, _ = W.parallel_plane_curves(v, f, 2, seed=3)
+    pv, ps = curves[0]
+    cases = [
+        (gpu.desc(gpu.SPHERE, [1.0]), oracle.sphere_desc(), 1.0),
+        (gpu.desc(gpu.TORUS, [1.0, 0.4], (-1.4, 1.4)), oracle.torus_desc(1.0, 0.4, (-1.4, 1.4)), 1.4),
+        (gpu.desc(gpu.CIRCLE3D, [0.8, 0.0, 0.0, 0.3, 0.0, 0.0, 1.0]),
+         oracle.make_desc(oracle.CIRCLE3D, [0.8, 0.0, 0.0, 0.3, 0.0, 0.0, 1.0]), 1.0),
+        (gpu.desc(gpu.POINT, [0.36, 0.48, 0.8]), oracle.make_desc(oracle.POINT, [0.36, 0.48, 0.8]), 1.0),
+        (gpu.desc(gpu.TRIANGULATION, (), bb, verts=v, prims=f),
+         oracle.make_desc(oracle.TRIANGULATION, (), bb, verts=v, prims=f), 0.6),
+        (gpu.desc(gpu.POLYLINE, (), bb, verts=pv, prims=ps), oracle.make_desc(oracle.POLYLINE, (), bb, verts=pv, prims=ps), 0.6),
+    ]
+    for gd, od, ext in cases:
+        x = rng.uniform(-ext, ext, (300, 3))
+        cp, dist = gpu.closest_points(gd, x)
+        cr, dr = oracle.closest_points(od, x)
+        assert np.max(np.abs(cp - cr)) <= 1e-12 and np.max(np.abs(dist - dr)) <= 1e-12
+    gd = cases[4][0]
+    x = rng.uniform(-0.6, 0.6, (400, 3))
+    cp, dist = gpu.closest_points(gd, x)
+    cpb, distb = gpu.closest_points(gd, x, max_dist=0.1)
+    near = dist < 0.1
+    assert near.sum() > 20 and np.all(distb[~near] > 0.1)
+    assert np.array_equal(cpb[near], cp[near]) and np.array_equal(distb[near], dist[near])
+
+
 def test_interp_query_matches_oracle_rows(gpu, oracle):
     dx = 0.1
     P = oracle.RefProblem(oracle.sphere_desc(), [], 3, dx)
