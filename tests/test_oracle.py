@@ -79,7 +79,7 @@ def test_ibc_subset_equals_brute_force(oracle):
     assert dof == sorted(np.nonzero(d < P.radius)[0].tolist())
 
 
-def test_grid_sizing_matches_survey_table(oracle):
+def test_grid_sizing_matches_reference_formulas(oracle):
     """Tube::ConstructTube sizing (src/Tube.cpp:131-157) at the sphere and torus configs."""
     P = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1)
     assert P.N1d == 33 and abs(P.xstart - (-1.6)) < 1e-15
