@@ -159,7 +159,7 @@ def replicas_value(world, n_per_rank, t_max):
 
 
 def cpu_baseline_sample(threads, tubes=None, iters_per_solve=None, x_check=None, vals=None):
-    """The oracle on the host: C2 setup, then a bounded BiCGStab sample (20 iterations)
+    """The oracle on the host: setup of the sphere with two circle IBCs at dx = 0.025, then a bounded BiCGStab sample (20 iterations)
     scaled to solves/s by the iteration count of a full solve of the same system."""
     import oracle_lib as ol
 
@@ -211,7 +211,7 @@ def run_reference(args):
         "config": {"workload": WORKLOAD, "rows": P.D, "tube_nodes": P.N, "l2": "host run (no GPU)"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"oracle (C++17 restatement of the reference custom BiCGStab, SpMV serial, vector ops "
-                                   f"OpenMP) on the C2 system: 1 full solve ({iters_per_solve} iterations) fixes the "
+                                   f"OpenMP) on the two-circle sphere system: 1 full solve ({iters_per_solve} iterations) fixes the "
                                    f"iteration count; each step times 20 iterations and scales to one solve"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "reference_note": "the reference (nathandking/cpm-ibc) needs Eigen3, fcpw and LBFGS++, absent here; "
@@ -555,7 +555,7 @@ def main():
         its = int(np.median(plain_iters))
         c = cpu_baseline_sample(threads, iters_per_solve=its)
         cpu = {"value": c["solves_per_s"], "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"oracle C2 system, 20 BiCGStab iterations timed ({c['s_per_iter'] * 1e3:.1f} ms/iteration) "
+               "sample": f"oracle sphere + two circle IBCs system (dx 0.025), 20 BiCGStab iterations timed ({c['s_per_iter'] * 1e3:.1f} ms/iteration) "
                          f"x {its} iterations per solve (the plain FP64 GPU path's count, same algorithm); "
                          f"setup {c['setup_s']:.1f} s not included"}
 

@@ -2,8 +2,8 @@
 // convergence studies drive cpm-ibc (Tube, Solver::Init/Solve,
 // PoissonWithIBC::GetRHS/Solve, GeodesicDistance::ComputeDistance) and writes
 // the solutions, in the reference's row layout, to a binary file:
-//   int64 n, then n doubles, for each of: C1 solution, C2 FP64 solution,
-//   C2 mixed solution, geodesic distance, the nearest-node Poisson baselines,
+//   int64 n, then n doubles, for each of: the screened Poisson solution, the two-circle
+//   IBC Laplace FP64 and mixed solutions, geodesic distance, the nearest-node Poisson baselines,
 //   the nearest-node geodesic distance and three plotted values of it.
 #include <cmath>
 #include <cstdio>

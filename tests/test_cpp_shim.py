@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 import studies as S
-from test_gpu_setup import c2_ibcs
+from test_gpu_setup import two_circle_ibcs
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "shim_example.cpp")
@@ -52,14 +52,14 @@ def test_shim_example_matches_oracle(gpu, oracle, tmp_path):
     out = str(tmp_path / "out.bin")
     subprocess.run([exe, out], check=True)
     c1, c2, c2m, geo, n_u, n_id, n_b, f_u, f_id, f_b, gn, gn_plot = _read(out)
-    # C1
+    # screened Poisson on the sphere, dx = 0.1
     P1 = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1)
     b1 = 3.0 * P1.rows()["point"][:, 2]
     x1, _ = P1.solve(1.0, -1.0, b1)
     assert len(c1) == P1.D
     assert np.max(np.abs(c1 - x1)) / np.max(np.abs(x1)) <= 1e-8
-    # C2 at dx = 0.05
-    P2 = oracle.RefProblem(oracle.sphere_desc(), c2_ibcs(oracle, 0.05), 3, 0.05)
+    # Laplace with the two circle IBCs at dx = 0.05
+    P2 = oracle.RefProblem(oracle.sphere_desc(), two_circle_ibcs(oracle, 0.05), 3, 0.05)
     b2 = S.build_rhs(P2.rows(), lambda x: np.zeros(len(x)), lambda c, x: np.full(len(x), 1.0 if c == 0 else 0.0))
     x2, _ = P2.solve(0.0, -1.0, b2)
     assert len(c2) == P2.D

@@ -1,18 +1,18 @@
 """The configurations at full size, through properties that hold at any size
 (the oracle finishes only the small cases in seconds):
 
-* C2, the sphere with two circle IBCs at dx = 0.025 (215,662 rows): the
+* The sphere with two circle IBCs at dx = 0.025 (215,662 rows): the
   batched mixed-precision solve is linear in the right-hand side (solve(a b1 +
   b2) = a solve(b1) + solve(b2), within the solver tolerance) and equals the
   FP64 solves (<= 1e-8 relative l_inf).
-* C3, the torus R = 1, r = 0.4 at dx = 0.01 (1.31 M nodes): the heat-method
+* The torus R = 1, r = 0.4 at dx = 0.01 (1.31 M nodes): the heat-method
   geodesic distance from a tube node's closest point is >= 0 up to the
   discretisation error, smallest at the source, and orders the points near the
   source as the chord length does (geodesic and Euclidean distances agree to
   second order there; the heat method's own error near a point source is
   10 - 30 %, so the order, not the value, is checked: rank correlation >= 0.85
   within chord 0.2, where no chord crosses the tube of minor radius 0.4).
-* C4, the perturbed icosphere at level 7 (327,680 triangles) with 16 polyline
+* The perturbed icosphere at level 7 (327,680 triangles) with 16 polyline
   IBCs at dx = 0.005: device closest points equal the oracle's exact FP64
   point-triangle closest points on a sample of tube nodes (<= 1e-12), and the
   3-RHS mixed solve equals the FP64 solves (<= 1e-8)."""
@@ -20,14 +20,14 @@ import numpy as np
 import pytest
 
 from cpm_gb300 import workloads as W
-from test_gpu_setup import c2_ibcs
+from test_gpu_setup import two_circle_ibcs
 
 pytestmark = pytest.mark.gpu
 
 
-def test_c2_full_size_linearity_and_fp64_agreement(gpu):
+def test_two_circle_sphere_full_size_linearity_and_fp64_agreement(gpu):
     dx = 0.025
-    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), c2_ibcs(gpu, dx))
+    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), two_circle_ibcs(gpu, dx))
     rows = O.rows()
     d = rows["kind"] == 2
     rng = np.random.default_rng(21)
@@ -46,7 +46,7 @@ def test_c2_full_size_linearity_and_fp64_agreement(gpu):
         assert np.max(np.abs(X[j] - x64[0])) <= 1e-8 * np.max(np.abs(x64[0]))
 
 
-def test_c3_full_size_geodesic_near_source(gpu):
+def test_torus_full_size_geodesic_near_source(gpu):
     dx = 0.01
     T = gpu.Tube(gpu.desc(gpu.TORUS, [1.0, 0.4], (-1.4, 1.4)), 3, dx)
     g = T.export()
@@ -62,7 +62,7 @@ def test_c3_full_size_geodesic_near_source(gpu):
     assert np.corrcoef(rank(phi[near]), rank(chord[near]))[0, 1] >= 0.85
 
 
-def test_c4_full_size_closest_points_and_solves(gpu, oracle):
+def test_mesh_full_size_closest_points_and_solves(gpu, oracle):
     dx = 0.005
     v, f = W.perturbed_icosphere(7, seed=3)
     bb = W.mesh_bbox(v)

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import studies as S
-from test_gpu_setup import c2_ibcs
+from test_gpu_setup import two_circle_ibcs
 
 pytestmark = pytest.mark.gpu
 
@@ -20,7 +20,7 @@ def _rel(a, b):
 
 def _setup(gpu, dx=0.05):
     T = gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx)
-    O = gpu.OpSet(T, c2_ibcs(gpu, dx, 2))
+    O = gpu.OpSet(T, two_circle_ibcs(gpu, dx, 2))
     rows = O.rows()
     return T, O, rows
 

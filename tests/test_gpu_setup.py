@@ -139,8 +139,8 @@ def test_interp_query_matches_oracle_rows(gpu, oracle):
         assert np.max(np.abs(np.array([v for _, v in a]) - np.array([v for _, v in b]))) < 1e-14
 
 
-def c2_ibcs(mod, dx, order=2):
-    """Config C2: circles z = 0.3 (u = 1) and z = -0.5 (u = 0) on the unit sphere."""
+def two_circle_ibcs(mod, dx, order=2):
+    """The two circle IBCs: z = 0.3 (u = 1) and z = -0.5 (u = 0) on the unit sphere."""
     mk = (lambda R, c, n: mod.circle3d_desc(R, c, n, dx, order)) if hasattr(mod, "circle3d_desc") else (
         lambda R, c, n: mod.desc(mod.CIRCLE3D, [R, *c, *n], (-1.0, 1.0), boundary_order=order, on_ibc_tolerance=0.1 * dx * dx))
     return [mk(math.sqrt(1 - 0.09), (0, 0, 0.3), (0, 0, 1)), mk(math.sqrt(1 - 0.25), (0, 0, -0.5), (0, 0, 1))]
@@ -148,9 +148,9 @@ def c2_ibcs(mod, dx, order=2):
 
 @pytest.mark.parametrize("dx,order", [(0.1, 2), (0.05, 2), (0.05, 1)])
 def test_ibc_subsets_bit_exact(gpu, oracle, dx, order):
-    P = oracle.RefProblem(oracle.sphere_desc(), c2_ibcs(oracle, dx, order), 3, dx, record_visited=True)
+    P = oracle.RefProblem(oracle.sphere_desc(), two_circle_ibcs(oracle, dx, order), 3, dx, record_visited=True)
     T = gpu.Tube.from_closest_points(gpu.desc(gpu.SPHERE, [1.0]), 3, dx, *P.visited())
-    O = gpu.OpSet(T, c2_ibcs(gpu, dx, order))
+    O = gpu.OpSet(T, two_circle_ibcs(gpu, dx, order))
     ref, g = P.tube(), T.export()
     assert O.D == P.D and O.total_ibc_dofs == P.total_ibc_dofs and O.num2 == P.num2
     for c in range(2):
@@ -176,9 +176,9 @@ def _permuted_csr(gpu_csr, m_inv_full, D):
 def test_ibc_operator_rows_match_oracle(gpu, oracle, which):
     """Lfull / Efull rows (with IBC column moves) equal the oracle's up to rounding of the weights' products."""
     dx = 0.1
-    P = oracle.RefProblem(oracle.sphere_desc(), c2_ibcs(oracle, dx), 3, dx, record_visited=True)
+    P = oracle.RefProblem(oracle.sphere_desc(), two_circle_ibcs(oracle, dx), 3, dx, record_visited=True)
     T = gpu.Tube.from_closest_points(gpu.desc(gpu.SPHERE, [1.0]), 3, dx, *P.visited())
-    O = gpu.OpSet(T, c2_ibcs(gpu, dx))
+    O = gpu.OpSet(T, two_circle_ibcs(gpu, dx))
     ref, g = P.tube(), T.export()
     m = ref_to_gpu_index(ref["rec"], g["rec"])
     full = np.arange(O.D)
@@ -221,9 +221,9 @@ def test_plot_interpolation_with_ibc_columns_matches_oracle(gpu, oracle, dx):
     """Evaluation-point rows (GetPlotInterpMatrix + AddIBCPlotInterpolation) equal the
     oracle's: the same columns, moved to IBC DOF columns across the curves, and the
     same values."""
-    P = oracle.RefProblem(oracle.sphere_desc(), c2_ibcs(oracle, dx), 3, dx, record_visited=True)
+    P = oracle.RefProblem(oracle.sphere_desc(), two_circle_ibcs(oracle, dx), 3, dx, record_visited=True)
     T = gpu.Tube.from_closest_points(gpu.desc(gpu.SPHERE, [1.0]), 3, dx, *P.visited())
-    O = gpu.OpSet(T, c2_ibcs(gpu, dx))
+    O = gpu.OpSet(T, two_circle_ibcs(gpu, dx))
     ref, g = P.tube(), T.export()
     m = ref_to_gpu_index(ref["rec"], g["rec"])
     full = np.arange(O.D)
@@ -251,7 +251,7 @@ def test_explicit_heat_step_matches_lfull_efull(gpu, oracle):
     identity rows included (Lfull and Efull hold 1 on their diagonal there)."""
     dx = 0.1
     dt = 0.1 * dx * dx
-    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), c2_ibcs(gpu, dx))
+    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), two_circle_ibcs(gpu, dx))
     rng = np.random.default_rng(3)
     u = rng.standard_normal((2, O.D))
     got = O.explicit_step(dt, u)
@@ -269,7 +269,7 @@ def test_gray_scott_step_matches_lfull_efull(gpu, oracle):
     exported Lfull / Efull, the reaction terms from the old u, v."""
     dx = 0.1
     dt = 0.2
-    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), c2_ibcs(gpu, dx))
+    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), two_circle_ibcs(gpu, dx))
     rng = np.random.default_rng(4)
     u, v = rng.uniform(0, 1, O.D), rng.uniform(0, 0.5, O.D)
     gu, gv = O.gray_scott_step(dt, u, v)
@@ -292,7 +292,7 @@ def test_nearest_baseline_operator_matches_oracle(gpu, oracle):
     reaches the tolerance on that operator."""
     dx = 0.1
     P0 = oracle.RefProblem(oracle.sphere_desc(), [], 3, dx, record_visited=True)
-    PI = oracle.RefProblem(oracle.sphere_desc(), c2_ibcs(oracle, dx), 3, dx)
+    PI = oracle.RefProblem(oracle.sphere_desc(), two_circle_ibcs(oracle, dx), 3, dx)
     T = gpu.Tube.from_closest_points(gpu.desc(gpu.SPHERE, [1.0]), 3, dx, *P0.visited())
     ref, g = P0.tube(), T.export()
     m = ref_to_gpu_index(ref["rec"], g["rec"])  # reference tube row -> device row

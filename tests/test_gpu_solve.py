@@ -12,18 +12,18 @@ import numpy as np
 import pytest
 
 import studies as S
-from test_gpu_setup import c2_ibcs, ref_to_gpu_index
+from test_gpu_setup import two_circle_ibcs, ref_to_gpu_index
 
 pytestmark = pytest.mark.gpu
 
 
 def _pair(gpu, oracle, dx, ibc=False, order=2):
     if ibc:
-        P = oracle.RefProblem(oracle.sphere_desc(), c2_ibcs(oracle, dx, order), 3, dx, record_visited=True)
+        P = oracle.RefProblem(oracle.sphere_desc(), two_circle_ibcs(oracle, dx, order), 3, dx, record_visited=True)
     else:
         P = oracle.RefProblem(oracle.sphere_desc(), [], 3, dx, record_visited=True)
     T = gpu.Tube.from_closest_points(gpu.desc(gpu.SPHERE, [1.0]), 3, dx, *P.visited())
-    O = gpu.OpSet(T, c2_ibcs(gpu, dx, order) if ibc else [])
+    O = gpu.OpSet(T, two_circle_ibcs(gpu, dx, order) if ibc else [])
     ref, g = P.tube(), T.export()
     m = ref_to_gpu_index(ref["rec"], g["rec"])
     g_of_ref = np.arange(O.D)
@@ -56,7 +56,7 @@ def test_fp32_batched_apply_matches_fp64(gpu):
 
     dx = 0.05
     T = gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx)
-    O = gpu.OpSet(T, c2_ibcs(gpu, dx))
+    O = gpu.OpSet(T, two_circle_ibcs(gpu, dx))
     gen = torch.Generator().manual_seed(4)
     x = (torch.rand((O.D, 32), generator=gen, dtype=torch.float32) * 2 - 1).cuda()
     x64 = x.double()
@@ -71,8 +71,8 @@ def test_fp32_batched_apply_matches_fp64(gpu):
     assert _rel_inf(t.cpu().double().numpy(), t64.cpu().numpy()) <= 1e-5
 
 
-def test_plain_fp64_solve_matches_oracle_c1(gpu, oracle):
-    """Config C1: -Delta_S u + u = f on the unit sphere, f = 3z (exact u = z), dx = 0.1."""
+def test_plain_fp64_solve_matches_oracle_screened_poisson(gpu, oracle):
+    """Screened Poisson -Delta_S u + u = f on the unit sphere, f = 3z (exact u = z), dx = 0.1."""
     dx = 0.1
     P, T, O, gr = _pair(gpu, oracle, dx)
     rows = P.rows()
@@ -109,7 +109,7 @@ def test_plain_fp64_ibc_solve_matches_oracle(gpu, oracle):
 @pytest.mark.parametrize("precond,sweeps", [(0, 0), (2, 1), (2, 25)])
 def test_preconditioners_match_oracle(gpu, oracle, precond, sweeps, kslots):
     """Identity and damped-Jacobi preconditioning (src/GeneralizedBiCGStabSystem.h:350-385)
-    on the backward-Euler heat operator with the C2 IBCs at dx = 0.1."""
+    on the backward-Euler heat operator with the two circle IBCs at dx = 0.1."""
     dx = 0.1
     P, T, O, gr = _pair(gpu, oracle, dx, ibc=True)
     rows = P.rows()
