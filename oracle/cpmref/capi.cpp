@@ -363,6 +363,23 @@ int cpmref_geodesic_nearest(void *hp, int64_t n_ibc, const int64_t *ibc_idx, int
     GUARD_END
 }
 
+int cpmref_heat_nearest(void *hp, int64_t n_ibc, const int64_t *ibc_idx, int64_t n_inside, const int64_t *inside_idx,
+                        const double *inside_dist, double dt, int32_t step1_jacobi_iters, double *u_out) {
+    GUARD_BEGIN
+    Problem &P = *((Handle *)hp)->prob;
+    std::vector<size_t> a((size_t)n_ibc), b((size_t)n_inside);
+    std::vector<double> d((size_t)n_inside);
+    for (int64_t i = 0; i < n_ibc; ++i) a[i] = (size_t)ibc_idx[i];
+    for (int64_t i = 0; i < n_inside; ++i) {
+        b[i] = (size_t)inside_idx[i];
+        d[i] = inside_dist[i];
+    }
+    std::vector<double> u = P.HeatNearest(a, b, d, dt, step1_jacobi_iters);
+    std::copy(u.begin(), u.end(), u_out);
+    return 0;
+    GUARD_END
+}
+
 // Closest point of an arbitrary point set to a surface (CP-accuracy tests).
 int cpmref_closest_points(const cpmref_surface_desc *surf, int64_t n, const double *x, double *cp, double *dist) {
     GUARD_BEGIN

@@ -192,11 +192,11 @@ static std::vector<double> DenseSolve(const SpMat &A, const std::vector<double> 
     return x;
 }
 
-// GeodesicDistanceNearest::ComputeDistance (problems/GeodesicDistanceNearest.cpp:11-53) with
-// Step1 (:60-147), Step2 (:154-236), ComputeDivergence (:298-308), Step3 (:244-293).
-std::vector<double> Problem::GeodesicDistanceNearest(const std::vector<size_t> &ibc_idx, const std::vector<size_t> &inside_idx,
-                                                     const std::vector<double> &inside_dist, double dt,
-                                                     int step1_jacobi_iters, std::vector<int> *iters) const {
+// GeodesicDistanceNearest::Step1 (problems/GeodesicDistanceNearest.cpp:60-133): the smoothed
+// sources and the solve of the transposed implicit-Euler matrix with identity rows.
+std::vector<double> Problem::HeatNearest(const std::vector<size_t> &ibc_idx, const std::vector<size_t> &inside_idx,
+                                         const std::vector<double> &inside_dist, double dt, int step1_jacobi_iters,
+                                         int *iters) const {
     if (has_ibc) throw std::runtime_error("oracle: GeodesicDistanceNearest runs on a problem without IBCs");
     const size_t N = tube.nNodes();
     std::vector<bool> ident(N, false);
@@ -255,7 +255,7 @@ std::vector<double> Problem::GeodesicDistanceNearest(const std::vector<size_t> &
     std::vector<double> u;
     if (step1_jacobi_iters <= 0) {
         u = DenseSolve(Ar, rhs);
-        if (iters) iters->push_back(0);
+        if (iters) *iters = 0;
     } else {
         // the device's substitute for the direct solve: BiCGStab preconditioned by damped
         // Jacobi sweeps with the reference's matrix-free diagonal m + n L_kk = 1 - dt L_kk
@@ -275,8 +275,22 @@ std::vector<double> Problem::GeodesicDistanceNearest(const std::vector<size_t> &
         };
         u.assign(N, 0.0);
         SolveStats st = BiCGStabSolveOp(mul, prec, u, rhs, 1e-10, 100000);
-        if (iters) iters->push_back(st.iterations);
+        if (iters) *iters = st.iterations;
     }
+    return u;
+}
+
+// GeodesicDistanceNearest::ComputeDistance (problems/GeodesicDistanceNearest.cpp:11-53) with
+// Step1 (:60-147), Step2 (:154-236), ComputeDivergence (:298-308), Step3 (:244-293).
+std::vector<double> Problem::GeodesicDistanceNearest(const std::vector<size_t> &ibc_idx, const std::vector<size_t> &inside_idx,
+                                                     const std::vector<double> &inside_dist, double dt,
+                                                     int step1_jacobi_iters, std::vector<int> *iters) const {
+    const size_t N = tube.nNodes();
+    std::vector<bool> ident(N, false);
+    for (size_t i : ibc_idx) ident[i] = true;
+    int heat_iters = 0;
+    std::vector<double> u = HeatNearest(ibc_idx, inside_idx, inside_dist, dt, step1_jacobi_iters, &heat_iters);
+    if (iters) iters->push_back(heat_iters);
     std::vector<double> eu;
     E.Multiply(u, eu);  // u = m_E * u (:136)
     for (size_t i = 0; i < N; ++i) u[i] = -eu[i];  // u = -Step1 (:25)

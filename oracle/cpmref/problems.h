@@ -61,6 +61,11 @@ class Problem {
     std::vector<double> GeodesicDistanceNearest(const std::vector<size_t> &ibc_idx, const std::vector<size_t> &inside_idx,
                                                 const std::vector<double> &inside_dist, double dt, int step1_jacobi_iters,
                                                 std::vector<int> *iters = nullptr) const;
+    // Its heat step alone (:60-133): the solution of the transposed implicit-Euler system, before
+    // the extension u = E u (:136).
+    std::vector<double> HeatNearest(const std::vector<size_t> &ibc_idx, const std::vector<size_t> &inside_idx,
+                                    const std::vector<double> &inside_dist, double dt, int step1_jacobi_iters,
+                                    int *iters = nullptr) const;
 
     // (Re)assemble L, E and, with IBCs, the rewritten Lfull/Efull on the current tube.
     void Assemble(const std::vector<SurfaceSpec> &ibcs);

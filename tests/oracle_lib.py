@@ -130,6 +130,8 @@ def lib():
             L.cpmref_geodesic.argtypes = [vp, ctypes.c_double, ctypes.c_int32, vp, vp]
             L.cpmref_geodesic_nearest.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, ctypes.c_double,
                                                   ctypes.c_int32, vp, vp]
+            L.cpmref_heat_nearest.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, ctypes.c_double,
+                                              ctypes.c_int32, vp]
             L.cpmref_closest_points.argtypes = [P(SurfaceDesc), ctypes.c_int64, vp, vp, vp]
             _lib = L
         return _lib
@@ -269,6 +271,17 @@ class RefProblem:
         its = np.zeros(8, np.int32)
         _check(lib().cpmref_geodesic(self.h, dt, step1_jacobi_iters, _ptr(phi), _ptr(its)))
         return phi, its[:4].tolist()
+
+    def heat_nearest(self, ibc_idx, inside_idx, inside_dist, dt, step1_jacobi_iters=0):
+        """GeodesicDistanceNearest's heat step: the solution of the transposed implicit-Euler
+        system (before u = E u)."""
+        a = np.ascontiguousarray(ibc_idx, np.int64)
+        b = np.ascontiguousarray(inside_idx, np.int64)
+        d = np.ascontiguousarray(inside_dist, np.float64)
+        u = np.zeros(self.N)
+        _check(lib().cpmref_heat_nearest(self.h, len(a), _ptr(a), len(b), _ptr(b), _ptr(d), dt, step1_jacobi_iters,
+                                         _ptr(u)))
+        return u
 
     def geodesic_nearest(self, ibc_idx, inside_idx, inside_dist, dt, step1_jacobi_iters=0):
         """GeodesicDistanceNearest::ComputeDistance on this (IBC-free) problem; phi on the tube

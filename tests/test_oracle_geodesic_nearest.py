@@ -16,6 +16,7 @@ point curve: constraint rows where the curve's closest point equals the
 node's surface closest point (< 1e-6), inside rows where the node lies within
 the tube radius of the curve, with that distance."""
 import numpy as np
+import pytest
 
 
 def point_constraints(t, src, dx):
@@ -62,3 +63,36 @@ def test_nearest_geodesic_follows_great_circle_distance(oracle):
     e -= np.median(e)
     assert np.mean(np.abs(e)) < 0.03 and np.max(np.abs(e)) < 0.1
     assert its[0] >= 1 and all(i > 0 for i in its[1:])
+
+
+def test_nearest_heat_matrix_matches_sparse_lu_of_scipy_assembly(oracle):
+    """The transposed implicit-Euler heat matrix assembled independently with
+    scipy.sparse from the oracle's L and E, its constraint rows set to identity
+    rows, and solved by SuperLU (a sparse LU, as the reference's SparseLU):
+    equal to the oracle's dense-LU heat solution within 1e-10, and to its
+    Jacobi-preconditioned BiCGStab solution within 1e-8 (relative l_inf)."""
+    sp = pytest.importorskip("scipy.sparse")
+    spla = pytest.importorskip("scipy.sparse.linalg")
+    dx = 0.2
+    P, t, src = _sphere_point(oracle, dx, 7)
+    ibc, ins, dist = point_constraints(t, src, dx)
+    dt = dx * dx
+    N = P.N
+    Lm = sp.csr_matrix(tuple(reversed(P.csr(2))), shape=(N, N))
+    Em = sp.csr_matrix(tuple(reversed(P.csr(3))), shape=(N, N))
+    dL = sp.diags(Lm.diagonal())
+    A = sp.identity(N, format="csr") - dt * (dL + (Lm - dL) @ Em)
+    Ar = A.T.tolil()
+    for k in ibc:
+        Ar.rows[k] = [int(k)]
+        Ar.data[k] = [1.0]
+    scale = np.arctanh(1 - dx) / P.radius
+    smooth = lambda s: 0.5 * np.tanh(-scale * s) + 0.5
+    rhs = np.zeros(N)
+    rhs[ibc] = smooth(-np.linalg.norm(t["x"][ibc] - t["cp"][ibc], axis=1))
+    rhs[ins] = smooth(-dist)
+    u = spla.spsolve(Ar.tocsc(), rhs)
+    ud = P.heat_nearest(ibc, ins, dist, dt, 0)
+    uj = P.heat_nearest(ibc, ins, dist, dt, 2000)
+    assert np.max(np.abs(ud - u)) <= 1e-10 * np.max(np.abs(u))
+    assert np.max(np.abs(uj - u)) <= 1e-8 * np.max(np.abs(u))
