@@ -84,3 +84,43 @@ def test_grid_sizing_matches_reference_formulas(oracle):
     P = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1)
     assert P.N1d == 33 and abs(P.xstart - (-1.6)) < 1e-15
     assert abs(P.radius - 1.0001 * math.sqrt(17) * 0.1) < 1e-15
+
+
+@pytest.mark.parametrize("case", ["screened_poisson", "two_circle_laplace"])
+def test_bicgstab_solution_matches_sparse_lu(oracle, case):
+    """The oracle's matrix-free BiCGStab (tol 1e-10) against a direct solve of the
+    same system assembled as a matrix with scipy.sparse from the exported Lfull
+    and Efull (GeneralizedBiCGStabSystem::Multiply, src/GeneralizedBiCGStabSystem.h:191-233:
+    identity rows y = x, other rows m x_q + n (L_qq x_q + sum_{c != q} L_qc t_c) with
+    t = Efull x on non-identity rows and t = x on identity rows), solved by SuperLU:
+    relative l_inf <= 1e-8."""
+    sp = pytest.importorskip("scipy.sparse")
+    spla = pytest.importorskip("scipy.sparse.linalg")
+    dx = 0.1
+    if case == "screened_poisson":
+        P = oracle.RefProblem(oracle.sphere_desc(), [], 3, dx)
+        m, n = 1.0, -1.0
+        f, g = (lambda x: 3.0 * x[:, 2]), (lambda c, x: np.zeros(len(x)))
+    else:
+        ibcs = [oracle.circle3d_desc(math.sqrt(1 - 0.09), (0, 0, 0.3), (0, 0, 1), dx),
+                oracle.circle3d_desc(math.sqrt(1 - 0.25), (0, 0, -0.5), (0, 0, 1), dx)]
+        P = oracle.RefProblem(oracle.sphere_desc(), ibcs, 3, dx)
+        m, n = 0.0, -1.0
+        f, g = (lambda x: np.zeros(len(x))), (lambda c, x: np.full(len(x), 1.0 if c == 0 else 0.0))
+    rows = P.rows()
+    b = S.build_rhs(rows, f, g)
+    D = P.D
+    Lf = sp.csr_matrix(tuple(reversed(P.csr(0))), shape=(D, D))
+    Ef = sp.csr_matrix(tuple(reversed(P.csr(1))), shape=(D, D)).tolil()
+    ident = np.nonzero(rows["identity"])[0]
+    for k in ident:
+        Ef.rows[k] = [int(k)]
+        Ef.data[k] = [1.0]
+    dL = sp.diags(Lf.diagonal())
+    A = (m * sp.identity(D, format="csr") + n * (dL + (Lf - dL) @ Ef.tocsr())).tolil()
+    for k in ident:
+        A.rows[k] = [int(k)]
+        A.data[k] = [1.0]
+    x_lu = spla.spsolve(A.tocsc(), b)
+    x, st = P.solve(m, n, b)
+    assert np.max(np.abs(x - x_lu)) <= 1e-8 * np.max(np.abs(x_lu))
