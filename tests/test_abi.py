@@ -45,3 +45,27 @@ def test_error_string_without_gpu_call():
     rc = L.cpm_tube_build(None, 3, 0.1, ctypes.byref(h))
     assert rc == -1
     assert b"invalid" in L.cpm_last_error()
+
+
+def test_new_entry_points_reject_invalid_arguments_on_the_host():
+    """cpm_closest_points and cpm_geodesic_nearest_* validate their arguments before any
+    device work (status -1, CPM_ERR_INVALID_ARG)."""
+    sys.path.insert(0, os.path.join(ROOT, "cpm-ibc_gb300", "python"))
+    import cpm_gb300
+
+    L = cpm_gb300.lib()
+    vp = ctypes.c_void_p
+    L.cpm_closest_points.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_double, vp, vp]
+    L.cpm_geodesic_nearest_create.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, vp]
+    L.cpm_geodesic_nearest_run.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, vp, vp]
+    x = (ctypes.c_double * 3)()
+    out = (ctypes.c_double * 3)()
+    d = cpm_gb300.desc(cpm_gb300.SPHERE, [1.0])
+    assert L.cpm_closest_points(None, 1, x, 0.0, out, out) == -1
+    assert L.cpm_closest_points(ctypes.byref(d), -1, x, 0.0, out, out) == -1
+    assert L.cpm_closest_points(ctypes.byref(d), 1, None, 0.0, out, out) == -1
+    assert L.cpm_closest_points(ctypes.byref(d), 0, None, 0.0, None, None) == 0  # nothing to do
+    h = vp()
+    assert L.cpm_geodesic_nearest_create(None, 0, None, 0, None, None, ctypes.byref(h)) == -1
+    assert L.cpm_geodesic_nearest_run(None, 0.01, 0, 1e-10, 0, out, None) == -1
+    assert b"invalid" in L.cpm_last_error()
