@@ -380,6 +380,12 @@ int cpmref_heat_nearest(void *hp, int64_t n_ibc, const int64_t *ibc_idx, int64_t
     GUARD_END
 }
 
+// Row loops of the sparse products on OpenMP threads (1) or serial (0, the default).
+int cpmref_set_parallel_rows(int32_t on) {
+    ParallelRows() = on != 0;
+    return 0;
+}
+
 // Closest point of an arbitrary point set to a surface (CP-accuracy tests).
 int cpmref_closest_points(const cpmref_surface_desc *surf, int64_t n, const double *x, double *cp, double *dist) {
     GUARD_BEGIN

@@ -29,7 +29,9 @@ void GeneralizedSystem::SetComponents(double m_in, double n_in, const SpMat &L_i
 // identity rows copy x; other rows sum val*x[col] in ascending column order.
 void GeneralizedSystem::Interp(const std::vector<double> &x, std::vector<double> &t) const {
     t.assign(dofs + nD, 0.0);
-    for (size_t k = 0; k < E.rows; ++k) {
+#pragma omp parallel for schedule(static) if (ParallelRows())
+    for (long long kk = 0; kk < (long long)E.rows; ++kk) {
+        const size_t k = (size_t)kk;
         if (identity_rows[k]) {
             t[k] = x[k];
         } else {
@@ -47,7 +49,9 @@ void GeneralizedSystem::Multiply(const std::vector<double> &x, std::vector<doubl
     Interp(x, t);
     result.assign(x.size(), 0.0);
     // LnodiagTimesX (:93-115)
-    for (size_t k = 0; k < L.rows; ++k) {
+#pragma omp parallel for schedule(static) if (ParallelRows())
+    for (long long kk = 0; kk < (long long)L.rows; ++kk) {
+        const size_t k = (size_t)kk;
         double acc = 0.0;
         for (size_t e = L.ptr[k]; e < L.ptr[k + 1]; ++e)
             if (L.idx[e] != k) acc += L.val[e] * t[L.idx[e]];

@@ -6,7 +6,8 @@
 //   BiCGStabVector ops          src/BiCGStabVector.h:23-72 (OpenMP-parallel, as in the reference)
 //   Solver Init/Solve/Multiply  src/Solver.cpp:8-138
 // The sparse products run serially (the reference's OPENMP macro is never
-// defined); vector updates run OpenMP-parallel; dot products are serial sums
+// defined; tests may put their rows on OpenMP threads, ParallelRows() in
+// sparse.h, which changes no result); vector updates run OpenMP-parallel; dot products are serial sums
 // (the reference uses Eigen's dot, whose vectorised summation order is not
 // pinned by any version in the reference tree).
 #pragma once

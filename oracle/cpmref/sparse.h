@@ -20,6 +20,14 @@ struct Triplet {
     double val;
 };
 
+// Row loops of the sparse products run serially, as the reference's do (its OPENMP macro
+// is never defined); tests may run them on OpenMP threads, which changes no result (each
+// row is summed by one thread in its own order).  The CPU baseline keeps them serial.
+inline bool &ParallelRows() {
+    static bool on = false;
+    return on;
+}
+
 struct SpMat {
     size_t rows = 0, cols = 0;
     std::vector<size_t> ptr{0};
@@ -82,10 +90,13 @@ struct SpMat {
         return 0.0;
     }
 
-    // y = A x, each row summed from 0 in ascending column order.
+    // y = A x, each row summed from 0 in ascending column order (rows on OpenMP threads
+    // when ParallelRows() is set: every row's sum is unchanged).
     void Multiply(const std::vector<double> &x, std::vector<double> &y) const {
         y.assign(rows, 0.0);
-        for (size_t i = 0; i < rows; ++i) {
+#pragma omp parallel for schedule(static) if (ParallelRows())
+        for (long long ii = 0; ii < (long long)rows; ++ii) {
+            const size_t i = (size_t)ii;
             double s = 0.0;
             for (size_t k = ptr[i]; k < ptr[i + 1]; ++k) s += val[k] * x[idx[k]];
             y[i] = s;

@@ -130,6 +130,7 @@ def lib():
             L.cpmref_geodesic.argtypes = [vp, ctypes.c_double, ctypes.c_int32, vp, vp]
             L.cpmref_geodesic_nearest.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, ctypes.c_double,
                                                   ctypes.c_int32, vp, vp]
+            L.cpmref_set_parallel_rows.argtypes = [ctypes.c_int32]
             L.cpmref_heat_nearest.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, ctypes.c_double,
                                               ctypes.c_int32, vp]
             L.cpmref_closest_points.argtypes = [P(SurfaceDesc), ctypes.c_int64, vp, vp, vp]
@@ -301,6 +302,12 @@ def csr_matvec(ptr, idx, val, x):
     rows = len(ptr) - 1
     r = np.repeat(np.arange(rows), np.diff(ptr))
     return np.bincount(r, weights=val * x[idx], minlength=rows)
+
+
+def set_parallel_rows(on):
+    """Row loops of the oracle's sparse products on OpenMP threads (results unchanged;
+    the default, serial, is what the CPU baseline times)."""
+    lib().cpmref_set_parallel_rows(1 if on else 0)
 
 
 def closest_points(surface, x):

@@ -6,8 +6,10 @@ following the reference's convergence-study drivers:
   PoissonSphereCircleIBC   convergence_studies/PoissonProblemsWithIBC/PoissonProblemsWithIBC.cpp:230-272
   PoissonSpherePointIBC    convergence_studies/PoissonProblemsWithIBC/PoissonProblemsWithIBC.cpp:274-317
   ComputeCircle3DParams    convergence_studies/PoissonProblemsWithIBC/PoissonProblemsWithIBC.cpp:117-139
+  HeatSphereCircleIBC      convergence_studies/HeatProblemsWithIBC/HeatProblemsWithIBC.cpp:68-139,141-283
 Golden average orders (the reference's own pass/fail pins, +-1e-2):
-  PoissonProblems.cpp:169 and PoissonProblemsWithIBC.cpp:375-379.
+  PoissonProblems.cpp:169, PoissonProblemsWithIBC.cpp:375-379 and
+  HeatProblemsWithIBC.cpp:307 (Dirichlet, boundary order 2).
 """
 import math
 
@@ -64,6 +66,61 @@ def sphere_point_ibc(dx, i):
     ibc = ol.point_desc(p, dx, boundary_order=2)
     return dict(surface=ol.sphere_desc(), ibcs=[ibc], m=0.0, n=-1.0, f=lambda x: 30.0 * sphere_harmonic(x),
                 g=lambda c, x: sphere_harmonic(x), exact=sphere_harmonic)
+
+
+# HeatProblemsWithIBC.cpp:307, problems 3-5 (the sphere): explicit, backward Euler, Crank-Nicolson
+GOLDEN_HEAT_SPHERE_CIRCLE = [1.98885, 1.15183, 2.01012]
+DX_HEAT_3D = [0.1, 0.05, 0.025]  # Helpers::ConvergenceStudy(0.1, 3, ...) (HeatProblemsWithIBC.cpp:367)
+HEAT_FINAL_TIME = 0.1  # g_final_time (HeatProblemsWithIBC.cpp:19)
+
+
+def heat_circle_params():
+    """ComputeCircle3DParams (HeatProblemsWithIBC.cpp:68-86) for the plane of SphereCircleIBC
+    (:96-100): normal (1.1, 1.234, 1.321), point r = 0.27, theta = 0.132, phi = 0.221."""
+    n = np.array([1.1, 1.234, 1.321])
+    n = n / math.sqrt(float(np.dot(n, n)))
+    r, th, ph = 0.27, 0.132, 0.221
+    pop = np.array([r * math.cos(ph) * math.sin(th), r * math.sin(ph) * math.sin(th), r * math.cos(th)])
+    rho = -float(np.dot(pop, n))
+    return math.sqrt(1 - rho * rho), rho * n, n
+
+
+def heat_sphere_circle_error(dx, method):
+    """SphereCircleIBC (HeatProblemsWithIBC.cpp:88-283) through the oracle: u = cos(phi) = z on
+    the unit sphere decays as exp(-2t); Dirichlet circle, boundary order 2; method 0 explicit
+    (dt = 0.1 dx^2), 1 backward Euler, 2 Crank-Nicolson (dt = 0.1 dx), both adjusted to an
+    integer number of steps to t = 0.1 (:118-129); HeatWithIBC::TimeStep and SetDirichletValue
+    (problems/HeatWithIBC.cpp:50-100).  Returns the l_inf error at the plot points (:24-40)."""
+    R, c, n = heat_circle_params()
+    P = ol.RefProblem(ol.sphere_desc(), [ol.circle3d_desc(R, c, n, dx, boundary_order=2)], 3, dx)
+    rows = P.rows()
+    T = HEAT_FINAL_TIME
+    dt = 0.1 * dx if method > 0 else 0.1 * dx * dx
+    steps = math.ceil(T / dt)
+    dt = T / steps
+    f = lambda x: x[:, 2]
+    u = f(rows["point"])
+    dirichlet = rows["kind"] == 2
+    fd = f(rows["point"][dirichlet])
+    if method == 0:
+        import scipy.sparse as sp
+
+        Lf = sp.csr_matrix(tuple(reversed(P.csr(0))), shape=(P.D, P.D))
+        Ef = sp.csr_matrix(tuple(reversed(P.csr(1))), shape=(P.D, P.D))
+    for k in range(steps):
+        t = (k + 1) * dt
+        if method == 0:
+            u = Ef @ (u + dt * (Lf @ u))
+            u[dirichlet] = math.exp(-2 * t) * fd
+        else:
+            if method == 2:
+                u = P.apply(1.0, 0.5 * dt, u)
+            u = np.array(u, copy=True)
+            u[dirichlet] = math.exp(-2 * t) * fd
+            u, _ = P.solve(1.0, -(1.0 if method == 1 else 0.5) * dt, u)
+    ptr, idx, val = P.csr(4)
+    up = ol.csr_matvec(ptr, idx, val, u)
+    return float(np.max(np.abs(up - math.exp(-2 * T) * f(P.xp()))))
 
 
 def build_rhs(rows, f, g):

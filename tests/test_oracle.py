@@ -124,3 +124,21 @@ def test_bicgstab_solution_matches_sparse_lu(oracle, case):
     x_lu = spla.spsolve(A.tocsc(), b)
     x, st = P.solve(m, n, b)
     assert np.max(np.abs(x - x_lu)) <= 1e-8 * np.max(np.abs(x_lu))
+
+
+@pytest.mark.parametrize("method", [0, 1, 2])
+def test_heat_sphere_circle_golden_order(oracle, method):
+    """HeatProblemsWithIBC's sphere-circle study (explicit, backward Euler, Crank-Nicolson
+    time stepping with a 2nd-order Dirichlet circle) through the oracle: the average
+    convergence order over dx = 0.1, 0.05, 0.025 equals the reference's golden value
+    within 1e-2 (HeatProblemsWithIBC.cpp:307, :372).  The oracle's sparse rows run on
+    OpenMP threads here, which changes no result."""
+    if method == 0:
+        pytest.importorskip("scipy.sparse")
+    oracle.set_parallel_rows(True)
+    try:
+        errs = [S.heat_sphere_circle_error(dx, method) for dx in S.DX_HEAT_3D]
+    finally:
+        oracle.set_parallel_rows(False)
+    avg, _ = S.convergence_order(errs, S.DX_HEAT_3D)
+    assert abs(avg - S.GOLDEN_HEAT_SPHERE_CIRCLE[method]) < 1e-2
