@@ -7,9 +7,10 @@ following the reference's convergence-study drivers:
   PoissonSpherePointIBC    convergence_studies/PoissonProblemsWithIBC/PoissonProblemsWithIBC.cpp:274-317
   ComputeCircle3DParams    convergence_studies/PoissonProblemsWithIBC/PoissonProblemsWithIBC.cpp:117-139
   HeatSphereCircleIBC      convergence_studies/HeatProblemsWithIBC/HeatProblemsWithIBC.cpp:68-139,141-283
+  HeatSphere               convergence_studies/HeatProblems/HeatProblems.cpp:125-145
 Golden average orders (the reference's own pass/fail pins, +-1e-2):
   PoissonProblems.cpp:169, PoissonProblemsWithIBC.cpp:375-379 and
-  HeatProblemsWithIBC.cpp:307 (Dirichlet, boundary order 2).
+  HeatProblemsWithIBC.cpp:307 (Dirichlet, boundary order 2) and HeatProblems.cpp:156-158.
 """
 import math
 
@@ -121,6 +122,36 @@ def heat_sphere_circle_error(dx, method):
     ptr, idx, val = P.csr(4)
     up = ol.csr_matvec(ptr, idx, val, u)
     return float(np.max(np.abs(up - math.exp(-2 * T) * f(P.xp()))))
+
+
+# HeatProblems.cpp:156-158, problem 3 (the sphere): explicit, implicit Euler
+GOLDEN_HEAT_SPHERE = {False: 2.39477, True: 2.08643}
+
+
+def heat_sphere_error(dx, implicit):
+    """Sphere (convergence_studies/HeatProblems/HeatProblems.cpp:125-145) through the oracle:
+    u = cos(phi) = z decays as exp(-2t) to t = 0.1 with dt = 0.2 dx^2 adjusted to an integer
+    number of steps (problems/Heat.cpp:118-120); Heat::TimeStep (:77-92) explicit
+    u = E (u + dt L u) or implicit Euler Solve(1, -dt); l_inf error at the plot points (:54-77)."""
+    P = ol.RefProblem(ol.sphere_desc(), [], 3, dx)
+    T = 0.1
+    dt = 0.2 * dx * dx
+    steps = math.ceil(T / dt)
+    dt = T / steps
+    u = P.rows()["point"][:, 2].copy()
+    if not implicit:
+        import scipy.sparse as sp
+
+        Lm = sp.csr_matrix(tuple(reversed(P.csr(2))), shape=(P.N, P.N))
+        Em = sp.csr_matrix(tuple(reversed(P.csr(3))), shape=(P.N, P.N))
+    for _ in range(steps):
+        if implicit:
+            u, _ = P.solve(1.0, -dt, u)
+        else:
+            u = Em @ (u + dt * (Lm @ u))
+    ptr, idx, val = P.csr(4)
+    up = ol.csr_matvec(ptr, idx, val, u)
+    return float(np.max(np.abs(up - math.exp(-2 * T) * P.xp()[:, 2])))
 
 
 def build_rhs(rows, f, g):

@@ -142,3 +142,19 @@ def test_heat_sphere_circle_golden_order(oracle, method):
         oracle.set_parallel_rows(False)
     avg, _ = S.convergence_order(errs, S.DX_HEAT_3D)
     assert abs(avg - S.GOLDEN_HEAT_SPHERE_CIRCLE[method]) < 1e-2
+
+
+@pytest.mark.parametrize("implicit", [False, True])
+def test_heat_sphere_golden_order(oracle, implicit):
+    """HeatProblems' sphere study (Heat::TimeStep, explicit or implicit Euler) through the
+    oracle: the average order over dx = 0.2, 0.1, 0.05 equals the reference's golden value
+    within 1e-2 (HeatProblems.cpp:156-158, :206)."""
+    if not implicit:
+        pytest.importorskip("scipy.sparse")
+    oracle.set_parallel_rows(True)
+    try:
+        errs = [S.heat_sphere_error(dx, implicit) for dx in S.DX_3D]
+    finally:
+        oracle.set_parallel_rows(False)
+    avg, _ = S.convergence_order(errs, S.DX_3D)
+    assert abs(avg - S.GOLDEN_HEAT_SPHERE[implicit]) < 1e-2
