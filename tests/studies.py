@@ -8,9 +8,12 @@ following the reference's convergence-study drivers:
   ComputeCircle3DParams    convergence_studies/PoissonProblemsWithIBC/PoissonProblemsWithIBC.cpp:117-139
   HeatSphereCircleIBC      convergence_studies/HeatProblemsWithIBC/HeatProblemsWithIBC.cpp:68-139,141-283
   HeatSphere               convergence_studies/HeatProblems/HeatProblems.cpp:125-145
+  nearest-node baselines   PoissonProblemsWithIBC.cpp:230-317 (ibc_type 1, 2) with
+                           problems/PoissonWithIBCNearest.cpp:5-89
 Golden average orders (the reference's own pass/fail pins, +-1e-2):
   PoissonProblems.cpp:169, PoissonProblemsWithIBC.cpp:375-379 and
-  HeatProblemsWithIBC.cpp:307 (Dirichlet, boundary order 2) and HeatProblems.cpp:156-158.
+  HeatProblemsWithIBC.cpp:307 (Dirichlet, boundary order 2), HeatProblems.cpp:156-158 and
+  PoissonProblemsWithIBC.cpp:383-386 (nearest-node baselines).
 """
 import math
 
@@ -57,7 +60,8 @@ def sphere_circle_ibc(dx, i):
     R, centre, normal = circle3d_params([RAND_NUM[i], RAND_NUM2[i], RAND_NUM3[i]])
     ibc = ol.circle3d_desc(R, centre, normal, dx, boundary_order=2)
     return dict(surface=ol.sphere_desc(), ibcs=[ibc], m=0.0, n=-1.0, f=lambda x: 30.0 * sphere_harmonic(x),
-                g=lambda c, x: sphere_harmonic(x), exact=sphere_harmonic)
+                g=lambda c, x: sphere_harmonic(x), exact=sphere_harmonic,
+                ibc_xp=circle3d_plot_points(R, centre, normal))
 
 
 def sphere_point_ibc(dx, i):
@@ -66,7 +70,7 @@ def sphere_point_ibc(dx, i):
     p = [math.cos(ph) * math.cos(th), math.cos(ph) * math.sin(th), math.sin(ph)]
     ibc = ol.point_desc(p, dx, boundary_order=2)
     return dict(surface=ol.sphere_desc(), ibcs=[ibc], m=0.0, n=-1.0, f=lambda x: 30.0 * sphere_harmonic(x),
-                g=lambda c, x: sphere_harmonic(x), exact=sphere_harmonic)
+                g=lambda c, x: sphere_harmonic(x), exact=sphere_harmonic, ibc_xp=np.array([p]))
 
 
 # HeatProblemsWithIBC.cpp:307, problems 3-5 (the sphere): explicit, backward Euler, Crank-Nicolson
@@ -152,6 +156,87 @@ def heat_sphere_error(dx, implicit):
     ptr, idx, val = P.csr(4)
     up = ol.csr_matvec(ptr, idx, val, u)
     return float(np.max(np.abs(up - math.exp(-2 * T) * P.xp()[:, 2])))
+
+
+# PoissonProblemsWithIBC.cpp:383-386: problems 3 / 6 (freeze_nearest) and 4 / 7 (DOF-subset nodes)
+GOLDEN_SPHERE_CIRCLE_NEAREST = {True: [0.945984, 0.82667, 0.98775, 0.703821, 1.18035, 1.12101, 0.867009, 1.09471,
+                                       0.962311, 0.786675],
+                                False: [0.626507, 0.64894, 0.659936, 0.804202, 0.608543, 0.790434, 0.892918, 0.639867,
+                                        0.666589, 0.727743]}
+GOLDEN_SPHERE_POINT_NEAREST = {True: [2.15041, 2.23765, 0.959175, 0.911574, 1.21328, 2.55332, 1.55977, 1.03094, 1.15633,
+                                      1.03559],
+                               False: [2.15603, 1.17371, 0.763936, 0.639966, 0.838463, 0.896607, 0.640536, 0.59289,
+                                       0.304371, 1.15492]}
+
+
+def circle3d_plot_points(R, centre, normal, n_points=100):
+    """Surface::paramCircle3D (src/Surface.cpp:1881-1904) with ComputeOrthogonalBasis (:442-460)."""
+    nrm = np.asarray(normal, np.float64)
+    if abs(nrm[0]) > abs(nrm[1]):
+        t1 = np.array([-nrm[2], 0.0, nrm[0]])
+    else:
+        t1 = np.array([0.0, nrm[2], -nrm[1]])
+    t2 = np.cross(nrm, t1)
+    t1 = t1 / math.sqrt(float(np.dot(t1, t1)))
+    t2 = t2 / math.sqrt(float(np.dot(t2, t2)))
+    th = np.arange(n_points) * (2 * math.pi / (n_points - 1))
+    return np.asarray(centre)[None, :] + R * (np.cos(th)[:, None] * t1[None, :] + np.sin(th)[:, None] * t2[None, :])
+
+
+def nearest_baseline_error(spec, dx, freeze):
+    """PoissonWithIBCNearest (problems/PoissonWithIBCNearest.cpp:5-89) on a convergence-study
+    problem: identity rows at Tube::NearestTubeIndex of the IBC's plot points (freeze_nearest) or at the
+    IBC DOF subset's nodes, holding the exact solution there; f at the closest points
+    elsewhere; error at the plot points through the plain plot interpolation.  Solved
+    matrix-free by scipy's BiCGStab to relative residual 1e-10 with the reference's diagonal
+    preconditioner m + n L_qq (src/GeneralizedBiCGStabSystem.h:281-340)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+
+    P = ol.RefProblem(spec["surface"], spec["ibcs"], 3, dx)
+    P0 = ol.RefProblem(spec["surface"], [], 3, dx)
+    t = P0.tube()
+    N = P0.N
+    exact = spec["exact"]
+    if freeze:
+        pts = spec["ibc_xp"]
+        key = np.round((pts - P0.xstart) / dx).astype(np.int64)
+        rec = (key[:, 0] * P0.N1d + key[:, 1]) * P0.N1d + key[:, 2]
+        order = np.argsort(t["rec"])
+        pos = np.searchsorted(t["rec"][order], rec)
+        idx = order[pos]
+        assert np.array_equal(t["rec"][idx], rec)
+        vals = exact(pts)
+    else:
+        sub = P.ibc_subsets(0)
+        idx, vals = sub["dof_set"], exact(sub["dof_cp"])
+    b = spec["f"](t["cp"])
+    b[idx] = vals
+    Lm = sp.csr_matrix(tuple(reversed(P0.csr(2))), shape=(N, N))
+    Em = sp.csr_matrix(tuple(reversed(P0.csr(3))), shape=(N, N)).tolil()
+    ident = np.unique(idx)
+    for k in ident:
+        Em.rows[k] = [int(k)]
+        Em.data[k] = [1.0]
+    Em = Em.tocsr()
+    ld = Lm.diagonal()
+    Loff = (Lm - sp.diags(ld)).tocsr()
+    m, n = spec["m"], spec["n"]
+    is_id = np.zeros(N, bool)
+    is_id[ident] = True
+
+    def mv(x):  # GeneralizedBiCGStabSystem::Multiply (src/GeneralizedBiCGStabSystem.h:191-233)
+        y = m * x + n * (ld * x + Loff @ (Em @ x))
+        y[is_id] = x[is_id]
+        return y
+
+    d = np.where(is_id, 1.0, m + n * ld)
+    A = spla.LinearOperator((N, N), matvec=mv, dtype=np.float64)
+    M = spla.LinearOperator((N, N), matvec=lambda r: r / d, dtype=np.float64)
+    u, info = spla.bicgstab(A, b, rtol=1e-10, atol=0.0, maxiter=100000, M=M)
+    assert info == 0
+    ptr, pidx, pval = P0.csr(4)
+    return float(np.max(np.abs(ol.csr_matvec(ptr, pidx, pval, u) - exact(P0.xp()))))
 
 
 def build_rhs(rows, f, g):

@@ -158,3 +158,19 @@ def test_heat_sphere_golden_order(oracle, implicit):
         oracle.set_parallel_rows(False)
     avg, _ = S.convergence_order(errs, S.DX_3D)
     assert abs(avg - S.GOLDEN_HEAT_SPHERE[implicit]) < 1e-2
+
+
+@pytest.mark.parametrize("kind", ["circle", "point"])
+@pytest.mark.parametrize("freeze", [True, False])
+@pytest.mark.parametrize("i", [0, 1])
+def test_nearest_baseline_golden_order(oracle, kind, freeze, i):
+    """PoissonWithIBCNearest in the reference's IBC study (problems 3, 4, 6, 7 of
+    PoissonProblemsWithIBC.cpp:453-469): identity rows at the nodes nearest the IBC's plot
+    points (freeze_nearest) or at its DOF subset's nodes, on the oracle's tube, L and E.
+    The average order over dx = 0.2, 0.1, 0.05 equals the golden value within 1e-2
+    (:383-386)."""
+    pytest.importorskip("scipy.sparse.linalg")
+    build = S.sphere_circle_ibc if kind == "circle" else S.sphere_point_ibc
+    errs = [S.nearest_baseline_error(build(dx, i), dx, freeze) for dx in S.DX_3D]
+    golden = (S.GOLDEN_SPHERE_CIRCLE_NEAREST if kind == "circle" else S.GOLDEN_SPHERE_POINT_NEAREST)[freeze][i]
+    assert abs(S.convergence_order(errs, S.DX_3D)[0] - golden) < 1e-2
