@@ -25,6 +25,10 @@ GOLDEN_SHIFTED_POISSON_SPHERE = 2.18548
 # order-2 lists, PoissonProblemsWithIBC.cpp:377-378
 GOLDEN_SPHERE_CIRCLE = [2.03624, 2.20571, 2.09173, 2.0828, 2.1572, 2.10696, 1.97858, 1.97003, 2.17008, 1.9772]
 GOLDEN_SPHERE_POINT = [2.16283, 2.13198, 1.92074, 2.22093, 2.27176, 2.36021, 1.89006, 2.12619, 2.22663, 2.70325]
+# order-1 lists, PoissonProblemsWithIBC.cpp:369-370
+GOLDEN_SPHERE_CIRCLE_ORDER1 = [0.954594, 0.990541, 1.07685, 0.865972, 0.784669, 0.922806, 0.991011, 0.987983, 0.90721,
+                               0.956464]
+GOLDEN_SPHERE_POINT_ORDER1 = [2.42046, 2.03873, 1.03422, 0.973755, 1.54908, 2.12488, 2.12239, 1.02281, 1.05949, 1.37816]
 # PoissonProblemsWithIBC.cpp:399-424
 RAND_NUM = [0.0, 0.170, 0.297, 0.331, 0.481, 0.511, 0.631, 0.735, 0.813, 0.973]
 RAND_NUM2 = [0.25, 0.874, 0.473, 0.973, 0.812, 0.693, 0.873, 0.912, 0.945, 1.0]
@@ -56,19 +60,19 @@ def shifted_poisson_sphere(dx):
                 exact=sphere_harmonic)
 
 
-def sphere_circle_ibc(dx, i):
+def sphere_circle_ibc(dx, i, order=2):
     R, centre, normal = circle3d_params([RAND_NUM[i], RAND_NUM2[i], RAND_NUM3[i]])
-    ibc = ol.circle3d_desc(R, centre, normal, dx, boundary_order=2)
+    ibc = ol.circle3d_desc(R, centre, normal, dx, boundary_order=order)
     return dict(surface=ol.sphere_desc(), ibcs=[ibc], m=0.0, n=-1.0, f=lambda x: 30.0 * sphere_harmonic(x),
                 g=lambda c, x: sphere_harmonic(x), exact=sphere_harmonic,
                 ibc_xp=circle3d_plot_points(R, centre, normal))
 
 
-def sphere_point_ibc(dx, i):
+def sphere_point_ibc(dx, i, order=2):
     th = 2.0 * math.pi * RAND_NUM[i] - math.pi
     ph = 2.0 * math.pi * RAND_NUM2[i] - math.pi
     p = [math.cos(ph) * math.cos(th), math.cos(ph) * math.sin(th), math.sin(ph)]
-    ibc = ol.point_desc(p, dx, boundary_order=2)
+    ibc = ol.point_desc(p, dx, boundary_order=order)
     return dict(surface=ol.sphere_desc(), ibcs=[ibc], m=0.0, n=-1.0, f=lambda x: 30.0 * sphere_harmonic(x),
                 g=lambda c, x: sphere_harmonic(x), exact=sphere_harmonic, ibc_xp=np.array([p]))
 

@@ -174,3 +174,19 @@ def test_nearest_baseline_golden_order(oracle, kind, freeze, i):
     errs = [S.nearest_baseline_error(build(dx, i), dx, freeze) for dx in S.DX_3D]
     golden = (S.GOLDEN_SPHERE_CIRCLE_NEAREST if kind == "circle" else S.GOLDEN_SPHERE_POINT_NEAREST)[freeze][i]
     assert abs(S.convergence_order(errs, S.DX_3D)[0] - golden) < 1e-2
+
+
+@pytest.mark.parametrize("kind", ["circle", "point"])
+@pytest.mark.parametrize("i", [0, 1])
+def test_order1_ibc_golden_order(oracle, kind, i):
+    """First-order Dirichlet IBCs (boundary_order 1) in the reference's IBC study: the
+    average order over dx = 0.2, 0.1, 0.05 equals the golden value within 1e-2
+    (PoissonProblemsWithIBC.cpp:369-370)."""
+    build = S.sphere_circle_ibc if kind == "circle" else S.sphere_point_ibc
+    oracle.set_parallel_rows(True)
+    try:
+        errs = [S.oracle_error(build(dx, i, order=1), dx)[0] for dx in S.DX_3D]
+    finally:
+        oracle.set_parallel_rows(False)
+    golden = (S.GOLDEN_SPHERE_CIRCLE_ORDER1 if kind == "circle" else S.GOLDEN_SPHERE_POINT_ORDER1)[i]
+    assert abs(S.convergence_order(errs, S.DX_3D)[0] - golden) < 1e-2
