@@ -19,6 +19,9 @@ def oracle():
     import oracle_lib
 
     oracle_lib.build()
+    # the oracle's sparse rows on OpenMP threads: no result changes (each row keeps its
+    # own summation order); bench.py's CPU baseline keeps them serial
+    oracle_lib.set_parallel_rows(True)
     return oracle_lib
 
 

@@ -131,15 +131,10 @@ def test_heat_sphere_circle_golden_order(oracle, method):
     """HeatProblemsWithIBC's sphere-circle study (explicit, backward Euler, Crank-Nicolson
     time stepping with a 2nd-order Dirichlet circle) through the oracle: the average
     convergence order over dx = 0.1, 0.05, 0.025 equals the reference's golden value
-    within 1e-2 (HeatProblemsWithIBC.cpp:307, :372).  The oracle's sparse rows run on
-    OpenMP threads here, which changes no result."""
+    within 1e-2 (HeatProblemsWithIBC.cpp:307, :372)."""
     if method == 0:
         pytest.importorskip("scipy.sparse")
-    oracle.set_parallel_rows(True)
-    try:
-        errs = [S.heat_sphere_circle_error(dx, method) for dx in S.DX_HEAT_3D]
-    finally:
-        oracle.set_parallel_rows(False)
+    errs = [S.heat_sphere_circle_error(dx, method) for dx in S.DX_HEAT_3D]
     avg, _ = S.convergence_order(errs, S.DX_HEAT_3D)
     assert abs(avg - S.GOLDEN_HEAT_SPHERE_CIRCLE[method]) < 1e-2
 
@@ -151,11 +146,7 @@ def test_heat_sphere_golden_order(oracle, implicit):
     within 1e-2 (HeatProblems.cpp:156-158, :206)."""
     if not implicit:
         pytest.importorskip("scipy.sparse")
-    oracle.set_parallel_rows(True)
-    try:
-        errs = [S.heat_sphere_error(dx, implicit) for dx in S.DX_3D]
-    finally:
-        oracle.set_parallel_rows(False)
+    errs = [S.heat_sphere_error(dx, implicit) for dx in S.DX_3D]
     avg, _ = S.convergence_order(errs, S.DX_3D)
     assert abs(avg - S.GOLDEN_HEAT_SPHERE[implicit]) < 1e-2
 
@@ -183,10 +174,6 @@ def test_order1_ibc_golden_order(oracle, kind, i):
     average order over dx = 0.2, 0.1, 0.05 equals the golden value within 1e-2
     (PoissonProblemsWithIBC.cpp:369-370)."""
     build = S.sphere_circle_ibc if kind == "circle" else S.sphere_point_ibc
-    oracle.set_parallel_rows(True)
-    try:
-        errs = [S.oracle_error(build(dx, i, order=1), dx)[0] for dx in S.DX_3D]
-    finally:
-        oracle.set_parallel_rows(False)
+    errs = [S.oracle_error(build(dx, i, order=1), dx)[0] for dx in S.DX_3D]
     golden = (S.GOLDEN_SPHERE_CIRCLE_ORDER1 if kind == "circle" else S.GOLDEN_SPHERE_POINT_ORDER1)[i]
     assert abs(S.convergence_order(errs, S.DX_3D)[0] - golden) < 1e-2
