@@ -79,13 +79,19 @@ def sphere_point_ibc(dx, i, order=2):
 
 # HeatProblemsWithIBC.cpp:307, problems 3-5 (the sphere): explicit, backward Euler, Crank-Nicolson
 GOLDEN_HEAT_SPHERE_CIRCLE = [1.98885, 1.15183, 2.01012]
+GOLDEN_HEAT_SPHERE_CIRCLE_NEUMANN = [2.07915, 1.15527, 2.04239]  # :318
 DX_HEAT_3D = [0.1, 0.05, 0.025]  # Helpers::ConvergenceStudy(0.1, 3, ...) (HeatProblemsWithIBC.cpp:367)
 HEAT_FINAL_TIME = 0.1  # g_final_time (HeatProblemsWithIBC.cpp:19)
 
 
-def heat_circle_params():
+def heat_circle_params(boundary_type=0):
     """ComputeCircle3DParams (HeatProblemsWithIBC.cpp:68-86) for the plane of SphereCircleIBC
-    (:96-100): normal (1.1, 1.234, 1.321), point r = 0.27, theta = 0.132, phi = 0.221."""
+    (:94-106): Dirichlet, normal (1.1, 1.234, 1.321) through the point r = 0.27, theta = 0.132,
+    phi = 0.221; Neumann, normal (0, 1, 0) through the origin."""
+    if boundary_type == 1:
+        n, pop = np.array([0.0, 1.0, 0.0]), np.zeros(3)
+        rho = -float(np.dot(pop, n))
+        return math.sqrt(1 - rho * rho), rho * n, n
     n = np.array([1.1, 1.234, 1.321])
     n = n / math.sqrt(float(np.dot(n, n)))
     r, th, ph = 0.27, 0.132, 0.221
@@ -94,14 +100,16 @@ def heat_circle_params():
     return math.sqrt(1 - rho * rho), rho * n, n
 
 
-def heat_sphere_circle_error(dx, method):
+def heat_sphere_circle_error(dx, method, boundary_type=0):
     """SphereCircleIBC (HeatProblemsWithIBC.cpp:88-283) through the oracle: u = cos(phi) = z on
     the unit sphere decays as exp(-2t); Dirichlet circle, boundary order 2; method 0 explicit
     (dt = 0.1 dx^2), 1 backward Euler, 2 Crank-Nicolson (dt = 0.1 dx), both adjusted to an
     integer number of steps to t = 0.1 (:118-129); HeatWithIBC::TimeStep and SetDirichletValue
     (problems/HeatWithIBC.cpp:50-100).  Returns the l_inf error at the plot points (:24-40)."""
-    R, c, n = heat_circle_params()
-    P = ol.RefProblem(ol.sphere_desc(), [ol.circle3d_desc(R, c, n, dx, boundary_order=2)], 3, dx)
+    R, c, n = heat_circle_params(boundary_type)
+    ibc = ol.circle3d_desc(R, c, n, dx, boundary_order=2)
+    ibc.boundary_type[0] = boundary_type
+    P = ol.RefProblem(ol.sphere_desc(), [ibc], 3, dx)
     rows = P.rows()
     T = HEAT_FINAL_TIME
     dt = 0.1 * dx if method > 0 else 0.1 * dx * dx

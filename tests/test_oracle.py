@@ -177,3 +177,12 @@ def test_order1_ibc_golden_order(oracle, kind, i):
     errs = [S.oracle_error(build(dx, i, order=1), dx)[0] for dx in S.DX_3D]
     golden = (S.GOLDEN_SPHERE_CIRCLE_ORDER1 if kind == "circle" else S.GOLDEN_SPHERE_POINT_ORDER1)[i]
     assert abs(S.convergence_order(errs, S.DX_3D)[0] - golden) < 1e-2
+
+
+def test_heat_sphere_circle_neumann_golden_order(oracle):
+    """The same heat study with a zero-Neumann great circle (boundary_type 1, order 2) and
+    backward Euler: average order within 1e-2 of the golden value
+    (HeatProblemsWithIBC.cpp:318), pinning the oracle's Neumann IBC rows."""
+    errs = [S.heat_sphere_circle_error(dx, 1, boundary_type=1) for dx in S.DX_HEAT_3D]
+    avg, _ = S.convergence_order(errs, S.DX_HEAT_3D)
+    assert abs(avg - S.GOLDEN_HEAT_SPHERE_CIRCLE_NEUMANN[1]) < 1e-2
