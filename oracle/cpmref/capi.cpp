@@ -242,6 +242,17 @@ int cpmref_csr_export(void *hp, int32_t which, int64_t *ptr, int64_t *idx, doubl
     return 0;
 }
 
+// y = A x for one of the exported matrices (rows summed in ascending column order)
+int cpmref_csr_multiply(void *hp, int32_t which, const double *x, double *y) {
+    GUARD_BEGIN
+    const SpMat &A = Pick((Handle *)hp, which);
+    std::vector<double> xv(x, x + A.cols), yv;
+    A.Multiply(xv, yv);
+    std::copy(yv.begin(), yv.end(), y);
+    return 0;
+    GUARD_END
+}
+
 int cpmref_rows_export(void *hp, uint8_t *identity, int32_t *kind, int32_t *ibc, double *point) {
     Problem &P = *((Handle *)hp)->prob;
     for (size_t r = 0; r < P.D(); ++r) {

@@ -131,6 +131,7 @@ def lib():
             L.cpmref_geodesic_nearest.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, ctypes.c_double,
                                                   ctypes.c_int32, vp, vp]
             L.cpmref_set_parallel_rows.argtypes = [ctypes.c_int32]
+            L.cpmref_csr_multiply.argtypes = [vp, ctypes.c_int32, vp, vp]
             L.cpmref_heat_nearest.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, ctypes.c_double,
                                               ctypes.c_int32, vp]
             L.cpmref_closest_points.argtypes = [P(SurfaceDesc), ctypes.c_int64, vp, vp, vp]
@@ -222,6 +223,14 @@ class RefProblem:
         val = np.zeros(nnz)
         L.cpmref_csr_export(self.h, which, _ptr(ptr), _ptr(idx), _ptr(val))
         return ptr, idx, val
+
+    def csr_multiply(self, which, x):
+        """y = A x for the exported matrix `which` (see csr), in the oracle."""
+        x = np.ascontiguousarray(x, np.float64)
+        rows = int(lib().cpmref_csr_rows(self.h, which))
+        y = np.zeros(rows)
+        _check(lib().cpmref_csr_multiply(self.h, which, _ptr(x), _ptr(y)))
+        return y
 
     def rows(self):
         D = self.D

@@ -119,15 +119,10 @@ def heat_sphere_circle_error(dx, method, boundary_type=0):
     u = f(rows["point"])
     dirichlet = rows["kind"] == 2
     fd = f(rows["point"][dirichlet])
-    if method == 0:
-        import scipy.sparse as sp
-
-        Lf = sp.csr_matrix(tuple(reversed(P.csr(0))), shape=(P.D, P.D))
-        Ef = sp.csr_matrix(tuple(reversed(P.csr(1))), shape=(P.D, P.D))
     for k in range(steps):
         t = (k + 1) * dt
         if method == 0:
-            u = Ef @ (u + dt * (Lf @ u))
+            u = P.csr_multiply(1, u + dt * P.csr_multiply(0, u))
             u[dirichlet] = math.exp(-2 * t) * fd
         else:
             if method == 2:

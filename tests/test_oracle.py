@@ -132,8 +132,6 @@ def test_heat_sphere_circle_golden_order(oracle, method):
     time stepping with a 2nd-order Dirichlet circle) through the oracle: the average
     convergence order over dx = 0.1, 0.05, 0.025 equals the reference's golden value
     within 1e-2 (HeatProblemsWithIBC.cpp:307, :372)."""
-    if method == 0:
-        pytest.importorskip("scipy.sparse")
     errs = [S.heat_sphere_circle_error(dx, method) for dx in S.DX_HEAT_3D]
     avg, _ = S.convergence_order(errs, S.DX_HEAT_3D)
     assert abs(avg - S.GOLDEN_HEAT_SPHERE_CIRCLE[method]) < 1e-2
