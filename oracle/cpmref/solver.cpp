@@ -59,12 +59,17 @@ void GeneralizedSystem::Multiply(const std::vector<double> &x, std::vector<doubl
     }
     // LdiagTimesX (:65-91)
     std::vector<double> tmp(dofs + nD, 0.0);
-    for (size_t k = 0; k < dofs; ++k)
+#pragma omp parallel for schedule(static) if (ParallelRows())
+    for (long long kk = 0; kk < (long long)dofs; ++kk) {
+        const size_t k = (size_t)kk;
         for (size_t e = L.ptr[k]; e < L.ptr[k + 1]; ++e)
             if (L.idx[e] == k) tmp[k] += L.val[e] * x[k];
+    }
     for (int i = 0; i < nD; ++i) tmp[dofs + i] = (m_in - n_in) * x[dofs + i];
     // FinalizeMultiplication (:166-189)
-    for (size_t q = 0; q < dofs; ++q) {
+#pragma omp parallel for schedule(static) if (ParallelRows())
+    for (long long qq = 0; qq < (long long)dofs; ++qq) {
+        const size_t q = (size_t)qq;
         if (identity_rows[q])
             result[q] = x[q];
         else
