@@ -42,6 +42,13 @@ def test_sphere_circle_ibc_golden_order_all(oracle, i):
     assert abs(S.convergence_order(errs, S.DX_3D)[0] - S.GOLDEN_SPHERE_CIRCLE[i]) < 1e-2
 
 
+@pytest.mark.slow
+@pytest.mark.parametrize("i", range(2, 10))
+def test_sphere_point_ibc_golden_order_all(oracle, i):
+    errs = [S.oracle_error(S.sphere_point_ibc(dx, i), dx)[0] for dx in S.DX_3D]
+    assert abs(S.convergence_order(errs, S.DX_3D)[0] - S.GOLDEN_SPHERE_POINT[i]) < 1e-2
+
+
 def test_interpolation_rows_sum_to_one(oracle):
     P = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1)
     ptr, idx, val = P.csr(3)
