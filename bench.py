@@ -158,65 +158,96 @@ def replicas_value(world, n_per_rank, t_max):
     return world * n_per_rank / t_max
 
 
-def cpu_baseline_sample(threads, tubes=None, iters_per_solve=None, x_check=None, vals=None):
-    """The oracle on the host: setup of the sphere with two circle IBCs at dx = 0.025, then a bounded BiCGStab sample (20 iterations)
-    scaled to solves/s by the iteration count of a full solve of the same system."""
+def cpu_model():
+    """the host CPU's model name (lscpu, else /proc/cpuinfo, else the platform string)"""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+EBCG_NOTE = "unavailable on this box (Eigen not installed, no network): the reference's Eigen BiCGSTAB path is not timed"
+
+
+def bench_config(D, N, ibc_dofs, world):
+    """the workload's config dict, shared by the GPU arm and the reference arm"""
+    return {"workload": WORKLOAD, "rows": int(D), "tube_nodes": int(N), "ibc_dofs": int(ibc_dofs), "tol": TOL,
+            "requests": "Laplace right-hand sides with circle values U[0,1] (seeded)",
+            "l2": "no flush: the solve's working set (the GPU arm's 10 FP32 + 4 FP64 [D][32] arrays, "
+                  f"{(10 * 4 + 4 * 8) * D * KSLOTS / 1e6:.0f} MB) exceeds the 129 MB L2",
+            "parallelism": f"replicas x{world}"}
+
+
+def oracle_c2():
+    """the oracle's C2 problem (the reference's custom-solver path restated on the host)"""
+    import oracle_lib as ol
+
+    ol.build()
+    return ol, ol.RefProblem(ol.sphere_desc(), circles(ol, DX), 3, DX)
+
+
+def timed_oracle_solve(P, b, threads, tol=TOL):
+    """one whole oracle BiCGStab solve of b on `threads` OpenMP threads: (x, stats)"""
     import oracle_lib as ol
 
     os.environ["OMP_NUM_THREADS"] = str(threads)
-    ol.build()
-    t0 = time.perf_counter()
-    P = ol.RefProblem(ol.sphere_desc(), circles(ol, DX), 3, DX)
-    setup_s = time.perf_counter() - t0
-    rows = P.rows()
-    b = rhs_from_rows(rows, vals if vals is not None else [1.0, 0.0])
-    sample_iters = 20
-    _, st = P.solve(0.0, -1.0, b, max_iters=sample_iters)
-    s_per_iter = st["seconds"] / max(1, st["iterations"])
-    out = dict(setup_s=setup_s, s_per_iter=s_per_iter, sample_iters=sample_iters, problem=P, rows=rows)
-    if iters_per_solve:
-        out["solves_per_s"] = 1.0 / (s_per_iter * iters_per_solve)
-    return out
+    ol.lib().cpmref_set_num_threads(int(threads))
+    x, st = P.solve(0.0, -1.0, b, tol=tol)
+    return x, st
 
 
 def run_reference(args):
-    # the host reference: rank 0 alone runs it (no process group needed); other ranks exit
+    """The reference arm: whole solves of the C2 system by the oracle (the C++17
+    restatement of the reference's custom BiCGStab path) on the host's cores,
+    one right-hand side per step, no extrapolation."""
+    # rank 0 alone runs it (no process group needed); other ranks exit
     world, rank, _ = ranks()
     if rank != 0:
         return
-    import oracle_lib as ol
-
     threads = os.cpu_count() or 1
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    ol.build()
-    P = ol.RefProblem(ol.sphere_desc(), circles(ol, DX), 3, DX)
+    t0 = time.perf_counter()
+    ol, P = oracle_c2()
+    setup_s = time.perf_counter() - t0
     rows = P.rows()
     rng = np.random.default_rng(1234)
-    # one full solve (warm-up) fixes the iteration count of the custom BiCGStab on this system
-    b = rhs_from_rows(rows, rng.uniform(0, 1, 2))
-    _, full = P.solve(0.0, -1.0, b)
-    iters_per_solve = max(1, full["iterations"])
-    for _ in range(max(0, args.warmup - 1)):
-        P.solve(0.0, -1.0, rhs_from_rows(rows, rng.uniform(0, 1, 2)), max_iters=20)
-    times = []
+    for _ in range(args.warmup):
+        timed_oracle_solve(P, rhs_from_rows(rows, rng.uniform(0, 1, 2)), threads)
+    times, iters = [], []
+    t_run = time.perf_counter()
     for _ in range(args.steps):
-        _, st = P.solve(0.0, -1.0, rhs_from_rows(rows, rng.uniform(0, 1, 2)), max_iters=20)
-        times.append(st["seconds"] / max(1, st["iterations"]) * iters_per_solve)
+        _, st = timed_oracle_solve(P, rhs_from_rows(rows, rng.uniform(0, 1, 2)), threads)
+        times.append(st["seconds"])
+        iters.append(st["iterations"])
+    wall = time.perf_counter() - t_run
     sec_per_solve = float(np.mean(times))
     v = 1.0 / sec_per_solve
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sec_per_solve * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "rows": P.D, "tube_nodes": P.N, "l2": "host run (no GPU)"},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"oracle (C++17 restatement of the reference custom BiCGStab, SpMV serial, vector ops "
-                                   f"OpenMP) on the two-circle sphere system: 1 full solve ({iters_per_solve} iterations) fixes the "
-                                   f"iteration count; each step times 20 iterations and scales to one solve"},
+        "config": bench_config(P.D, P.N, P.total_ibc_dofs, world),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+                         "sample": f"{args.steps} whole solves (tol {TOL}, x0 = 0, diagonal preconditioner) of the "
+                                   f"two-circle sphere system by the oracle (C++17 restatement of the reference's custom "
+                                   f"BiCGStab: SpMV serial, vector ops OpenMP), one right-hand side per step",
+                         "ebcg": EBCG_NOTE},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "latency_ms": {"p50": float(np.percentile(times, 50) * 1e3), "p99": float(np.percentile(times, 99) * 1e3)},
         "reference_note": "the reference (nathandking/cpm-ibc) needs Eigen3, fcpw and LBFGS++, absent here; "
                           "its custom solve path is timed through the oracle restatement",
-        "iterations_per_solve": iters_per_solve, "setup_s": P.setup_seconds,
+        "iterations_per_solve": int(np.median(iters)), "setup_s": setup_s, "timed_wall_s": wall,
     }
     print(json.dumps(line), flush=True)
 
@@ -548,16 +579,35 @@ def main():
     if os.path.exists(prof):
         traffic = json.load(open(prof)).get("bytes_per_apply")
 
-    # ---- CPU baseline (rank 0, N = 1 only)
-    cpu = None
+    # ---- CPU baseline and the error against the oracle (rank 0, N = 1 only): whole oracle solves
+    cpu, rel_err_oracle = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        its = int(np.median(plain_iters))
-        c = cpu_baseline_sample(threads, iters_per_solve=its)
-        cpu = {"value": c["solves_per_s"], "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"oracle sphere + two circle IBCs system (dx 0.025), 20 BiCGStab iterations timed ({c['s_per_iter'] * 1e3:.1f} ms/iteration) "
-                         f"x {its} iterations per solve (the plain FP64 GPU path's count, same algorithm); "
-                         f"setup {c['setup_s']:.1f} s not included"}
+        t0 = time.perf_counter()
+        ol, P = oracle_c2()
+        oracle_setup_s = time.perf_counter() - t0
+        prow = P.rows()
+        k0 = sel[0]
+        # the served solution of request k0 against the oracle's solve of the same system to tol 1e-12,
+        # compared on the tube rows (matched by grid index)
+        g_rec, r_rec = T.export()["rec"], P.tube()["rec"]
+        o = np.argsort(g_rec)
+        pos = np.searchsorted(g_rec[o], r_rec)
+        if P.N == O.N and np.array_equal(g_rec[o][pos], r_rec):
+            m = o[pos]
+            x_ref, _ = timed_oracle_solve(P, rhs_from_rows(prow, vals[k0]), threads, tol=1e-12)
+            xs0 = x_dev[k0].cpu().numpy()[m]
+            rel_err_oracle = float(np.max(np.abs(xs0 - x_ref[:P.N])) / np.max(np.abs(x_ref[:P.N])))
+        b_cpu = rhs_from_rows(prow, vals[sel[1]])
+        _, st_all = timed_oracle_solve(P, b_cpu, threads)
+        _, st_one = timed_oracle_solve(P, b_cpu, 1)
+        cpu = {"value": 1.0 / st_all["seconds"], "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+               "sample": f"one whole solve (tol {TOL}, {st_all['iterations']} iterations) of the two-circle sphere system "
+                         f"(dx 0.025) by the oracle on {threads} threads (SpMV serial, vector ops OpenMP, as the "
+                         f"reference runs); setup {oracle_setup_s:.1f} s not included",
+               "one_thread": {"value": 1.0 / st_one["seconds"], "unit": UNIT, "cores": 1,
+                              "iterations": st_one["iterations"]},
+               "ebcg": EBCG_NOTE}
 
     clocks = clk.summary()
     if rank == 0:
@@ -565,19 +615,17 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-inner/f64-refine", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "rows": D, "tube_nodes": O.N, "ibc_dofs": O.total_ibc_dofs,
-                       "slots": KSLOTS, "requests_per_step": KSLOTS, "tol": TOL,
-                       "refine_every": args.refine_every or 32, "inner_tol": args.inner_tol or 0.1,
-                       "serving": "continuous batching: every step's 32 requests submitted at t=0 with RHS resident "
-                                  "in HBM; slots refill as solves finish",
-                       "l2": "no flush: the served working set (10 FP32 + 4 FP64 [D][32] arrays, "
-                             f"{(10 * 4 + 4 * 8) * D * KSLOTS / 1e6:.0f} MB) exceeds the 129 MB L2",
-                       "parallelism": f"replicas x{world}"},
-            "latency_ms": {"p50": float(np.percentile(latency, 50) * 1e3), "p99": float(np.percentile(latency, 99) * 1e3),
-                           "service_p50": float(np.percentile(service, 50) * 1e3),
-                           "service_p99": float(np.percentile(service, 99) * 1e3),
-                           "note": "latency = submit to result with every request queued at t=0; service = admission "
-                                   "into a slot to result"},
+            "config": bench_config(D, O.N, O.total_ibc_dofs, world),
+            "serving": {"slots": KSLOTS, "requests_per_step": KSLOTS, "refine_every": args.refine_every or 32,
+                        "inner_tol": args.inner_tol or 0.1,
+                        "how": "continuous batching: every step's 32 requests submitted at once with their right-hand "
+                               "sides resident in HBM; slots refill as solves finish"},
+            "latency_ms": {"p50": float(np.percentile(service, 50) * 1e3), "p99": float(np.percentile(service, 99) * 1e3),
+                           "what": "admission into a slot to result (service time)"},
+            "queue_order_ms": {"p50": float(np.percentile(latency, 50) * 1e3),
+                               "p99": float(np.percentile(latency, 99) * 1e3),
+                               "what": "submit to result with all of a step's requests submitted at once: the order "
+                                       "in the queue, not a serving latency"},
             "fp64_plain": {"solves_per_s": plain_sps, "p50_ms": float(np.percentile(plain_t, 50) * 1e3),
                            "p99_ms": float(np.percentile(plain_t, 99) * 1e3),
                            "iterations": int(np.median(plain_iters)),
@@ -588,6 +636,9 @@ def main():
             "static_batch_32": {"solves_per_s": KSLOTS / static_s, "ms": static_s * 1e3,
                                 "iterations_max": int(max(x["iterations"] for x in sst))},
             "rel_err_vs_fp64": rel_err,
+            "rel_err_vs_oracle": rel_err_oracle,
+            "rel_err_vs_oracle_what": "relative l_inf on the tube rows of one served (mixed) solution against the "
+                                      "oracle's FP64 solve of the same right-hand side to tol 1e-12",
             "iterations_p50": float(np.median(iters)), "iterations_max": int(max(iters)),
             "refinements_p50": float(np.median(refs)),
             "fp64_fallbacks": int(sum(int(x.get("fp64_fallback", 0)) for x in st_timed)),

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <unordered_map>
 
 #include "eig3.h"
 #include "opset.h"
@@ -380,8 +381,61 @@ static void ibc_xp0(const cpm_surface_desc &d, const std::vector<double> &verts,
     }
 }
 
+// Caller-supplied closest points (cpm_opset_create_from_cp): a table from query
+// points, matched by the exact bits of their three coordinates, to the closest
+// point and distance the caller computed there.  Points the table lacks keep
+// the device's own closest point.
+struct CpTable {
+    struct Key {
+        uint64_t a, b, c;
+        bool operator==(const Key &o) const { return a == o.a && b == o.b && c == o.c; }
+    };
+    struct Hash {
+        size_t operator()(const Key &k) const {
+            uint64_t h = k.a * 0x9E3779B97F4A7C15ull;
+            h ^= k.b + 0x7F4A7C159E3779B9ull + (h << 6) + (h >> 2);
+            h ^= k.c + 0x94D049BB133111EBull + (h << 6) + (h >> 2);
+            return (size_t)h;
+        }
+    };
+    std::unordered_map<Key, int64_t, Hash> index;
+    std::vector<double> cp, dist;  // copies: an operator set keeps its tables for later evaluation queries
+    static Key key(const double *x) {
+        Key k;
+        memcpy(&k.a, x, 8);
+        memcpy(&k.b, x + 1, 8);
+        memcpy(&k.c, x + 2, 8);
+        return k;
+    }
+    void load(const cpm_cp_table *t) {
+        index.clear();
+        cp.clear();
+        dist.clear();
+        if (!t || t->n <= 0 || !t->x || !t->cp) return;
+        cp.assign(t->cp, t->cp + 3 * t->n);
+        if (t->dist) dist.assign(t->dist, t->dist + t->n);
+        index.reserve((size_t)t->n);
+        for (int64_t i = 0; i < t->n; ++i) index.emplace(key(t->x + 3 * i), i);
+    }
+    bool empty() const { return index.empty(); }
+    // overrides cp_out (and dist_out when the table has distances) for a point it holds
+    bool lookup(const double *x, double *cp_out, double *dist_out) const {
+        auto it = index.find(key(x));
+        if (it == index.end()) return false;
+        for (int k = 0; k < 3; ++k) cp_out[k] = cp[3 * it->second + k];
+        if (!dist.empty() && dist_out) *dist_out = dist[it->second];
+        return true;
+    }
+};
+
+struct CpOverrides {
+    std::vector<CpTable> ibc;  // per IBC: its closest points at tube-node coordinates
+    CpTable surface;           // the tube surface's closest points at the cp-bar projections
+};
+
 static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_desc &desc, const std::vector<double> &normals,
-                          const DBuf<double> &xdev, IBCData &ib) {
+                          const DBuf<double> &xdev, const CpTable *cpt, const CpTable *surf_cpt,
+                          IBCData &ib) {
     const int64_t N = ht.N;
     const double r = ht.radius;
     ib.desc = desc;
@@ -400,6 +454,12 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
     std::vector<double> cpc, distc;
     CPM_TRY(dcp.download(cpc, 3 * N));
     CPM_TRY(dd.download(distc, N));
+    if (cpt && !cpt->empty())
+        for (int64_t q = 0; q < N; ++q) {
+            double xq[3];
+            ht.x(q, xq);
+            cpt->lookup(xq, &cpc[3 * q], &distc[q]);
+        }
     // open polylines tag closest points at their end points (src/Surface.cpp:2614-2637)
     bool open_poly = false;
     if (desc.kind == CPM_POLYLINE && desc.nverts > 1) {
@@ -513,6 +573,8 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
         CPM_TRY(ddist.alloc(nd));
         CPM_TRY(closest_points_dev(t->surf.params(), (int64_t)nd, dp.p, dc.p, ddist.p, 4.0 * r));
         CPM_TRY(dc.download(ib.dof_cpbar, 3 * nd));
+        if (surf_cpt && !surf_cpt->empty())
+            for (size_t i = 0; i < nd; ++i) surf_cpt->lookup(&proj[3 * i], &ib.dof_cpbar[3 * i], nullptr);
         CPM_TRY(query_weights(t, ib.dof_cpbar, ib.dof_rows));
     } else {
         CPM_TRY(query_weights(t, ib.dof_cp, ib.dof_rows));
@@ -597,7 +659,7 @@ int opset_tube_normals(cpm_opset_s *o) {
     return o->normals.upload(normals);
 }
 
-static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs) {
+static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, const CpOverrides *ovr) {
     cpm_tube_s *t = o->tube;
     HostTube ht;
     CPM_TRY(ht.load(t));
@@ -615,7 +677,9 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs) {
     k_node_coords<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, t->key.p, t->g.xstart, t->g.dx, xdev.p);
     CPM_CUDA_TRY(cudaGetLastError());
     std::vector<IBCData> ibs(n_ibc);
-    for (int c = 0; c < n_ibc; ++c) CPM_TRY(build_ibc_data(t, ht, descs[c], normals, xdev, ibs[c]));
+    for (int c = 0; c < n_ibc; ++c)
+        CPM_TRY(build_ibc_data(t, ht, descs[c], normals, xdev, ovr ? &ovr->ibc[c] : nullptr, ovr ? &ovr->surface : nullptr,
+                               ibs[c]));
     o->ibc_desc.assign(descs, descs + n_ibc);
     o->ibc_verts.assign(n_ibc, {});
     o->ibc_prims.assign(n_ibc, {});
@@ -1097,13 +1161,13 @@ static int build_schedule(cpm_opset_s *o) {
 
 using namespace cpm;
 
-extern "C" int cpm_opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, cpm_opset_t *out) {
+static int opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, const CpOverrides *ovr, cpm_opset_t *out) {
     if (!t || !out || n_ibc < 0 || (n_ibc > 0 && !ibcs)) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
     *out = nullptr;
     cpm_opset_s *o = new cpm_opset_s();
     o->tube = t;
     int rc = build_base(o);
-    if (!rc && n_ibc > 0) rc = build_ibc(o, n_ibc, ibcs);
+    if (!rc && n_ibc > 0) rc = build_ibc(o, n_ibc, ibcs, ovr);
     if (!rc) rc = build_schedule(o);
     if (!rc) rc = make_float_copies(o);
     if (!rc) {
@@ -1115,6 +1179,21 @@ extern "C" int cpm_opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_d
         return rc;
     }
     *out = o;
+    return 0;
+}
+
+extern "C" int cpm_opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, cpm_opset_t *out) {
+    return opset_create(t, n_ibc, ibcs, nullptr, out);
+}
+
+extern "C" int cpm_opset_create_from_cp(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs,
+                                        const cpm_cp_table *ibc_cp, const cpm_cp_table *surface_cp, cpm_opset_t *out) {
+    CpOverrides ovr;
+    ovr.ibc.resize(n_ibc > 0 ? n_ibc : 0);
+    for (int c = 0; c < n_ibc && ibc_cp; ++c) ovr.ibc[c].load(&ibc_cp[c]);
+    ovr.surface.load(surface_cp);
+    CPM_TRY(opset_create(t, n_ibc, ibcs, &ovr, out));
+    (*out)->cp_ovr = std::make_shared<CpOverrides>(std::move(ovr));
     return 0;
 }
 
@@ -1314,7 +1393,10 @@ extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp
     k_node_coords<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, t->key.p, t->g.xstart, t->g.dx, xdev.p);
     CPM_CUDA_TRY(cudaGetLastError());
     std::vector<IBCData> ibs(n_ibc);
-    for (int c = 0; c < n_ibc; ++c) CPM_TRY(build_ibc_data(t, ht, op->ibc_desc[c], normals, xdev, ibs[c]));
+    const CpOverrides *ovr = op->cp_ovr.get();
+    for (int c = 0; c < n_ibc; ++c)
+        CPM_TRY(build_ibc_data(t, ht, op->ibc_desc[c], normals, xdev, ovr ? &ovr->ibc[c] : nullptr, ovr ? &ovr->surface : nullptr,
+                               ibs[c]));
     std::vector<double> hx(xp, xp + 3 * n);
     DBuf<double> dxp;
     CPM_TRY(dxp.upload(hx));

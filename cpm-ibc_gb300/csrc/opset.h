@@ -2,6 +2,8 @@
 // device-side row functions of the closest-point operator.
 #pragma once
 
+#include <memory>
+
 #include "cpm_internal.h"
 
 namespace cpm {
@@ -497,6 +499,9 @@ __device__ __forceinline__ void l_rows4(const OpView<float> &op, const int64_t (
     }
 }
 
+// caller-supplied closest points of an operator set built by cpm_opset_create_from_cp
+struct CpOverrides;
+
 }  // namespace cpm
 
 struct cpm_opset_s {
@@ -538,6 +543,7 @@ struct cpm_opset_s {
     std::vector<std::vector<int64_t>> ibc_prims;
     std::vector<int64_t> col_start, dcol_start;
     int64_t identity_rows_start = 0;
+    std::shared_ptr<cpm::CpOverrides> cp_ovr;  // set by cpm_opset_create_from_cp
 
     template <class T>
     cpm::OpView<T> view() const;

@@ -49,6 +49,25 @@ class SurfaceDesc(ctypes.Structure):
     ]
 
 
+class CpTable(ctypes.Structure):
+    """struct cpm_cp_table: caller-computed closest points at query points"""
+
+    _fields_ = [("n", ctypes.c_int64), ("x", ctypes.c_void_p), ("cp", ctypes.c_void_p), ("dist", ctypes.c_void_p)]
+
+
+def cp_table(x, cp, dist=None):
+    """a CpTable over numpy arrays (kept alive on the returned object)"""
+    x = np.ascontiguousarray(x, np.float64).reshape(-1, 3)
+    cp = np.ascontiguousarray(cp, np.float64).reshape(-1, 3)
+    t = CpTable(n=len(x), x=x.ctypes.data, cp=cp.ctypes.data)
+    t._keep = [x, cp]
+    if dist is not None:
+        d = np.ascontiguousarray(dist, np.float64).reshape(-1)
+        t.dist = d.ctypes.data
+        t._keep.append(d)
+    return t
+
+
 class TubeInfo(ctypes.Structure):
     _fields_ = [("n_nodes", ctypes.c_int64), ("n1d", ctypes.c_int64), ("n_bricks", ctypes.c_int64),
                 ("n_visited", ctypes.c_int64), ("dx", ctypes.c_double), ("xstart", ctypes.c_double),
@@ -137,6 +156,7 @@ def lib():
         L.cpm_tube_destroy.argtypes = [vp]
         L.cpm_opset_create.argtypes = [vp, ctypes.c_int32, P(SurfaceDesc), P(vp)]
         L.cpm_opset_create_identity.argtypes = [vp, ctypes.c_int64, vp, P(vp)]
+        L.cpm_opset_create_from_cp.argtypes = [vp, ctypes.c_int32, P(SurfaceDesc), P(CpTable), P(CpTable), P(vp)]
         L.cpm_tube_nearest.argtypes = [vp, ctypes.c_int64, vp, vp]
         L.cpm_ibc_plot_points.argtypes = [P(SurfaceDesc), vp, vp]
         L.cpm_opset_sizes.argtypes = [vp, vp]
@@ -252,13 +272,21 @@ class Tube:
 class OpSet:
     """Lfull / Efull / identity rows (Helpers::SetupMatrices + IBCMatrixManipulations) on the device."""
 
-    def __init__(self, tube, ibcs=(), identity_rows=None):
+    def __init__(self, tube, ibcs=(), identity_rows=None, ibc_cp=None, surface_cp=None):
         """identity_rows (device tube indices): the nearest-node baselines' operator,
-        plain L and E with Dirichlet rows there (no IBC columns; ibcs must be empty)"""
+        plain L and E with Dirichlet rows there (no IBC columns; ibcs must be empty).
+        ibc_cp (one CpTable per IBC) and surface_cp (a CpTable): closest points
+        computed by the caller (cpm_opset_create_from_cp)"""
         self.tube = tube
         self.ibcs = list(ibcs)
         h = ctypes.c_void_p()
-        if identity_rows is not None:
+        if ibc_cp is not None or surface_cp is not None:
+            arr = (SurfaceDesc * max(1, len(ibcs)))(*ibcs) if ibcs else None
+            tabs = (CpTable * max(1, len(ibcs)))(*(ibc_cp or [CpTable() for _ in ibcs])) if ibcs else None
+            _check(lib().cpm_opset_create_from_cp(tube.h, len(ibcs), arr, tabs,
+                                                  ctypes.byref(surface_cp) if surface_cp is not None else None,
+                                                  ctypes.byref(h)))
+        elif identity_rows is not None:
             if ibcs:
                 raise ValueError("identity_rows and IBC curves are exclusive")
             rows = np.ascontiguousarray(identity_rows, np.int64)

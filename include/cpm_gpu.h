@@ -160,6 +160,27 @@ int cpm_tube_destroy(cpm_tube_t t);
  * rows in the reference's column layout (src/IBCSubsets.cpp:74-116). */
 int cpm_opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, cpm_opset_t *out);
 
+/* Closest points computed by the caller: n query points x (3n), their closest
+ * points cp (3n) and distances dist (n, or NULL).  A point is matched by the
+ * exact bits of its three coordinates. */
+typedef struct cpm_cp_table {
+    int64_t n;
+    const double *x;
+    const double *cp;
+    const double *dist;
+} cpm_cp_table;
+
+/* cpm_opset_create "given the same closest points", the operator-set
+ * counterpart of cpm_tube_build_from_cp.  IBCSubset::ComputeSubsetNearIBC
+ * (src/IBCSubset.cpp:39-109) takes IBC c's closest point and distance at a
+ * tube node's grid coordinates from ibc_cp[c], and IBCDOFSubset's cp-bar
+ * (src/IBCDOFSubset.cpp:63-73) takes the surface's closest point at the
+ * projection 2 cp_c - x from surface_cp.  Points a table lacks (and a NULL
+ * table) keep the device's own closest points.  The tables are copied; later
+ * evaluation queries (cpm_opset_plot_interp) use them too. */
+int cpm_opset_create_from_cp(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, const cpm_cp_table *ibc_cp,
+                             const cpm_cp_table *surface_cp, cpm_opset_t *out);
+
 /* sizes (9 entries): [D, N, total_ibc_dofs, num_2nd_order_rows, n_ibc, n_patched_rows,
  * n_moved_entries, rows whose E row is patched, moved E stencil points] */
 int cpm_opset_sizes(cpm_opset_t op, int64_t *sizes);
@@ -231,6 +252,10 @@ int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslots, int32_t
  * D * kslots * (4 or 8 bytes) above that limit returns CPM_ERR_INVALID_ARG.
  * The first call on a device looks up the array's device address; make that
  * first call before any stream capture, with the library's device current.
+ * The address is kept for the life of the process and stays valid only while
+ * the device's primary context lives: after cudaDeviceReset (or anything else
+ * that destroys the primary context) this entry point must not be called again
+ * in the same process.
  * All calls share the one array, which keeps the previous call's contents
  * (every entry is rewritten before it is read, nothing needs clearing):
  * calls that overlap on the GPU race. */

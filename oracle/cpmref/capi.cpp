@@ -3,6 +3,8 @@
 // C entry points of the CPU restatement, loaded by the tests and by the
 // cpu_baseline / reference legs of bench.py through ctypes.  Nothing in the
 // product library links or calls this file.
+#include <omp.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cstdint>
@@ -394,6 +396,14 @@ int cpmref_heat_nearest(void *hp, int64_t n_ibc, const int64_t *ibc_idx, int64_t
 // Row loops of the sparse products on OpenMP threads (1) or serial (0, the default).
 int cpmref_set_parallel_rows(int32_t on) {
     ParallelRows() = on != 0;
+    return 0;
+}
+
+// OpenMP threads of the vector operations (the timed CPU baselines run with all
+// host threads and with one).
+int cpmref_set_num_threads(int32_t n) {
+    if (n < 1) return -1;
+    omp_set_num_threads(n);
     return 0;
 }
 

@@ -4,7 +4,8 @@
 // the solutions, in the reference's row layout, to a binary file:
 //   int64 n, then n doubles, for each of: the screened Poisson solution, the two-circle
 //   IBC Laplace FP64 and mixed solutions, geodesic distance, the nearest-node Poisson baselines,
-//   the nearest-node geodesic distance and three plotted values of it.
+//   the nearest-node geodesic distance and three plotted values of it, and three
+//   HeatWithIBC steps (Crank-Nicolson, Dirichlet circle; backward Euler, Neumann circle).
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -89,6 +90,36 @@ int main(int argc, char **argv) {
             VectorX phin = gn.ComputeDistance(tube, con, ins, insd, 0.01);
             put(f, phin);
             put(f, GeodesicDistanceNearest::Plot(tube, phin, {Point3{0, 0, 1}, Point3{0.6, 0, 0.8}, Point3{-1, 0, 0}}));
+        }
+        // HeatWithIBC on the heat study's circles (HeatProblemsWithIBC.cpp:68-106, :307, :318),
+        // dx = 0.1, u(0) = z, dt = 0.01, three steps each: Crank-Nicolson with the 2nd-order
+        // Dirichlet circle (u = exp(-2t) z there), backward Euler with the zero-Neumann great circle
+        {
+            const double hdx = 0.1, hdt = 0.01;
+            double nv[3] = {1.1, 1.234, 1.321};
+            const double nn = std::sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+            for (double &v : nv) v /= nn;
+            const double r = 0.27, th = 0.132, ph = 0.221;
+            const double pop[3] = {r * std::cos(ph) * std::sin(th), r * std::sin(ph) * std::sin(th), r * std::cos(th)};
+            const double rho = -(pop[0] * nv[0] + pop[1] * nv[1] + pop[2] * nv[2]);
+            SurfaceSpecifier dcirc = SurfaceSpecifier::Circle3D(std::sqrt(1 - rho * rho), {rho * nv[0], rho * nv[1], rho * nv[2]},
+                                                                {nv[0], nv[1], nv[2]}, {-1, 1})
+                                         .boundary_order(2)
+                                         .on_ibc_tolerance(0.1 * hdx * hdx);
+            SurfaceSpecifier ncirc = SurfaceSpecifier::Circle3D(1.0, {0, 0, 0}, {0, 1, 0}, {-1, 1})
+                                         .boundary_order(2)
+                                         .boundary_type(1, 0)
+                                         .on_ibc_tolerance(0.1 * hdx * hdx);
+            for (int which = 0; which < 2; ++which) {
+                HeatWithIBC heat(sphere, {which == 0 ? dcirc : ncirc}, hdx, hdt, which == 0 ? 2 : 1);
+                VectorX u(heat.system().rows());
+                for (size_t q = 0; q < u.size(); ++q) u[q] = heat.system().point(q)[2];
+                for (int k = 1; k <= 3; ++k) {
+                    const double t = k * hdt;
+                    u = heat.TimeStep(u, [t](size_t, size_t, const Point3 &x) { return std::exp(-2.0 * t) * x[2]; });
+                }
+                put(f, u);
+            }
         }
         printf("nodes %zu rows %zu ibc_dofs %zu iterations %d\n", tube.nNodes(), p.system().rows(),
                p.system().TotalIBCDOFs(), p.solver().stats().iterations);

@@ -131,6 +131,7 @@ def lib():
             L.cpmref_geodesic_nearest.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, ctypes.c_double,
                                                   ctypes.c_int32, vp, vp]
             L.cpmref_set_parallel_rows.argtypes = [ctypes.c_int32]
+            L.cpmref_set_num_threads.argtypes = [ctypes.c_int32]
             L.cpmref_csr_multiply.argtypes = [vp, ctypes.c_int32, vp, vp]
             L.cpmref_heat_nearest.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, ctypes.c_double,
                                               ctypes.c_int32, vp]

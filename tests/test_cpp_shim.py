@@ -6,7 +6,9 @@ numbering), equal the oracle's vectors entry by entry, with no permutation:
 screened Poisson on the sphere and the two-circle IBC Laplace (FP64) within
 1e-8 relative l_inf (the device computes its own closest points, which differ
 from glibc's by ulps), mixed precision within 1e-8 of the FP64 run, and the
-geodesic and the nearest-node geodesic within 1e-6 of the oracle's."""
+geodesic and the nearest-node geodesic within 1e-6 of the oracle's, and three
+HeatWithIBC time steps (Crank-Nicolson with a Dirichlet circle, backward Euler
+with a zero-Neumann circle) within 1e-8."""
 import os
 import shutil
 import subprocess
@@ -51,7 +53,7 @@ def test_shim_example_matches_oracle(gpu, oracle, tmp_path):
                     f"-Wl,-rpath,{libdir}", "-o", exe], check=True)
     out = str(tmp_path / "out.bin")
     subprocess.run([exe, out], check=True)
-    c1, c2, c2m, geo, n_u, n_id, n_b, f_u, f_id, f_b, gn, gn_plot = _read(out)
+    c1, c2, c2m, geo, n_u, n_id, n_b, f_u, f_id, f_b, gn, gn_plot, heat_cn, heat_be_neu = _read(out)
     # screened Poisson on the sphere, dx = 0.1
     P1 = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.1)
     b1 = 3.0 * P1.rows()["point"][:, 2]
@@ -90,3 +92,22 @@ def test_shim_example_matches_oracle(gpu, oracle, tmp_path):
     assert len(gn) == P1n.N
     assert np.max(np.abs(gn - ref)) / np.max(np.abs(ref)) <= 1e-6
     assert len(gn_plot) == 3 and np.all(np.isfinite(gn_plot)) and np.all(gn_plot >= -0.1)
+    # HeatWithIBC::TimeStep (problems/HeatWithIBC.cpp:104-132): three Crank-Nicolson steps with the
+    # Dirichlet circle and three backward-Euler steps with the zero-Neumann circle, dx = 0.1, dt = 0.01
+    for got, bt, method in ((heat_cn, 0, 2), (heat_be_neu, 1, 1)):
+        R, c, n = S.heat_circle_params(boundary_type=bt)
+        ibc = oracle.circle3d_desc(R, c, n, 0.1, boundary_order=2)
+        ibc.boundary_type[0] = bt
+        Ph = oracle.RefProblem(oracle.sphere_desc(), [ibc], 3, 0.1)
+        rows = Ph.rows()
+        u = rows["point"][:, 2].copy()
+        dirichlet = rows["kind"] == 2
+        for k in range(1, 4):
+            t = k * 0.01
+            if method == 2:
+                u = Ph.apply(1.0, 0.5 * 0.01, u)
+            u = np.array(u, copy=True)
+            u[dirichlet] = np.exp(-2 * t) * rows["point"][dirichlet, 2]
+            u, _ = Ph.solve(1.0, -(0.5 if method == 2 else 1.0) * 0.01, u)
+        assert len(got) == Ph.D
+        assert np.max(np.abs(got - u)) / np.max(np.abs(u)) <= 1e-8

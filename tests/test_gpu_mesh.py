@@ -6,13 +6,15 @@ point-triangle and point-segment closest points), so the device's closest
 points are checked against that (<= 1e-12) and the rest of the pipeline is
 bit-exact given the oracle's closest points, as for the analytic surfaces.
 
-Tolerances: closest points and distances <= 1e-12; tube, base points, weights
-and IBC subsets bit-exact given the same closest points; FP64 solve <= 1e-9
-relative l_inf of the oracle's; mixed precision <= 1e-8."""
+Tolerances: closest points and distances <= 1e-12; tube, base points, weights,
+IBC subsets and operator rows bit-exact given the same closest points; FP64
+solve <= 1e-10 relative l_inf of the oracle's, both solved to relative
+residual 1e-12; mixed precision <= 1e-8."""
 import numpy as np
 import pytest
 
 import studies as S
+from test_gpu_parity_c2 import assert_rows_bit_exact, same_cp_pair
 from test_gpu_setup import ref_to_gpu_index
 from cpm_gb300 import workloads as W
 
@@ -75,19 +77,17 @@ def test_mesh_device_closest_points_match_oracle(gpu, oracle):
 def test_polyline_ibcs_on_mesh_match_oracle(gpu, oracle):
     v, f, bb = _mesh()
     od, gd = _descs(gpu, oracle, v, f, bb)
-    P = oracle.RefProblem(od, _curves(oracle, v, f, bb, 2, DX), 3, DX, record_visited=True)
-    T = gpu.Tube.from_closest_points(gd, 3, DX, *P.visited())
-    O = gpu.OpSet(T, _curves(gpu, v, f, bb, 2, DX))
+    P, T, O, gr = same_cp_pair(gpu, oracle, DX, _curves(oracle, v, f, bb, 2, DX), _curves(gpu, v, f, bb, 2, DX),
+                               surface=(od, gd))
     ref, g = P.tube(), T.export()
     assert O.D == P.D and O.total_ibc_dofs == P.total_ibc_dofs
     for c in range(2):
         rs, gs = P.ibc_subsets(c), O.ibc_subsets(c)
         assert np.array_equal(g["rec"][gs["tag_set"]], ref["rec"][rs["tag_set"]])
         assert np.array_equal(g["rec"][gs["dof_set"]], ref["rec"][rs["dof_set"]])
+    for which in (0, 1):
+        assert_rows_bit_exact(P, O, gr, which)
     # diffusion-curves Laplace, one right-hand side per colour channel
-    m = ref_to_gpu_index(ref["rec"], g["rec"])
-    gr = np.arange(O.D)
-    gr[:P.N] = m
     rows = P.rows()
     rgb = np.random.default_rng(8).uniform(0, 1, size=(2, 3))
     B = [S.build_rhs(rows, lambda x: np.zeros(len(x)), lambda c, x, ch=ch: np.full(len(x), rgb[c, ch]))
@@ -96,11 +96,11 @@ def test_polyline_ibcs_on_mesh_match_oracle(gpu, oracle):
     for ch in range(3):
         Bg[ch][gr] = B[ch]
     solver = gpu.Solver(O, 0.0, -1.0, kslots=32)
-    X64, st = solver.solve(Bg, tol=1e-10, precision=0)
+    X64, st = solver.solve(Bg, tol=1e-12, precision=0)
     X32, st32 = solver.solve(Bg, tol=1e-10, precision=1)
     for ch in range(3):
-        x_ref, _ = P.solve(0.0, -1.0, B[ch])
+        x_ref, _ = P.solve(0.0, -1.0, B[ch], tol=1e-12)
         scale = np.max(np.abs(x_ref))
         assert st[ch]["status"] == 0 and st32[ch]["status"] == 0
-        assert np.max(np.abs(X64[ch][gr] - x_ref)) / scale <= 1e-9
+        assert np.max(np.abs(X64[ch][gr] - x_ref)) / scale <= 1e-10
         assert np.max(np.abs(X32[ch][gr] - x_ref)) / scale <= 1e-8

@@ -1,0 +1,196 @@
+"""Parity with the oracle at the size of the two-circle Laplace configuration
+(unit sphere, Dirichlet circles z = 0.3 and z = -0.5, dx = 0.025: 166,390 tube
+nodes, 215,662 rows) and on the Neumann IBC rows.
+
+"Given the same closest points" means: the tube is built from the oracle's
+closest points (cpm_tube_build_from_cp), and the IBC build takes the oracle's
+IBC closest points at the tube nodes and its cp-bar closest points
+(cpm_opset_create_from_cp).  Then, bit for bit:
+  * tube membership, coordinates, base points, tricubic weights, neighbours;
+  * IBC tagging and DOF subsets in the reference's BFS order, DOF closest
+    points, the column layout, every Lfull and Efull entry (no exemptions).
+FP64 solves: both sides solved to relative residual 1e-12, solutions within
+relative l_inf 1e-10.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import studies as S
+from test_gpu_setup import ref_to_gpu_index, two_circle_ibcs
+
+pytestmark = pytest.mark.gpu
+
+FP64_SOLVE_TOL = 1e-12  # relative residual both sides are solved to
+FP64_PARITY = 1e-10     # relative l_inf between the device and the oracle solutions
+
+
+def _rel_inf(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def same_cp_pair(gpu, oracle, dx, ibcs_oracle, ibcs_gpu, surface=None):
+    """(oracle problem, device tube, device opset, device row of each reference row)
+    with the device built from the oracle's closest points"""
+    od = surface[0] if surface else oracle.sphere_desc()
+    gd = surface[1] if surface else gpu.desc(gpu.SPHERE, [1.0])
+    P = oracle.RefProblem(od, ibcs_oracle, 3, dx, record_visited=True)
+    T = gpu.Tube.from_closest_points(gd, 3, dx, *P.visited())
+    g = T.export()
+    tabs = []
+    for d in ibcs_oracle:
+        cp, dist = oracle.closest_points(d, g["x"])
+        tabs.append(gpu.cp_table(g["x"], cp, dist))
+    # cp-bar: the surface's closest points at 2 cp_c - x of every DOF (order 2)
+    proj, cpb = [], []
+    ref = P.tube()
+    for c in range(len(ibcs_oracle)):
+        s = P.ibc_subsets(c)
+        if len(s["dof_set"]) and ibcs_oracle[c].boundary_order == 2:
+            p = 2.0 * s["dof_cp"] - ref["x"][s["dof_set"]]
+            proj.append(p)
+            cpb.append(oracle.closest_points(od, p)[0])
+    surf = gpu.cp_table(np.concatenate(proj), np.concatenate(cpb)) if proj else None
+    O = gpu.OpSet(T, ibcs_gpu, ibc_cp=tabs, surface_cp=surf)
+    m = ref_to_gpu_index(ref["rec"], g["rec"])
+    g_of_ref = np.arange(O.D)
+    g_of_ref[:P.N] = m
+    return P, T, O, g_of_ref
+
+
+def _csr_triplets(ptr, idx, val, row_map=None, col_map=None):
+    rows = np.repeat(np.arange(len(ptr) - 1), np.diff(ptr))
+    cols = np.asarray(idx)
+    keep = val != 0.0
+    rows, cols, vals = rows[keep], cols[keep], val[keep]
+    if row_map is not None:
+        rows = row_map[rows]
+    if col_map is not None:
+        cols = col_map[cols]
+    o = np.lexsort((cols, rows))
+    return rows[o], cols[o], vals[o]
+
+
+def assert_rows_bit_exact(P, O, g_of_ref, which):
+    """Lfull (which 0) / Efull (1): every reference row equals its device row, entry by entry"""
+    ref_of_g = np.empty(O.D, np.int64)
+    ref_of_g[g_of_ref] = np.arange(O.D)
+    a = _csr_triplets(*P.csr(which))
+    b = _csr_triplets(*O.csr(which), row_map=ref_of_g, col_map=ref_of_g)
+    assert len(a[0]) == len(b[0])
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(a[2], b[2]), np.max(np.abs(a[2] - b[2]))
+
+
+@pytest.fixture(scope="module")
+def c2(gpu, oracle):
+    dx = 0.025
+    return same_cp_pair(gpu, oracle, dx, two_circle_ibcs(oracle, dx), two_circle_ibcs(gpu, dx))
+
+
+def test_c2_tube_bit_exact(c2):
+    P, T, O, gr = c2
+    ref, g = P.tube(), T.export()
+    assert T.N == P.N == 166390 and T.N1d == P.N1d and T.xstart == P.xstart and T.radius == P.radius
+    m = gr[:P.N]
+    assert np.array_equal(g["rec"][m], ref["rec"])
+    assert np.array_equal(g["x"][m], ref["x"]) and np.array_equal(g["cp"][m], ref["cp"])
+    assert np.array_equal(g["bpt"][m], ref["rec"][ref["bpt"]])
+    assert np.array_equal(g["w"][m], P.weights())
+    inv = np.empty(T.N, np.int64)
+    inv[m] = np.arange(T.N)
+    gn = g["nbr"][m]
+    assert np.array_equal(np.where(gn >= 0, inv[np.maximum(gn, 0)], -1), ref["nbr"])
+    assert np.array_equal(T.reference_order(), m)
+
+
+def test_c2_ibc_subsets_bit_exact(c2):
+    P, T, O, gr = c2
+    ref, g = P.tube(), T.export()
+    assert O.D == P.D == 215662 and O.total_ibc_dofs == P.total_ibc_dofs and O.num2 == P.num2
+    for c in range(2):
+        rs, gs = P.ibc_subsets(c), O.ibc_subsets(c)
+        assert np.array_equal(g["rec"][gs["tag_set"]], ref["rec"][rs["tag_set"]])
+        assert np.array_equal(g["rec"][gs["dof_set"]], ref["rec"][rs["dof_set"]])
+        assert np.array_equal(gs["dof_cp"], rs["dof_cp"])
+        assert gs["col_start"] == rs["col_start"] and gs["dcol_start"] == rs["dcol_start"]
+        assert gs["identity_rows_start"] == rs["identity_rows_start"]
+    rr, gg = P.rows(), O.rows()
+    assert np.array_equal(rr["identity"], gg["identity"][gr])
+    assert np.array_equal(rr["kind"], gg["kind"][gr])
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_c2_operator_rows_bit_exact(c2, which):
+    P, T, O, gr = c2
+    assert_rows_bit_exact(P, O, gr, which)
+
+
+def test_c2_plain_fp64_solve_within_1e10(gpu, c2):
+    """The plain FP64 GPU path against the oracle's solve of the same system:
+    Laplace with circle values U[0,1], both to relative residual 1e-12."""
+    P, T, O, gr = c2
+    rows = P.rows()
+    vals = np.random.default_rng(31).uniform(0, 1, 2)
+    b = S.build_rhs(rows, lambda x: np.zeros(len(x)), lambda c, x: np.full(len(x), vals[c]))
+    x_ref, st_ref = P.solve(0.0, -1.0, b, tol=FP64_SOLVE_TOL)
+    bg = np.empty(O.D)
+    bg[gr] = b
+    x_gpu, st = gpu.Solver(O, 0.0, -1.0).solve(bg, tol=FP64_SOLVE_TOL, precision=0)
+    assert st[0]["status"] == 0 and st[0]["rel_residual"] <= FP64_SOLVE_TOL
+    assert _rel_inf(x_gpu[0][gr], x_ref) <= FP64_PARITY
+
+
+@pytest.mark.parametrize("dx", [0.1, 0.05])
+@pytest.mark.parametrize("order", [1, 2])
+def test_two_circle_rows_bit_exact(gpu, oracle, dx, order):
+    P, T, O, gr = same_cp_pair(gpu, oracle, dx, two_circle_ibcs(oracle, dx, order), two_circle_ibcs(gpu, dx, order))
+    for which in (0, 1):
+        assert_rows_bit_exact(P, O, gr, which)
+
+
+# ---- Neumann IBC rows (boundary_type 1): the zero-Neumann great circle of the
+# heat study (convergence_studies/HeatProblemsWithIBC/HeatProblemsWithIBC.cpp:318)
+
+def _neumann_circle(mod, dx, order):
+    R, c, n = S.heat_circle_params(boundary_type=1)
+    if hasattr(mod, "circle3d_desc"):
+        d = mod.circle3d_desc(R, tuple(c), tuple(n), dx, boundary_order=order)
+    else:
+        d = mod.desc(mod.CIRCLE3D, [R, *c, *n], (-1.0, 1.0), boundary_order=order, on_ibc_tolerance=0.1 * dx * dx)
+    d.boundary_type[0] = 1
+    return d
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("dx", [0.1, 0.05])
+def test_neumann_rows_bit_exact(gpu, oracle, dx, order):
+    P, T, O, gr = same_cp_pair(gpu, oracle, dx, [_neumann_circle(oracle, dx, order)], [_neumann_circle(gpu, dx, order)])
+    assert O.D == P.D and O.total_ibc_dofs == P.total_ibc_dofs and O.num2 == P.num2 == 0
+    rr, gg = P.rows(), O.rows()
+    assert np.array_equal(rr["identity"], gg["identity"][gr]) and not rr["identity"].any()
+    for which in (0, 1):
+        assert_rows_bit_exact(P, O, gr, which)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_neumann_apply_and_backward_euler_match_oracle(gpu, oracle, order):
+    """Apply (relative l_inf <= 1e-14) and one backward-Euler heat step
+    (I - dt L E) u1 = u0 of the Neumann system (<= 1e-10 at tol 1e-12)."""
+    dx = 0.05
+    P, T, O, gr = same_cp_pair(gpu, oracle, dx, [_neumann_circle(oracle, dx, order)], [_neumann_circle(gpu, dx, order)])
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(P.D)
+    xg = np.empty(O.D)
+    xg[gr] = x
+    dt = 0.1 * dx
+    for m, n in ((1.0, -dt), (0.0, -1.0)):
+        assert _rel_inf(O.apply(m, n, xg)[0][gr], P.apply(m, n, x)) <= 1e-14
+    u0 = P.rows()["point"][:, 2].copy()
+    u_ref, _ = P.solve(1.0, -dt, u0, tol=FP64_SOLVE_TOL)
+    ug = np.empty(O.D)
+    ug[gr] = u0
+    u_gpu, st = gpu.Solver(O, 1.0, -dt).solve(ug, tol=FP64_SOLVE_TOL, precision=0)
+    assert st[0]["status"] == 0
+    assert _rel_inf(u_gpu[0][gr], u_ref) <= FP64_PARITY
