@@ -68,6 +68,7 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
     v.pe_old = o->pe_old.p;
     v.pe_w = pe_w;
     v.n_pl = o->n_pl;
+    v.eb = o->ebrick();
     return v;
 }
 
@@ -826,14 +827,13 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
             for (int k = 0; k < 3; ++k) point[3 * row + k] = ib.dof_cp[3 * i + k];
             rowibc[row] = c;
             if (ib.dirichlet && !ib.order2) {
-                // order-1 Dirichlet: identity DOF rows carrying the value
+                // order-1 Dirichlet: identity DOF rows carrying the value.  Their L row
+                // is still assembled (below): the reference's Lfull holds it, and only
+                // identity_rows makes the solve skip it
                 flags[row] = F_IDENT;
                 ident[row] = 1;
                 kind[row] = 2;
-                lptr.push_back((int32_t)lcol.size());
-                ldiag.push_back(0.0);
-                continue;
-            }
+            } else {
             kind[row] = 1;
             // E row: E_ibc stencil (at cp-bar for order 2), tags with the DOF
             // direction and flip -1, scaled by -1 for Dirichlet
@@ -869,6 +869,7 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
                 p_xval.push_back(0.0);
             }
             flags[row] = f;
+            }
             // L row (AddFiniteDifferenceIBCRows, src/IBCMatrixManipulations.cpp:219-251):
             // across the curve -> the original tube node; same side and in the DOF
             // subset -> that DOF's column; otherwise dropped.
@@ -1120,14 +1121,19 @@ static int build_schedule(cpm_opset_s *o) {
     std::vector<uint32_t> base;
     CPM_TRY(o->flags.download(flags, D));
     CPM_TRY(o->base.download(base, D));
-    std::vector<std::pair<uint32_t, int32_t>> rows;
+    // rows sorted by (base brick, base point, row): a base brick's groups are contiguous
+    const int NB = o->tube->g.NB;
+    auto bbkey = [&](uint32_t b) -> uint64_t {
+        return (((uint64_t)(unpack_i(b) >> 2) * NB + (uint64_t)(unpack_j(b) >> 2)) * NB + (uint64_t)(unpack_k(b) >> 2));
+    };
+    std::vector<std::pair<uint64_t, int32_t>> rows;
     std::vector<int32_t> ident;
     rows.reserve(D);
     for (int64_t r = 0; r < D; ++r) {
         if (flags[r] & F_IDENT)
             ident.push_back((int32_t)r);
         else
-            rows.push_back({base[r], (int32_t)r});
+            rows.push_back({(bbkey(base[r]) << 32) | (uint64_t)base[r], (int32_t)r});
     }
     std::sort(rows.begin(), rows.end());
     std::vector<int32_t> ord(rows.size()), grp;
@@ -1157,9 +1163,216 @@ static int build_schedule(cpm_opset_s *o) {
     return build_patch_list(o, flags);
 }
 
+// Units of the brick-staged E pass (see EBrick).  A unit is a run of groups of
+// one base brick whose stage (the 2 x 2 x 2 node bricks at the base brick's
+// corner, then the distinct extra columns its patch entries read) fits
+// EB_MAX_ROWS rows (opset.h); units are ordered by decreasing row count so that blocks
+// taking them in turn finish together.
+
+static int build_brick_sched(cpm_opset_s *o) {
+    cpm_tube_s *t = o->tube;
+    const int NB = t->g.NB;
+    const int64_t D = o->D, n_grp = o->n_grp;
+    std::vector<int32_t> bmap, bstart, ord, grp, pl_row, pl_off, pl_xcol, pe_new, patch;
+    std::vector<uint64_t> bmask, p_emask;
+    std::vector<uint32_t> base;
+    std::vector<uint8_t> flags, pl_neg;
+    std::vector<float> pl_xval, pe_w;
+    CPM_TRY(t->bmap.download(bmap, (size_t)NB * NB * NB));
+    CPM_TRY(t->bstart.download(bstart, t->nbricks));
+    CPM_TRY(t->bmask.download(bmask, t->nbricks));
+    CPM_TRY(o->ord.download(ord, std::max<int64_t>(1, o->n_ord)));
+    CPM_TRY(o->grp.download(grp, n_grp + 1));
+    CPM_TRY(o->base.download(base, D));
+    CPM_TRY(o->flags.download(flags, D));
+    const int64_t n_pl = o->n_pl, n_pe = o->n_pe;
+    std::vector<int32_t> pl_of_row(D, -1);
+    if (n_pl > 0) {
+        CPM_TRY(o->pl_row.download(pl_row, n_pl));
+        CPM_TRY(o->pl_off.download(pl_off, n_pl + 1));
+        CPM_TRY(o->pl_xcol.download(pl_xcol, n_pl));
+        CPM_TRY(o->pl_neg.download(pl_neg, n_pl));
+        CPM_TRY(o->pl_xval32.download(pl_xval, n_pl));
+        CPM_TRY(o->pe_new.download(pe_new, std::max<int64_t>(1, n_pe)));
+        CPM_TRY(o->pe_w32.download(pe_w, std::max<int64_t>(1, n_pe)));
+        CPM_TRY(o->patch.download(patch, D));
+        CPM_TRY(o->p_emask.download(p_emask, o->p_emask.n));
+        for (int64_t q = 0; q < n_pl; ++q) pl_of_row[pl_row[q]] = (int32_t)q;
+    }
+    auto brick_rank = [&](int X, int Y, int Z) -> int {
+        if (X >= NB || Y >= NB || Z >= NB) return -1;
+        return bmap[((size_t)X * NB + Y) * NB + Z];
+    };
+    std::vector<int4> u_hdr;
+    std::vector<int2> u_brick;
+    std::vector<int32_t> u_extra, g_pq(n_grp + 1, 0);
+    std::vector<uint32_t> gslot(64 * std::max<int64_t>(1, n_grp), 0);
+    std::vector<int4> pq;
+    std::vector<float> pq_xval, pqe_w;
+    std::vector<uint8_t> pq_neg;
+    std::vector<uint2> pqe;
+    std::vector<int64_t> unit_rows;
+    int stage_rows = 0;
+    int64_t g = 0;
+    while (g < n_grp) {
+        // the run of groups of one base brick
+        const uint32_t b0 = base[ord[grp[g]]];
+        const int X = unpack_i(b0) >> 2, Y = unpack_j(b0) >> 2, Z = unpack_k(b0) >> 2;
+        int64_t gend = g + 1;
+        while (gend < n_grp) {
+            const uint32_t b = base[ord[grp[gend]]];
+            if ((unpack_i(b) >> 2) != X || (unpack_j(b) >> 2) != Y || (unpack_k(b) >> 2) != Z) break;
+            ++gend;
+        }
+        int2 bricks[8];
+        uint64_t masks[8];
+        int off[9];
+        off[0] = 0;
+        for (int c = 0; c < 8; ++c) {
+            const int rk = brick_rank(X + (c & 1), Y + ((c >> 1) & 1), Z + ((c >> 2) & 1));
+            masks[c] = rk >= 0 ? bmask[rk] : 0ull;
+            bricks[c] = make_int2(rk >= 0 ? bstart[rk] : 0, __builtin_popcountll(masks[c]));
+            off[c + 1] = off[c] + bricks[c].y;
+        }
+        const int brick_rows = off[8];
+        // stage offsets of every group's 64 stencil nodes
+        for (int64_t h = g; h < gend; ++h) {
+            const uint32_t b = base[ord[grp[h]]];
+            for (int sidx = 0; sidx < 64; ++sidx) {
+                const int i = unpack_i(b) + (sidx >> 4), j = unpack_j(b) + ((sidx >> 2) & 3), k = unpack_k(b) + (sidx & 3);
+                const int c = ((i >> 2) - X) | (((j >> 2) - Y) << 1) | (((k >> 2) - Z) << 2);
+                const int l = ((i & 3) << 4) | ((j & 3) << 2) | (k & 3);
+                if (!((masks[c] >> l) & 1ull)) return fail(CPM_ERR_BASEPOINT_OUTSIDE_TUBE, "an interpolation stencil leaves the tube");
+                gslot[64 * h + sidx] = (uint32_t)(off[c] + __builtin_popcountll(masks[c] & ((1ull << l) - 1ull))) * 128u;
+            }
+        }
+        // units: runs of these groups whose extra columns fit the stage
+        int64_t u0 = g;
+        while (u0 < gend) {
+            std::vector<int32_t> extra;
+            auto extra_slot = [&](int32_t col) -> uint32_t {
+                for (size_t e = 0; e < extra.size(); ++e)
+                    if (extra[e] == col) return (uint32_t)(brick_rows + (int)e) * 128u;
+                extra.push_back(col);
+                return (uint32_t)(brick_rows + (int)extra.size() - 1) * 128u;
+            };
+            int64_t h = u0;
+            int64_t rows_in_unit = 0;
+            for (; h < gend; ++h) {
+                // the group's patch records and the extra columns they add
+                std::vector<int4> rec;
+                std::vector<float> rx;
+                std::vector<uint8_t> rn;
+                std::vector<uint2> ent;
+                std::vector<float> ew;
+                const size_t extra_before = extra.size();
+                for (int32_t pos = grp[h]; pos < grp[h + 1]; ++pos) {
+                    const int32_t r = ord[pos];
+                    const int32_t q = pl_of_row[r];
+                    if (q < 0) continue;
+                    uint64_t em = (flags[r] & F_EMOVE) ? p_emask[patch[r]] : 0ull;
+                    const int e_first = (int)(pqe.size() + ent.size());
+                    for (int32_t e = pl_off[q]; e < pl_off[q + 1]; ++e) {
+                        if (!em) return fail(CPM_ERR_CUDA, "internal: patch entries exceed the moved-column mask");
+                        const int sidx = __builtin_ctzll(em);
+                        em &= em - 1;
+                        ent.push_back(make_uint2(gslot[64 * h + sidx], extra_slot(pe_new[e])));
+                        ew.push_back(pe_w[e]);
+                    }
+                    const int xoff = pl_xcol[q] >= 0 ? (int)extra_slot(pl_xcol[q]) : -1;
+                    rec.push_back(make_int4(pos - grp[h], e_first, (int)(pqe.size() + ent.size()), xoff));
+                    rx.push_back(pl_xval[q]);
+                    rn.push_back(pl_neg[q]);
+                }
+                if (brick_rows + (int)extra.size() > EB_MAX_ROWS) {
+                    if (h == u0) return fail(CPM_ERR_UNSUPPORTED, "a base group's IBC patch reads more columns than a stage holds");
+                    extra.resize(extra_before);  // this group starts the next unit
+                    break;
+                }
+                g_pq[h] = (int32_t)pq.size();
+                pq.insert(pq.end(), rec.begin(), rec.end());
+                pq_xval.insert(pq_xval.end(), rx.begin(), rx.end());
+                pq_neg.insert(pq_neg.end(), rn.begin(), rn.end());
+                pqe.insert(pqe.end(), ent.begin(), ent.end());
+                pqe_w.insert(pqe_w.end(), ew.begin(), ew.end());
+                rows_in_unit += grp[h + 1] - grp[h];
+            }
+            u_hdr.push_back(make_int4((int)u0, (int)h, (int)u_extra.size(), (int)(u_extra.size() + extra.size())));
+            for (int c = 0; c < 8; ++c) u_brick.push_back(bricks[c]);
+            u_extra.insert(u_extra.end(), extra.begin(), extra.end());
+            unit_rows.push_back(rows_in_unit);
+            stage_rows = std::max(stage_rows, brick_rows + (int)extra.size());
+            u0 = h;
+        }
+        g = gend;
+    }
+    g_pq[n_grp] = (int32_t)pq.size();
+    // decreasing row count (the order of units changes no result)
+    const int64_t nu = (int64_t)u_hdr.size();
+    std::vector<int64_t> uo(nu);
+    for (int64_t u = 0; u < nu; ++u) uo[u] = u;
+    std::stable_sort(uo.begin(), uo.end(), [&](int64_t a, int64_t b) { return unit_rows[a] > unit_rows[b]; });
+    std::vector<int4> hs(nu);
+    std::vector<int2> bs(8 * nu);
+    for (int64_t u = 0; u < nu; ++u) {
+        hs[u] = u_hdr[uo[u]];
+        for (int c = 0; c < 8; ++c) bs[8 * u + c] = u_brick[8 * uo[u] + c];
+    }
+    if (hs.empty()) {
+        hs.push_back(make_int4(0, 0, 0, 0));
+        bs.assign(8, make_int2(0, 0));
+    }
+    if (u_extra.empty()) u_extra.push_back(0);
+    if (pq.empty()) {
+        pq.push_back(make_int4(0, 0, 0, -1));
+        pq_xval.push_back(0.f);
+        pq_neg.push_back(0);
+    }
+    if (pqe.empty()) {
+        pqe.push_back(make_uint2(0, 0));
+        pqe_w.push_back(0.f);
+    }
+    CPM_TRY(o->eb_uhdr.upload(hs));
+    CPM_TRY(o->eb_ubrick.upload(bs));
+    CPM_TRY(o->eb_uextra.upload(u_extra));
+    CPM_TRY(o->eb_gslot.upload(gslot));
+    CPM_TRY(o->eb_gpq.upload(g_pq));
+    CPM_TRY(o->eb_pq.upload(pq));
+    CPM_TRY(o->eb_pqxval.upload(pq_xval));
+    CPM_TRY(o->eb_pqneg.upload(pq_neg));
+    CPM_TRY(o->eb_pqe.upload(pqe));
+    CPM_TRY(o->eb_pqew.upload(pqe_w));
+    CPM_TRY(o->eb_ctr.alloc(2));
+    CPM_TRY(o->eb_ctr.zero());
+    CPM_TRY(o->eb_err.alloc(1));
+    CPM_TRY(o->eb_err.zero());
+    o->eb_units = nu;
+    o->eb_stage_rows = stage_rows;
+    return 0;
+}
+
 }  // namespace cpm
 
 using namespace cpm;
+
+EBrick cpm_opset_s::ebrick() const {
+    EBrick e;
+    e.u_hdr = eb_uhdr.p;
+    e.u_brick = eb_ubrick.p;
+    e.u_extra = eb_uextra.p;
+    e.gslot = eb_gslot.p;
+    e.g_pq = eb_gpq.p;
+    e.pq = eb_pq.p;
+    e.pq_xval = eb_pqxval.p;
+    e.pq_neg = eb_pqneg.p;
+    e.pqe = eb_pqe.p;
+    e.pqe_w = eb_pqew.p;
+    e.ctr = eb_ctr.p;
+    e.err = eb_err.p;
+    e.n_units = eb_units;
+    e.stage_rows = eb_stage_rows;
+    return e;
+}
 
 static int opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, const CpOverrides *ovr, cpm_opset_t *out) {
     if (!t || !out || n_ibc < 0 || (n_ibc > 0 && !ibcs)) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
@@ -1170,6 +1383,7 @@ static int opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibc
     if (!rc && n_ibc > 0) rc = build_ibc(o, n_ibc, ibcs, ovr);
     if (!rc) rc = build_schedule(o);
     if (!rc) rc = make_float_copies(o);
+    if (!rc) rc = build_brick_sched(o);
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(stream());
         if (e != cudaSuccess) rc = fail(CPM_ERR_CUDA, cudaGetErrorString(e));
@@ -1222,6 +1436,7 @@ extern "C" int cpm_opset_create_identity(cpm_tube_t t, int64_t n_rows, const int
     }
     if (!rc) rc = build_schedule(o);
     if (!rc) rc = make_float_copies(o);
+    if (!rc) rc = build_brick_sched(o);
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(stream());
         if (e != cudaSuccess) rc = fail(CPM_ERR_CUDA, cudaGetErrorString(e));
@@ -1311,7 +1526,11 @@ extern "C" int cpm_opset_export_csr(cpm_opset_t o, int32_t which, int64_t *nnz, 
     for (int64_t r = 0; r < D; ++r) {
         row.clear();
         uint8_t f = flags[r];
-        if (f & F_IDENT) {
+        // identity rows are identity rows of Efull (Helpers::SetIdentityRows on E, src/Helpers.cpp:403-431);
+        // Lfull keeps the L rows of the tube and of the IBC DOFs, and the 2nd-order Dirichlet value rows
+        // hold their 1 (src/IBCMatrixManipulations.cpp:54-62)
+        const bool ident_row = (f & F_IDENT) && (which == 1 || r >= N + o->total_ibc);
+        if (ident_row) {
             row.push_back({r, 1.0});
         } else if (which == 1) {
             int pi = patch[r];

@@ -17,6 +17,32 @@ enum RowFlags : uint8_t {
     F_EXTRA = 32,  // E row has one extra entry (2 * Dirichlet value)
 };
 
+// Schedule of the brick-staged E pass (k_ebrick32, FP32, 32 slots).  Rows are
+// grouped by base point and the groups by the 4^3 brick of grid points their
+// base lies in (a base brick).  The stencils of a base brick's groups cover the
+// 2 x 2 x 2 node bricks at its corner, whose nodes are contiguous runs of the
+// tube's node order, so a unit of work stages them with eight bulk copies (plus
+// one per IBC column its patch entries read) and computes every row of its
+// groups from shared memory.  Offsets are bytes into the unit's stage, one
+// 128-byte row (32 FP32 slots) per staged node.
+constexpr int EB_MAX_ROWS = 560;  // stage rows of one unit: 70 KB of FP32 32-slot rows, three blocks per SM
+struct EBrick {
+    const int4 *u_hdr;      // per unit {first group, end group, first extra row, end extra row}
+    const int2 *u_brick;    // per unit 8 x {first node, node count}
+    const int32_t *u_extra; // rows staged after the bricks (moved IBC columns and Dirichlet value rows)
+    const uint32_t *gslot;  // 64 per group: stage offset of stencil node s = 16 i + 4 j + k
+    const int32_t *g_pq;    // per group: first patch record (n_grp + 1 entries)
+    const int4 *pq;         // patch record {row position in the group, first entry, end entry, extra-column offset or -1}
+    const float *pq_xval;   // the extra entry's value
+    const uint8_t *pq_neg;  // 1: the row is negated (2nd-order Dirichlet DOF rows)
+    const uint2 *pqe;       // patch entry {offset of the bulk stencil node, offset of the moved column}
+    const float *pqe_w;     // its stencil weight (wx_i wy_j) wz_k
+    unsigned int *ctr;      // two work counters, zero between launches (the last block resets them)
+    int *err;               // set to 1 when a stage copy did not arrive within the wait limit
+    int64_t n_units;
+    int stage_rows;         // rows of the largest stage
+};
+
 template <class T>
 struct OpView {
     BrickView bv;
@@ -55,6 +81,7 @@ struct OpView {
     const int32_t *pe_new, *pe_old;           // moved column and the bulk column it replaces
     const T *pe_w;                            // stencil weight (wx_i wy_j) wz_k of the moved point
     int64_t n_ord, n_grp, n_ident, n_pl;
+    EBrick eb;                                // brick-staged E pass (FP32 weights)
 };
 
 // ---------------------------------------------------------------------------
@@ -527,6 +554,19 @@ struct cpm_opset_s {
     cpm::DBuf<float> w_ord32;
     cpm::DBuf<uint8_t> fl_ord;
     int64_t n_ord = 0, n_grp = 0, n_ident = 0;
+    // brick-staged E pass schedule
+    cpm::DBuf<int4> eb_uhdr, eb_pq;
+    cpm::DBuf<int2> eb_ubrick;
+    cpm::DBuf<int32_t> eb_uextra, eb_gpq;
+    cpm::DBuf<uint32_t> eb_gslot;
+    cpm::DBuf<float> eb_pqxval, eb_pqew;
+    cpm::DBuf<uint8_t> eb_pqneg;
+    cpm::DBuf<uint2> eb_pqe;
+    cpm::DBuf<unsigned int> eb_ctr;
+    cpm::DBuf<int> eb_err;
+    int64_t eb_units = 0;
+    int eb_stage_rows = 0;
+    cpm::EBrick ebrick() const;
     // host-side row layout for right-hand sides
     std::vector<uint8_t> h_identity;
     std::vector<int32_t> h_kind, h_ibc;

@@ -409,6 +409,253 @@ __global__ void __launch_bounds__(128) k_epass32w(OpView<float> op, const Slot *
         }
 }
 
+// ---- brick-staged E pass for 32 FP32 slots, IBC patch included (k_ebrick32).
+// A block takes units of work in turn (a work counter): it stages the unit's
+// 2 x 2 x 2 node bricks and its extra columns into shared memory with bulk
+// asynchronous copies (TMA, cp.async.bulk, one per contiguous node run,
+// completing on an mbarrier), then its warps compute the unit's base groups
+// from shared memory with the arithmetic of k_epass32w, and the rows on the
+// IBC patch list get k_epatch32's correction in registers before the one
+// store.  Results are bit for bit those of k_epass32w followed by k_epatch32.
+
+// shared-memory address of a generic pointer
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// bulk copy of `bytes` (multiple of 16) from global to shared memory, completing on mbarrier `bar`
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+
+// waits for phase `parity` of mbarrier `bar` to complete, polling at most
+// ~2^22 times with a short sleep (about a second); false if it did not
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t done;
+        asm volatile("{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+        if (it > 64) __nanosleep(256);
+    }
+    return false;
+}
+
+// k_epatch32's correction of one patched row, lane = slot, from the stage:
+// sign (bulk + sum_e w_e (x[new_e] - x[old_e])) + xval x[xcol]
+__device__ __forceinline__ float eb_patch(const EBrick &eb, const char *stage, int lane, int pr, const int4 &rec, float acc) {
+    const float xv = eb.pq_xval[pr];
+    const bool neg = eb.pq_neg[pr] != 0;
+    const float xe = rec.w >= 0 ? *(const float *)(stage + rec.w + 4 * lane) : 0.f;
+    for (int base = rec.y; base < rec.z; base += 32) {
+        const int cnt = min(32, rec.z - base);
+        uint32_t oo = 0, nn = 0;
+        float w = 0.f;
+        if (lane < cnt) {
+            const uint2 e = eb.pqe[base + lane];
+            oo = e.x;
+            nn = e.y;
+            w = eb.pqe_w[base + lane];
+        }
+        for (int u0 = 0; u0 < cnt; u0 += 8) {
+            float xn[8], xo[8], ww[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int k = u0 + u;
+                const uint32_t nk = (uint32_t)__shfl_sync(FULL, nn, k & 31), ok = (uint32_t)__shfl_sync(FULL, oo, k & 31);
+                ww[u] = __shfl_sync(FULL, w, k & 31);
+                const bool valid = k < cnt;
+                xn[u] = valid ? *(const float *)(stage + nk + 4 * lane) : 0.f;
+                xo[u] = valid ? *(const float *)(stage + ok + 4 * lane) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (u0 + u < cnt) acc += ww[u] * (xn[u] - xo[u]);
+        }
+    }
+    if (neg) acc = -acc;
+    if (rec.w >= 0) acc += xv * xe;
+    return acc;
+}
+
+constexpr int EB_THREADS = 256;
+__global__ void __launch_bounds__(EB_THREADS, 3) k_ebrick32(OpView<float> op, const Slot *__restrict__ sl, int ph,
+                                                          const float *__restrict__ x, float *__restrict__ t) {
+    extern __shared__ __align__(128) unsigned char eb_stage[];
+    __shared__ __align__(16) float sw[EB_THREADS / 32][EW_ROWS * 12];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int s_unit;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, tid = threadIdx.x;
+    constexpr int NW = EB_THREADS / 32;
+    const bool act = (ph < 0) || sl[lane].phase == ph;
+    if (!__any_sync(FULL, act)) return;  // the same 32 slots in every warp: grid-uniform
+    const EBrick &eb = op.eb;
+    const char *stage = (const char *)eb_stage;
+    const uint32_t sbar = smem_u32(&bar), sstage = smem_u32(eb_stage);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_unit = (int)atomicAdd(eb.ctr, 1u);
+    }
+    __syncthreads();
+    uint32_t parity = 0;
+    float *w = sw[warp];
+    int u = s_unit;
+    while (u < eb.n_units) {
+        const int4 hd = eb.u_hdr[u];
+        // stage: the eight node bricks, then the extra rows
+        int2 bk[8];
+        int brick_rows = 0, my_off = 0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            bk[c] = eb.u_brick[8 * (int64_t)u + c];
+            if (c < tid) my_off += bk[c].y;
+            brick_rows += bk[c].y;
+        }
+        const int nextra = hd.w - hd.z;
+        if (tid == 0)
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                         ::"r"(sbar), "r"((uint32_t)(brick_rows + nextra) * 128u) : "memory");
+        __syncthreads();  // the expected byte count is posted before any copy is issued
+        if (tid < 8) {
+            int2 b = bk[0];
+#pragma unroll
+            for (int c = 1; c < 8; ++c)
+                if (c == tid) b = bk[c];
+            if (b.y > 0) bulk_g2s(sstage + (uint32_t)my_off * 128u, x + (size_t)b.x * 32, (uint32_t)b.y * 128u, sbar);
+        } else {
+            for (int e = tid - 8; e < nextra; e += EB_THREADS - 8) {
+                const int col = eb.u_extra[hd.z + e];
+                bulk_g2s(sstage + (uint32_t)(brick_rows + e) * 128u, x + (size_t)col * 32, 128u, sbar);
+            }
+        }
+        const bool ok = mbar_wait(sbar, parity);
+        parity ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            // a copy did not arrive: record it, give the copies one more bounded wait, stop
+            if (tid == 0) atomicExch(eb.err, 1);
+            mbar_wait(sbar, parity ^ 1u);
+            return;
+        }
+        for (int64_t g = hd.x + warp; g < hd.y; g += NW) {
+            const int p0 = op.grp[g], p1 = op.grp[g + 1];
+            int pr = eb.g_pq[g];
+            const int pr_end = eb.g_pq[g + 1];
+            const uint4 *gs = (const uint4 *)(eb.gslot + 64 * g);
+            for (int c0 = p0; c0 < p1; c0 += EW_ROWS) {
+                const int nr = min(p1 - c0, EW_ROWS), np = (nr + 1) >> 1;
+                __syncwarp();
+                for (int e = lane; e < 24 * np; e += 32) {
+                    const int q = e / 12, c = e - 12 * q;
+                    w[24 * (q >> 1) + 2 * c + (q & 1)] = q < nr ? op.w_ord[12 * (size_t)(c0 + q) + c] : 0.f;
+                }
+                const int row = lane < nr ? op.ord[c0 + lane] : 0;  // lane q: row q of the chunk
+                __syncwarp();
+                uint64_t acc[EW_ROWS / 2];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    float xb[16];
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) {
+                        const uint4 o4 = __ldg(gs + 4 * i + v);
+                        xb[4 * v] = *(const float *)(stage + o4.x + 4 * lane);
+                        xb[4 * v + 1] = *(const float *)(stage + o4.y + 4 * lane);
+                        xb[4 * v + 2] = *(const float *)(stage + o4.z + 4 * lane);
+                        xb[4 * v + 3] = *(const float *)(stage + o4.w + 4 * lane);
+                    }
+                    uint64_t x2[16];
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) x2[q] = f2_pack(xb[q], xb[q]);
+#pragma unroll
+                    for (int p = 0; p < EW_ROWS / 2; ++p)
+                        if (p < np) {
+                            const float *wp = w + 24 * p;
+                            const uint64_t wx2 = *(const uint64_t *)(wp + 2 * i);
+                            const ulonglong2 y01 = *(const ulonglong2 *)(wp + 8), y23 = *(const ulonglong2 *)(wp + 12);
+                            const ulonglong2 z01 = *(const ulonglong2 *)(wp + 16), z23 = *(const ulonglong2 *)(wp + 20);
+                            const uint64_t wy2[4] = {y01.x, y01.y, y23.x, y23.y}, wz2[4] = {z01.x, z01.y, z23.x, z23.y};
+                            uint64_t ay2 = 0ull;
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) {
+                                uint64_t az2 = f2_mul(wz2[0], x2[4 * j]);
+                                az2 = f2_fma(wz2[1], x2[4 * j + 1], az2);
+                                az2 = f2_fma(wz2[2], x2[4 * j + 2], az2);
+                                az2 = f2_fma(wz2[3], x2[4 * j + 3], az2);
+                                ay2 = j == 0 ? f2_mul(wy2[0], az2) : f2_fma(wy2[j], az2, ay2);
+                            }
+                            const uint64_t part = f2_mul(wx2, ay2);
+                            acc[p] = i == 0 ? part : f2_add(acc[p], part);
+                        }
+                }
+#pragma unroll
+                for (int p = 0; p < EW_ROWS / 2; ++p)
+                    if (2 * p < nr) {
+                        float v2[2];
+                        f2_unpack(acc[p], v2[0], v2[1]);
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const int q = 2 * p + h;
+                            if (q >= nr) break;
+                            const int r = __shfl_sync(FULL, row, q);
+                            float v = v2[h];
+                            if (pr < pr_end) {
+                                const int4 rec = eb.pq[pr];
+                                if (rec.x == c0 - p0 + q) {
+                                    v = eb_patch(eb, stage, lane, pr, rec, v);
+                                    ++pr;
+                                }
+                            }
+                            if (act) t[(uint32_t)r * 32u + lane] = v;
+                        }
+                    }
+            }
+        }
+        // every thread is done with the stage and with s_unit before the next unit's copies
+        __syncthreads();
+        if (tid == 0) s_unit = (int)atomicAdd(eb.ctr, 1u);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        u = s_unit;
+    }
+    // identity rows: t = x
+    if (act)
+        for (int64_t q = (int64_t)blockIdx.x * NW + warp; q < op.n_ident; q += (int64_t)gridDim.x * NW) {
+            const uint32_t r = (uint32_t)op.ident[q];
+            t[r * 32u + lane] = x[r * 32u + lane];
+        }
+    // the last block to finish resets the work counters for the next launch
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(eb.ctr + 1, 1u) == gridDim.x - 1) {
+            eb.ctr[0] = 0u;
+            eb.ctr[1] = 0u;
+            __threadfence();
+        }
+    }
+}
+
+// grid of k_ebrick32: every block resident at once (three per SM at the
+// largest stage), each taking units in turn
+static inline int ebrick_grid(const EBrick &eb) {
+    static int blocks_per_sm = -1;
+    static size_t smem_set = 0;
+    const size_t smem = (size_t)eb.stage_rows * 128u;
+    if (smem_set == 0) {
+        cudaFuncSetAttribute(k_ebrick32, cudaFuncAttributeMaxDynamicSharedMemorySize, EB_MAX_ROWS * 128);
+        smem_set = 1;
+    }
+    int b = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ebrick32, EB_THREADS, smem);
+    if (blocks_per_sm < 0) blocks_per_sm = b;
+    b = std::max(1, b);
+    const int64_t want = (int64_t)b * sm_count();
+    return (int)std::max<int64_t>(1, std::min<int64_t>(want, std::max<int64_t>(eb.n_units, 1)));
+}
+
+// k_ebrick32 applies: a schedule built and a 16-byte aligned x
+static inline bool ebrick_ok(const OpView<float> &op, const float *x) {
+    return op.eb.n_units > 0 && op.eb.stage_rows > 0 && ((uintptr_t)x % 16) == 0 && op.D * 32 <= (int64_t)UINT32_MAX;
+}
+
 // 1 slot: one thread per row, rows visited in base-point order so that the
 // threads of a warp that share a base read the same cache lines.
 template <class T>
@@ -491,9 +738,11 @@ __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__re
     }
 }
 
-// kernels one E pass launches
+// kernels one E pass launches (the brick-staged FP32 pass includes the patch)
 template <class T, int K>
 static inline int epass_kernels(const OpView<T> &op) {
+    if constexpr (K == 32 && sizeof(T) == 4)
+        if (op.eb.n_units > 0) return 1;
     return (K == 32 && op.n_pl > 0) ? 2 : 1;
 }
 
@@ -502,6 +751,10 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
     static_assert(K == 1 || K == 32, "slot widths 1 and 32");
     if constexpr (K == 32) {
         if constexpr (sizeof(T) == 4) {
+            if (ebrick_ok(op, x)) {
+                k_ebrick32<<<(unsigned)ebrick_grid(op.eb), EB_THREADS, (size_t)op.eb.stage_rows * 128u, st>>>(op, sl, ph, x, t);
+                return;
+            }
             const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_grp + 3) / 4, 32LL * sm_count()));
             k_epass32w<<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
         } else {

@@ -179,3 +179,29 @@ def test_golden_order_through_device_solver(gpu, oracle):
         errs.append(float(np.max(np.abs(uplot - spec["exact"](xp)))))
     order, _ = S.convergence_order(errs, S.DX_3D)
     assert abs(order - S.GOLDEN_SHIFTED_POISSON_SPHERE) < 1e-2
+
+
+@pytest.mark.parametrize("dx", [0.05, 0.025])
+def test_brick_staged_e_pass_equals_gather_pass_bitwise(gpu, dx):
+    """The brick-staged FP32 32-slot E pass (k_ebrick32: TMA-staged node bricks,
+    IBC patch in registers) gives the same bits as the gather pass it replaces
+    (k_epass32w then k_epatch32), which cpm_apply_device still runs for an input
+    that is not 16-byte aligned."""
+    import torch
+
+    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), two_circle_ibcs(gpu, dx))
+    gen = torch.Generator().manual_seed(9)
+    x = (torch.rand((O.D, 32), generator=gen, dtype=torch.float32) * 2 - 1).cuda()
+    buf = torch.empty(O.D * 32 + 4, dtype=torch.float32, device="cuda")
+    xm = buf[1:1 + O.D * 32].view(O.D, 32)  # 4 bytes past a 16-byte boundary
+    xm.copy_(x)
+    assert xm.data_ptr() % 16 == 4
+    t_new, y_new = torch.full_like(x, float("nan")), torch.empty_like(x)
+    t_old, y_old = torch.full_like(x, float("nan")), torch.empty_like(x)
+    torch.cuda.synchronize()
+    for _ in range(2):  # the second launch checks that the work counters were reset
+        O.apply_device(0.0, -1.0, 32, True, x.data_ptr(), t_new.data_ptr(), y_new.data_ptr())
+        O.apply_device(0.0, -1.0, 32, True, xm.data_ptr(), t_old.data_ptr(), y_old.data_ptr())
+        gpu.sync()
+        assert torch.equal(t_new, t_old)
+    assert _rel_inf(y_new.cpu().double().numpy(), y_old.cpu().double().numpy()) <= 1e-6
