@@ -1348,6 +1348,9 @@ static int build_brick_sched(cpm_opset_s *o) {
     CPM_TRY(o->eb_err.zero());
     o->eb_units = nu;
     o->eb_stage_rows = stage_rows;
+    EBrick e = o->ebrick();
+    CPM_TRY(ebrick_setup(e));
+    o->eb_grid = e.grid;
     return 0;
 }
 
@@ -1371,6 +1374,7 @@ EBrick cpm_opset_s::ebrick() const {
     e.err = eb_err.p;
     e.n_units = eb_units;
     e.stage_rows = eb_stage_rows;
+    e.grid = eb_grid;
     return e;
 }
 

@@ -41,7 +41,11 @@ struct EBrick {
     int *err;               // set to 1 when a stage copy did not arrive within the wait limit
     int64_t n_units;
     int stage_rows;         // rows of the largest stage
+    int grid;               // blocks of a launch: all resident at once
 };
+// sets k_ebrick32's shared-memory limit and the schedule's grid (at operator
+// build time, outside any stream capture)
+int ebrick_setup(EBrick &eb);
 
 template <class T>
 struct OpView {
@@ -565,7 +569,7 @@ struct cpm_opset_s {
     cpm::DBuf<unsigned int> eb_ctr;
     cpm::DBuf<int> eb_err;
     int64_t eb_units = 0;
-    int eb_stage_rows = 0;
+    int eb_stage_rows = 0, eb_grid = 1;
     cpm::EBrick ebrick() const;
     // host-side row layout for right-hand sides
     std::vector<uint8_t> h_identity;

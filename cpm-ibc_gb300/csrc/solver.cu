@@ -633,22 +633,33 @@ __global__ void __launch_bounds__(EB_THREADS, 3) k_ebrick32(OpView<float> op, co
     }
 }
 
-// grid of k_ebrick32: every block resident at once (three per SM at the
-// largest stage), each taking units in turn
-static inline int ebrick_grid(const EBrick &eb) {
-    static int blocks_per_sm = -1;
-    static size_t smem_set = 0;
-    const size_t smem = (size_t)eb.stage_rows * 128u;
-    if (smem_set == 0) {
-        cudaFuncSetAttribute(k_ebrick32, cudaFuncAttributeMaxDynamicSharedMemorySize, EB_MAX_ROWS * 128);
-        smem_set = 1;
+// k_ebrick32's dynamic shared-memory limit (set once) and the schedule's grid:
+// every block resident at once (three per SM at the largest stage), each
+// taking units in turn
+int ebrick_setup(EBrick &eb) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        CPM_CUDA_TRY(cudaFuncSetAttribute(k_ebrick32, cudaFuncAttributeMaxDynamicSharedMemorySize, EB_MAX_ROWS * 128));
+        attr_set = true;
     }
     int b = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ebrick32, EB_THREADS, smem);
-    if (blocks_per_sm < 0) blocks_per_sm = b;
+    CPM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ebrick32, EB_THREADS, (size_t)eb.stage_rows * 128u));
     b = std::max(1, b);
-    const int64_t want = (int64_t)b * sm_count();
-    return (int)std::max<int64_t>(1, std::min<int64_t>(want, std::max<int64_t>(eb.n_units, 1)));
+    eb.grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)b * sm_count(), std::max<int64_t>(eb.n_units, 1)));
+    return 0;
+}
+
+// the brick-staged E pass's error flag: a stage copy that did not arrive within
+// its wait limit (the flag is cleared when read)
+static int ebrick_status(cpm_opset_s *o) {
+    if (!o->eb_err.p) return 0;
+    int h = 0;
+    CPM_CUDA_TRY(cudaMemcpyAsync(&h, o->eb_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
+    if (!h) return 0;
+    CPM_CUDA_TRY(cudaMemsetAsync(o->eb_err.p, 0, sizeof(int), stream()));
+    CPM_CUDA_TRY(cudaMemsetAsync(o->eb_ctr.p, 0, 2 * sizeof(unsigned int), stream()));
+    return fail(CPM_ERR_TIMEOUT, "brick-staged E pass: a stage copy did not complete within the wait limit");
 }
 
 // k_ebrick32 applies: a schedule built and a 16-byte aligned x
@@ -752,7 +763,7 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
     if constexpr (K == 32) {
         if constexpr (sizeof(T) == 4) {
             if (ebrick_ok(op, x)) {
-                k_ebrick32<<<(unsigned)ebrick_grid(op.eb), EB_THREADS, (size_t)op.eb.stage_rows * 128u, st>>>(op, sl, ph, x, t);
+                k_ebrick32<<<(unsigned)op.eb.grid, EB_THREADS, (size_t)op.eb.stage_rows * 128u, st>>>(op, sl, ph, x, t);
                 return;
             }
             const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_grp + 3) / 4, 32LL * sm_count()));
@@ -1896,7 +1907,7 @@ static int solve_pass(cpm_solver_s *s, const SolveParams &P, const std::vector<c
     CPM_CUDA_TRY(cudaEventSynchronize(s->e1));
     *ms = 0;
     cudaEventElapsedTime(ms, s->e0, s->e1);
-    return 0;
+    return ebrick_status(s->op);
 }
 
 // Solve k right-hand sides.  A mixed-precision slot that does not converge
