@@ -749,11 +749,11 @@ __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__re
     }
 }
 
-// kernels one E pass launches (the brick-staged FP32 pass includes the patch)
+// kernels one E pass of x launches (the brick-staged FP32 pass includes the patch)
 template <class T, int K>
-static inline int epass_kernels(const OpView<T> &op) {
+static inline int epass_kernels(const OpView<T> &op, const T *x) {
     if constexpr (K == 32 && sizeof(T) == 4)
-        if (op.eb.n_units > 0) return 1;
+        if (ebrick_ok(op, x)) return 1;
     return (K == 32 && op.n_pl > 0) ? 2 : 1;
 }
 
@@ -776,7 +776,7 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
         const int64_t threads = op.n_ord + op.n_ident;
         k_epass1<T><<<(unsigned)((threads + BS - 1) / BS), BS, 0, st>>>(op, sl, ph, x, t);
     }
-    if (epass_kernels<T, K>(op) == 2) {
+    if (K == 32 && op.n_pl > 0) {  // the gather passes correct the IBC patch rows afterwards
         const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_pl + 3) / 4, 16LL * sm_count()));
         k_epatch32<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
     }
@@ -1829,8 +1829,8 @@ static inline long long graph_launches(const cpm_solver_s *s, const SolveParams 
     const int chunk = graph_chunk(s, P);
     // an iteration: 5 vector / L-pass kernels and two E passes; a Jacobi sweep: an E
     // pass and the sweep; a reliable update: 4 kernels and an FP64 E pass
-    const long long e32 = s->K == 32 ? epass_kernels<float, 32>(s->op->view<float>()) : 1;
-    const long long e64 = s->K == 32 ? epass_kernels<double, 32>(s->op->view<double>()) : 1;
+    const long long e32 = s->K == 32 ? epass_kernels<float, 32>(s->op->view<float>(), s->fy.p) : 1;
+    const long long e64 = s->K == 32 ? epass_kernels<double, 32>(s->op->view<double>(), s->x64.p) : 1;
     const long long eit = P.mixed ? e32 : e64;
     return (5LL + 2 * eit + (P.precond == 2 ? 2LL * (P.sweeps - 1) * (e64 + 1) : 0)) * chunk +
            (P.mixed ? (4LL + e64) * (chunk / P.refine_every) : 0);
@@ -2413,7 +2413,9 @@ extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslo
             k_lpass<double, 32><<<row_grid(D, 32), BS, 0, st>>>(v, m, n, x, t, y);
         }
     }
-    count_launches((kslots == 32 && op->n_pl > 0) ? 3 : 2);
+    count_launches(1 + (kslots == 32 ? (fp32 ? epass_kernels<float, 32>(op->view<float>(), (const float *)x_dev)
+                                              : epass_kernels<double, 32>(op->view<double>(), (const double *)x_dev))
+                                      : 1));
     CPM_CUDA_TRY(cudaGetLastError());
     return 0;
 }
@@ -2485,7 +2487,9 @@ extern "C" int cpm_apply_device_noalloc(cpm_opset_t op, double m, double n, int3
             k_lpass<double, 32><<<row_grid(D, 32), BS, 0, st>>>(v, m, n, x, tt, y);
         }
     }
-    count_launches((kslots == 32 && op->n_pl > 0) ? 3 : 2);
+    count_launches(1 + (kslots == 32 ? (fp32 ? epass_kernels<float, 32>(op->view<float>(), (const float *)x_dev)
+                                              : epass_kernels<double, 32>(op->view<double>(), (const double *)x_dev))
+                                      : 1));
     CPM_CUDA_TRY(cudaGetLastError());
     return 0;
 }
