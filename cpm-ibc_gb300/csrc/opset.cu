@@ -1250,7 +1250,9 @@ static int build_brick_sched(cpm_opset_s *o) {
         int64_t u0 = g;
         while (u0 < gend) {
             std::vector<int32_t> extra;
+            bool global_cols = false;  // this group's extra columns are read from global memory
             auto extra_slot = [&](int32_t col) -> uint32_t {
+                if (global_cols) return EB_GLOBAL | (uint32_t)col;
                 for (size_t e = 0; e < extra.size(); ++e)
                     if (extra[e] == col) return (uint32_t)(brick_rows + (int)e) * 128u;
                 extra.push_back(col);
@@ -1266,6 +1268,7 @@ static int build_brick_sched(cpm_opset_s *o) {
                 std::vector<uint2> ent;
                 std::vector<float> ew;
                 const size_t extra_before = extra.size();
+              retry:
                 for (int32_t pos = grp[h]; pos < grp[h + 1]; ++pos) {
                     const int32_t r = ord[pos];
                     const int32_t q = pl_of_row[r];
@@ -1285,10 +1288,18 @@ static int build_brick_sched(cpm_opset_s *o) {
                     rn.push_back(pl_neg[q]);
                 }
                 if (brick_rows + (int)extra.size() > EB_MAX_ROWS) {
-                    if (h == u0) return fail(CPM_ERR_UNSUPPORTED, "a base group's IBC patch reads more columns than a stage holds");
-                    extra.resize(extra_before);  // this group starts the next unit
-                    break;
+                    extra.resize(extra_before);
+                    if (h != u0) break;  // this group starts the next unit
+                    // alone it still overflows the stage: its patch reads its columns from global memory
+                    global_cols = true;
+                    rec.clear();
+                    rx.clear();
+                    rn.clear();
+                    ent.clear();
+                    ew.clear();
+                    goto retry;
                 }
+                global_cols = false;
                 g_pq[h] = (int32_t)pq.size();
                 pq.insert(pq.end(), rec.begin(), rec.end());
                 pq_xval.insert(pq_xval.end(), rx.begin(), rx.end());

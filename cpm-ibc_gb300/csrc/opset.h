@@ -26,6 +26,9 @@ enum RowFlags : uint8_t {
 // groups from shared memory.  Offsets are bytes into the unit's stage, one
 // 128-byte row (32 FP32 slots) per staged node.
 constexpr int EB_MAX_ROWS = 560;  // stage rows of one unit: 70 KB of FP32 32-slot rows, three blocks per SM
+// a patch column offset with this bit set is a row index of x in global memory
+// (the columns of a group whose patch alone overflows the stage)
+constexpr uint32_t EB_GLOBAL = 0x80000000u;
 struct EBrick {
     const int4 *u_hdr;      // per unit {first group, end group, first extra row, end extra row}
     const int2 *u_brick;    // per unit 8 x {first node, node count}
@@ -33,6 +36,7 @@ struct EBrick {
     const uint32_t *gslot;  // 64 per group: stage offset of stencil node s = 16 i + 4 j + k
     const int32_t *g_pq;    // per group: first patch record (n_grp + 1 entries)
     const int4 *pq;         // patch record {row position in the group, first entry, end entry, extra-column offset or -1}
+                            // (offsets of moved and extra columns may carry EB_GLOBAL)
     const float *pq_xval;   // the extra entry's value
     const uint8_t *pq_neg;  // 1: the row is negated (2nd-order Dirichlet DOF rows)
     const uint2 *pqe;       // patch entry {offset of the bulk stencil node, offset of the moved column}

@@ -427,25 +427,31 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
                  :: "r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
 }
 
-// waits for phase `parity` of mbarrier `bar` to complete, polling at most
-// ~2^22 times with a short sleep (about a second); false if it did not
+// waits for phase `parity` of mbarrier `bar` to complete: at most 2^19 waits
+// of at most ~2 us each (the suspend-time hint), about a second in all;
+// false if it did not complete
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 22); ++it) {
+    for (int it = 0; it < (1 << 19); ++it) {
         uint32_t done;
-        asm volatile("{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(done) : "r"(bar), "r"(parity), "r"(2000) : "memory");
         if (done) return true;
-        if (it > 64) __nanosleep(256);
     }
     return false;
 }
 
 // k_epatch32's correction of one patched row, lane = slot, from the stage:
 // sign (bulk + sum_e w_e (x[new_e] - x[old_e])) + xval x[xcol]
-__device__ __forceinline__ float eb_patch(const EBrick &eb, const char *stage, int lane, int pr, const int4 &rec, float acc) {
+// a moved or extra column's value: from the stage, or from x where the offset carries EB_GLOBAL
+__device__ __forceinline__ float eb_col(const char *stage, const float *__restrict__ x, uint32_t off, int lane) {
+    return (off & EB_GLOBAL) ? x[(off & ~EB_GLOBAL) * 32u + lane] : *(const float *)(stage + off + 4 * lane);
+}
+
+__device__ __forceinline__ float eb_patch(const EBrick &eb, const char *stage, const float *__restrict__ x, int lane, int pr,
+                                          const int4 &rec, float acc) {
     const float xv = eb.pq_xval[pr];
     const bool neg = eb.pq_neg[pr] != 0;
-    const float xe = rec.w >= 0 ? *(const float *)(stage + rec.w + 4 * lane) : 0.f;
+    const float xe = rec.w != -1 ? eb_col(stage, x, (uint32_t)rec.w, lane) : 0.f;
     for (int base = rec.y; base < rec.z; base += 32) {
         const int cnt = min(32, rec.z - base);
         uint32_t oo = 0, nn = 0;
@@ -464,7 +470,7 @@ __device__ __forceinline__ float eb_patch(const EBrick &eb, const char *stage, i
                 const uint32_t nk = (uint32_t)__shfl_sync(FULL, nn, k & 31), ok = (uint32_t)__shfl_sync(FULL, oo, k & 31);
                 ww[u] = __shfl_sync(FULL, w, k & 31);
                 const bool valid = k < cnt;
-                xn[u] = valid ? *(const float *)(stage + nk + 4 * lane) : 0.f;
+                xn[u] = valid ? eb_col(stage, x, nk, lane) : 0.f;
                 xo[u] = valid ? *(const float *)(stage + ok + 4 * lane) : 0.f;
             }
 #pragma unroll
@@ -473,7 +479,7 @@ __device__ __forceinline__ float eb_patch(const EBrick &eb, const char *stage, i
         }
     }
     if (neg) acc = -acc;
-    if (rec.w >= 0) acc += xv * xe;
+    if (rec.w != -1) acc += xv * xe;
     return acc;
 }
 
@@ -600,7 +606,7 @@ __global__ void __launch_bounds__(EB_THREADS, 3) k_ebrick32(OpView<float> op, co
                             if (pr < pr_end) {
                                 const int4 rec = eb.pq[pr];
                                 if (rec.x == c0 - p0 + q) {
-                                    v = eb_patch(eb, stage, lane, pr, rec, v);
+                                    v = eb_patch(eb, stage, x, lane, pr, rec, v);
                                     ++pr;
                                 }
                             }
