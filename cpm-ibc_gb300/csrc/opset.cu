@@ -244,7 +244,14 @@ struct IBCData {
     std::vector<int64_t> dof_sub;       // N -> dof index or -1
     std::vector<double> dof_cp, dof_cpbar, dof_dir, dof_cpdiff;
     QueryRows dof_rows;                 // E_ibc stencils (at cp or cp-bar)
-    bool order2 = false, dirichlet = true;
+    std::vector<uint8_t> side;          // per DOF: which side of the curve (1 or 2; 1 when not oriented)
+    std::vector<int64_t> dir_sub;       // per DOF: index among the Dirichlet DOFs, or -1
+    int64_t n_dir = 0;                  // Dirichlet DOFs of a 2nd-order IBC (value rows)
+    bool order2 = false;
+    bool has_dir2 = false;              // 2nd order with a Dirichlet side (IBCSubsets::TotalDOFs)
+    // boundary type of DOF i's side (IBCMetaData::boundary_type[which_side - 1])
+    int bc_type(size_t i) const { return desc.boundary_type[(side[i] == 2) ? 1 : 0]; }
+    bool dof_dirichlet(size_t i) const { return bc_type(i) == 0; }
 };
 
 // Geometry::InterpolateUnorientedVectorFromNeighbours (src/Geometry.cpp:146-188).
@@ -339,6 +346,30 @@ static std::vector<Eig3> subset_jcp(const HostTube &ht, const IBCData &ib, const
         out[i] = sym_eig3(A);
     }
     return out;
+}
+
+// Geometry::UnorientedSurfaceNormals (src/Geometry.cpp:101-126) with its defaults
+// (normalised, zero_tol 1e-15): x - cp, interpolated from the neighbours where it
+// vanishes, then normalised (zero below the tolerance, src/VectorMath.cpp:40-56).
+// The frames of an IBC with use_Jcp_surface_normals off use these.
+static std::vector<double> unoriented_normals(const HostTube &ht) {
+    const int64_t N = ht.N;
+    std::vector<double> n(3 * N);
+    for (int64_t q = 0; q < N; ++q) {
+        double x[3];
+        ht.x(q, x);
+        for (int k = 0; k < 3; ++k) n[3 * q + k] = x[k] - ht.cp[3 * q + k];
+    }
+    std::vector<int64_t> ident(N);
+    for (int64_t q = 0; q < N; ++q) ident[q] = q;
+    const double zero_tol = 1e-15;
+    for (int64_t q = 0; q < N; ++q)
+        if (std::sqrt(hdot(&n[3 * q], &n[3 * q])) < zero_tol) interp_from_neighbours(ht, n, ident, ident, (size_t)q, zero_tol);
+    for (int64_t q = 0; q < N; ++q) {
+        const double nn = std::sqrt(hdot(&n[3 * q], &n[3 * q]));
+        for (int k = 0; k < 3; ++k) n[3 * q + k] = nn > zero_tol ? n[3 * q + k] / nn : 0.0;
+    }
+    return n;
 }
 
 // First parameterisation point of an IBC (IBCSubset::FindStartingPoint uses xp()[0]):
@@ -441,8 +472,7 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
     const double r = ht.radius;
     ib.desc = desc;
     ib.order2 = desc.boundary_order == 2;
-    if (desc.is_oriented) return fail(CPM_ERR_UNSUPPORTED, "oriented IBCs are not implemented on the device path");
-    ib.dirichlet = desc.boundary_type[0] == 0;
+    ib.has_dir2 = ib.order2 && (desc.boundary_type[0] == 0 || desc.boundary_type[1] == 0);
     // K6: IBC closest point + distance of every tube node (bounded at 2r for meshes)
     SurfaceObj s;
     CPM_TRY(surface_init(s, &desc, r));
@@ -512,16 +542,50 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
                 ib.tag_bdy[i] = 2;
         }
     }
-    // ComputeCPdiff (src/IBCSubset.cpp:156-187) with the S-perp fix-up.
+    // ComputeCPdiff (src/IBCSubset.cpp:156-187) with the S-perp fix-up: cp_S(x) - cp_c,
+    // or, at an open polyline's end points when use_cp_diff_directions is on,
+    // cp_c(p) - cp_S(p) at the reflection p = 2 cp_c - x
     ib.tag_cpdiff.resize(3 * nt);
     for (size_t i = 0; i < nt; ++i) {
         int64_t q = ib.tag_set[i];
         for (int k = 0; k < 3; ++k) ib.tag_cpdiff[3 * i + k] = ht.cp[3 * q + k] - ib.tag_cpc[3 * i + k];
     }
-    if (desc.use_cp_diff_directions) return fail(CPM_ERR_UNSUPPORTED, "cp_diff directions are not implemented on the device path");
+    if (desc.use_cp_diff_directions) {
+        std::vector<size_t> ends;
+        std::vector<double> proj;
+        for (size_t i = 0; i < nt; ++i)
+            if (ib.tag_bdy[i] > 0) {
+                double x[3];
+                ht.x(ib.tag_set[i], x);
+                ends.push_back(i);
+                for (int k = 0; k < 3; ++k) proj.push_back(2.0 * ib.tag_cpc[3 * i + k] - x[k]);
+            }
+        if (!ends.empty()) {
+            const int64_t ne = (int64_t)ends.size();
+            DBuf<double> dp, dcs, dds, dcc, ddc;
+            CPM_TRY(dp.upload(proj));
+            CPM_TRY(dcs.alloc(3 * ne));
+            CPM_TRY(dds.alloc(ne));
+            CPM_TRY(dcc.alloc(3 * ne));
+            CPM_TRY(ddc.alloc(ne));
+            const double inf = std::numeric_limits<double>::infinity();
+            CPM_TRY(closest_points_dev(t->surf.params(), ne, dp.p, dcs.p, dds.p, inf));
+            CPM_TRY(closest_points_dev(s.params(), ne, dp.p, dcc.p, ddc.p, inf));
+            std::vector<double> cps, cpc2;
+            CPM_TRY(dcs.download(cps, 3 * ne));
+            CPM_TRY(dcc.download(cpc2, 3 * ne));
+            for (int64_t e = 0; e < ne; ++e)
+                for (int k = 0; k < 3; ++k) ib.tag_cpdiff[3 * ends[e] + k] = cpc2[3 * e + k] - cps[3 * e + k];
+        }
+    }
     for (size_t i = 0; i < nt; ++i)
         if (std::sqrt(hdot(&ib.tag_cpdiff[3 * i], &ib.tag_cpdiff[3 * i])) < desc.on_ibc_tolerance)
             interp_from_neighbours(ht, ib.tag_cpdiff, ib.tag_set, ib.tag_sub, i, desc.on_ibc_tolerance);
+    if (desc.use_cp_diff_directions) {
+        // IBCSubset::ComputeSubset: the directions are cp_diff itself
+        ib.tag_dir = ib.tag_cpdiff;
+        ib.tag_binormal.assign(3 * nt, 0.0);
+    } else {
     // ComputeFrameBasedDirections (src/IBCSubset.cpp:190-268)
     QueryRows qc;
     CPM_TRY(query_weights(t, ib.tag_cpc, qc));
@@ -544,6 +608,7 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
             }
         }
     }
+    }
     // IBCDOFSubset::ComputeDOFSubset (src/IBCDOFSubset.cpp:10-93)
     const double rad = desc.dof_radius_scale * r;
     ib.dof_sub.assign(N, -1);
@@ -560,6 +625,74 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
             }
         }
     const size_t nd = ib.dof_set.size();
+    // which_side (OrientSubset, src/IBCDOFSubset.cpp:128-227): a breadth-first walk
+    // over the DOF subset from its first DOF off the curve, a neighbour takes the
+    // other side when its direction points against the current DOF's; then the
+    // sides are swapped if the DOF nearest point_on_side1 (among those 2 dx or
+    // more from the curve, on the point's side of it) came out on side 1
+    ib.side.assign(nd, 1);
+    if (desc.is_oriented && nd > 0) {
+        std::fill(ib.side.begin(), ib.side.end(), (uint8_t)0);
+        size_t start = 0;
+        for (size_t i = 0; i < nd; ++i)
+            if (std::sqrt(hdot(&ib.dof_dir[3 * i], &ib.dof_dir[3 * i])) >= desc.on_ibc_tolerance) {
+                start = i;
+                break;
+            }
+        ib.side[start] = 1;
+        std::vector<size_t> queue{start};
+        std::vector<uint8_t> seen(nd, 0);
+        for (size_t h = 0; h < queue.size(); ++h) {
+            const size_t f = queue[h];
+            if (seen[f]) continue;
+            seen[f] = 1;
+            for (int d = 0; d < 6; ++d) {
+                const int nb = ht.nbr(ib.dof_set[f], d);
+                if (nb < 0) continue;
+                const int64_t ns = ib.dof_sub[nb];
+                if (ns < 0) continue;
+                if (ib.side[ns] == 0)
+                    ib.side[ns] = hdot(&ib.dof_dir[3 * f], &ib.dof_dir[3 * ns]) < 0 ? (ib.side[f] == 1 ? 2 : 1) : ib.side[f];
+                queue.push_back((size_t)ns);
+            }
+        }
+        if (desc.has_point_on_side1) {
+            const double *ps = desc.point_on_side1;
+            DBuf<double> dps, dcpc, ddc;
+            CPM_TRY(dps.upload(ps, 3));
+            CPM_TRY(dcpc.alloc(3));
+            CPM_TRY(ddc.alloc(1));
+            CPM_TRY(closest_points_dev(s.params(), 1, dps.p, dcpc.p, ddc.p, std::numeric_limits<double>::infinity()));
+            std::vector<double> cpc_ps;
+            CPM_TRY(dcpc.download(cpc_ps, 3));
+            const double cpd[3] = {ps[0] - cpc_ps[0], ps[1] - cpc_ps[1], ps[2] - cpc_ps[2]};
+            size_t nearest = 0;
+            double best = std::numeric_limits<double>::max();
+            for (size_t i = 0; i < nd; ++i) {
+                double xi[3];
+                ht.x(ib.dof_set[i], xi);
+                double dd = 0.0;
+                for (int k = 0; k < 3; ++k) dd += (ps[k] - xi[k]) * (ps[k] - xi[k]);
+                dd = std::sqrt(dd);
+                const double *cd = &ib.dof_cpdiff[3 * i];
+                if (dd < best && std::sqrt(hdot(cd, cd)) >= 2.0 * ht.dx && hdot(cpd, cd) > 0) {
+                    best = dd;
+                    nearest = i;
+                }
+            }
+            if (ib.side[nearest] == 1)
+                for (auto &w : ib.side) w = (w == 1) ? 2 : (w == 2 ? 1 : w);
+        }
+        // a DOF the walk did not reach (a DOF subset in pieces) keeps side 1
+        for (auto &w : ib.side)
+            if (w == 0) w = 1;
+    }
+    // the Dirichlet DOFs of a 2nd-order IBC, in DOF order (their value rows)
+    ib.dir_sub.assign(nd, -1);
+    ib.n_dir = 0;
+    if (ib.has_dir2)
+        for (size_t i = 0; i < nd; ++i)
+            if (ib.dof_dirichlet(i)) ib.dir_sub[i] = ib.n_dir++;
     if (ib.order2) {
         // cp-bar = cp_S(2 cp_c - x)  (src/IBCDOFSubset.cpp:63-73)
         std::vector<double> proj(3 * nd);
@@ -582,6 +715,10 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
     }
     return 0;
 }
+
+// IBCDOFSubset::which_side as the reference hands it to the boundary-value
+// function: the side of an oriented IBC's DOF, 0 when the IBC is not oriented
+static inline int32_t desc_side(const IBCData &ib, size_t i) { return ib.desc.is_oriented ? (int32_t)ib.side[i] : 0; }
 
 // tag of the stencil entry (row director dir_r, column node col) for one IBC
 // (TagStencils, src/IBCMatrixManipulations.cpp:424-463).
@@ -665,22 +802,25 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
     HostTube ht;
     CPM_TRY(ht.load(t));
     const int64_t N = ht.N;
-    bool need_normals = false;
+    // the surface normals on the tube the IBC frames use: eigenvector 0 of the
+    // symmetrised closest-point Jacobian, or x - cp (use_Jcp_surface_normals off)
+    bool need_normals = false, need_xn = false;
     for (int c = 0; c < n_ibc; ++c)
-        if (!descs[c].use_cp_diff_directions) need_normals = true;
-    std::vector<double> normals;
+        if (!descs[c].use_cp_diff_directions) (descs[c].use_Jcp_surface_normals ? need_normals : need_xn) = true;
+    std::vector<double> normals, normals_x;
     if (need_normals) {
         CPM_TRY(tube_normals(o, normals));
         CPM_TRY(o->normals.upload(normals));
     }
+    if (need_xn) normals_x = unoriented_normals(ht);
     DBuf<double> xdev;
     CPM_TRY(xdev.alloc(3 * N));
     k_node_coords<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, t->key.p, t->g.xstart, t->g.dx, xdev.p);
     CPM_CUDA_TRY(cudaGetLastError());
     std::vector<IBCData> ibs(n_ibc);
     for (int c = 0; c < n_ibc; ++c)
-        CPM_TRY(build_ibc_data(t, ht, descs[c], normals, xdev, ovr ? &ovr->ibc[c] : nullptr, ovr ? &ovr->surface : nullptr,
-                               ibs[c]));
+        CPM_TRY(build_ibc_data(t, ht, descs[c], descs[c].use_Jcp_surface_normals ? normals : normals_x, xdev,
+                               ovr ? &ovr->ibc[c] : nullptr, ovr ? &ovr->surface : nullptr, ibs[c]));
     o->ibc_desc.assign(descs, descs + n_ibc);
     o->ibc_verts.assign(n_ibc, {});
     o->ibc_prims.assign(n_ibc, {});
@@ -701,17 +841,19 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
     o->dcol_start.assign(n_ibc, 0);
     if (n_ibc > 0) o->col_start[0] = o->dcol_start[0] = N;
     for (int c = 1; c < n_ibc; ++c) {
+        // the reference numbers an order-1 IBC's Dirichlet value rows from
+        // IdentityRowsStart too (IBCMatrixManipulations::DirichletValueRow), which is
+        // past the last row once another IBC is 2nd order: mixed orders are refused
         if (ibs[c].order2 != ibs[0].order2)
             return fail(CPM_ERR_UNSUPPORTED, "IBCs of mixed boundary order are not implemented on the device path");
         o->col_start[c] = o->col_start[c - 1] + (int64_t)ibs[c - 1].dof_set.size();
-        int64_t prev_dirichlet = (ibs[c - 1].dirichlet && ibs[c - 1].order2) ? (int64_t)ibs[c - 1].dof_set.size() : 0;
-        if (ibs[c].dirichlet && ibs[c].order2) o->dcol_start[c] = o->dcol_start[c - 1] + prev_dirichlet;
+        if (ibs[c].has_dir2) o->dcol_start[c] = o->dcol_start[c - 1] + ibs[c - 1].n_dir;
     }
     int64_t total = 0, num2 = 0, idstart = 0;
     for (int c = 0; c < n_ibc; ++c) {
-        if (ibs[c].dirichlet && ibs[c].order2) {
+        if (ibs[c].has_dir2) {
             idstart += 1;
-            num2 += (int64_t)ibs[c].dof_set.size();
+            num2 += ibs[c].n_dir;
         }
         total += (int64_t)ibs[c].dof_set.size();
     }
@@ -722,7 +864,7 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
     const int64_t D = N + total + num2;
     o->D = D;
     auto value_row = [&](int c, int64_t i) -> int64_t {  // DirichletValueRow
-        if (ibs[c].order2) return idstart + i + o->dcol_start[c];
+        if (ibs[c].order2) return idstart + ibs[c].dir_sub[i] + o->dcol_start[c];
         return idstart + i + o->col_start[c];
     };
 
@@ -744,7 +886,7 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
         std::copy(tw.begin(), tw.end(), w.begin());
     }
     std::vector<uint8_t> ident(D, 0);
-    std::vector<int32_t> kind(D, 3), rowibc(D, -1);
+    std::vector<int32_t> kind(D, 3), rowibc(D, -1), rowside(D, 0);
     std::vector<double> point(3 * D, 0.0);
     for (int64_t q = 0; q < N; ++q) {
         kind[q] = 0;
@@ -826,7 +968,8 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
             const int64_t node = ib.dof_set[i];
             for (int k = 0; k < 3; ++k) point[3 * row + k] = ib.dof_cp[3 * i + k];
             rowibc[row] = c;
-            if (ib.dirichlet && !ib.order2) {
+            rowside[row] = desc_side(ib, i);
+            if (ib.dof_dirichlet(i) && !ib.order2) {
                 // order-1 Dirichlet: identity DOF rows carrying the value.  Their L row
                 // is still assembled (below): the reference's Lfull holds it, and only
                 // identity_rows makes the solve skip it
@@ -860,7 +1003,7 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
             nmoved += (int64_t)etarget.size();
             uint8_t f = F_LCSR;
             if (emask) f |= F_EMOVE;
-            if (ib.dirichlet) {
+            if (ib.dof_dirichlet(i)) {
                 f |= F_ENEG | F_EXTRA;
                 p_xcol.push_back((int32_t)value_row(c, i));
                 p_xval.push_back(2.0);
@@ -897,12 +1040,13 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
         ldiag.push_back(0.0);
     }
     for (int c = 0; c < n_ibc; ++c)
-        if (ibs[c].dirichlet)
-            for (int64_t i = 0; i < (int64_t)ibs[c].dof_set.size(); ++i) {
+        for (int64_t i = 0; i < (int64_t)ibs[c].dof_set.size(); ++i)
+            if (ibs[c].dof_dirichlet(i)) {
                 int64_t vr = value_row(c, i);
                 ident[vr] = 1;
                 kind[vr] = 2;
                 rowibc[vr] = c;
+                rowside[vr] = desc_side(ibs[c], i);
                 for (int k = 0; k < 3; ++k) point[3 * vr + k] = ibs[c].dof_cp[3 * i + k];
             }
     if ((int64_t)lptr.size() != D - N + 1) return fail(CPM_ERR_CUDA, "internal: IBC row count mismatch");
@@ -941,6 +1085,7 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
     o->h_identity = ident;
     o->h_kind = kind;
     o->h_ibc = rowibc;
+    o->h_side = rowside;
     o->h_point = point;
     o->tag_set.resize(n_ibc);
     o->dof_set.resize(n_ibc);
@@ -1490,6 +1635,12 @@ extern "C" int cpm_opset_rows(cpm_opset_t o, uint8_t *identity, int32_t *kind, i
     return 0;
 }
 
+extern "C" int cpm_opset_row_sides(cpm_opset_t o, int32_t *side) {
+    if (!o || !side) return fail(CPM_ERR_INVALID_ARG, "null argument");
+    for (int64_t r = 0; r < o->D; ++r) side[r] = (r < (int64_t)o->h_side.size()) ? o->h_side[r] : 0;
+    return 0;
+}
+
 extern "C" int cpm_opset_ibc_sizes(cpm_opset_t o, int32_t c, int64_t *s) {
     if (!o || c < 0 || c >= o->n_ibc || !s) return fail(CPM_ERR_INVALID_ARG, "invalid IBC index");
     s[0] = (int64_t)o->tag_set[c].size();
@@ -1612,16 +1763,17 @@ extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp
     CPM_TRY(ht.load(t));
     const int64_t N = ht.N;
     const double r = ht.radius;
-    std::vector<double> normals;
-    bool need_normals = false;
+    std::vector<double> normals, normals_x;
+    bool need_normals = false, need_xn = false;
     for (int c = 0; c < n_ibc; ++c)
-        if (!op->ibc_desc[c].use_cp_diff_directions) need_normals = true;
+        if (!op->ibc_desc[c].use_cp_diff_directions) (op->ibc_desc[c].use_Jcp_surface_normals ? need_normals : need_xn) = true;
     if (need_normals) {
         if (op->normals.n >= (size_t)(3 * N))
             CPM_TRY(op->normals.download(normals, 3 * N));
         else
             CPM_TRY(tube_normals(op, normals));
     }
+    if (need_xn) normals_x = unoriented_normals(ht);
     DBuf<double> xdev;
     CPM_TRY(xdev.alloc(3 * N));
     k_node_coords<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, t->key.p, t->g.xstart, t->g.dx, xdev.p);
@@ -1629,8 +1781,8 @@ extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp
     std::vector<IBCData> ibs(n_ibc);
     const CpOverrides *ovr = op->cp_ovr.get();
     for (int c = 0; c < n_ibc; ++c)
-        CPM_TRY(build_ibc_data(t, ht, op->ibc_desc[c], normals, xdev, ovr ? &ovr->ibc[c] : nullptr, ovr ? &ovr->surface : nullptr,
-                               ibs[c]));
+        CPM_TRY(build_ibc_data(t, ht, op->ibc_desc[c], op->ibc_desc[c].use_Jcp_surface_normals ? normals : normals_x, xdev,
+                               ovr ? &ovr->ibc[c] : nullptr, ovr ? &ovr->surface : nullptr, ibs[c]));
     std::vector<double> hx(xp, xp + 3 * n);
     DBuf<double> dxp;
     CPM_TRY(dxp.upload(hx));

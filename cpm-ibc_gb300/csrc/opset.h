@@ -577,7 +577,7 @@ struct cpm_opset_s {
     cpm::EBrick ebrick() const;
     // host-side row layout for right-hand sides
     std::vector<uint8_t> h_identity;
-    std::vector<int32_t> h_kind, h_ibc;
+    std::vector<int32_t> h_kind, h_ibc, h_side;
     std::vector<double> h_point;
     // IBC subsets (device tube indices, reference BFS order)
     std::vector<std::vector<int64_t>> tag_set, dof_set;

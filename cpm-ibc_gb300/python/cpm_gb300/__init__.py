@@ -161,6 +161,7 @@ def lib():
         L.cpm_ibc_plot_points.argtypes = [P(SurfaceDesc), vp, vp]
         L.cpm_opset_sizes.argtypes = [vp, vp]
         L.cpm_opset_rows.argtypes = [vp] * 5
+        L.cpm_opset_row_sides.argtypes = [vp, vp]
         L.cpm_opset_ibc_sizes.argtypes = [vp, ctypes.c_int32, vp]
         L.cpm_opset_ibc_export.argtypes = [vp, ctypes.c_int32, vp, vp, vp]
         L.cpm_opset_export_csr.argtypes = [vp, ctypes.c_int32, vp, vp, vp, vp]
@@ -314,7 +315,9 @@ class OpSet:
         ibc = np.zeros(D, np.int32)
         point = np.zeros((D, 3))
         _check(lib().cpm_opset_rows(self.h, _p(ident), _p(kind), _p(ibc), _p(point)))
-        return dict(identity=ident.astype(bool), kind=kind, ibc=ibc, point=point)
+        side = np.zeros(D, np.int32)
+        _check(lib().cpm_opset_row_sides(self.h, _p(side)))
+        return dict(identity=ident.astype(bool), kind=kind, ibc=ibc, point=point, side=side)
 
     def ibc_subsets(self, c):
         s = np.zeros(5, np.int64)

@@ -190,6 +190,12 @@ int cpm_opset_sizes(cpm_opset_t op, int64_t *sizes);
  * closest point), 2 Dirichlet value row (IBC value), 3 other.  point: 3*D. */
 int cpm_opset_rows(cpm_opset_t op, uint8_t *identity, int32_t *kind, int32_t *ibc, double *point);
 
+/* Side of the curve of every row (IBCDOFSubset::which_side, src/IBCDOFSubset.cpp:128-227):
+ * 1 or 2 on an IBC's DOF and Dirichlet value rows (always 1 unless the IBC is
+ * oriented), 0 on other rows.  PoissonWithIBC::GetRHS passes it to the boundary
+ * value function (problems/PoissonWithIBC.cpp:92-133). */
+int cpm_opset_row_sides(cpm_opset_t op, int32_t *side);
+
 /* IBC subsets of IBC c (IBCSubset / IBCDOFSubset, src/IBCSubset.h, src/IBCDOFSubset.h):
  * sizes [tagging, dof, column start, dirichlet column start, identity rows start]
  * and the subsets as device tube indices in the reference's BFS order. */

@@ -352,6 +352,8 @@ class SystemOperator {
         ibc_.resize(D);
         std::vector<Scalar> pt(3 * D);
         check(cpm_opset_rows(o, ident.data(), kind_.data(), ibc_.data(), pt.data()));
+        side_.resize(D);
+        check(cpm_opset_row_sides(o, side_.data()));
         // reference row r -> device row
         dev_.resize(D);
         for (size_t r = 0; r < D; ++r) dev_[r] = r < (size_t)N_ ? tube.device_index()[r] : (int64_t)r;
@@ -374,6 +376,8 @@ class SystemOperator {
     // IBC; the point its right-hand side is evaluated at
     int kind(size_t r) const { return kind_[(size_t)dev_[r]]; }
     int ibc(size_t r) const { return ibc_[(size_t)dev_[r]]; }
+    // IBCDOFSubset::which_side of an IBC row (1 or 2 on an oriented IBC, 0 otherwise)
+    size_t side(size_t r) const { return (size_t)side_[(size_t)dev_[r]]; }
     const Point3 &point(size_t r) const { return point_[r]; }
     VectorX to_device(const VectorX &ref) const {
         VectorX d(ref.size());
@@ -413,7 +417,7 @@ class SystemOperator {
     std::unique_ptr<cpm_opset_s, Del> h_;
     int64_t D_ = 0, N_ = 0, total_ibc_dofs_ = 0, n_ibc_ = 0;
     std::vector<int64_t> dev_;
-    std::vector<int32_t> kind_, ibc_;
+    std::vector<int32_t> kind_, ibc_, side_;
     std::vector<Point3> point_;
     std::vector<bool> identity_;
 };
@@ -488,7 +492,7 @@ class PoissonWithIBC {
     VectorX GetRHS(const SourceFn &f, const IBCFn &ibc_exact) const {
         VectorX b(op_.rows(), 0.0);
         for (size_t r = 0; r < b.size(); ++r)
-            b[r] = op_.kind(r) == 2 ? ibc_exact((size_t)op_.ibc(r), 0, op_.point(r)) : f(op_.point(r));
+            b[r] = op_.kind(r) == 2 ? ibc_exact((size_t)op_.ibc(r), op_.side(r), op_.point(r)) : f(op_.point(r));
         return b;
     }
     VectorX Solve(const VectorX &rhs) { return sv_.Solve(rhs); }
@@ -612,7 +616,7 @@ class HeatWithIBC {
     // SetDirichletValue (problems/HeatWithIBC.cpp:62-85)
     void set_dirichlet(VectorX &ufull, const IBCFn &ibc_exact) const {
         for (size_t r = 0; r < ufull.size(); ++r)
-            if (op_.kind(r) == 2) ufull[r] = ibc_exact((size_t)op_.ibc(r), 0, op_.point(r));
+            if (op_.kind(r) == 2) ufull[r] = ibc_exact((size_t)op_.ibc(r), op_.side(r), op_.point(r));
     }
     Tube tube_;
     SystemOperator op_;
@@ -644,7 +648,7 @@ class ReactionDiffusionWithIBC {
     // SetDirichletValue (problems/ReactionDiffusionWithIBC.cpp:60-90)
     void set_dirichlet(VectorX &ufull, const IBCFn &ibc_exact) const {
         for (size_t r = 0; r < ufull.size(); ++r)
-            if (op_.kind(r) == 2) ufull[r] = ibc_exact((size_t)op_.ibc(r), 0, op_.point(r));
+            if (op_.kind(r) == 2) ufull[r] = ibc_exact((size_t)op_.ibc(r), op_.side(r), op_.point(r));
     }
     Tube tube_;
     SystemOperator op_;

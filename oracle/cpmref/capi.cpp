@@ -267,6 +267,25 @@ int cpmref_rows_export(void *hp, uint8_t *identity, int32_t *kind, int32_t *ibc,
     return 0;
 }
 
+// IBCDOFSubset::which_side of every IBC DOF row and Dirichlet value row (0 elsewhere),
+// as PoissonWithIBC::GetRHS hands it to the boundary-value function
+int cpmref_row_sides(void *hp, int32_t *side) {
+    Problem &P = *((Handle *)hp)->prob;
+    for (size_t r = 0; r < P.D(); ++r) side[r] = 0;
+    if (!P.has_ibc) return 0;
+    for (size_t c = 0; c < P.ibc.NumIBCs(); ++c) {
+        const IBCDOFSubset &dof = P.ibc.DOFSubset()[c];
+        const IBCMeta &mc = P.ibc.meta(c);
+        for (size_t i = 0; i < dof.size(); ++i) {
+            const int32_t w = (int32_t)dof.which_side()[i];
+            side[i + P.ibc.IBCColumnStartIndex(c)] = w;
+            const size_t bc = mc.is_oriented ? dof.which_side()[i] - 1 : 0;
+            if (mc.boundary_type[bc] == 0) side[DirichletValueRow(P.ibc, c, i)] = w;
+        }
+    }
+    return 0;
+}
+
 int cpmref_xp_export(void *hp, double *xp) {
     Problem &P = *((Handle *)hp)->prob;
     const auto &v = P.tube.surface().xp();

@@ -161,6 +161,29 @@ std::vector<V3> NormalsFromJcp(const Tube &t) {
     return n;
 }
 
+// Geometry::UnorientedSurfaceNormals (src/Geometry.cpp:101-126) with its defaults
+// (normalised, zero_tol 1e-15): x - cp, interpolated from the neighbours where it
+// vanishes, then Normalize (src/VectorMath.cpp:40-56: zero below the tolerance).
+std::vector<V3> UnorientedSurfaceNormals(const Tube &t) {
+    const size_t N = t.nNodes();
+    std::vector<V3> n(N);
+    for (size_t i = 0; i < N; ++i) n[i] = Sub(t.x()[i], t.cpx()[i]);
+    std::vector<size_t> s2(N);
+    std::vector<int64_t> s1(N);
+    for (size_t i = 0; i < N; ++i) {
+        s1[i] = (int64_t)i;
+        s2[i] = i;
+    }
+    const double zero_tol = 1e-15;
+    for (size_t i = 0; i < N; ++i)
+        if (Norm(n[i]) < zero_tol) InterpolateUnorientedVectorFromNeighbours(t, n, s2, s1, i, zero_tol);
+    for (size_t i = 0; i < N; ++i) {
+        const double nn = Norm(n[i]);
+        n[i] = nn > zero_tol ? Div(n[i], nn) : V3{0.0, 0.0, 0.0};
+    }
+    return n;
+}
+
 // ---------------------------------------------------------------------------
 // IBCSubset (src/IBCSubset.cpp:12-268)
 
@@ -368,12 +391,17 @@ void IBCSubsets::Initialize(const Tube &t, const std::vector<SurfaceSpec> &specs
     m_surf.clear();
     for (const auto &s : specs) m_surf.emplace_back(s);
     std::vector<V3> normals;
-    bool need = false;
+    // the surface normals on the tube each IBC's frames use (IBCSubset::ComputeFrameBasedDirections,
+    // src/IBCSubset.cpp:190-215): Jcp eigenvectors, or x - cp when use_Jcp_surface_normals is off
+    std::vector<V3> normals_x;
+    bool need = false, need_x = false;
     for (const auto &s : specs)
-        if (!s.meta.use_cp_diff_directions) need = true;
+        if (!s.meta.use_cp_diff_directions) (s.meta.use_Jcp_surface_normals ? need : need_x) = true;
     if (need) normals = NormalsFromJcp(t);
+    if (need_x) normals_x = UnorientedSurfaceNormals(t);
     m_tag.assign(m_num, IBCSubset());
-    for (size_t c = 0; c < m_num; ++c) m_tag[c].ComputeSubset(m_surf[c], t, normals);
+    for (size_t c = 0; c < m_num; ++c)
+        m_tag[c].ComputeSubset(m_surf[c], t, specs[c].meta.use_Jcp_surface_normals ? normals : normals_x);
     m_dof.assign(m_num, IBCDOFSubset());
     for (size_t c = 0; c < m_num; ++c) m_dof[c].ComputeDOFSubset(m_surf[c], m_tag[c], t);
     // IBCStartingColumns (:74-94)

@@ -122,6 +122,7 @@ def lib():
             L.cpmref_csr_export.argtypes = [vp, ctypes.c_int32, vp, vp, vp]
             L.cpmref_rows_export.argtypes = [vp] * 5
             L.cpmref_xp_export.argtypes = [vp, vp]
+            L.cpmref_row_sides.argtypes = [vp, vp]
             L.cpmref_ibc_sizes.argtypes = [vp, ctypes.c_int32, vp]
             L.cpmref_ibc_export.argtypes = [vp, ctypes.c_int32] + [vp] * 7
             L.cpmref_apply.argtypes = [vp, ctypes.c_double, ctypes.c_double, vp, vp]
@@ -240,7 +241,9 @@ class RefProblem:
         ibc = np.zeros(D, np.int32)
         point = np.zeros((D, 3))
         lib().cpmref_rows_export(self.h, _ptr(ident), _ptr(kind), _ptr(ibc), _ptr(point))
-        return dict(identity=ident.astype(bool), kind=kind, ibc=ibc, point=point)
+        side = np.zeros(D, np.int32)
+        lib().cpmref_row_sides(self.h, _ptr(side))
+        return dict(identity=ident.astype(bool), kind=kind, ibc=ibc, point=point, side=side)
 
     def xp(self):
         xp = np.zeros((self.n_plot, 3))

@@ -194,3 +194,80 @@ def test_neumann_apply_and_backward_euler_match_oracle(gpu, oracle, order):
     u_gpu, st = gpu.Solver(O, 1.0, -dt).solve(ug, tol=FP64_SOLVE_TOL, precision=0)
     assert st[0]["status"] == 0
     assert _rel_inf(u_gpu[0][gr], u_ref) <= FP64_PARITY
+
+
+# ---- oriented IBCs (IBCMetaData::is_oriented, point_on_side1; IBCDOFSubset::OrientSubset,
+# src/IBCDOFSubset.cpp:128-227), as the reference's diffusion-curve programs set them
+# (examples/DiffusionCurvesNefertiti/DiffusionCurvesNefertiti.cpp:233-235): the circle
+# z = 0.3 on the unit sphere, side 1 toward the point above it
+
+def _oriented_circle(mod, dx, order, bt):
+    R = math.sqrt(1 - 0.09)
+    if hasattr(mod, "circle3d_desc"):
+        d = mod.circle3d_desc(R, (0, 0, 0.3), (0, 0, 1), dx, boundary_order=order)
+    else:
+        d = mod.desc(mod.CIRCLE3D, [R, 0, 0, 0.3, 0, 0, 1], (-1.0, 1.0), boundary_order=order,
+                     on_ibc_tolerance=0.1 * dx * dx)
+    d.is_oriented = 1
+    d.has_point_on_side1 = 1
+    z = 0.45
+    d.point_on_side1[0], d.point_on_side1[1], d.point_on_side1[2] = math.sqrt(1 - z * z), 0.0, z
+    d.boundary_type[0], d.boundary_type[1] = bt
+    return d
+
+
+@pytest.mark.parametrize("order,bt", [(2, (0, 0)), (2, (0, 1)), (1, (0, 0)), (1, (1, 0))])
+def test_oriented_rows_bit_exact(gpu, oracle, order, bt):
+    dx = 0.05
+    P, T, O, gr = same_cp_pair(gpu, oracle, dx, [_oriented_circle(oracle, dx, order, bt)],
+                               [_oriented_circle(gpu, dx, order, bt)])
+    assert O.D == P.D and O.total_ibc_dofs == P.total_ibc_dofs and O.num2 == P.num2
+    rr, gg = P.rows(), O.rows()
+    for k in ("identity", "kind", "ibc", "side"):
+        assert np.array_equal(rr[k], gg[k][gr]), k
+    sides = rr["side"][P.N:P.N + P.total_ibc_dofs]
+    assert set(np.unique(sides).tolist()) == {1, 2}  # both sides of the curve carry DOFs
+    for which in (0, 1):
+        assert_rows_bit_exact(P, O, gr, which)
+
+
+def test_oriented_two_valued_dirichlet_solve_within_1e10(gpu, oracle):
+    """A curve with a different Dirichlet value on each side (a diffusion curve's two
+    colours): GetRHS hands the side to the boundary-value function; the FP64 solve
+    equals the oracle's within 1e-10 (both to tol 1e-12)."""
+    dx = 0.05
+    P, T, O, gr = same_cp_pair(gpu, oracle, dx, [_oriented_circle(oracle, dx, 2, (0, 0))],
+                               [_oriented_circle(gpu, dx, 2, (0, 0))])
+    rows = P.rows()
+    value = {1: 1.0, 2: 0.25}
+    b = np.zeros(P.D)
+    d = rows["kind"] == 2
+    b[d] = [value[int(s)] for s in rows["side"][d]]
+    x_ref, _ = P.solve(0.0, -1.0, b, tol=FP64_SOLVE_TOL)
+    bg = np.empty(O.D)
+    bg[gr] = b
+    x_gpu, st = gpu.Solver(O, 0.0, -1.0).solve(bg, tol=FP64_SOLVE_TOL, precision=0)
+    assert st[0]["status"] == 0
+    assert _rel_inf(x_gpu[0][gr], x_ref) <= FP64_PARITY
+    # the two sides really differ: just above and below the curve the solution differs
+    up = rows["point"][:P.N, 2] > 0.34
+    down = (rows["point"][:P.N, 2] < 0.26) & (rows["point"][:P.N, 2] > 0.2)
+    assert np.mean(x_ref[:P.N][up]) > np.mean(x_ref[:P.N][down]) + 0.1
+
+
+@pytest.mark.parametrize("option", ["use_cp_diff_directions", "no_jcp_normals"])
+def test_ibc_direction_options_rows_bit_exact(gpu, oracle, option):
+    """IBCMetaData::use_cp_diff_directions (directions = cp_diff, src/IBCSubset.cpp:156-187)
+    and use_Jcp_surface_normals = false (frames from the normals x - cp,
+    src/Geometry.cpp:101-126) on the two circles, order 2."""
+    dx = 0.05
+    io, ig = two_circle_ibcs(oracle, dx), two_circle_ibcs(gpu, dx)
+    for d in io + ig:
+        if option == "use_cp_diff_directions":
+            d.use_cp_diff_directions = 1
+        else:
+            d.use_Jcp_surface_normals = 0
+    P, T, O, gr = same_cp_pair(gpu, oracle, dx, io, ig)
+    assert O.D == P.D and O.total_ibc_dofs == P.total_ibc_dofs
+    for which in (0, 1):
+        assert_rows_bit_exact(P, O, gr, which)
