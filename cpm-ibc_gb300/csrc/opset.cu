@@ -68,7 +68,7 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
     v.pe_old = o->pe_old.p;
     v.pe_w = pe_w;
     v.n_pl = o->n_pl;
-    v.eb = o->ebrick();
+    v.et = o->etma();
     return v;
 }
 
@@ -1308,27 +1308,18 @@ static int build_schedule(cpm_opset_s *o) {
     return build_patch_list(o, flags);
 }
 
-// Units of the brick-staged E pass (see EBrick).  A unit is a run of groups of
-// one base brick whose stage (the 2 x 2 x 2 node bricks at the base brick's
-// corner, then the distinct extra columns its patch entries read) fits
-// EB_MAX_ROWS rows (opset.h); units are ordered by decreasing row count so that blocks
-// taking them in turn finish together.
-
-static int build_brick_sched(cpm_opset_s *o) {
-    cpm_tube_s *t = o->tube;
-    const int NB = t->g.NB;
+// Patch records of the TMA-staged E pass (see ETma): per base group, its rows on
+// the IBC patch list in row order, each entry with the stage offset of the bulk
+// stencil node it replaces (the k-th set bit s of the row's moved-column mask,
+// offset s * 128) and its moved column.
+static int build_etma_sched(cpm_opset_s *o) {
     const int64_t D = o->D, n_grp = o->n_grp;
-    std::vector<int32_t> bmap, bstart, ord, grp, pl_row, pl_off, pl_xcol, pe_new, patch;
-    std::vector<uint64_t> bmask, p_emask;
-    std::vector<uint32_t> base;
+    std::vector<int32_t> ord, grp, pl_row, pl_off, pl_xcol, pe_new, patch;
+    std::vector<uint64_t> p_emask;
     std::vector<uint8_t> flags, pl_neg;
     std::vector<float> pl_xval, pe_w;
-    CPM_TRY(t->bmap.download(bmap, (size_t)NB * NB * NB));
-    CPM_TRY(t->bstart.download(bstart, t->nbricks));
-    CPM_TRY(t->bmask.download(bmask, t->nbricks));
     CPM_TRY(o->ord.download(ord, std::max<int64_t>(1, o->n_ord)));
     CPM_TRY(o->grp.download(grp, n_grp + 1));
-    CPM_TRY(o->base.download(base, D));
     CPM_TRY(o->flags.download(flags, D));
     const int64_t n_pl = o->n_pl, n_pe = o->n_pe;
     std::vector<int32_t> pl_of_row(D, -1);
@@ -1344,141 +1335,32 @@ static int build_brick_sched(cpm_opset_s *o) {
         CPM_TRY(o->p_emask.download(p_emask, o->p_emask.n));
         for (int64_t q = 0; q < n_pl; ++q) pl_of_row[pl_row[q]] = (int32_t)q;
     }
-    auto brick_rank = [&](int X, int Y, int Z) -> int {
-        if (X >= NB || Y >= NB || Z >= NB) return -1;
-        return bmap[((size_t)X * NB + Y) * NB + Z];
-    };
-    std::vector<int4> u_hdr;
-    std::vector<int2> u_brick;
-    std::vector<int32_t> u_extra, g_pq(n_grp + 1, 0);
-    std::vector<uint32_t> gslot(64 * std::max<int64_t>(1, n_grp), 0);
+    std::vector<int32_t> g_pq(n_grp + 1, 0);
     std::vector<int4> pq;
     std::vector<float> pq_xval, pqe_w;
     std::vector<uint8_t> pq_neg;
     std::vector<uint2> pqe;
-    std::vector<int64_t> unit_rows;
-    int stage_rows = 0;
-    int64_t g = 0;
-    while (g < n_grp) {
-        // the run of groups of one base brick
-        const uint32_t b0 = base[ord[grp[g]]];
-        const int X = unpack_i(b0) >> 2, Y = unpack_j(b0) >> 2, Z = unpack_k(b0) >> 2;
-        int64_t gend = g + 1;
-        while (gend < n_grp) {
-            const uint32_t b = base[ord[grp[gend]]];
-            if ((unpack_i(b) >> 2) != X || (unpack_j(b) >> 2) != Y || (unpack_k(b) >> 2) != Z) break;
-            ++gend;
-        }
-        int2 bricks[8];
-        uint64_t masks[8];
-        int off[9];
-        off[0] = 0;
-        for (int c = 0; c < 8; ++c) {
-            const int rk = brick_rank(X + (c & 1), Y + ((c >> 1) & 1), Z + ((c >> 2) & 1));
-            masks[c] = rk >= 0 ? bmask[rk] : 0ull;
-            bricks[c] = make_int2(rk >= 0 ? bstart[rk] : 0, __builtin_popcountll(masks[c]));
-            off[c + 1] = off[c] + bricks[c].y;
-        }
-        const int brick_rows = off[8];
-        // stage offsets of every group's 64 stencil nodes
-        for (int64_t h = g; h < gend; ++h) {
-            const uint32_t b = base[ord[grp[h]]];
-            for (int sidx = 0; sidx < 64; ++sidx) {
-                const int i = unpack_i(b) + (sidx >> 4), j = unpack_j(b) + ((sidx >> 2) & 3), k = unpack_k(b) + (sidx & 3);
-                const int c = ((i >> 2) - X) | (((j >> 2) - Y) << 1) | (((k >> 2) - Z) << 2);
-                const int l = ((i & 3) << 4) | ((j & 3) << 2) | (k & 3);
-                if (!((masks[c] >> l) & 1ull)) return fail(CPM_ERR_BASEPOINT_OUTSIDE_TUBE, "an interpolation stencil leaves the tube");
-                gslot[64 * h + sidx] = (uint32_t)(off[c] + __builtin_popcountll(masks[c] & ((1ull << l) - 1ull))) * 128u;
+    for (int64_t h = 0; h < n_grp; ++h) {
+        g_pq[h] = (int32_t)pq.size();
+        for (int32_t pos = grp[h]; pos < grp[h + 1]; ++pos) {
+            const int32_t r = ord[pos];
+            const int32_t q = pl_of_row[r];
+            if (q < 0) continue;
+            uint64_t em = (flags[r] & F_EMOVE) ? p_emask[patch[r]] : 0ull;
+            const int e_first = (int)pqe.size();
+            for (int32_t e = pl_off[q]; e < pl_off[q + 1]; ++e) {
+                if (!em) return fail(CPM_ERR_CUDA, "internal: patch entries exceed the moved-column mask");
+                const int sidx = __builtin_ctzll(em);
+                em &= em - 1;
+                pqe.push_back(make_uint2((uint32_t)sidx * 128u, (uint32_t)pe_new[e]));
+                pqe_w.push_back(pe_w[e]);
             }
+            pq.push_back(make_int4(pos - grp[h], e_first, (int)pqe.size(), pl_xcol[q]));
+            pq_xval.push_back(pl_xval[q]);
+            pq_neg.push_back(pl_neg[q]);
         }
-        // units: runs of these groups whose extra columns fit the stage
-        int64_t u0 = g;
-        while (u0 < gend) {
-            std::vector<int32_t> extra;
-            bool global_cols = false;  // this group's extra columns are read from global memory
-            auto extra_slot = [&](int32_t col) -> uint32_t {
-                if (global_cols) return EB_GLOBAL | (uint32_t)col;
-                for (size_t e = 0; e < extra.size(); ++e)
-                    if (extra[e] == col) return (uint32_t)(brick_rows + (int)e) * 128u;
-                extra.push_back(col);
-                return (uint32_t)(brick_rows + (int)extra.size() - 1) * 128u;
-            };
-            int64_t h = u0;
-            int64_t rows_in_unit = 0;
-            for (; h < gend; ++h) {
-                // the group's patch records and the extra columns they add
-                std::vector<int4> rec;
-                std::vector<float> rx;
-                std::vector<uint8_t> rn;
-                std::vector<uint2> ent;
-                std::vector<float> ew;
-                const size_t extra_before = extra.size();
-              retry:
-                for (int32_t pos = grp[h]; pos < grp[h + 1]; ++pos) {
-                    const int32_t r = ord[pos];
-                    const int32_t q = pl_of_row[r];
-                    if (q < 0) continue;
-                    uint64_t em = (flags[r] & F_EMOVE) ? p_emask[patch[r]] : 0ull;
-                    const int e_first = (int)(pqe.size() + ent.size());
-                    for (int32_t e = pl_off[q]; e < pl_off[q + 1]; ++e) {
-                        if (!em) return fail(CPM_ERR_CUDA, "internal: patch entries exceed the moved-column mask");
-                        const int sidx = __builtin_ctzll(em);
-                        em &= em - 1;
-                        ent.push_back(make_uint2(gslot[64 * h + sidx], extra_slot(pe_new[e])));
-                        ew.push_back(pe_w[e]);
-                    }
-                    const int xoff = pl_xcol[q] >= 0 ? (int)extra_slot(pl_xcol[q]) : -1;
-                    rec.push_back(make_int4(pos - grp[h], e_first, (int)(pqe.size() + ent.size()), xoff));
-                    rx.push_back(pl_xval[q]);
-                    rn.push_back(pl_neg[q]);
-                }
-                if (brick_rows + (int)extra.size() > EB_MAX_ROWS) {
-                    extra.resize(extra_before);
-                    if (h != u0) break;  // this group starts the next unit
-                    // alone it still overflows the stage: its patch reads its columns from global memory
-                    global_cols = true;
-                    rec.clear();
-                    rx.clear();
-                    rn.clear();
-                    ent.clear();
-                    ew.clear();
-                    goto retry;
-                }
-                global_cols = false;
-                g_pq[h] = (int32_t)pq.size();
-                pq.insert(pq.end(), rec.begin(), rec.end());
-                pq_xval.insert(pq_xval.end(), rx.begin(), rx.end());
-                pq_neg.insert(pq_neg.end(), rn.begin(), rn.end());
-                pqe.insert(pqe.end(), ent.begin(), ent.end());
-                pqe_w.insert(pqe_w.end(), ew.begin(), ew.end());
-                rows_in_unit += grp[h + 1] - grp[h];
-            }
-            u_hdr.push_back(make_int4((int)u0, (int)h, (int)u_extra.size(), (int)(u_extra.size() + extra.size())));
-            for (int c = 0; c < 8; ++c) u_brick.push_back(bricks[c]);
-            u_extra.insert(u_extra.end(), extra.begin(), extra.end());
-            unit_rows.push_back(rows_in_unit);
-            stage_rows = std::max(stage_rows, brick_rows + (int)extra.size());
-            u0 = h;
-        }
-        g = gend;
     }
     g_pq[n_grp] = (int32_t)pq.size();
-    // decreasing row count (the order of units changes no result)
-    const int64_t nu = (int64_t)u_hdr.size();
-    std::vector<int64_t> uo(nu);
-    for (int64_t u = 0; u < nu; ++u) uo[u] = u;
-    std::stable_sort(uo.begin(), uo.end(), [&](int64_t a, int64_t b) { return unit_rows[a] > unit_rows[b]; });
-    std::vector<int4> hs(nu);
-    std::vector<int2> bs(8 * nu);
-    for (int64_t u = 0; u < nu; ++u) {
-        hs[u] = u_hdr[uo[u]];
-        for (int c = 0; c < 8; ++c) bs[8 * u + c] = u_brick[8 * uo[u] + c];
-    }
-    if (hs.empty()) {
-        hs.push_back(make_int4(0, 0, 0, 0));
-        bs.assign(8, make_int2(0, 0));
-    }
-    if (u_extra.empty()) u_extra.push_back(0);
     if (pq.empty()) {
         pq.push_back(make_int4(0, 0, 0, -1));
         pq_xval.push_back(0.f);
@@ -1488,25 +1370,18 @@ static int build_brick_sched(cpm_opset_s *o) {
         pqe.push_back(make_uint2(0, 0));
         pqe_w.push_back(0.f);
     }
-    CPM_TRY(o->eb_uhdr.upload(hs));
-    CPM_TRY(o->eb_ubrick.upload(bs));
-    CPM_TRY(o->eb_uextra.upload(u_extra));
-    CPM_TRY(o->eb_gslot.upload(gslot));
-    CPM_TRY(o->eb_gpq.upload(g_pq));
-    CPM_TRY(o->eb_pq.upload(pq));
-    CPM_TRY(o->eb_pqxval.upload(pq_xval));
-    CPM_TRY(o->eb_pqneg.upload(pq_neg));
-    CPM_TRY(o->eb_pqe.upload(pqe));
-    CPM_TRY(o->eb_pqew.upload(pqe_w));
-    CPM_TRY(o->eb_ctr.alloc(2));
-    CPM_TRY(o->eb_ctr.zero());
-    CPM_TRY(o->eb_err.alloc(1));
-    CPM_TRY(o->eb_err.zero());
-    o->eb_units = nu;
-    o->eb_stage_rows = stage_rows;
-    EBrick e = o->ebrick();
-    CPM_TRY(ebrick_setup(e));
-    o->eb_grid = e.grid;
+    CPM_TRY(o->et_gpq.upload(g_pq));
+    CPM_TRY(o->et_pq.upload(pq));
+    CPM_TRY(o->et_pqxval.upload(pq_xval));
+    CPM_TRY(o->et_pqneg.upload(pq_neg));
+    CPM_TRY(o->et_pqe.upload(pqe));
+    CPM_TRY(o->et_pqew.upload(pqe_w));
+    CPM_TRY(o->et_err.alloc(1));
+    CPM_TRY(o->et_err.zero());
+    o->et_ready = true;
+    ETma e = o->etma();
+    CPM_TRY(etma_setup(e));
+    o->et_grid = e.grid;
     return 0;
 }
 
@@ -1514,23 +1389,17 @@ static int build_brick_sched(cpm_opset_s *o) {
 
 using namespace cpm;
 
-EBrick cpm_opset_s::ebrick() const {
-    EBrick e;
-    e.u_hdr = eb_uhdr.p;
-    e.u_brick = eb_ubrick.p;
-    e.u_extra = eb_uextra.p;
-    e.gslot = eb_gslot.p;
-    e.g_pq = eb_gpq.p;
-    e.pq = eb_pq.p;
-    e.pq_xval = eb_pqxval.p;
-    e.pq_neg = eb_pqneg.p;
-    e.pqe = eb_pqe.p;
-    e.pqe_w = eb_pqew.p;
-    e.ctr = eb_ctr.p;
-    e.err = eb_err.p;
-    e.n_units = eb_units;
-    e.stage_rows = eb_stage_rows;
-    e.grid = eb_grid;
+ETma cpm_opset_s::etma() const {
+    ETma e;
+    e.g_pq = et_gpq.p;
+    e.pq = et_pq.p;
+    e.pq_xval = et_pqxval.p;
+    e.pq_neg = et_pqneg.p;
+    e.pqe = et_pqe.p;
+    e.pqe_w = et_pqew.p;
+    e.err = et_err.p;
+    e.grid = et_grid;
+    e.ready = et_ready ? 1 : 0;
     return e;
 }
 
@@ -1543,7 +1412,7 @@ static int opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibc
     if (!rc && n_ibc > 0) rc = build_ibc(o, n_ibc, ibcs, ovr);
     if (!rc) rc = build_schedule(o);
     if (!rc) rc = make_float_copies(o);
-    if (!rc) rc = build_brick_sched(o);
+    if (!rc) rc = build_etma_sched(o);
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(stream());
         if (e != cudaSuccess) rc = fail(CPM_ERR_CUDA, cudaGetErrorString(e));
@@ -1596,7 +1465,7 @@ extern "C" int cpm_opset_create_identity(cpm_tube_t t, int64_t n_rows, const int
     }
     if (!rc) rc = build_schedule(o);
     if (!rc) rc = make_float_copies(o);
-    if (!rc) rc = build_brick_sched(o);
+    if (!rc) rc = build_etma_sched(o);
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(stream());
         if (e != cudaSuccess) rc = fail(CPM_ERR_CUDA, cudaGetErrorString(e));

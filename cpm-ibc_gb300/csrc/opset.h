@@ -25,31 +25,28 @@ enum RowFlags : uint8_t {
 // one per IBC column its patch entries read) and computes every row of its
 // groups from shared memory.  Offsets are bytes into the unit's stage, one
 // 128-byte row (32 FP32 slots) per staged node.
-constexpr int EB_MAX_ROWS = 560;  // stage rows of one unit: 70 KB of FP32 32-slot rows, three blocks per SM
-// a patch column offset with this bit set is a row index of x in global memory
-// (the columns of a group whose patch alone overflows the stage)
-constexpr uint32_t EB_GLOBAL = 0x80000000u;
-struct EBrick {
-    const int4 *u_hdr;      // per unit {first group, end group, first extra row, end extra row}
-    const int2 *u_brick;    // per unit 8 x {first node, node count}
-    const int32_t *u_extra; // rows staged after the bricks (moved IBC columns and Dirichlet value rows)
-    const uint32_t *gslot;  // 64 per group: stage offset of stencil node s = 16 i + 4 j + k
+// Schedule of the TMA-staged E pass (k_etma32, FP32, 32 slots).  Each warp runs
+// its own two-stage pipeline over base groups: the group's 64 stencil rows of x
+// (32 FP32 slots, 128 bytes each) are gathered into the warp's shared-memory
+// stage by TMA (tile::gather4, four rows an instruction) while the warp computes
+// the previous group from the other stage.  Rows on the IBC patch list are
+// corrected in registers before their one store: per group, its patch records
+// in row order; an entry names the bulk stencil node it replaces by its stage
+// offset and the moved column by its row of x.
+struct ETma {
     const int32_t *g_pq;    // per group: first patch record (n_grp + 1 entries)
-    const int4 *pq;         // patch record {row position in the group, first entry, end entry, extra-column offset or -1}
-                            // (offsets of moved and extra columns may carry EB_GLOBAL)
+    const int4 *pq;         // patch record {row position in the group, first entry, end entry, extra column or -1}
     const float *pq_xval;   // the extra entry's value
     const uint8_t *pq_neg;  // 1: the row is negated (2nd-order Dirichlet DOF rows)
-    const uint2 *pqe;       // patch entry {offset of the bulk stencil node, offset of the moved column}
+    const uint2 *pqe;       // patch entry {stage offset of the bulk stencil node (s * 128), moved column}
     const float *pqe_w;     // its stencil weight (wx_i wy_j) wz_k
-    unsigned int *ctr;      // two work counters, zero between launches (the last block resets them)
     int *err;               // set to 1 when a stage copy did not arrive within the wait limit
-    int64_t n_units;
-    int stage_rows;         // rows of the largest stage
-    int grid;               // blocks of a launch: all resident at once
+    int grid;               // blocks of a launch (all resident at once)
+    int ready;              // the schedule was built
 };
-// sets k_ebrick32's shared-memory limit and the schedule's grid (at operator
-// build time, outside any stream capture)
-int ebrick_setup(EBrick &eb);
+// sets k_etma32's shared-memory limit and the launch grid (at operator build
+// time, outside any stream capture)
+int etma_setup(ETma &et);
 
 template <class T>
 struct OpView {
@@ -89,7 +86,7 @@ struct OpView {
     const int32_t *pe_new, *pe_old;           // moved column and the bulk column it replaces
     const T *pe_w;                            // stencil weight (wx_i wy_j) wz_k of the moved point
     int64_t n_ord, n_grp, n_ident, n_pl;
-    EBrick eb;                                // brick-staged E pass (FP32 weights)
+    ETma et;                                  // TMA-staged E pass (FP32 weights)
 };
 
 // ---------------------------------------------------------------------------
@@ -562,19 +559,16 @@ struct cpm_opset_s {
     cpm::DBuf<float> w_ord32;
     cpm::DBuf<uint8_t> fl_ord;
     int64_t n_ord = 0, n_grp = 0, n_ident = 0;
-    // brick-staged E pass schedule
-    cpm::DBuf<int4> eb_uhdr, eb_pq;
-    cpm::DBuf<int2> eb_ubrick;
-    cpm::DBuf<int32_t> eb_uextra, eb_gpq;
-    cpm::DBuf<uint32_t> eb_gslot;
-    cpm::DBuf<float> eb_pqxval, eb_pqew;
-    cpm::DBuf<uint8_t> eb_pqneg;
-    cpm::DBuf<uint2> eb_pqe;
-    cpm::DBuf<unsigned int> eb_ctr;
-    cpm::DBuf<int> eb_err;
-    int64_t eb_units = 0;
-    int eb_stage_rows = 0, eb_grid = 1;
-    cpm::EBrick ebrick() const;
+    // TMA-staged E pass schedule
+    cpm::DBuf<int4> et_pq;
+    cpm::DBuf<int32_t> et_gpq;
+    cpm::DBuf<float> et_pqxval, et_pqew;
+    cpm::DBuf<uint8_t> et_pqneg;
+    cpm::DBuf<uint2> et_pqe;
+    cpm::DBuf<int> et_err;
+    int et_grid = 1;
+    bool et_ready = false;
+    cpm::ETma etma() const;
     // host-side row layout for right-hand sides
     std::vector<uint8_t> h_identity;
     std::vector<int32_t> h_kind, h_ibc, h_side;

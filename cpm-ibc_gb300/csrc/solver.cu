@@ -28,6 +28,9 @@
 #include <mutex>
 #include <string>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "opset.h"
 
 namespace cpm {
@@ -409,23 +412,21 @@ __global__ void __launch_bounds__(128) k_epass32w(OpView<float> op, const Slot *
         }
 }
 
-// ---- brick-staged E pass for 32 FP32 slots, IBC patch included (k_ebrick32).
-// A block takes units of work in turn (a work counter): it stages the unit's
-// 2 x 2 x 2 node bricks and its extra columns into shared memory with bulk
-// asynchronous copies (TMA, cp.async.bulk, one per contiguous node run,
-// completing on an mbarrier), then its warps compute the unit's base groups
-// from shared memory with the arithmetic of k_epass32w, and the rows on the
-// IBC patch list get k_epatch32's correction in registers before the one
-// store.  Results are bit for bit those of k_epass32w followed by k_epatch32.
+// ---- TMA-staged E pass for 32 FP32 slots, IBC patch included (k_etma32).
+// Every warp runs its own two-stage pipeline over base groups (a static
+// stride): it gathers the next group's 64 stencil rows of x into one of its
+// shared-memory stages with TMA (cp.async.bulk.tensor tile::gather4, four
+// 128-byte rows an instruction, completing on the stage's mbarrier) and
+// computes the current group from the other stage, with the arithmetic of
+// k_epass32w; rows on the IBC patch list get k_epatch32's correction in
+// registers before their one store.  Results are bit for bit those of
+// k_epass32w followed by k_epatch32.
+constexpr int ET_WARPS = 4;       // warps per block
+constexpr int ET_STAGES = 2;      // stages per warp
+constexpr int ET_STAGE = 64 * 128; // one group's 64 rows of 32 FP32 slots
 
 // shared-memory address of a generic pointer
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// bulk copy of `bytes` (multiple of 16) from global to shared memory, completing on mbarrier `bar`
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 :: "r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
-}
 
 // waits for phase `parity` of mbarrier `bar` to complete: at most 2^19 waits
 // of at most ~2 us each (the suspend-time hint), about a second in all;
@@ -440,27 +441,22 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-// k_epatch32's correction of one patched row, lane = slot, from the stage:
-// sign (bulk + sum_e w_e (x[new_e] - x[old_e])) + xval x[xcol]
-// a moved or extra column's value: from the stage, or from x where the offset carries EB_GLOBAL
-__device__ __forceinline__ float eb_col(const char *stage, const float *__restrict__ x, uint32_t off, int lane) {
-    return (off & EB_GLOBAL) ? x[(off & ~EB_GLOBAL) * 32u + lane] : *(const float *)(stage + off + 4 * lane);
-}
-
-__device__ __forceinline__ float eb_patch(const EBrick &eb, const char *stage, const float *__restrict__ x, int lane, int pr,
+// k_epatch32's correction of one patched row, lane = slot: the bulk stencil
+// values from the stage, the moved and extra columns from x
+__device__ __forceinline__ float et_patch(const ETma &et, const char *stage, const float *__restrict__ x, int lane, int pr,
                                           const int4 &rec, float acc) {
-    const float xv = eb.pq_xval[pr];
-    const bool neg = eb.pq_neg[pr] != 0;
-    const float xe = rec.w != -1 ? eb_col(stage, x, (uint32_t)rec.w, lane) : 0.f;
+    const float xv = et.pq_xval[pr];
+    const bool neg = et.pq_neg[pr] != 0;
+    const float xe = rec.w >= 0 ? x[(uint32_t)rec.w * 32u + lane] : 0.f;
     for (int base = rec.y; base < rec.z; base += 32) {
         const int cnt = min(32, rec.z - base);
         uint32_t oo = 0, nn = 0;
         float w = 0.f;
         if (lane < cnt) {
-            const uint2 e = eb.pqe[base + lane];
+            const uint2 e = et.pqe[base + lane];
             oo = e.x;
             nn = e.y;
-            w = eb.pqe_w[base + lane];
+            w = et.pqe_w[base + lane];
         }
         for (int u0 = 0; u0 < cnt; u0 += 8) {
             float xn[8], xo[8], ww[8];
@@ -470,7 +466,7 @@ __device__ __forceinline__ float eb_patch(const EBrick &eb, const char *stage, c
                 const uint32_t nk = (uint32_t)__shfl_sync(FULL, nn, k & 31), ok = (uint32_t)__shfl_sync(FULL, oo, k & 31);
                 ww[u] = __shfl_sync(FULL, w, k & 31);
                 const bool valid = k < cnt;
-                xn[u] = valid ? eb_col(stage, x, nk, lane) : 0.f;
+                xn[u] = valid ? x[nk * 32u + lane] : 0.f;
                 xo[u] = valid ? *(const float *)(stage + ok + 4 * lane) : 0.f;
             }
 #pragma unroll
@@ -479,198 +475,193 @@ __device__ __forceinline__ float eb_patch(const EBrick &eb, const char *stage, c
         }
     }
     if (neg) acc = -acc;
-    if (rec.w != -1) acc += xv * xe;
+    if (rec.w >= 0) acc += xv * xe;
     return acc;
 }
 
-constexpr int EB_THREADS = 256;
-__global__ void __launch_bounds__(EB_THREADS, 3) k_ebrick32(OpView<float> op, const Slot *__restrict__ sl, int ph,
-                                                          const float *__restrict__ x, float *__restrict__ t) {
-    extern __shared__ __align__(128) unsigned char eb_stage[];
-    __shared__ __align__(16) float sw[EB_THREADS / 32][EW_ROWS * 12];
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ int s_unit;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, tid = threadIdx.x;
-    constexpr int NW = EB_THREADS / 32;
+// the four rows c of x (32 FP32 slots each) into 512 contiguous bytes of shared memory
+__device__ __forceinline__ void tma_gather4(uint32_t dst, const CUtensorMap *map, int4 c, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+        ::"r"(dst), "l"(map), "r"(0), "r"(c.x), "r"(c.y), "r"(c.z), "r"(c.w), "r"(bar) : "memory");
+}
+
+__global__ void __launch_bounds__(ET_WARPS * 32, 3) k_etma32(const __grid_constant__ CUtensorMap xmap, OpView<float> op,
+                                                             const Slot *__restrict__ sl, int ph, const float *__restrict__ x,
+                                                             float *__restrict__ t) {
+    extern __shared__ __align__(1024) unsigned char et_smem[];
+    __shared__ __align__(16) float sw[ET_WARPS][EW_ROWS * 12];
+    __shared__ __align__(8) uint64_t bars[ET_WARPS][ET_STAGES];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool act = (ph < 0) || sl[lane].phase == ph;
     if (!__any_sync(FULL, act)) return;  // the same 32 slots in every warp: grid-uniform
-    const EBrick &eb = op.eb;
-    const char *stage = (const char *)eb_stage;
-    const uint32_t sbar = smem_u32(&bar), sstage = smem_u32(eb_stage);
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+    const ETma &et = op.et;
+    const char *stages = (const char *)et_smem + (size_t)warp * ET_STAGES * ET_STAGE;
+    const uint32_t sst = smem_u32(stages), sbar = smem_u32(&bars[warp][0]);
+    if (lane == 0) {
+#pragma unroll
+        for (int s = 0; s < ET_STAGES; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar + 8 * s) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_unit = (int)atomicAdd(eb.ctr, 1u);
     }
-    __syncthreads();
-    uint32_t parity = 0;
+    __syncwarp();
     float *w = sw[warp];
-    int u = s_unit;
-    while (u < eb.n_units) {
-        const int4 hd = eb.u_hdr[u];
-        // stage: the eight node bricks, then the extra rows
-        int2 bk[8];
-        int brick_rows = 0, my_off = 0;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            bk[c] = eb.u_brick[8 * (int64_t)u + c];
-            if (c < tid) my_off += bk[c].y;
-            brick_rows += bk[c].y;
+    const int64_t W = (int64_t)gridDim.x * ET_WARPS;
+    // the 64 stencil rows of group g into stage s
+    auto issue = [&](int64_t g, int s) {
+        if (lane == 0)
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar + 8 * s), "r"(ET_STAGE) : "memory");
+        __syncwarp();
+        if (lane < 16) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const int4 c = __ldg((const int4 *)(op.gcols + 64 * g) + lane);
+            tma_gather4(sst + (uint32_t)s * ET_STAGE + 512u * lane, &xmap, c, sbar + 8 * s);
         }
-        const int nextra = hd.w - hd.z;
-        if (tid == 0)
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                         ::"r"(sbar), "r"((uint32_t)(brick_rows + nextra) * 128u) : "memory");
-        __syncthreads();  // the expected byte count is posted before any copy is issued
-        if (tid < 8) {
-            int2 b = bk[0];
-#pragma unroll
-            for (int c = 1; c < 8; ++c)
-                if (c == tid) b = bk[c];
-            if (b.y > 0) bulk_g2s(sstage + (uint32_t)my_off * 128u, x + (size_t)b.x * 32, (uint32_t)b.y * 128u, sbar);
-        } else {
-            for (int e = tid - 8; e < nextra; e += EB_THREADS - 8) {
-                const int col = eb.u_extra[hd.z + e];
-                bulk_g2s(sstage + (uint32_t)(brick_rows + e) * 128u, x + (size_t)col * 32, 128u, sbar);
-            }
-        }
-        const bool ok = mbar_wait(sbar, parity);
-        parity ^= 1u;
-        if (__syncthreads_or(!ok)) {
-            // a copy did not arrive: record it, give the copies one more bounded wait, stop
-            if (tid == 0) atomicExch(eb.err, 1);
-            mbar_wait(sbar, parity ^ 1u);
+    };
+    uint32_t phases = 0;
+    int64_t g = (int64_t)blockIdx.x * ET_WARPS + warp;
+    if (g < op.n_grp) issue(g, 0);
+    for (int k = 0; g < op.n_grp; g += W, ++k) {
+        const int s = k & 1;
+        if (g + W < op.n_grp) issue(g + W, s ^ 1);  // the other stage was read in the previous round
+        const bool ok = mbar_wait(sbar + 8 * s, (phases >> s) & 1u);
+        phases ^= 1u << s;
+        if (!__all_sync(FULL, ok)) {
+            // a copy did not arrive: record it, give both stages' copies one more bounded wait, stop
+            if (lane == 0) atomicExch(et.err, 1);
+            mbar_wait(sbar + 8 * s, ((phases >> s) & 1u) ^ 1u);
+            if (g + W < op.n_grp) mbar_wait(sbar + 8 * (s ^ 1), (phases >> (s ^ 1)) & 1u);
             return;
         }
-        for (int64_t g = hd.x + warp; g < hd.y; g += NW) {
-            const int p0 = op.grp[g], p1 = op.grp[g + 1];
-            int pr = eb.g_pq[g];
-            const int pr_end = eb.g_pq[g + 1];
-            const uint4 *gs = (const uint4 *)(eb.gslot + 64 * g);
-            for (int c0 = p0; c0 < p1; c0 += EW_ROWS) {
-                const int nr = min(p1 - c0, EW_ROWS), np = (nr + 1) >> 1;
-                __syncwarp();
-                for (int e = lane; e < 24 * np; e += 32) {
-                    const int q = e / 12, c = e - 12 * q;
-                    w[24 * (q >> 1) + 2 * c + (q & 1)] = q < nr ? op.w_ord[12 * (size_t)(c0 + q) + c] : 0.f;
-                }
-                const int row = lane < nr ? op.ord[c0 + lane] : 0;  // lane q: row q of the chunk
-                __syncwarp();
-                uint64_t acc[EW_ROWS / 2];
+        const char *stage = stages + (size_t)s * ET_STAGE;
+        const int p0 = op.grp[g], p1 = op.grp[g + 1];
+        int pr = et.g_pq[g];
+        const int pr_end = et.g_pq[g + 1];
+        for (int c0 = p0; c0 < p1; c0 += EW_ROWS) {
+            const int nr = min(p1 - c0, EW_ROWS), np = (nr + 1) >> 1;
+            __syncwarp();
+            for (int e = lane; e < 24 * np; e += 32) {
+                const int q = e / 12, c = e - 12 * q;
+                w[24 * (q >> 1) + 2 * c + (q & 1)] = q < nr ? op.w_ord[12 * (size_t)(c0 + q) + c] : 0.f;
+            }
+            const int row = lane < nr ? op.ord[c0 + lane] : 0;  // lane q: row q of the chunk
+            __syncwarp();
+            uint64_t acc[EW_ROWS / 2];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    float xb[16];
+            for (int i = 0; i < 4; ++i) {
+                float xb[16];
 #pragma unroll
-                    for (int v = 0; v < 4; ++v) {
-                        const uint4 o4 = __ldg(gs + 4 * i + v);
-                        xb[4 * v] = *(const float *)(stage + o4.x + 4 * lane);
-                        xb[4 * v + 1] = *(const float *)(stage + o4.y + 4 * lane);
-                        xb[4 * v + 2] = *(const float *)(stage + o4.z + 4 * lane);
-                        xb[4 * v + 3] = *(const float *)(stage + o4.w + 4 * lane);
-                    }
-                    uint64_t x2[16];
+                for (int q = 0; q < 16; ++q) xb[q] = *(const float *)(stage + 128 * (16 * i + q) + 4 * lane);
+                uint64_t x2[16];
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) x2[q] = f2_pack(xb[q], xb[q]);
-#pragma unroll
-                    for (int p = 0; p < EW_ROWS / 2; ++p)
-                        if (p < np) {
-                            const float *wp = w + 24 * p;
-                            const uint64_t wx2 = *(const uint64_t *)(wp + 2 * i);
-                            const ulonglong2 y01 = *(const ulonglong2 *)(wp + 8), y23 = *(const ulonglong2 *)(wp + 12);
-                            const ulonglong2 z01 = *(const ulonglong2 *)(wp + 16), z23 = *(const ulonglong2 *)(wp + 20);
-                            const uint64_t wy2[4] = {y01.x, y01.y, y23.x, y23.y}, wz2[4] = {z01.x, z01.y, z23.x, z23.y};
-                            uint64_t ay2 = 0ull;
-#pragma unroll
-                            for (int j = 0; j < 4; ++j) {
-                                uint64_t az2 = f2_mul(wz2[0], x2[4 * j]);
-                                az2 = f2_fma(wz2[1], x2[4 * j + 1], az2);
-                                az2 = f2_fma(wz2[2], x2[4 * j + 2], az2);
-                                az2 = f2_fma(wz2[3], x2[4 * j + 3], az2);
-                                ay2 = j == 0 ? f2_mul(wy2[0], az2) : f2_fma(wy2[j], az2, ay2);
-                            }
-                            const uint64_t part = f2_mul(wx2, ay2);
-                            acc[p] = i == 0 ? part : f2_add(acc[p], part);
-                        }
-                }
+                for (int q = 0; q < 16; ++q) x2[q] = f2_pack(xb[q], xb[q]);
 #pragma unroll
                 for (int p = 0; p < EW_ROWS / 2; ++p)
-                    if (2 * p < nr) {
-                        float v2[2];
-                        f2_unpack(acc[p], v2[0], v2[1]);
+                    if (p < np) {
+                        const float *wp = w + 24 * p;
+                        const uint64_t wx2 = *(const uint64_t *)(wp + 2 * i);
+                        const ulonglong2 y01 = *(const ulonglong2 *)(wp + 8), y23 = *(const ulonglong2 *)(wp + 12);
+                        const ulonglong2 z01 = *(const ulonglong2 *)(wp + 16), z23 = *(const ulonglong2 *)(wp + 20);
+                        const uint64_t wy2[4] = {y01.x, y01.y, y23.x, y23.y}, wz2[4] = {z01.x, z01.y, z23.x, z23.y};
+                        uint64_t ay2 = 0ull;
 #pragma unroll
-                        for (int h = 0; h < 2; ++h) {
-                            const int q = 2 * p + h;
-                            if (q >= nr) break;
+                        for (int j = 0; j < 4; ++j) {
+                            uint64_t az2 = f2_mul(wz2[0], x2[4 * j]);
+                            az2 = f2_fma(wz2[1], x2[4 * j + 1], az2);
+                            az2 = f2_fma(wz2[2], x2[4 * j + 2], az2);
+                            az2 = f2_fma(wz2[3], x2[4 * j + 3], az2);
+                            ay2 = j == 0 ? f2_mul(wy2[0], az2) : f2_fma(wy2[j], az2, ay2);
+                        }
+                        const uint64_t part = f2_mul(wx2, ay2);
+                        acc[p] = i == 0 ? part : f2_add(acc[p], part);
+                    }
+            }
+#pragma unroll
+            for (int p = 0; p < EW_ROWS / 2; ++p)
+                if (2 * p < nr) {
+                    float v2[2];
+                    f2_unpack(acc[p], v2[0], v2[1]);
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int q = 2 * p + h;
+                        if (q < nr) {
                             const int r = __shfl_sync(FULL, row, q);
                             float v = v2[h];
                             if (pr < pr_end) {
-                                const int4 rec = eb.pq[pr];
+                                const int4 rec = et.pq[pr];
                                 if (rec.x == c0 - p0 + q) {
-                                    v = eb_patch(eb, stage, x, lane, pr, rec, v);
+                                    v = et_patch(et, stage, x, lane, pr, rec, v);
                                     ++pr;
                                 }
                             }
                             if (act) t[(uint32_t)r * 32u + lane] = v;
                         }
                     }
-            }
+                }
         }
-        // every thread is done with the stage and with s_unit before the next unit's copies
-        __syncthreads();
-        if (tid == 0) s_unit = (int)atomicAdd(eb.ctr, 1u);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        u = s_unit;
+        __syncwarp();  // the stage is read before it is refilled
     }
     // identity rows: t = x
     if (act)
-        for (int64_t q = (int64_t)blockIdx.x * NW + warp; q < op.n_ident; q += (int64_t)gridDim.x * NW) {
+        for (int64_t q = (int64_t)blockIdx.x * ET_WARPS + warp; q < op.n_ident; q += W) {
             const uint32_t r = (uint32_t)op.ident[q];
             t[r * 32u + lane] = x[r * 32u + lane];
         }
-    // the last block to finish resets the work counters for the next launch
-    if (tid == 0) {
-        __threadfence();
-        if (atomicAdd(eb.ctr + 1, 1u) == gridDim.x - 1) {
-            eb.ctr[0] = 0u;
-            eb.ctr[1] = 0u;
-            __threadfence();
-        }
-    }
 }
 
-// k_ebrick32's dynamic shared-memory limit (set once) and the schedule's grid:
-// every block resident at once (three per SM at the largest stage), each
-// taking units in turn
-int ebrick_setup(EBrick &eb) {
+// k_etma32's dynamic shared-memory size (set once) and its grid: every block
+// resident at once
+int etma_setup(ETma &et) {
     static bool attr_set = false;
+    const int smem = ET_WARPS * ET_STAGES * ET_STAGE;
     if (!attr_set) {
-        CPM_CUDA_TRY(cudaFuncSetAttribute(k_ebrick32, cudaFuncAttributeMaxDynamicSharedMemorySize, EB_MAX_ROWS * 128));
+        CPM_CUDA_TRY(cudaFuncSetAttribute(k_etma32, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr_set = true;
     }
     int b = 1;
-    CPM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ebrick32, EB_THREADS, (size_t)eb.stage_rows * 128u));
-    b = std::max(1, b);
-    eb.grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)b * sm_count(), std::max<int64_t>(eb.n_units, 1)));
+    CPM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_etma32, ET_WARPS * 32, (size_t)smem));
+    et.grid = std::max(1, b) * sm_count();
     return 0;
 }
 
-// the brick-staged E pass's error flag: a stage copy that did not arrive within
-// its wait limit (the flag is cleared when read)
-static int ebrick_status(cpm_opset_s *o) {
-    if (!o->eb_err.p) return 0;
-    int h = 0;
-    CPM_CUDA_TRY(cudaMemcpyAsync(&h, o->eb_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
-    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
-    if (!h) return 0;
-    CPM_CUDA_TRY(cudaMemsetAsync(o->eb_err.p, 0, sizeof(int), stream()));
-    CPM_CUDA_TRY(cudaMemsetAsync(o->eb_ctr.p, 0, 2 * sizeof(unsigned int), stream()));
-    return fail(CPM_ERR_TIMEOUT, "brick-staged E pass: a stage copy did not complete within the wait limit");
+// the tensor map of a [D][32] FP32 array for tile::gather4: rows of 128 bytes,
+// boxes one row high (cuTensorMapEncodeTiled, reached through the runtime's
+// driver entry point so the library needs no link to the driver library)
+static int x_tensor_map(const float *x, int64_t D, CUtensorMap *map) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        CPM_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn) return fail(CPM_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+        encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    const cuuint64_t dims[2] = {32, (cuuint64_t)D};
+    const cuuint64_t strides[1] = {128};
+    const cuuint32_t box[2] = {32, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)x, dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(CPM_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return 0;
 }
 
-// k_ebrick32 applies: a schedule built and a 16-byte aligned x
-static inline bool ebrick_ok(const OpView<float> &op, const float *x) {
-    return op.eb.n_units > 0 && op.eb.stage_rows > 0 && ((uintptr_t)x % 16) == 0 && op.D * 32 <= (int64_t)UINT32_MAX;
+// the TMA-staged E pass's error flag: a stage copy that did not arrive within
+// its wait limit (the flag is cleared when read)
+static int etma_status(cpm_opset_s *o) {
+    if (!o->et_err.p) return 0;
+    int h = 0;
+    CPM_CUDA_TRY(cudaMemcpyAsync(&h, o->et_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
+    if (!h) return 0;
+    CPM_CUDA_TRY(cudaMemsetAsync(o->et_err.p, 0, sizeof(int), stream()));
+    return fail(CPM_ERR_TIMEOUT, "TMA-staged E pass: a stage copy did not complete within the wait limit");
+}
+
+// k_etma32 applies: a schedule built and a 16-byte aligned x
+static inline bool etma_ok(const OpView<float> &op, const float *x) {
+    return op.et.ready && op.n_grp > 0 && ((uintptr_t)x % 16) == 0 && op.D * 32 <= (int64_t)UINT32_MAX &&
+           op.D <= (int64_t)INT32_MAX;
 }
 
 // 1 slot: one thread per row, rows visited in base-point order so that the
@@ -759,7 +750,7 @@ __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__re
 template <class T, int K>
 static inline int epass_kernels(const OpView<T> &op, const T *x) {
     if constexpr (K == 32 && sizeof(T) == 4)
-        if (ebrick_ok(op, x)) return 1;
+        if (etma_ok(op, x)) return 1;
     return (K == 32 && op.n_pl > 0) ? 2 : 1;
 }
 
@@ -768,9 +759,12 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
     static_assert(K == 1 || K == 32, "slot widths 1 and 32");
     if constexpr (K == 32) {
         if constexpr (sizeof(T) == 4) {
-            if (ebrick_ok(op, x)) {
-                k_ebrick32<<<(unsigned)op.eb.grid, EB_THREADS, (size_t)op.eb.stage_rows * 128u, st>>>(op, sl, ph, x, t);
-                return;
+            if (etma_ok(op, x)) {
+                CUtensorMap xm;
+                if (x_tensor_map(x, op.D, &xm) == 0) {
+                    k_etma32<<<(unsigned)op.et.grid, ET_WARPS * 32, ET_WARPS * ET_STAGES * ET_STAGE, st>>>(xm, op, sl, ph, x, t);
+                    return;
+                }
             }
             const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_grp + 3) / 4, 32LL * sm_count()));
             k_epass32w<<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
@@ -1913,7 +1907,7 @@ static int solve_pass(cpm_solver_s *s, const SolveParams &P, const std::vector<c
     CPM_CUDA_TRY(cudaEventSynchronize(s->e1));
     *ms = 0;
     cudaEventElapsedTime(ms, s->e0, s->e1);
-    return ebrick_status(s->op);
+    return etma_status(s->op);
 }
 
 // Solve k right-hand sides.  A mixed-precision slot that does not converge
