@@ -25,7 +25,7 @@ namespace cpm {
 
 template <class T>
 static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, const T *lval, const T *ldiag, const T *w_ord,
-                           const T *pl_xval, const T *pe_w) {
+                           const T *pl_xval, const T *pe_w, const T *sp_w) {
     OpView<T> v;
     v.bv = o->tube->view();
     v.N = o->N;
@@ -69,6 +69,11 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
     v.pe_w = pe_w;
     v.n_pl = o->n_pl;
     v.et = o->etma();
+    v.n_sp_rows = o->n_sp_rows;
+    v.sp_ptr = o->n_sp_rows ? o->sp_ptr.p : nullptr;
+    v.sp_rec = o->sp_rec.p;
+    v.sp_w = sp_w;
+    v.sp_rows = o->sp_rows.p;
     return v;
 }
 
@@ -76,11 +81,11 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
 
 template <>
 cpm::OpView<double> cpm_opset_s::view<double>() const {
-    return cpm::make_view<double>(this, w.p, p_xval.p, lval.p, ldiag.p, w_ord.p, pl_xval.p, pe_w.p);
+    return cpm::make_view<double>(this, w.p, p_xval.p, lval.p, ldiag.p, w_ord.p, pl_xval.p, pe_w.p, sp_w.p);
 }
 template <>
 cpm::OpView<float> cpm_opset_s::view<float>() const {
-    return cpm::make_view<float>(this, w32.p, p_xval32.p, lval32.p, ldiag32.p, w_ord32.p, pl_xval32.p, pe_w32.p);
+    return cpm::make_view<float>(this, w32.p, p_xval32.p, lval32.p, ldiag32.p, w_ord32.p, pl_xval32.p, pe_w32.p, sp_w32.p);
 }
 
 namespace cpm {
@@ -1444,6 +1449,142 @@ extern "C" int cpm_opset_create_from_cp(cpm_tube_t t, int32_t n_ibc, const cpm_s
 // problems/PoissonWithIBCNearest.cpp:73-89): plain L and E of the tube (no IBC
 // columns) with identity rows at the given tube rows (device indices), which
 // hold Dirichlet values
+namespace cpm {
+static int build_point_batch(cpm_opset_s *o, int n_src, const double *sources, PointBatchInfo &info) {
+    cpm_tube_s *t = o->tube;
+    HostTube ht;
+    CPM_TRY(ht.load(t));
+    const int64_t N = ht.N;
+    std::vector<double> normals;
+    CPM_TRY(tube_normals(o, normals));
+    CPM_TRY(o->normals.upload(normals));
+    DBuf<double> xdev;
+    CPM_TRY(xdev.alloc(3 * N));
+    k_node_coords<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, t->key.p, t->g.xstart, t->g.dx, xdev.p);
+    CPM_CUDA_TRY(cudaGetLastError());
+    std::vector<uint32_t> base;
+    std::vector<double> w;
+    CPM_TRY(t->base.download(base, N));
+    CPM_TRY(t->w.download(w, 12 * N));
+    // per tube row: its records {slot, kind, replaced column, DOF column} and E weights
+    std::vector<std::vector<std::pair<int4, double>>> recs(N);
+    int64_t M = 0;
+    info.dof_set.assign(n_src, {});
+    info.dof_cpdiff.assign(n_src, {});
+    for (int k = 0; k < n_src; ++k) {
+        // GeodesicDistance's point IBC (cpm_geodesic_create): order 1, Dirichlet, on_ibc_tolerance 0.1 dx^2
+        cpm_surface_desc pd;
+        memset(&pd, 0, sizeof(pd));
+        pd.kind = CPM_POINT;
+        pd.nparams = 3;
+        for (int d = 0; d < 3; ++d) pd.params[d] = sources[3 * k + d];
+        pd.bbox[0] = t->surf.desc.bbox[0];
+        pd.bbox[1] = t->surf.desc.bbox[1];
+        pd.boundary_order = 1;
+        pd.use_Jcp_surface_normals = 1;
+        pd.on_ibc_tolerance = 0.1 * t->g.dx * t->g.dx;
+        pd.dof_radius_scale = 1.0;
+        IBCData ib;
+        CPM_TRY(build_ibc_data(t, ht, pd, normals, xdev, nullptr, nullptr, ib));
+        M = std::max<int64_t>(M, (int64_t)ib.dof_set.size());
+        // MoveToIBCColumns for this slot's IBC alone (one IBC: a stencil entry moves at most once)
+        for (size_t i = 0; i < ib.tag_set.size(); ++i) {
+            const int64_t q = ib.tag_set[i];
+            const double *dir = &ib.tag_dir[3 * i];
+            for (int sidx = 0; sidx < 64; ++sidx) {
+                const int a = sidx >> 4, b = (sidx >> 2) & 3, c = sidx & 3;
+                const int col = ht.node(unpack_i(base[q]) + a, unpack_j(base[q]) + b, unpack_k(base[q]) + c);
+                if (col >= 0 && tagged(ib, dir, col, 1.0) && ib.dof_sub[col] >= 0)
+                    recs[q].push_back({make_int4(k, 0, col, (int)(N + ib.dof_sub[col])),
+                                       (w[12 * q + a] * w[12 * q + 4 + b]) * w[12 * q + 8 + c]});
+            }
+            for (int d = 0; d < 6; ++d) {
+                const int col = ht.nbr(q, d);
+                if (col >= 0 && tagged(ib, dir, col, 1.0) && ib.dof_sub[col] >= 0)
+                    recs[q].push_back({make_int4(k, 1, col, (int)(N + ib.dof_sub[col])), 0.0});
+            }
+        }
+        info.dof_set[k] = ib.dof_set;
+        info.dof_cpdiff[k] = ib.dof_cpdiff;
+    }
+    // rows N .. N + M: identity rows (slot k's DOF values)
+    const int64_t D = N + M;
+    o->D = D;
+    std::vector<uint8_t> flags(D, 0), ident(D, 0);
+    for (int64_t r = N; r < D; ++r) {
+        flags[r] = F_IDENT;
+        ident[r] = 1;
+    }
+    std::vector<int32_t> sp_ptr(D + 1, 0), sp_rows;
+    std::vector<int4> sp_rec;
+    std::vector<double> sp_w;
+    for (int64_t q = 0; q < D; ++q) {
+        sp_ptr[q] = (int32_t)sp_rec.size();
+        if (q < N && !recs[q].empty()) {
+            flags[q] |= F_SLOTP;
+            sp_rows.push_back((int32_t)q);
+            for (auto &e : recs[q]) {
+                sp_rec.push_back(e.first);
+                sp_w.push_back(e.second);
+            }
+        }
+    }
+    sp_ptr[D] = (int32_t)sp_rec.size();
+    o->n_sp_rows = (int64_t)sp_rows.size();
+    if (sp_rows.empty()) sp_rows.push_back(0);
+    if (sp_rec.empty()) {
+        sp_rec.push_back(make_int4(-1, 0, 0, 0));
+        sp_w.push_back(0.0);
+    }
+    std::vector<uint32_t> base_d(D, 0);
+    std::vector<double> w_d(12 * D, 0.0);
+    std::copy(base.begin(), base.end(), base_d.begin());
+    std::copy(w.begin(), w.end(), w_d.begin());
+    std::vector<int32_t> patch(D, -1), lptr(D - N + 1, 0);
+    std::vector<double> ldiag(D - N + 1, 0.0);
+    CPM_TRY(o->base.upload(base_d));
+    CPM_TRY(o->w.upload(w_d));
+    CPM_TRY(o->flags.upload(flags));
+    CPM_TRY(o->patch.upload(patch));
+    CPM_TRY(o->lptr.upload(lptr));
+    CPM_TRY(o->ldiag.upload(ldiag));
+    CPM_TRY(o->sp_ptr.upload(sp_ptr));
+    CPM_TRY(o->sp_rows.upload(sp_rows));
+    CPM_TRY(o->sp_rec.upload(sp_rec));
+    CPM_TRY(o->sp_w.upload(sp_w));
+    std::vector<float> sp_w32(sp_w.begin(), sp_w.end());
+    CPM_TRY(o->sp_w32.upload(sp_w32));
+    o->h_identity = ident;
+    o->h_kind.assign(D, 0);
+    o->h_ibc.assign(D, -1);
+    for (int64_t r = N; r < D; ++r) o->h_kind[r] = 2;
+    o->h_point.resize(3 * D, 0.0);
+    return 0;
+}
+
+int opset_create_point_batch(cpm_tube_s *t, int n_src, const double *sources, cpm_opset_s **out, PointBatchInfo &info) {
+    if (!t || !out || n_src < 1 || n_src > 32 || !sources) return fail(CPM_ERR_INVALID_ARG, "point batch: 1 to 32 sources");
+    *out = nullptr;
+    cpm_opset_s *o = new cpm_opset_s();
+    o->tube = t;
+    int rc = build_base(o);
+    if (!rc) rc = build_point_batch(o, n_src, sources, info);
+    if (!rc) rc = build_schedule(o);
+    if (!rc) rc = make_float_copies(o);
+    if (!rc) rc = build_etma_sched(o);
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(stream());
+        if (e != cudaSuccess) rc = fail(CPM_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (rc) {
+        delete o;
+        return rc;
+    }
+    *out = o;
+    return 0;
+}
+}  // namespace cpm
+
 extern "C" int cpm_opset_create_identity(cpm_tube_t t, int64_t n_rows, const int64_t *rows, cpm_opset_t *out) {
     if (!t || !out || n_rows < 0 || (n_rows > 0 && !rows)) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
     *out = nullptr;

@@ -15,6 +15,7 @@ enum RowFlags : uint8_t {
     F_LCSR = 8,    // L row stored as CSR (IBC DOF rows)
     F_ENEG = 16,   // E row negated (2nd-order Dirichlet DOF rows)
     F_EXTRA = 32,  // E row has one extra entry (2 * Dirichlet value)
+    F_SLOTP = 64,  // tube row with per-slot patch records (a batch with one point IBC per slot)
 };
 
 // Schedule of the brick-staged E pass (k_ebrick32, FP32, 32 slots).  Rows are
@@ -87,7 +88,28 @@ struct OpView {
     const T *pe_w;                            // stencil weight (wx_i wy_j) wz_k of the moved point
     int64_t n_ord, n_grp, n_ident, n_pl;
     ETma et;                                  // TMA-staged E pass (FP32 weights)
+    // per-slot patches of a batch whose slots each carry their own point IBC
+    // (cpm_geodesic_batch_*): row r's records sp_rec[sp_ptr[r] .. sp_ptr[r + 1]),
+    // {slot, 0 E entry / 1 L entry, the column it replaces, the slot's DOF column};
+    // E entries carry the stencil weight.  Null when the operator has none.
+    const int32_t *sp_ptr;
+    const int4 *sp_rec;
+    const T *sp_w;
+    const int32_t *sp_rows;                   // rows with records
+    int64_t n_sp_rows;
 };
+
+// the per-slot L corrections of row r, slot s (K-wide batch): a moved neighbour
+// reads the slot's DOF column of t instead of the tube node's
+template <class T, int K>
+__device__ __forceinline__ T slot_l_correction(const OpView<T> &op, int64_t r, int s, T n, const T *__restrict__ t) {
+    T c = 0;
+    for (int e = op.sp_ptr[r]; e < op.sp_ptr[r + 1]; ++e) {
+        const int4 rec = op.sp_rec[e];
+        if (rec.x == s && rec.y == 1) c += t[(int64_t)rec.w * K + s] - t[(int64_t)rec.z * K + s];
+    }
+    return n * (op.Loff * c);
+}
 
 // ---------------------------------------------------------------------------
 // A 4^3 stencil based at (bi,bj,bk) touches at most 2x2x2 bricks: corner c =
@@ -456,6 +478,7 @@ __device__ __forceinline__ void l_rows(const OpView<T> &op, const int64_t (&r)[U
             for (int d = 0; d < 6; ++d)
                 if (c[u][d] >= 0 && act && !(fl[u] & F_IDENT)) off += t[(int64_t)c[u][d] * K + s];
             y[u] = (fl[u] & F_IDENT) ? xr[u] : m * xr[u] + n * (op.Ldiag * xr[u] + op.Loff * off);
+            if ((fl[u] & F_SLOTP) && act) y[u] += slot_l_correction<T, K>(op, r[u], s, n, t);
         }
     } else {
         // FP32: the same row as Loff (sum_d (t_d - x) + (k - 6) x) with k present
@@ -473,6 +496,7 @@ __device__ __forceinline__ void l_rows(const OpView<T> &op, const int64_t (&r)[U
                 }
             off += (T)(k - 6) * xr[u];
             y[u] = (fl[u] & F_IDENT) ? xr[u] : m * xr[u] + n * (op.Loff * off);
+            if ((fl[u] & F_SLOTP) && act) y[u] += slot_l_correction<T, K>(op, r[u], s, n, t);
         }
     }
 }
@@ -586,6 +610,12 @@ struct cpm_opset_s {
     std::vector<int64_t> col_start, dcol_start;
     int64_t identity_rows_start = 0;
     std::shared_ptr<cpm::CpOverrides> cp_ovr;  // set by cpm_opset_create_from_cp
+    // per-slot patches (a batch with one point IBC per slot)
+    cpm::DBuf<int32_t> sp_ptr, sp_rows;
+    cpm::DBuf<int4> sp_rec;
+    cpm::DBuf<double> sp_w;
+    cpm::DBuf<float> sp_w32;
+    int64_t n_sp_rows = 0;
 
     template <class T>
     cpm::OpView<T> view() const;
@@ -594,4 +624,17 @@ struct cpm_opset_s {
 namespace cpm {
 // whole-tube Jcp surface normals (eigenvector 0) of the operator's tube, uploaded to o->normals
 int opset_tube_normals(cpm_opset_s *o);
+
+// A batch of point IBCs, one per slot (the heat-method geodesic from n_src
+// sources at once): the plain tube operator with M = the largest DOF count
+// identity rows appended (slot k's DOF i is row N + i, holding its Dirichlet
+// value) and, as per-slot patch records, each slot's moved E and L columns of
+// the tube rows near its source (AddIBCExtension / AddIBCFiniteDifference of
+// an order-1 Dirichlet point IBC).  info: each source's DOF subset (tube
+// rows) and cp_diff, for the heat step's right-hand side.
+struct PointBatchInfo {
+    std::vector<std::vector<int64_t>> dof_set;
+    std::vector<std::vector<double>> dof_cpdiff;
+};
+int opset_create_point_batch(cpm_tube_s *t, int n_src, const double *sources, cpm_opset_s **out, PointBatchInfo &info);
 }  // namespace cpm

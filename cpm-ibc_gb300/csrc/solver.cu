@@ -28,9 +28,6 @@
 #include <mutex>
 #include <string>
 
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
 #include "opset.h"
 
 namespace cpm {
@@ -412,34 +409,20 @@ __global__ void __launch_bounds__(128) k_epass32w(OpView<float> op, const Slot *
         }
 }
 
-// ---- TMA-staged E pass for 32 FP32 slots, IBC patch included (k_etma32).
+// ---- Staged E pass for 32 FP32 slots, IBC patch included (k_etma32).
 // Every warp runs its own two-stage pipeline over base groups (a static
-// stride): it gathers the next group's 64 stencil rows of x into one of its
-// shared-memory stages with TMA (cp.async.bulk.tensor tile::gather4, four
-// 128-byte rows an instruction, completing on the stage's mbarrier) and
-// computes the current group from the other stage, with the arithmetic of
-// k_epass32w; rows on the IBC patch list get k_epatch32's correction in
-// registers before their one store.  Results are bit for bit those of
-// k_epass32w followed by k_epatch32.
+// stride): it copies the next group's 64 stencil rows of x into one of its
+// shared-memory stages with 16-byte asynchronous copies (cp.async, eight lanes
+// a 128-byte row, one commit group per stage) and computes the current group
+// from the other stage, with the arithmetic of k_epass32w; rows on the IBC
+// patch list get k_epatch32's correction in registers before their one store.
+// Results are bit for bit those of k_epass32w followed by k_epatch32.
 constexpr int ET_WARPS = 4;       // warps per block
 constexpr int ET_STAGES = 2;      // stages per warp
 constexpr int ET_STAGE = 64 * 128; // one group's 64 rows of 32 FP32 slots
 
 // shared-memory address of a generic pointer
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// waits for phase `parity` of mbarrier `bar` to complete: at most 2^19 waits
-// of at most ~2 us each (the suspend-time hint), about a second in all;
-// false if it did not complete
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 19); ++it) {
-        uint32_t done;
-        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
-                     : "=r"(done) : "r"(bar), "r"(parity), "r"(2000) : "memory");
-        if (done) return true;
-    }
-    return false;
-}
 
 // k_epatch32's correction of one patched row, lane = slot: the bulk stencil
 // values from the stage, the moved and extra columns from x
@@ -479,59 +462,40 @@ __device__ __forceinline__ float et_patch(const ETma &et, const char *stage, con
     return acc;
 }
 
-// the four rows c of x (32 FP32 slots each) into 512 contiguous bytes of shared memory
-__device__ __forceinline__ void tma_gather4(uint32_t dst, const CUtensorMap *map, int4 c, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
-        ::"r"(dst), "l"(map), "r"(0), "r"(c.x), "r"(c.y), "r"(c.z), "r"(c.w), "r"(bar) : "memory");
-}
-
-__global__ void __launch_bounds__(ET_WARPS * 32, 3) k_etma32(const __grid_constant__ CUtensorMap xmap, OpView<float> op,
-                                                             const Slot *__restrict__ sl, int ph, const float *__restrict__ x,
-                                                             float *__restrict__ t) {
+__global__ void __launch_bounds__(ET_WARPS * 32, 3) k_etma32(OpView<float> op, const Slot *__restrict__ sl, int ph,
+                                                             const float *__restrict__ x, float *__restrict__ t) {
     extern __shared__ __align__(1024) unsigned char et_smem[];
     __shared__ __align__(16) float sw[ET_WARPS][EW_ROWS * 12];
-    __shared__ __align__(8) uint64_t bars[ET_WARPS][ET_STAGES];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool act = (ph < 0) || sl[lane].phase == ph;
     if (!__any_sync(FULL, act)) return;  // the same 32 slots in every warp: grid-uniform
     const ETma &et = op.et;
     const char *stages = (const char *)et_smem + (size_t)warp * ET_STAGES * ET_STAGE;
-    const uint32_t sst = smem_u32(stages), sbar = smem_u32(&bars[warp][0]);
-    if (lane == 0) {
-#pragma unroll
-        for (int s = 0; s < ET_STAGES; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar + 8 * s) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncwarp();
+    const uint32_t sst = smem_u32(stages);
     float *w = sw[warp];
     const int64_t W = (int64_t)gridDim.x * ET_WARPS;
-    // the 64 stencil rows of group g into stage s
+    const int sub = lane >> 3, chunk = lane & 7;  // row within a slab of four, 16-byte chunk of the row
+    // the 64 stencil rows of group g into stage s (one commit group)
     auto issue = [&](int64_t g, int s) {
-        if (lane == 0)
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar + 8 * s), "r"(ET_STAGE) : "memory");
-        __syncwarp();
-        if (lane < 16) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const int4 c = __ldg((const int4 *)(op.gcols + 64 * g) + lane);
-            tma_gather4(sst + (uint32_t)s * ET_STAGE + 512u * lane, &xmap, c, sbar + 8 * s);
+        if (g < op.n_grp) {
+            const int32_t *gc = op.gcols + 64 * g;
+#pragma unroll
+            for (int m = 0; m < 16; ++m) {
+                const int rrow = 4 * m + sub;
+                const uint32_t col = (uint32_t)__ldg(gc + rrow);
+                const uint32_t dst = sst + (uint32_t)s * ET_STAGE + (uint32_t)rrow * 128u + 16u * chunk;
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(x + col * 32u + 4 * chunk) : "memory");
+            }
         }
+        asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    uint32_t phases = 0;
     int64_t g = (int64_t)blockIdx.x * ET_WARPS + warp;
-    if (g < op.n_grp) issue(g, 0);
+    issue(g, 0);
     for (int k = 0; g < op.n_grp; g += W, ++k) {
         const int s = k & 1;
-        if (g + W < op.n_grp) issue(g + W, s ^ 1);  // the other stage was read in the previous round
-        const bool ok = mbar_wait(sbar + 8 * s, (phases >> s) & 1u);
-        phases ^= 1u << s;
-        if (!__all_sync(FULL, ok)) {
-            // a copy did not arrive: record it, give both stages' copies one more bounded wait, stop
-            if (lane == 0) atomicExch(et.err, 1);
-            mbar_wait(sbar + 8 * s, ((phases >> s) & 1u) ^ 1u);
-            if (g + W < op.n_grp) mbar_wait(sbar + 8 * (s ^ 1), (phases >> (s ^ 1)) & 1u);
-            return;
-        }
+        issue(g + W, s ^ 1);  // the other stage was read in the previous round
+        asm volatile("cp.async.wait_group 1;" ::: "memory");  // this lane's copies of stage s are done
+        __syncwarp();                                         // and every lane's
         const char *stage = stages + (size_t)s * ET_STAGE;
         const int p0 = op.grp[g], p1 = op.grp[g + 1];
         int pr = et.g_pq[g];
@@ -600,6 +564,7 @@ __global__ void __launch_bounds__(ET_WARPS * 32, 3) k_etma32(const __grid_consta
         }
         __syncwarp();  // the stage is read before it is refilled
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     // identity rows: t = x
     if (act)
         for (int64_t q = (int64_t)blockIdx.x * ET_WARPS + warp; q < op.n_ident; q += W) {
@@ -620,29 +585,6 @@ int etma_setup(ETma &et) {
     int b = 1;
     CPM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_etma32, ET_WARPS * 32, (size_t)smem));
     et.grid = std::max(1, b) * sm_count();
-    return 0;
-}
-
-// the tensor map of a [D][32] FP32 array for tile::gather4: rows of 128 bytes,
-// boxes one row high (cuTensorMapEncodeTiled, reached through the runtime's
-// driver entry point so the library needs no link to the driver library)
-static int x_tensor_map(const float *x, int64_t D, CUtensorMap *map) {
-    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    if (!encode) {
-        void *fn = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        CPM_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
-        if (q != cudaDriverEntryPointSuccess || !fn) return fail(CPM_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
-        encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-    }
-    const cuuint64_t dims[2] = {32, (cuuint64_t)D};
-    const cuuint64_t strides[1] = {128};
-    const cuuint32_t box[2] = {32, 1};
-    const cuuint32_t estr[2] = {1, 1};
-    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)x, dims, strides, box, estr,
-                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(CPM_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
     return 0;
 }
 
@@ -746,12 +688,44 @@ __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__re
     }
 }
 
+// per-slot E corrections of a batch with one point IBC per slot (OpView::sp_*),
+// after the bulk E pass: warp per row with records, lane = slot,
+// t += sum over the slot's E entries of w (x[DOF column] - x[replaced column])
+template <class T>
+__global__ void __launch_bounds__(128) k_slot_epatch32(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x,
+                                                       T *__restrict__ t) {
+    const int lane = threadIdx.x & 31;
+    const bool act = (ph < 0) || sl[lane].phase == ph;
+    if (!__any_sync(FULL, act)) return;
+    const int64_t warps = (int64_t)gridDim.x * 4;
+    for (int64_t q = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5); q < op.n_sp_rows; q += warps) {
+        const int64_t r = op.sp_rows[q];
+        T c = 0;
+        bool any = false;
+        for (int e = op.sp_ptr[r]; e < op.sp_ptr[r + 1]; ++e) {
+            const int4 rec = op.sp_rec[e];
+            if (rec.x == lane && rec.y == 0) {
+                c += op.sp_w[e] * (x[(int64_t)rec.w * 32 + lane] - x[(int64_t)rec.z * 32 + lane]);
+                any = true;
+            }
+        }
+        if (act && any) t[r * 32 + lane] += c;
+    }
+}
+
+template <class T>
+static void slot_epatch(const OpView<T> &op, const Slot *sl, int ph, const T *x, T *t, cudaStream_t st) {
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_sp_rows + 3) / 4, 16LL * sm_count()));
+    k_slot_epatch32<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
+}
+
 // kernels one E pass of x launches (the brick-staged FP32 pass includes the patch)
 template <class T, int K>
 static inline int epass_kernels(const OpView<T> &op, const T *x) {
+    const int sp = (K == 32 && op.n_sp_rows > 0) ? 1 : 0;
     if constexpr (K == 32 && sizeof(T) == 4)
-        if (etma_ok(op, x)) return 1;
-    return (K == 32 && op.n_pl > 0) ? 2 : 1;
+        if (etma_ok(op, x)) return 1 + sp;
+    return ((K == 32 && op.n_pl > 0) ? 2 : 1) + sp;
 }
 
 template <class T, int K>
@@ -760,11 +734,9 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
     if constexpr (K == 32) {
         if constexpr (sizeof(T) == 4) {
             if (etma_ok(op, x)) {
-                CUtensorMap xm;
-                if (x_tensor_map(x, op.D, &xm) == 0) {
-                    k_etma32<<<(unsigned)op.et.grid, ET_WARPS * 32, ET_WARPS * ET_STAGES * ET_STAGE, st>>>(xm, op, sl, ph, x, t);
-                    return;
-                }
+                k_etma32<<<(unsigned)op.et.grid, ET_WARPS * 32, ET_WARPS * ET_STAGES * ET_STAGE, st>>>(op, sl, ph, x, t);
+                if (op.n_sp_rows > 0) slot_epatch(op, sl, ph, x, t, st);
+                return;
             }
             const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_grp + 3) / 4, 32LL * sm_count()));
             k_epass32w<<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
@@ -780,6 +752,7 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
         const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_pl + 3) / 4, 16LL * sm_count()));
         k_epatch32<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
     }
+    if (K == 32 && op.n_sp_rows > 0) slot_epatch(op, sl, ph, x, t, st);
 }
 
 // Row loops: thread (row group, slot s) with K slots per row; each trip
