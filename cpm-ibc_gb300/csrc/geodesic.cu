@@ -251,6 +251,103 @@ __global__ void k_zero_rows(int64_t n, const int32_t *__restrict__ rows, double 
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) b[rows[i]] = 0.0;
 }
+// ---- the same steps for 32-slot batches ([rows][32], one source per slot)
+
+// central differences along each axis of every slot: gx, gy, gz ([D][32]; rows >= N untouched)
+__global__ void k_grad3_32(int64_t N, const int32_t *__restrict__ nbr6, double dx, const double *__restrict__ u,
+                           double *__restrict__ gx, double *__restrict__ gy, double *__restrict__ gz) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= N * 32) return;
+    const int64_t q = i >> 5;
+    const int k = (int)(i & 31);
+    const double cp = 0.5 / dx, cm = -0.5 / dx;
+    double *g[3] = {gx, gy, gz};
+    for (int d = 0; d < 3; ++d) {
+        const int a = nbr6[6 * q + 2 * d], b = nbr6[6 * q + 2 * d + 1];
+        double s = 0.0;
+        if (a >= 0) s += cp * u[(int64_t)a * 32 + k];
+        if (b >= 0) s += cm * u[(int64_t)b * 32 + k];
+        g[d][i] = s;
+    }
+}
+
+// g -= (g.n) n ; g /= |g| for every tube row and slot
+__global__ void k_project_normalise32(int64_t N, const double *__restrict__ nrm, double *__restrict__ gx, double *__restrict__ gy,
+                                      double *__restrict__ gz) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= N * 32) return;
+    const int64_t q = i >> 5;
+    double v[3] = {gx[i], gy[i], gz[i]}, n[3] = {nrm[3 * q], nrm[3 * q + 1], nrm[3 * q + 2]};
+    double dn = 0.0;
+    for (int d = 0; d < 3; ++d) dn += v[d] * n[d];
+    for (int d = 0; d < 3; ++d) v[d] = v[d] - dn * n[d];
+    double nn = 0.0;
+    for (int d = 0; d < 3; ++d) nn += v[d] * v[d];
+    nn = sqrt(nn);
+    if (nn != 0.0)
+        for (int d = 0; d < 3; ++d) v[d] /= nn;
+    gx[i] = v[0];
+    gy[i] = v[1];
+    gz[i] = v[2];
+}
+
+// div = sum_d Dc_d g_d on the tube rows of every slot; rows >= N are 0
+__global__ void k_divergence32(int64_t N, int64_t D, const int32_t *__restrict__ nbr6, double dx, const double *__restrict__ gx,
+                               const double *__restrict__ gy, const double *__restrict__ gz, double *__restrict__ b) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= D * 32) return;
+    const int64_t q = i >> 5;
+    const int k = (int)(i & 31);
+    if (q >= N) {
+        b[i] = 0.0;
+        return;
+    }
+    const double cp = 0.5 / dx, cm = -0.5 / dx;
+    const double *g[3] = {gx, gy, gz};
+    double div = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        const int a = nbr6[6 * q + 2 * d], c = nbr6[6 * q + 2 * d + 1];
+        double s = 0.0;
+        if (a >= 0) s += cp * g[d][(int64_t)a * 32 + k];
+        if (c >= 0) s += cm * g[d][(int64_t)c * 32 + k];
+        div = div + s;
+    }
+    b[i] = div;
+}
+
+// b = -a on the first n rows of a [rows][32] batch
+__global__ void k_negate32(int64_t n, const double *__restrict__ a, double *__restrict__ b) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n * 32) b[i] = -a[i];
+}
+
+// per-slot minimum over D rows: block partial minima part[block][32]
+__global__ void k_colmin32(int64_t D, const double *__restrict__ a, double *__restrict__ part) {
+    __shared__ double sh[8][32];
+    const int k = threadIdx.x & 31, rw = threadIdx.x >> 5;
+    double v = 1.7976931348623157e308;
+    for (int64_t q = (int64_t)blockIdx.x * 8 + rw; q < D; q += (int64_t)gridDim.x * 8) v = fmin(v, a[q * 32 + k]);
+    sh[rw][k] = v;
+    __syncthreads();
+    if (rw == 0) {
+        for (int j = 1; j < 8; ++j) v = fmin(v, sh[j][k]);
+        part[(int64_t)blockIdx.x * 32 + k] = v;
+    }
+}
+
+// phi -= min over the slot's rows (the partial minima of k_colmin32)
+__global__ void k_sub_colmin32(int64_t D, int nparts, const double *__restrict__ part, double *__restrict__ a) {
+    __shared__ double mn[32];
+    if (threadIdx.x < 32) {
+        double v = 1.7976931348623157e308;
+        for (int p = 0; p < nparts; ++p) v = fmin(v, part[(int64_t)p * 32 + threadIdx.x]);
+        mn[threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D * 32; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] -= mn[i & 31];
+}
+
 }  // namespace cpm
 
 using namespace cpm;
@@ -386,6 +483,139 @@ extern "C" int cpm_geodesic_run(cpm_geodesic_t g, double dt, int32_t precision, 
 }
 
 extern "C" int cpm_geodesic_destroy(cpm_geodesic_t g) {
+    delete g;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// The heat-method geodesic distance from up to 32 sources at once.  No
+// counterpart in the reference, whose GeodesicDistance::ComputeDistance
+// (problems/GeodesicDistance.cpp:11-69) serves one source per call with its own
+// point-IBC operator.  Here the sources share one operator: the tube's bulk
+// stencils with every source's point IBC as per-slot patch records
+// (opset_create_point_batch), so each step is one 32-slot solve in which every
+// slot carries exactly its own source's operator; Step 2 runs on all slots at
+// once.  Each source's result equals its one-source run up to rounding.
+struct cpm_geodesic_batch_s {
+    cpm_tube_s *tube = nullptr;
+    cpm_opset_s *op = nullptr;
+    PointBatchInfo info;
+    int n_src = 0;
+    int64_t N = 0, D = 0;
+    ~cpm_geodesic_batch_s() { delete op; }
+};
+
+extern "C" int cpm_geodesic_batch_create(cpm_tube_t t, int32_t n_src, const double *sources, cpm_geodesic_batch_t *out,
+                                         int64_t *D_out) {
+    if (!t || !sources || !out || n_src < 1 || n_src > 32)
+        return fail(CPM_ERR_INVALID_ARG, "geodesic_batch_create: 1 to 32 sources");
+    *out = nullptr;
+    cpm_geodesic_batch_s *g = new cpm_geodesic_batch_s();
+    g->tube = t;
+    g->n_src = n_src;
+    const int rc = opset_create_point_batch(t, n_src, sources, &g->op, g->info);
+    if (rc) {
+        delete g;
+        return rc;
+    }
+    g->N = g->op->N;
+    g->D = g->op->D;
+    if (D_out) *D_out = g->D;
+    *out = g;
+    return 0;
+}
+
+extern "C" int cpm_geodesic_batch_run(cpm_geodesic_batch_t g, double dt, double tol, int32_t heat_sweeps, double *phi_out,
+                                      int32_t *iters_out) {
+    if (!g || !phi_out || dt <= 0) return fail(CPM_ERR_INVALID_ARG, "geodesic_batch_run: invalid arguments");
+    const int64_t N = g->N, D = g->D;
+    const int K = 32, ns = g->n_src;
+    const double dx = g->tube->g.dx;
+    const int32_t *nbr6 = g->op->nbr6.p;  // tube rows: the plain neighbours (no L moves in the bulk)
+    cudaStream_t st = stream();
+    // Step 1 right-hand sides: SmoothH at the DOF rows (Dirichlet values) and at the DOF nodes' tube rows
+    const double extent = g->tube->g.radius, tolr = g->tube->g.dx;
+    const double scale = std::atanh(1 - tolr) / extent;
+    auto smooth = [scale](double x) { return 0.5 * std::tanh(-scale * x) + 0.5; };
+    std::vector<double> hb((size_t)D * K, 0.0);
+    for (int k = 0; k < ns; ++k) {
+        const auto &dof = g->info.dof_set[k];
+        const auto &cd = g->info.dof_cpdiff[k];
+        for (size_t i = 0; i < dof.size(); ++i) {
+            double n2 = 0.0;
+            for (int c = 0; c < 3; ++c) n2 += cd[3 * i + c] * cd[3 * i + c];
+            hb[(size_t)(N + (int64_t)i) * K + k] = smooth(-std::sqrt(n2));
+        }
+        for (size_t i = 0; i < dof.size(); ++i) {
+            double n2 = 0.0;
+            for (int c = 0; c < 3; ++c) n2 += cd[3 * i + c] * cd[3 * i + c];
+            hb[(size_t)dof[i] * K + k] = smooth(std::sqrt(n2));
+        }
+    }
+    DBuf<double> b, x, u, gx, gy, gz, part;
+    CPM_TRY(b.upload(hb));
+    for (auto *a : {&x, &u, &gx, &gy, &gz}) {
+        CPM_TRY(a->alloc((size_t)D * K));
+        CPM_TRY(a->zero());
+    }
+    const int nparts = 256;
+    CPM_TRY(part.alloc((size_t)nparts * K));
+    cpm_solve_opts o;
+    memset(&o, 0, sizeof(o));
+    o.tol = tol > 0 ? tol : 1e-10;
+    o.max_iters = 100000;
+    o.precision = 0;
+    o.precond = 2;
+    o.precond_iters = heat_sweeps > 0 ? heat_sweeps : 2000;
+    std::vector<cpm_solve_stats> ss(ns);
+    cpm_solver_t heat = nullptr, pois = nullptr;
+    CPM_TRY(cpm_solver_create(g->op, 1.0, -dt, K, &heat));
+    int rc = cpm_solver_create(g->op, 0.0, 1.0, K, &pois);
+    auto cleanup = [&](int r) {
+        if (heat) cpm_solver_destroy(heat);
+        if (pois) cpm_solver_destroy(pois);
+        return r;
+    };
+    if (rc) return cleanup(rc);
+    const unsigned bN = (unsigned)((N * K + 255) / 256), bD = (unsigned)((D * K + 255) / 256);
+    // Step 1: heat flow from each source; u = -x[0:N]
+    if ((rc = cpm_solve_device(heat, ns, b.p, x.p, &o, ss.data()))) return cleanup(rc);
+    if (iters_out)
+        for (int k = 0; k < ns; ++k) iters_out[4 * k] = ss[k].iterations;
+    o.precond = 1;
+    o.precond_iters = 0;
+    k_negate32<<<bN, 256, 0, st>>>(N, x.p, u.p);
+    count_launches(1);
+    for (int round = 0; round < 3; ++round) {
+        if (round > 0) CPM_TRY(epass64_batch(g->op, false, x.p, u.p));  // u = E phi (plain E)
+        // Step 2 + ComputeDivergence
+        k_grad3_32<<<bN, 256, 0, st>>>(N, nbr6, dx, u.p, gx.p, gy.p, gz.p);
+        count_launches(1);
+        for (DBuf<double> *gd : {&gx, &gy, &gz}) {
+            CPM_TRY(epass64_batch(g->op, false, gd->p, b.p));
+            CPM_CUDA_TRY(cudaMemcpyAsync(gd->p, b.p, (size_t)N * K * 8, cudaMemcpyDeviceToDevice, st));
+        }
+        k_project_normalise32<<<bN, 256, 0, st>>>(N, g->op->normals.p, gx.p, gy.p, gz.p);
+        k_divergence32<<<bD, 256, 0, st>>>(N, D, nbr6, dx, gx.p, gy.p, gz.p, b.p);
+        count_launches(2);
+        CPM_CUDA_TRY(cudaGetLastError());
+        // Step 3: Poisson solve of every slot, then phi -= min phi per slot
+        if ((rc = cpm_solve_device(pois, ns, b.p, x.p, &o, ss.data()))) return cleanup(rc);
+        if (iters_out)
+            for (int k = 0; k < ns; ++k) iters_out[4 * k + 1 + round] = ss[k].iterations;
+        k_colmin32<<<nparts, 256, 0, st>>>(D, x.p, part.p);
+        k_sub_colmin32<<<bD, 256, 0, st>>>(D, nparts, part.p, x.p);
+        count_launches(2);
+    }
+    // phi of source k: [D] rows (tube rows, then its own DOF rows; the other DOF rows are 0)
+    std::vector<double> hx;
+    CPM_TRY(x.download(hx, (size_t)D * K));
+    for (int k = 0; k < ns; ++k)
+        for (int64_t r = 0; r < D; ++r) phi_out[(size_t)k * D + r] = hx[(size_t)r * K + k];
+    return cleanup(0);
+}
+
+extern "C" int cpm_geodesic_batch_destroy(cpm_geodesic_batch_t g) {
     delete g;
     return 0;
 }

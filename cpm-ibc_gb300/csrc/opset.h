@@ -637,4 +637,8 @@ struct PointBatchInfo {
     std::vector<std::vector<double>> dof_cpdiff;
 };
 int opset_create_point_batch(cpm_tube_s *t, int n_src, const double *sources, cpm_opset_s **out, PointBatchInfo &info);
+
+// E~ x of a [D][32] FP64 batch, every slot, on the library stream; slot_patches
+// false leaves out a batch operator's per-slot point-IBC patches (the plain E)
+int epass64_batch(const cpm_opset_s *o, bool slot_patches, const double *x, double *t);
 }  // namespace cpm

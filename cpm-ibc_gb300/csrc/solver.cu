@@ -420,6 +420,8 @@ __global__ void __launch_bounds__(128) k_epass32w(OpView<float> op, const Slot *
 constexpr int ET_WARPS = 4;       // warps per block
 constexpr int ET_STAGES = 2;      // stages per warp
 constexpr int ET_STAGE = 64 * 128; // one group's 64 rows of 32 FP32 slots
+constexpr int ET_WROWS = 16;       // rows of a group whose weights and row ids are staged with it
+constexpr int ET_STAGE_ALL = ET_STAGE + ET_WROWS * 48 + ET_WROWS * 4;  // 9024 bytes
 
 // shared-memory address of a generic pointer
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -470,44 +472,74 @@ __global__ void __launch_bounds__(ET_WARPS * 32, 3) k_etma32(OpView<float> op, c
     const bool act = (ph < 0) || sl[lane].phase == ph;
     if (!__any_sync(FULL, act)) return;  // the same 32 slots in every warp: grid-uniform
     const ETma &et = op.et;
-    const char *stages = (const char *)et_smem + (size_t)warp * ET_STAGES * ET_STAGE;
+    char *stages = (char *)et_smem + (size_t)warp * ET_STAGES * ET_STAGE_ALL;
     const uint32_t sst = smem_u32(stages);
     float *w = sw[warp];
     const int64_t W = (int64_t)gridDim.x * ET_WARPS;
     const int sub = lane >> 3, chunk = lane & 7;  // row within a slab of four, 16-byte chunk of the row
-    // the 64 stencil rows of group g into stage s (one commit group)
-    auto issue = [&](int64_t g, int s) {
+    // a group's metadata, loaded one round before its copies are issued
+    struct Meta {
+        int col[16];   // stencil rows 4 m + sub of the group
+        int p0, p1;    // its rows ord[p0 .. p1)
+    };
+    auto load_meta = [&](int64_t g, Meta &m) {
         if (g < op.n_grp) {
             const int32_t *gc = op.gcols + 64 * g;
 #pragma unroll
-            for (int m = 0; m < 16; ++m) {
-                const int rrow = 4 * m + sub;
-                const uint32_t col = (uint32_t)__ldg(gc + rrow);
-                const uint32_t dst = sst + (uint32_t)s * ET_STAGE + (uint32_t)rrow * 128u + 16u * chunk;
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(x + col * 32u + 4 * chunk) : "memory");
+            for (int q = 0; q < 16; ++q) m.col[q] = __ldg(gc + 4 * q + sub);
+            m.p0 = __ldg(op.grp + g);
+            m.p1 = __ldg(op.grp + g + 1);
+        }
+    };
+    // group g into stage s: its 64 stencil rows of x, then (up to ET_WROWS rows) its
+    // sorted weights and row ids; one commit group
+    auto issue = [&](int64_t g, const Meta &m, int s) {
+        if (g < op.n_grp) {
+            const uint32_t st0 = sst + (uint32_t)s * ET_STAGE_ALL;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const uint32_t dst = st0 + (uint32_t)(4 * q + sub) * 128u + 16u * chunk;
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(x + (uint32_t)m.col[q] * 32u + 4 * chunk)
+                             : "memory");
             }
+            const int nr = min(m.p1 - m.p0, ET_WROWS);
+            for (int c = lane; c < 3 * nr; c += 32)  // 48 bytes a row: three 16-byte chunks
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(st0 + ET_STAGE + 16u * c),
+                             "l"(op.w_ord + 12 * (size_t)m.p0 + 4 * c) : "memory");
+            if (lane < nr)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(st0 + ET_STAGE + ET_WROWS * 48u + 4u * lane),
+                             "l"(op.ord + m.p0 + lane) : "memory");
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
     int64_t g = (int64_t)blockIdx.x * ET_WARPS + warp;
-    issue(g, 0);
+    Meta cur, nxt;
+    load_meta(g, cur);
+    issue(g, cur, 0);
+    load_meta(g + W, nxt);
     for (int k = 0; g < op.n_grp; g += W, ++k) {
         const int s = k & 1;
-        issue(g + W, s ^ 1);  // the other stage was read in the previous round
-        asm volatile("cp.async.wait_group 1;" ::: "memory");  // this lane's copies of stage s are done
-        __syncwarp();                                         // and every lane's
-        const char *stage = stages + (size_t)s * ET_STAGE;
-        const int p0 = op.grp[g], p1 = op.grp[g + 1];
+        issue(g + W, nxt, s ^ 1);  // the other stage was read in the previous round
+        const int p0 = cur.p0, p1 = cur.p1;
+        cur = nxt;
+        load_meta(g + 2 * W, nxt);  // arrives while this group is computed
         int pr = et.g_pq[g];
         const int pr_end = et.g_pq[g + 1];
+        asm volatile("cp.async.wait_group 1;" ::: "memory");  // this lane's copies of stage s are done
+        __syncwarp();                                         // and every lane's
+        const char *stage = stages + (size_t)s * ET_STAGE_ALL;
+        const float *wst = (const float *)(stage + ET_STAGE);
+        const int *ost = (const int *)(stage + ET_STAGE + ET_WROWS * 48);
         for (int c0 = p0; c0 < p1; c0 += EW_ROWS) {
             const int nr = min(p1 - c0, EW_ROWS), np = (nr + 1) >> 1;
+            const bool staged = c0 + nr - p0 <= ET_WROWS;  // weights and row ids of this chunk in the stage
             __syncwarp();
             for (int e = lane; e < 24 * np; e += 32) {
                 const int q = e / 12, c = e - 12 * q;
-                w[24 * (q >> 1) + 2 * c + (q & 1)] = q < nr ? op.w_ord[12 * (size_t)(c0 + q) + c] : 0.f;
+                w[24 * (q >> 1) + 2 * c + (q & 1)] =
+                    q < nr ? (staged ? wst[12 * (c0 - p0 + q) + c] : op.w_ord[12 * (size_t)(c0 + q) + c]) : 0.f;
             }
-            const int row = lane < nr ? op.ord[c0 + lane] : 0;  // lane q: row q of the chunk
+            const int row = lane < nr ? (staged ? ost[c0 - p0 + lane] : op.ord[c0 + lane]) : 0;  // lane q: row q of the chunk
             __syncwarp();
             uint64_t acc[EW_ROWS / 2];
 #pragma unroll
@@ -577,7 +609,7 @@ __global__ void __launch_bounds__(ET_WARPS * 32, 3) k_etma32(OpView<float> op, c
 // resident at once
 int etma_setup(ETma &et) {
     static bool attr_set = false;
-    const int smem = ET_WARPS * ET_STAGES * ET_STAGE;
+    const int smem = ET_WARPS * ET_STAGES * ET_STAGE_ALL;
     if (!attr_set) {
         CPM_CUDA_TRY(cudaFuncSetAttribute(k_etma32, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr_set = true;
@@ -734,7 +766,7 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
     if constexpr (K == 32) {
         if constexpr (sizeof(T) == 4) {
             if (etma_ok(op, x)) {
-                k_etma32<<<(unsigned)op.et.grid, ET_WARPS * 32, ET_WARPS * ET_STAGES * ET_STAGE, st>>>(op, sl, ph, x, t);
+                k_etma32<<<(unsigned)op.et.grid, ET_WARPS * 32, ET_WARPS * ET_STAGES * ET_STAGE_ALL, st>>>(op, sl, ph, x, t);
                 if (op.n_sp_rows > 0) slot_epatch(op, sl, ph, x, t, st);
                 return;
             }
@@ -753,6 +785,18 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
         k_epatch32<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
     }
     if (K == 32 && op.n_sp_rows > 0) slot_epatch(op, sl, ph, x, t, st);
+}
+
+int epass64_batch(const cpm_opset_s *o, bool slot_patches, const double *x, double *t) {
+    OpView<double> v = o->view<double>();
+    if (!slot_patches) {
+        v.sp_ptr = nullptr;
+        v.n_sp_rows = 0;
+    }
+    launch_epass<double, 32>(v, nullptr, -1, x, t, stream());
+    count_launches(epass_kernels<double, 32>(v, x));
+    CPM_CUDA_TRY(cudaGetLastError());
+    return 0;
 }
 
 // Row loops: thread (row group, slot s) with K slots per row; each trip
@@ -1891,6 +1935,8 @@ template <int K>
 static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_stats *stats) {
     SolveParams P;
     CPM_TRY(parse_params(o, P));
+    if (P.mixed && s->op->n_sp_rows > 0)
+        return fail(CPM_ERR_UNSUPPORTED, "an operator with per-slot patches is solved in FP64 (precision 0)");
     std::vector<char> active(K, 0);
     for (int j = 0; j < k; ++j) active[j] = 1;
     float ms = 0;
@@ -1959,6 +2005,8 @@ static int run_solve(cpm_solver_s *s, int k, const cpm_solve_opts *o, cpm_solve_
 
 extern "C" int cpm_solver_create(cpm_opset_t op, double m, double n, int32_t kslots, cpm_solver_t *out) {
     if (!op || !out || kslots < 1 || kslots > 32) return fail(CPM_ERR_INVALID_ARG, "kslots must be in [1, 32]");
+    if (op->n_sp_rows > 0 && kslots != 32)
+        return fail(CPM_ERR_UNSUPPORTED, "an operator with per-slot patches is solved with 32 slots");
     *out = nullptr;
     cpm_solver_s *s = new cpm_solver_s();
     s->op = op;

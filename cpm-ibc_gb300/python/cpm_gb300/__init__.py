@@ -409,6 +409,39 @@ class Geodesic:
         return phi, its.tolist()
 
 
+class GeodesicBatch:
+    """The heat-method geodesic distance from up to 32 sources at once on one
+    operator (each source's point IBC applied to its own slot only)."""
+
+    def __init__(self, tube, sources):
+        L = lib()
+        L.cpm_geodesic_batch_create.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                                ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int64)]
+        L.cpm_geodesic_batch_run.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                             ctypes.c_void_p, ctypes.c_void_p]
+        L.cpm_geodesic_batch_destroy.argtypes = [ctypes.c_void_p]
+        self.tube = tube
+        src = np.ascontiguousarray(np.atleast_2d(sources), np.float64)
+        self.n = src.shape[0]
+        h, D = ctypes.c_void_p(), ctypes.c_int64()
+        _check(L.cpm_geodesic_batch_create(tube.h, self.n, _p(src), ctypes.byref(h), ctypes.byref(D)))
+        self.h, self.D = h, D.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().cpm_geodesic_batch_destroy(self.h)
+        except Exception:
+            pass
+
+    def run(self, dt, tol=1e-10, heat_sweeps=2000):
+        """phi (n, D): tube rows, then each source's own DOF rows; iterations (n, 4)"""
+        phi = np.zeros((self.n, self.D))
+        its = np.zeros((self.n, 4), np.int32)
+        _check(lib().cpm_geodesic_batch_run(self.h, dt, tol, heat_sweeps, _p(phi), _p(its)))
+        return phi, its
+
+
 class GeodesicNearest:
     """GeodesicDistanceNearest::ComputeDistance (problems/GeodesicDistanceNearest.cpp:11-53):
     identity rows at the constraint nodes `ibc_rows`, smoothed heat sources at

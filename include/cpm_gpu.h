@@ -325,6 +325,24 @@ int cpm_geodesic_run(cpm_geodesic_t g, double dt, int32_t precision, double tol,
                      int32_t *iters_out);
 int cpm_geodesic_destroy(cpm_geodesic_t g);
 
+/* Heat-method geodesic distance from up to 32 sources at once.  No counterpart
+ * in the reference, whose GeodesicDistance::ComputeDistance serves one source per
+ * call (problems/GeodesicDistance.cpp:11-69).  create builds one operator for all
+ * of them: the tube's stencils with each source's point IBC (order 1,
+ * on_ibc_tolerance 0.1 dx^2) applied to its own slot only; D_out = N + the
+ * largest DOF count.  run performs cpm_geodesic_run's steps on every source at
+ * once, in FP64 (the heat step with `heat_sweeps` damped Jacobi sweeps, <= 0:
+ * 2000), and writes phi source-major: phi_out[k * D + r], the tube rows in
+ * device order, then source k's own DOF rows (the rest of its rows are 0);
+ * iters_out[4 k .. 4 k + 3] the heat and three Poisson iteration counts.  Each
+ * source's phi equals its cpm_geodesic_run result up to rounding. */
+typedef struct cpm_geodesic_batch_s *cpm_geodesic_batch_t;
+int cpm_geodesic_batch_create(cpm_tube_t t, int32_t n_src, const double *sources, cpm_geodesic_batch_t *out,
+                              int64_t *D_out);
+int cpm_geodesic_batch_run(cpm_geodesic_batch_t g, double dt, double tol, int32_t heat_sweeps, double *phi_out,
+                           int32_t *iters_out);
+int cpm_geodesic_batch_destroy(cpm_geodesic_batch_t g);
+
 /* GeodesicDistanceNearest::ComputeDistance(Tube&, ibc_idx, inside_ibc_idx,
  * inside_ibc_idx_dist, dt) (problems/GeodesicDistanceNearest.cpp:11-53): the
  * plain tube operator with identity rows at the constraint nodes `ibc_rows`

@@ -66,3 +66,22 @@ def test_geodesic_mixed_precision_matches_fp64(gpu, oracle):
     exact = np.arccos(np.clip(t0["cp"][near] @ src, -1, 1))
     err = np.abs(phi32[m][near] - exact)
     assert np.mean(err) < 0.01 and np.max(err) < 0.02
+
+
+def test_geodesic_batch_equals_one_source_runs(gpu):
+    """cpm_geodesic_batch: three sources on one operator, each slot carrying only its
+    own point IBC, against cpm_geodesic_run of each source alone (FP64 both):
+    relative l_inf <= 1e-8 over the tube rows and the source's DOF rows."""
+    dx = 0.1
+    T = gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx)
+    cp = T.export()["cp"]
+    rng = np.random.default_rng(21)
+    src = cp[rng.choice(T.N, 3, replace=False)]
+    B = gpu.GeodesicBatch(T, src)
+    phib, itsb = B.run(dx * dx)
+    for k in range(3):
+        G = gpu.Geodesic(T, src[k])
+        phi, its = G.run(dx * dx, precision=0)
+        assert np.max(np.abs(phib[k][:G.D] - phi)) <= 1e-8 * np.max(np.abs(phi))
+        assert np.all(phib[k][G.D:] == 0.0)  # the rows of other sources' DOFs
+        assert abs(int(itsb[k][0]) - its[0]) <= 1
