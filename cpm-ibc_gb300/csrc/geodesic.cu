@@ -607,11 +607,13 @@ extern "C" int cpm_geodesic_batch_run(cpm_geodesic_batch_t g, double dt, double 
         k_sub_colmin32<<<bD, 256, 0, st>>>(D, nparts, part.p, x.p);
         count_launches(2);
     }
-    // phi of source k: [D] rows (tube rows, then its own DOF rows; the other DOF rows are 0)
+    // phi of source k: [D] rows (tube rows, then its own DOF rows; the rows past its DOFs are 0)
     std::vector<double> hx;
     CPM_TRY(x.download(hx, (size_t)D * K));
-    for (int k = 0; k < ns; ++k)
-        for (int64_t r = 0; r < D; ++r) phi_out[(size_t)k * D + r] = hx[(size_t)r * K + k];
+    for (int k = 0; k < ns; ++k) {
+        const int64_t Dk = N + (int64_t)g->info.dof_set[k].size();
+        for (int64_t r = 0; r < D; ++r) phi_out[(size_t)k * D + r] = r < Dk ? hx[(size_t)r * K + k] : 0.0;
+    }
     return cleanup(0);
 }
 

@@ -68,7 +68,6 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
     v.pe_old = o->pe_old.p;
     v.pe_w = pe_w;
     v.n_pl = o->n_pl;
-    v.et = o->etma();
     v.n_sp_rows = o->n_sp_rows;
     v.sp_ptr = o->n_sp_rows ? o->sp_ptr.p : nullptr;
     v.sp_rec = o->sp_rec.p;
@@ -1271,19 +1270,14 @@ static int build_schedule(cpm_opset_s *o) {
     std::vector<uint32_t> base;
     CPM_TRY(o->flags.download(flags, D));
     CPM_TRY(o->base.download(base, D));
-    // rows sorted by (base brick, base point, row): a base brick's groups are contiguous
-    const int NB = o->tube->g.NB;
-    auto bbkey = [&](uint32_t b) -> uint64_t {
-        return (((uint64_t)(unpack_i(b) >> 2) * NB + (uint64_t)(unpack_j(b) >> 2)) * NB + (uint64_t)(unpack_k(b) >> 2));
-    };
-    std::vector<std::pair<uint64_t, int32_t>> rows;
+    std::vector<std::pair<uint32_t, int32_t>> rows;
     std::vector<int32_t> ident;
     rows.reserve(D);
     for (int64_t r = 0; r < D; ++r) {
         if (flags[r] & F_IDENT)
             ident.push_back((int32_t)r);
         else
-            rows.push_back({(bbkey(base[r]) << 32) | (uint64_t)base[r], (int32_t)r});
+            rows.push_back({base[r], (int32_t)r});
     }
     std::sort(rows.begin(), rows.end());
     std::vector<int32_t> ord(rows.size()), grp;
@@ -1313,100 +1307,9 @@ static int build_schedule(cpm_opset_s *o) {
     return build_patch_list(o, flags);
 }
 
-// Patch records of the TMA-staged E pass (see ETma): per base group, its rows on
-// the IBC patch list in row order, each entry with the stage offset of the bulk
-// stencil node it replaces (the k-th set bit s of the row's moved-column mask,
-// offset s * 128) and its moved column.
-static int build_etma_sched(cpm_opset_s *o) {
-    const int64_t D = o->D, n_grp = o->n_grp;
-    std::vector<int32_t> ord, grp, pl_row, pl_off, pl_xcol, pe_new, patch;
-    std::vector<uint64_t> p_emask;
-    std::vector<uint8_t> flags, pl_neg;
-    std::vector<float> pl_xval, pe_w;
-    CPM_TRY(o->ord.download(ord, std::max<int64_t>(1, o->n_ord)));
-    CPM_TRY(o->grp.download(grp, n_grp + 1));
-    CPM_TRY(o->flags.download(flags, D));
-    const int64_t n_pl = o->n_pl, n_pe = o->n_pe;
-    std::vector<int32_t> pl_of_row(D, -1);
-    if (n_pl > 0) {
-        CPM_TRY(o->pl_row.download(pl_row, n_pl));
-        CPM_TRY(o->pl_off.download(pl_off, n_pl + 1));
-        CPM_TRY(o->pl_xcol.download(pl_xcol, n_pl));
-        CPM_TRY(o->pl_neg.download(pl_neg, n_pl));
-        CPM_TRY(o->pl_xval32.download(pl_xval, n_pl));
-        CPM_TRY(o->pe_new.download(pe_new, std::max<int64_t>(1, n_pe)));
-        CPM_TRY(o->pe_w32.download(pe_w, std::max<int64_t>(1, n_pe)));
-        CPM_TRY(o->patch.download(patch, D));
-        CPM_TRY(o->p_emask.download(p_emask, o->p_emask.n));
-        for (int64_t q = 0; q < n_pl; ++q) pl_of_row[pl_row[q]] = (int32_t)q;
-    }
-    std::vector<int32_t> g_pq(n_grp + 1, 0);
-    std::vector<int4> pq;
-    std::vector<float> pq_xval, pqe_w;
-    std::vector<uint8_t> pq_neg;
-    std::vector<uint2> pqe;
-    for (int64_t h = 0; h < n_grp; ++h) {
-        g_pq[h] = (int32_t)pq.size();
-        for (int32_t pos = grp[h]; pos < grp[h + 1]; ++pos) {
-            const int32_t r = ord[pos];
-            const int32_t q = pl_of_row[r];
-            if (q < 0) continue;
-            uint64_t em = (flags[r] & F_EMOVE) ? p_emask[patch[r]] : 0ull;
-            const int e_first = (int)pqe.size();
-            for (int32_t e = pl_off[q]; e < pl_off[q + 1]; ++e) {
-                if (!em) return fail(CPM_ERR_CUDA, "internal: patch entries exceed the moved-column mask");
-                const int sidx = __builtin_ctzll(em);
-                em &= em - 1;
-                pqe.push_back(make_uint2((uint32_t)sidx * 128u, (uint32_t)pe_new[e]));
-                pqe_w.push_back(pe_w[e]);
-            }
-            pq.push_back(make_int4(pos - grp[h], e_first, (int)pqe.size(), pl_xcol[q]));
-            pq_xval.push_back(pl_xval[q]);
-            pq_neg.push_back(pl_neg[q]);
-        }
-    }
-    g_pq[n_grp] = (int32_t)pq.size();
-    if (pq.empty()) {
-        pq.push_back(make_int4(0, 0, 0, -1));
-        pq_xval.push_back(0.f);
-        pq_neg.push_back(0);
-    }
-    if (pqe.empty()) {
-        pqe.push_back(make_uint2(0, 0));
-        pqe_w.push_back(0.f);
-    }
-    CPM_TRY(o->et_gpq.upload(g_pq));
-    CPM_TRY(o->et_pq.upload(pq));
-    CPM_TRY(o->et_pqxval.upload(pq_xval));
-    CPM_TRY(o->et_pqneg.upload(pq_neg));
-    CPM_TRY(o->et_pqe.upload(pqe));
-    CPM_TRY(o->et_pqew.upload(pqe_w));
-    CPM_TRY(o->et_err.alloc(1));
-    CPM_TRY(o->et_err.zero());
-    o->et_ready = true;
-    ETma e = o->etma();
-    CPM_TRY(etma_setup(e));
-    o->et_grid = e.grid;
-    return 0;
-}
-
 }  // namespace cpm
 
 using namespace cpm;
-
-ETma cpm_opset_s::etma() const {
-    ETma e;
-    e.g_pq = et_gpq.p;
-    e.pq = et_pq.p;
-    e.pq_xval = et_pqxval.p;
-    e.pq_neg = et_pqneg.p;
-    e.pqe = et_pqe.p;
-    e.pqe_w = et_pqew.p;
-    e.err = et_err.p;
-    e.grid = et_grid;
-    e.ready = et_ready ? 1 : 0;
-    return e;
-}
 
 static int opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, const CpOverrides *ovr, cpm_opset_t *out) {
     if (!t || !out || n_ibc < 0 || (n_ibc > 0 && !ibcs)) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
@@ -1417,7 +1320,6 @@ static int opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibc
     if (!rc && n_ibc > 0) rc = build_ibc(o, n_ibc, ibcs, ovr);
     if (!rc) rc = build_schedule(o);
     if (!rc) rc = make_float_copies(o);
-    if (!rc) rc = build_etma_sched(o);
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(stream());
         if (e != cudaSuccess) rc = fail(CPM_ERR_CUDA, cudaGetErrorString(e));
@@ -1571,7 +1473,6 @@ int opset_create_point_batch(cpm_tube_s *t, int n_src, const double *sources, cp
     if (!rc) rc = build_point_batch(o, n_src, sources, info);
     if (!rc) rc = build_schedule(o);
     if (!rc) rc = make_float_copies(o);
-    if (!rc) rc = build_etma_sched(o);
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(stream());
         if (e != cudaSuccess) rc = fail(CPM_ERR_CUDA, cudaGetErrorString(e));
@@ -1606,7 +1507,6 @@ extern "C" int cpm_opset_create_identity(cpm_tube_t t, int64_t n_rows, const int
     }
     if (!rc) rc = build_schedule(o);
     if (!rc) rc = make_float_copies(o);
-    if (!rc) rc = build_etma_sched(o);
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(stream());
         if (e != cudaSuccess) rc = fail(CPM_ERR_CUDA, cudaGetErrorString(e));

@@ -26,29 +26,6 @@ enum RowFlags : uint8_t {
 // one per IBC column its patch entries read) and computes every row of its
 // groups from shared memory.  Offsets are bytes into the unit's stage, one
 // 128-byte row (32 FP32 slots) per staged node.
-// Schedule of the TMA-staged E pass (k_etma32, FP32, 32 slots).  Each warp runs
-// its own two-stage pipeline over base groups: the group's 64 stencil rows of x
-// (32 FP32 slots, 128 bytes each) are gathered into the warp's shared-memory
-// stage by TMA (tile::gather4, four rows an instruction) while the warp computes
-// the previous group from the other stage.  Rows on the IBC patch list are
-// corrected in registers before their one store: per group, its patch records
-// in row order; an entry names the bulk stencil node it replaces by its stage
-// offset and the moved column by its row of x.
-struct ETma {
-    const int32_t *g_pq;    // per group: first patch record (n_grp + 1 entries)
-    const int4 *pq;         // patch record {row position in the group, first entry, end entry, extra column or -1}
-    const float *pq_xval;   // the extra entry's value
-    const uint8_t *pq_neg;  // 1: the row is negated (2nd-order Dirichlet DOF rows)
-    const uint2 *pqe;       // patch entry {stage offset of the bulk stencil node (s * 128), moved column}
-    const float *pqe_w;     // its stencil weight (wx_i wy_j) wz_k
-    int *err;               // set to 1 when a stage copy did not arrive within the wait limit
-    int grid;               // blocks of a launch (all resident at once)
-    int ready;              // the schedule was built
-};
-// sets k_etma32's shared-memory limit and the launch grid (at operator build
-// time, outside any stream capture)
-int etma_setup(ETma &et);
-
 template <class T>
 struct OpView {
     BrickView bv;
@@ -87,7 +64,6 @@ struct OpView {
     const int32_t *pe_new, *pe_old;           // moved column and the bulk column it replaces
     const T *pe_w;                            // stencil weight (wx_i wy_j) wz_k of the moved point
     int64_t n_ord, n_grp, n_ident, n_pl;
-    ETma et;                                  // TMA-staged E pass (FP32 weights)
     // per-slot patches of a batch whose slots each carry their own point IBC
     // (cpm_geodesic_batch_*): row r's records sp_rec[sp_ptr[r] .. sp_ptr[r + 1]),
     // {slot, 0 E entry / 1 L entry, the column it replaces, the slot's DOF column};
@@ -583,16 +559,6 @@ struct cpm_opset_s {
     cpm::DBuf<float> w_ord32;
     cpm::DBuf<uint8_t> fl_ord;
     int64_t n_ord = 0, n_grp = 0, n_ident = 0;
-    // TMA-staged E pass schedule
-    cpm::DBuf<int4> et_pq;
-    cpm::DBuf<int32_t> et_gpq;
-    cpm::DBuf<float> et_pqxval, et_pqew;
-    cpm::DBuf<uint8_t> et_pqneg;
-    cpm::DBuf<uint2> et_pqe;
-    cpm::DBuf<int> et_err;
-    int et_grid = 1;
-    bool et_ready = false;
-    cpm::ETma etma() const;
     // host-side row layout for right-hand sides
     std::vector<uint8_t> h_identity;
     std::vector<int32_t> h_kind, h_ibc, h_side;

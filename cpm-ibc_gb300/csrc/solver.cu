@@ -409,235 +409,6 @@ __global__ void __launch_bounds__(128) k_epass32w(OpView<float> op, const Slot *
         }
 }
 
-// ---- Staged E pass for 32 FP32 slots, IBC patch included (k_etma32).
-// Every warp runs its own two-stage pipeline over base groups (a static
-// stride): it copies the next group's 64 stencil rows of x into one of its
-// shared-memory stages with 16-byte asynchronous copies (cp.async, eight lanes
-// a 128-byte row, one commit group per stage) and computes the current group
-// from the other stage, with the arithmetic of k_epass32w; rows on the IBC
-// patch list get k_epatch32's correction in registers before their one store.
-// Results are bit for bit those of k_epass32w followed by k_epatch32.
-constexpr int ET_WARPS = 4;       // warps per block
-constexpr int ET_STAGES = 2;      // stages per warp
-constexpr int ET_STAGE = 64 * 128; // one group's 64 rows of 32 FP32 slots
-constexpr int ET_WROWS = 16;       // rows of a group whose weights and row ids are staged with it
-constexpr int ET_STAGE_ALL = ET_STAGE + ET_WROWS * 48 + ET_WROWS * 4;  // 9024 bytes
-
-// shared-memory address of a generic pointer
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// k_epatch32's correction of one patched row, lane = slot: the bulk stencil
-// values from the stage, the moved and extra columns from x
-__device__ __forceinline__ float et_patch(const ETma &et, const char *stage, const float *__restrict__ x, int lane, int pr,
-                                          const int4 &rec, float acc) {
-    const float xv = et.pq_xval[pr];
-    const bool neg = et.pq_neg[pr] != 0;
-    const float xe = rec.w >= 0 ? x[(uint32_t)rec.w * 32u + lane] : 0.f;
-    for (int base = rec.y; base < rec.z; base += 32) {
-        const int cnt = min(32, rec.z - base);
-        uint32_t oo = 0, nn = 0;
-        float w = 0.f;
-        if (lane < cnt) {
-            const uint2 e = et.pqe[base + lane];
-            oo = e.x;
-            nn = e.y;
-            w = et.pqe_w[base + lane];
-        }
-        for (int u0 = 0; u0 < cnt; u0 += 8) {
-            float xn[8], xo[8], ww[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int k = u0 + u;
-                const uint32_t nk = (uint32_t)__shfl_sync(FULL, nn, k & 31), ok = (uint32_t)__shfl_sync(FULL, oo, k & 31);
-                ww[u] = __shfl_sync(FULL, w, k & 31);
-                const bool valid = k < cnt;
-                xn[u] = valid ? x[nk * 32u + lane] : 0.f;
-                xo[u] = valid ? *(const float *)(stage + ok + 4 * lane) : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (u0 + u < cnt) acc += ww[u] * (xn[u] - xo[u]);
-        }
-    }
-    if (neg) acc = -acc;
-    if (rec.w >= 0) acc += xv * xe;
-    return acc;
-}
-
-__global__ void __launch_bounds__(ET_WARPS * 32, 3) k_etma32(OpView<float> op, const Slot *__restrict__ sl, int ph,
-                                                             const float *__restrict__ x, float *__restrict__ t) {
-    extern __shared__ __align__(1024) unsigned char et_smem[];
-    __shared__ __align__(16) float sw[ET_WARPS][EW_ROWS * 12];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const bool act = (ph < 0) || sl[lane].phase == ph;
-    if (!__any_sync(FULL, act)) return;  // the same 32 slots in every warp: grid-uniform
-    const ETma &et = op.et;
-    char *stages = (char *)et_smem + (size_t)warp * ET_STAGES * ET_STAGE_ALL;
-    const uint32_t sst = smem_u32(stages);
-    float *w = sw[warp];
-    const int64_t W = (int64_t)gridDim.x * ET_WARPS;
-    const int sub = lane >> 3, chunk = lane & 7;  // row within a slab of four, 16-byte chunk of the row
-    // a group's metadata, loaded one round before its copies are issued
-    struct Meta {
-        int col[16];   // stencil rows 4 m + sub of the group
-        int p0, p1;    // its rows ord[p0 .. p1)
-    };
-    auto load_meta = [&](int64_t g, Meta &m) {
-        if (g < op.n_grp) {
-            const int32_t *gc = op.gcols + 64 * g;
-#pragma unroll
-            for (int q = 0; q < 16; ++q) m.col[q] = __ldg(gc + 4 * q + sub);
-            m.p0 = __ldg(op.grp + g);
-            m.p1 = __ldg(op.grp + g + 1);
-        }
-    };
-    // group g into stage s: its 64 stencil rows of x, then (up to ET_WROWS rows) its
-    // sorted weights and row ids; one commit group
-    auto issue = [&](int64_t g, const Meta &m, int s) {
-        if (g < op.n_grp) {
-            const uint32_t st0 = sst + (uint32_t)s * ET_STAGE_ALL;
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const uint32_t dst = st0 + (uint32_t)(4 * q + sub) * 128u + 16u * chunk;
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(x + (uint32_t)m.col[q] * 32u + 4 * chunk)
-                             : "memory");
-            }
-            const int nr = min(m.p1 - m.p0, ET_WROWS);
-            for (int c = lane; c < 3 * nr; c += 32)  // 48 bytes a row: three 16-byte chunks
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(st0 + ET_STAGE + 16u * c),
-                             "l"(op.w_ord + 12 * (size_t)m.p0 + 4 * c) : "memory");
-            if (lane < nr)
-                asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(st0 + ET_STAGE + ET_WROWS * 48u + 4u * lane),
-                             "l"(op.ord + m.p0 + lane) : "memory");
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    int64_t g = (int64_t)blockIdx.x * ET_WARPS + warp;
-    Meta cur, nxt;
-    load_meta(g, cur);
-    issue(g, cur, 0);
-    load_meta(g + W, nxt);
-    for (int k = 0; g < op.n_grp; g += W, ++k) {
-        const int s = k & 1;
-        issue(g + W, nxt, s ^ 1);  // the other stage was read in the previous round
-        const int p0 = cur.p0, p1 = cur.p1;
-        cur = nxt;
-        load_meta(g + 2 * W, nxt);  // arrives while this group is computed
-        int pr = et.g_pq[g];
-        const int pr_end = et.g_pq[g + 1];
-        asm volatile("cp.async.wait_group 1;" ::: "memory");  // this lane's copies of stage s are done
-        __syncwarp();                                         // and every lane's
-        const char *stage = stages + (size_t)s * ET_STAGE_ALL;
-        const float *wst = (const float *)(stage + ET_STAGE);
-        const int *ost = (const int *)(stage + ET_STAGE + ET_WROWS * 48);
-        for (int c0 = p0; c0 < p1; c0 += EW_ROWS) {
-            const int nr = min(p1 - c0, EW_ROWS), np = (nr + 1) >> 1;
-            const bool staged = c0 + nr - p0 <= ET_WROWS;  // weights and row ids of this chunk in the stage
-            __syncwarp();
-            for (int e = lane; e < 24 * np; e += 32) {
-                const int q = e / 12, c = e - 12 * q;
-                w[24 * (q >> 1) + 2 * c + (q & 1)] =
-                    q < nr ? (staged ? wst[12 * (c0 - p0 + q) + c] : op.w_ord[12 * (size_t)(c0 + q) + c]) : 0.f;
-            }
-            const int row = lane < nr ? (staged ? ost[c0 - p0 + lane] : op.ord[c0 + lane]) : 0;  // lane q: row q of the chunk
-            __syncwarp();
-            uint64_t acc[EW_ROWS / 2];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                float xb[16];
-#pragma unroll
-                for (int q = 0; q < 16; ++q) xb[q] = *(const float *)(stage + 128 * (16 * i + q) + 4 * lane);
-                uint64_t x2[16];
-#pragma unroll
-                for (int q = 0; q < 16; ++q) x2[q] = f2_pack(xb[q], xb[q]);
-#pragma unroll
-                for (int p = 0; p < EW_ROWS / 2; ++p)
-                    if (p < np) {
-                        const float *wp = w + 24 * p;
-                        const uint64_t wx2 = *(const uint64_t *)(wp + 2 * i);
-                        const ulonglong2 y01 = *(const ulonglong2 *)(wp + 8), y23 = *(const ulonglong2 *)(wp + 12);
-                        const ulonglong2 z01 = *(const ulonglong2 *)(wp + 16), z23 = *(const ulonglong2 *)(wp + 20);
-                        const uint64_t wy2[4] = {y01.x, y01.y, y23.x, y23.y}, wz2[4] = {z01.x, z01.y, z23.x, z23.y};
-                        uint64_t ay2 = 0ull;
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            uint64_t az2 = f2_mul(wz2[0], x2[4 * j]);
-                            az2 = f2_fma(wz2[1], x2[4 * j + 1], az2);
-                            az2 = f2_fma(wz2[2], x2[4 * j + 2], az2);
-                            az2 = f2_fma(wz2[3], x2[4 * j + 3], az2);
-                            ay2 = j == 0 ? f2_mul(wy2[0], az2) : f2_fma(wy2[j], az2, ay2);
-                        }
-                        const uint64_t part = f2_mul(wx2, ay2);
-                        acc[p] = i == 0 ? part : f2_add(acc[p], part);
-                    }
-            }
-#pragma unroll
-            for (int p = 0; p < EW_ROWS / 2; ++p)
-                if (2 * p < nr) {
-                    float v2[2];
-                    f2_unpack(acc[p], v2[0], v2[1]);
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int q = 2 * p + h;
-                        if (q < nr) {
-                            const int r = __shfl_sync(FULL, row, q);
-                            float v = v2[h];
-                            if (pr < pr_end) {
-                                const int4 rec = et.pq[pr];
-                                if (rec.x == c0 - p0 + q) {
-                                    v = et_patch(et, stage, x, lane, pr, rec, v);
-                                    ++pr;
-                                }
-                            }
-                            if (act) t[(uint32_t)r * 32u + lane] = v;
-                        }
-                    }
-                }
-        }
-        __syncwarp();  // the stage is read before it is refilled
-    }
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
-    // identity rows: t = x
-    if (act)
-        for (int64_t q = (int64_t)blockIdx.x * ET_WARPS + warp; q < op.n_ident; q += W) {
-            const uint32_t r = (uint32_t)op.ident[q];
-            t[r * 32u + lane] = x[r * 32u + lane];
-        }
-}
-
-// k_etma32's dynamic shared-memory size (set once) and its grid: every block
-// resident at once
-int etma_setup(ETma &et) {
-    static bool attr_set = false;
-    const int smem = ET_WARPS * ET_STAGES * ET_STAGE_ALL;
-    if (!attr_set) {
-        CPM_CUDA_TRY(cudaFuncSetAttribute(k_etma32, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr_set = true;
-    }
-    int b = 1;
-    CPM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_etma32, ET_WARPS * 32, (size_t)smem));
-    et.grid = std::max(1, b) * sm_count();
-    return 0;
-}
-
-// the TMA-staged E pass's error flag: a stage copy that did not arrive within
-// its wait limit (the flag is cleared when read)
-static int etma_status(cpm_opset_s *o) {
-    if (!o->et_err.p) return 0;
-    int h = 0;
-    CPM_CUDA_TRY(cudaMemcpyAsync(&h, o->et_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
-    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
-    if (!h) return 0;
-    CPM_CUDA_TRY(cudaMemsetAsync(o->et_err.p, 0, sizeof(int), stream()));
-    return fail(CPM_ERR_TIMEOUT, "TMA-staged E pass: a stage copy did not complete within the wait limit");
-}
-
-// k_etma32 applies: a schedule built and a 16-byte aligned x
-static inline bool etma_ok(const OpView<float> &op, const float *x) {
-    return op.et.ready && op.n_grp > 0 && ((uintptr_t)x % 16) == 0 && op.D * 32 <= (int64_t)UINT32_MAX &&
-           op.D <= (int64_t)INT32_MAX;
-}
-
 // 1 slot: one thread per row, rows visited in base-point order so that the
 // threads of a warp that share a base read the same cache lines.
 template <class T>
@@ -751,12 +522,10 @@ static void slot_epatch(const OpView<T> &op, const Slot *sl, int ph, const T *x,
     k_slot_epatch32<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
 }
 
-// kernels one E pass of x launches (the brick-staged FP32 pass includes the patch)
+// kernels one E pass of x launches
 template <class T, int K>
-static inline int epass_kernels(const OpView<T> &op, const T *x) {
+static inline int epass_kernels(const OpView<T> &op, const T *) {
     const int sp = (K == 32 && op.n_sp_rows > 0) ? 1 : 0;
-    if constexpr (K == 32 && sizeof(T) == 4)
-        if (etma_ok(op, x)) return 1 + sp;
     return ((K == 32 && op.n_pl > 0) ? 2 : 1) + sp;
 }
 
@@ -765,11 +534,6 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
     static_assert(K == 1 || K == 32, "slot widths 1 and 32");
     if constexpr (K == 32) {
         if constexpr (sizeof(T) == 4) {
-            if (etma_ok(op, x)) {
-                k_etma32<<<(unsigned)op.et.grid, ET_WARPS * 32, ET_WARPS * ET_STAGES * ET_STAGE_ALL, st>>>(op, sl, ph, x, t);
-                if (op.n_sp_rows > 0) slot_epatch(op, sl, ph, x, t, st);
-                return;
-            }
             const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_grp + 3) / 4, 32LL * sm_count()));
             k_epass32w<<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
         } else {
@@ -1924,7 +1688,7 @@ static int solve_pass(cpm_solver_s *s, const SolveParams &P, const std::vector<c
     CPM_CUDA_TRY(cudaEventSynchronize(s->e1));
     *ms = 0;
     cudaEventElapsedTime(ms, s->e0, s->e1);
-    return etma_status(s->op);
+    return 0;
 }
 
 // Solve k right-hand sides.  A mixed-precision slot that does not converge
