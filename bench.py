@@ -305,25 +305,41 @@ def run_workload(args):
         cg.sync()
         t_tube = time.perf_counter() - t
         cp = T.export()["cp"]
-        src = cp[np.random.default_rng(12).integers(T.N)]
-        t = time.perf_counter()
-        G = cg.Geodesic(T, src)
-        t_setup = time.perf_counter() - t
-        res = {}
-        for prec in (0, 1):
-            G.run(dx * dx, precision=prec)  # warm-up (graph capture)
+        rng = np.random.default_rng(12)
+        srcs = cp[rng.choice(T.N, args.sources, replace=False)]
+        # one source at a time (the reference's way: its own point-IBC operator per source), FP64
+        n_solo = min(args.solo, args.sources)
+        solo, t_solo_setup, t_solo = [], 0.0, 0.0
+        for k in range(n_solo):
             t = time.perf_counter()
-            phi, its = G.run(dx * dx, precision=prec)
-            res[prec] = (time.perf_counter() - t, phi, its)
+            G = cg.Geodesic(T, srcs[k])
+            t_solo_setup += time.perf_counter() - t
+            if k == 0:
+                G.run(dx * dx, precision=0)  # warm-up (graph capture)
+            t = time.perf_counter()
+            phi, its = G.run(dx * dx, precision=0)
+            t_solo += time.perf_counter() - t
+            solo.append((G.D, phi, its))
+        # all sources at once on one slot-patched operator
+        t = time.perf_counter()
+        B = cg.GeodesicBatch(T, srcs)
+        t_batch_setup = time.perf_counter() - t
+        t = time.perf_counter()
+        phib, itsb = B.run(dx * dx)
+        t_batch = time.perf_counter() - t
+        err = max(float(np.max(np.abs(phib[k][:Dk] - phi)) / np.max(np.abs(phi))) for k, (Dk, phi, _) in enumerate(solo))
         line.update({
-            "config": {"surface": "torus R=1 r=0.4", "dx": dx, "tube_nodes": T.N, "rows": G.D,
-                       "source": "seeded random tube node's closest point", "dt": dx * dx,
-                       "heat_step": "FP64, 2000 damped Jacobi sweeps per preconditioner call"},
-            "tube_build_s": t_tube, "geodesic_setup_s": t_setup,
-            "fp64": {"seconds": res[0][0], "iterations": res[0][2]},
-            "mixed": {"seconds": res[1][0], "iterations": res[1][2]},
-            "mixed_rel_err_vs_fp64": float(np.max(np.abs(res[1][1] - res[0][1])) / np.max(np.abs(res[0][1]))),
-            "note": "Poisson steps whose FP32 inner iteration cannot converge are re-solved in FP64 (fp64_fallback)",
+            "config": {"surface": "torus R=1 r=0.4", "dx": dx, "tube_nodes": T.N, "sources": args.sources,
+                       "source": "seeded random tube nodes' closest points", "dt": dx * dx,
+                       "heat_step": "FP64, 2000 damped Jacobi sweeps per preconditioner call", "poisson_steps": "FP64"},
+            "tube_build_s": t_tube,
+            "one_at_a_time": {"sources": n_solo, "seconds": t_solo, "solves_per_s": n_solo / t_solo,
+                              "setup_s_per_source": t_solo_setup / n_solo,
+                              "iterations": [list(map(int, x[2])) for x in solo]},
+            "batched": {"sources": args.sources, "seconds": t_batch, "solves_per_s": args.sources / t_batch,
+                        "setup_s": t_batch_setup, "iterations_first": [int(v) for v in itsb[0]]},
+            "speedup_batched_vs_one_at_a_time": (args.sources / t_batch) / (n_solo / t_solo),
+            "batched_rel_err_vs_one_at_a_time": err,
         })
     elif args.workload == "mesh-curves":
         dx = 0.005
@@ -426,6 +442,8 @@ def main():
     ap.add_argument("--workload", choices=["torus-geodesic", "mesh-curves", "serving-mix"], default=None,
                     help="one line for another configuration instead of the headline benchmark")
     ap.add_argument("--requests", type=int, default=160, help="serving-mix: requests in the stream")
+    ap.add_argument("--sources", type=int, default=32, help="torus-geodesic: sources of the batched run")
+    ap.add_argument("--solo", type=int, default=2, help="torus-geodesic: sources also run one at a time")
     ap.add_argument("--rate", type=float, default=8.0, help="serving-mix: mean arrivals per second")
     ap.add_argument("--refine-every", type=int, default=0,
                     help="mixed precision: reliable-update period in iterations (0: the library default)")
