@@ -20,12 +20,20 @@ int fail(int code, const std::string &msg) {
 
 // One non-blocking stream per process: the library's work is ordered on it and
 // never synchronises the legacy default stream.
-cudaStream_t stream() {
+cudaStream_t library_stream() {
     static std::once_flag once;
     static cudaStream_t s = nullptr;
     std::call_once(once, [] { cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking); });
     return s;
 }
+
+// the stream of the calling thread's current StreamScope, if any
+static thread_local cudaStream_t g_scope = nullptr;
+
+cudaStream_t stream() { return g_scope ? g_scope : library_stream(); }
+
+StreamScope::StreamScope(cudaStream_t s) : prev(g_scope) { g_scope = s; }
+StreamScope::~StreamScope() { g_scope = prev; }
 
 }  // namespace cpm
 
@@ -54,11 +62,11 @@ extern "C" int cpm_device_info(char *name, int64_t name_len, int64_t *free_bytes
 }
 
 extern "C" int cpm_sync(void) {
-    CPM_CUDA_TRY(cudaStreamSynchronize(cpm::stream()));
+    CPM_CUDA_TRY(cudaStreamSynchronize(cpm::library_stream()));
     return 0;
 }
 
-extern "C" void *cpm_get_stream(void) { return (void *)cpm::stream(); }
+extern "C" void *cpm_get_stream(void) { return (void *)cpm::library_stream(); }
 
 namespace cpm {
 static std::atomic<long long> g_launches{0};

@@ -42,7 +42,18 @@ int fail(int code, const std::string &msg);
         if (_rc != 0) return _rc; \
     } while (0)
 
+// the stream the library's work is ordered on: the calling thread's current
+// StreamScope stream, else the library stream
 cudaStream_t stream();
+cudaStream_t library_stream();
+// while alive, stream() of this thread is s (a solver's own stream)
+struct StreamScope {
+    explicit StreamScope(cudaStream_t s);
+    ~StreamScope();
+    StreamScope(const StreamScope &) = delete;
+    StreamScope &operator=(const StreamScope &) = delete;
+    cudaStream_t prev;
+};
 // adds to the process-wide count of launched kernels (cpm_launch_count)
 void count_launches(long long n);
 

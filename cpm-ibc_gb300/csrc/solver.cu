@@ -1418,14 +1418,35 @@ struct cpm_solver_s {
     int chunk = 16;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cpm_solver_s *fb1 = nullptr;  // 32 slots: one-slot FP64 solver for a few mixed solves to redo
+    // the solver's own stream: its work is ordered after the caller's stream at every
+    // entry, and two solvers (of one server, say) run concurrently
+    cudaStream_t own = nullptr;
+    cudaEvent_t entry = nullptr;
     ~cpm_solver_s() {
+        if (own) cudaStreamSynchronize(own);
         if (g_plain) cudaGraphExecDestroy(g_plain);
         if (g_mixed) cudaGraphExecDestroy(g_mixed);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
+        if (entry) cudaEventDestroy(entry);
         delete fb1;
+        if (own) cudaStreamDestroy(own);
     }
 };
+
+namespace cpm {
+// a solver entry point's work on the solver's stream, ordered after the work the
+// calling thread has already queued on its current stream
+struct SolverScope {
+    StreamScope scope;
+    explicit SolverScope(cpm_solver_s *s) : scope(enter(s)) {}
+    static cudaStream_t enter(cpm_solver_s *s) {
+        cudaEventRecord(s->entry, stream());
+        cudaStreamWaitEvent(s->own, s->entry, 0);
+        return s->own;
+    }
+};
+}  // namespace cpm
 
 namespace cpm {
 
@@ -1773,6 +1794,12 @@ extern "C" int cpm_solver_create(cpm_opset_t op, double m, double n, int32_t ksl
         return fail(CPM_ERR_UNSUPPORTED, "an operator with per-slot patches is solved with 32 slots");
     *out = nullptr;
     cpm_solver_s *s = new cpm_solver_s();
+    if (cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->entry, cudaEventDisableTiming) != cudaSuccess) {
+        delete s;
+        return fail(CPM_ERR_CUDA, "solver_create: stream");
+    }
+    SolverScope sc(s);
     s->op = op;
     s->m = m;
     s->n = n;
@@ -1794,6 +1821,7 @@ extern "C" int cpm_solver_create(cpm_opset_t op, double m, double n, int32_t ksl
     if (cudaGetLastError() != cudaSuccess) return bail(fail(CPM_ERR_CUDA, "pden kernel"));
     cudaEventCreate(&s->e0);
     cudaEventCreate(&s->e1);
+    if (cudaStreamSynchronize(s->own) != cudaSuccess) return bail(fail(CPM_ERR_CUDA, "solver_create"));
     *out = s;
     return 0;
 }
@@ -1801,6 +1829,7 @@ extern "C" int cpm_solver_create(cpm_opset_t op, double m, double n, int32_t ksl
 extern "C" int cpm_solve_device(cpm_solver_t s, int32_t k, const void *b_dev, void *x_dev, const cpm_solve_opts *opts,
                                 cpm_solve_stats *stats) {
     if (!s || !opts || k < 1 || k > s->K) return fail(CPM_ERR_INVALID_ARG, "invalid solve arguments");
+    SolverScope sc(s);
     const size_t bytes = (size_t)s->D * s->K * sizeof(double);
     if (b_dev != s->b64.p) CPM_CUDA_TRY(cudaMemcpyAsync(s->b64.p, b_dev, bytes, cudaMemcpyDeviceToDevice, stream()));
     int rc = (s->K == 1) ? run_solve<1>(s, k, opts, stats) : run_solve<32>(s, k, opts, stats);
@@ -1811,6 +1840,7 @@ extern "C" int cpm_solve_device(cpm_solver_t s, int32_t k, const void *b_dev, vo
 
 extern "C" int cpm_solve(cpm_solver_t s, int32_t k, const double *b, double *x, const cpm_solve_opts *opts, cpm_solve_stats *stats) {
     if (!s || !b || !x || !opts || k < 1 || k > s->K) return fail(CPM_ERR_INVALID_ARG, "invalid solve arguments");
+    SolverScope sc(s);
     DBuf<double> stage;
     CPM_TRY(stage.upload(b, (size_t)s->D * k));
     k_scatter_cols<<<nblk(s->D * s->K), BS, 0, stream()>>>(s->D, s->K, k, stage.p, s->b64.p);
@@ -1829,14 +1859,16 @@ extern "C" int cpm_solver_destroy(cpm_solver_t s) {
 }
 
 // ================================================================= serving
-// Continuous batching over the 32 slots of one mixed-precision solver: a
-// request is admitted into a free slot as soon as one frees up (its column of
-// b is written and the slot alone is started, the other slots keep their
-// state), iteration graphs run while any slot is busy, and finished slots are
-// harvested after every graph.
+// Continuous batching over the slots of `nb` 32-slot solvers on one operator,
+// each on its own stream: a request is admitted into a free slot as soon as one
+// frees up (its column of b is written and the slot alone is started, the
+// other slots keep their state), every step launches one iteration graph per
+// busy solver, all of them queued before any is waited for, so one batch's
+// latency-bound E pass overlaps another's bandwidth-bound row kernels; finished
+// slots are harvested after the graphs.
 
 struct cpm_server_s {
-    cpm_solver_s *solver = nullptr;
+    std::vector<cpm_solver_s *> solvers;
     cpm_solver_s *fallback = nullptr;  // 1-slot solver for requests the mixed path cannot converge
     SolveParams P{};
     cpm_solve_opts opts{};
@@ -1860,20 +1892,23 @@ struct cpm_server_s {
         double latency;
     };
     std::deque<Req> queue;
-    std::vector<Busy> busy;
+    std::vector<Busy> busy;     // 32 per solver
     std::deque<Done> done;
-    double *h_stage = nullptr;  // pinned, [32][D]: one staging column per slot
-    DBuf<double> d_stage;       // device, [32][D]
+    double *h_stage = nullptr;  // pinned, [32 nb][D]: one staging column per slot
+    DBuf<double> d_stage;       // device, [32 nb][D]
     ~cpm_server_s() {
+        for (auto *s : solvers)
+            if (s) cudaStreamSynchronize(s->own);
         if (h_stage) cudaFreeHost(h_stage);
-        delete solver;
+        for (auto *s : solvers) delete s;
         delete fallback;
     }
 };
 
-extern "C" int cpm_server_create(cpm_opset_t op, double m, double n, const cpm_solve_opts *opts, cpm_server_t *out) {
+static int server_create(cpm_opset_t op, double m, double n, const cpm_solve_opts *opts, int nb, cpm_server_t *out) {
     if (!op || !opts || !out) return fail(CPM_ERR_INVALID_ARG, "server_create: null argument");
     *out = nullptr;
+    if (nb < 1 || nb > 8) return fail(CPM_ERR_INVALID_ARG, "server_create: 1 to 8 batches");
     if (opts->precision != 0 && opts->precision != 1) return fail(CPM_ERR_INVALID_ARG, "precision must be 0 or 1");
     if (opts->precond != 1) return fail(CPM_ERR_UNSUPPORTED, "the server runs the diagonal preconditioner");
     cpm_server_s *sv = new cpm_server_s();
@@ -1883,32 +1918,45 @@ extern "C" int cpm_server_create(cpm_opset_t op, double m, double n, const cpm_s
     };
     sv->opts = *opts;
     int rc = parse_params(opts, sv->P);
-    if (!rc) rc = cpm_solver_create(op, m, n, 32, &sv->solver);
-    if (!rc) rc = alloc_vectors(sv->solver, !sv->P.mixed, sv->P.mixed);
     if (rc) return bail(rc);
-    const int64_t D = sv->solver->D;
-    if (cudaMallocHost((void **)&sv->h_stage, sizeof(double) * 32 * (size_t)D) != cudaSuccess)
+    sv->solvers.assign(nb, nullptr);
+    for (int b = 0; b < nb && !rc; ++b) rc = cpm_solver_create(op, m, n, 32, &sv->solvers[b]);
+    if (rc) return bail(rc);
+    const int64_t D = op->D;
+    if (cudaMallocHost((void **)&sv->h_stage, sizeof(double) * 32 * nb * (size_t)D) != cudaSuccess)
         return bail(fail(CPM_ERR_OOM, "server_create: pinned staging"));
-    if ((rc = sv->d_stage.alloc(32 * (size_t)D))) return bail(rc);
-    sv->busy.assign(32, cpm_server_s::Busy());
-    for (int j = 0; j < 32; ++j) {
-        memset(&sv->solver->h_slots[j], 0, sizeof(Slot));
-        sv->solver->h_slots[j].phase = PH_IDLE;
+    if ((rc = sv->d_stage.alloc(32 * nb * (size_t)D))) return bail(rc);
+    sv->busy.assign(32 * nb, cpm_server_s::Busy());
+    for (cpm_solver_s *s : sv->solvers) {
+        SolverScope sc(s);
+        if ((rc = alloc_vectors(s, !sv->P.mixed, sv->P.mixed))) return bail(rc);
+        for (int j = 0; j < 32; ++j) {
+            memset(&s->h_slots[j], 0, sizeof(Slot));
+            s->h_slots[j].phase = PH_IDLE;
+        }
+        CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p, s->h_slots.data(), sizeof(Slot) * 32, cudaMemcpyHostToDevice, stream()));
+        cudaGraphExec_t g = nullptr;
+        if ((rc = prepare_graph<32>(s, sv->P, &g))) return bail(rc);
+        CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
     }
-    CPM_CUDA_TRY(cudaMemcpyAsync(sv->solver->slots.p, sv->solver->h_slots.data(), sizeof(Slot) * 32, cudaMemcpyHostToDevice,
-                                 stream()));
-    cudaGraphExec_t g = nullptr;
-    if ((rc = prepare_graph<32>(sv->solver, sv->P, &g))) return bail(rc);
-    CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
     *out = sv;
     return 0;
+}
+
+extern "C" int cpm_server_create(cpm_opset_t op, double m, double n, const cpm_solve_opts *opts, cpm_server_t *out) {
+    return server_create(op, m, n, opts, 1, out);
+}
+
+extern "C" int cpm_server_create_batches(cpm_opset_t op, double m, double n, const cpm_solve_opts *opts, int32_t batches,
+                                         cpm_server_t *out) {
+    return server_create(op, m, n, opts, batches, out);
 }
 
 extern "C" int cpm_server_submit(cpm_server_t sv, const double *b, int64_t tag) {
     if (!sv || !b) return fail(CPM_ERR_INVALID_ARG, "server_submit: null argument");
     cpm_server_s::Req r;
     r.tag = tag;
-    r.b.assign(b, b + sv->solver->D);
+    r.b.assign(b, b + sv->solvers[0]->D);
     r.t_submit = std::chrono::steady_clock::now();
     sv->queue.push_back(std::move(r));
     return 0;
@@ -1927,118 +1975,133 @@ extern "C" int cpm_server_submit_device(cpm_server_t sv, const void *b_dev, void
 
 extern "C" int cpm_server_step(cpm_server_t sv, int32_t *active, int32_t *queued, int32_t *finished) {
     if (!sv) return fail(CPM_ERR_INVALID_ARG, "server_step: null server");
-    cpm_solver_s *s = sv->solver;
-    const int64_t D = s->D;
-    cudaStream_t st = stream();
-    // admit queued requests into free slots
-    bool admitted = false;
-    for (int j = 0; j < 32 && !sv->queue.empty(); ++j) {
-        if (sv->busy[j].used) continue;
-        cpm_server_s::Req r = std::move(sv->queue.front());
-        sv->queue.pop_front();
-        double *hs = sv->h_stage + (size_t)j * D, *ds = sv->d_stage.p + (size_t)j * D;
-        const double *src = r.b_dev;
-        if (!src) {
-            memcpy(hs, r.b.data(), sizeof(double) * D);
-            CPM_CUDA_TRY(cudaMemcpyAsync(ds, hs, sizeof(double) * D, cudaMemcpyHostToDevice, st));
-            src = ds;
-        }
-        k_scatter_col<<<nblk(D), BS, 0, st>>>(D, 32, j, src, s->b64.p);
-        count_launches(1);
-        memset(&s->h_slots[j], 0, sizeof(Slot));
-        s->h_slots[j].phase = PH_START;
-        CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p + j, &s->h_slots[j], sizeof(Slot), cudaMemcpyHostToDevice, st));
-        sv->busy[j].used = true;
-        sv->busy[j].tag = r.tag;
-        sv->busy[j].x_dev = r.x_dev;
-        sv->busy[j].t_submit = r.t_submit;
-        sv->busy[j].t_admit = std::chrono::steady_clock::now();
-        admitted = true;
-    }
-    if (admitted) {
-        if (sv->P.mixed) {
-            mixed_start<32>(s, sv->P);
-        } else {
-            k_init<double, 32><<<s->G, BS, 0, st>>>(s->op->view<double>(), s->slots.p, sv->P, PH_START, s->b64.p, s->x64.p,
-                                                    s->dr.p, s->dr0.p, s->dp.p, s->dv.p, s->partial.p, s->counter.p);
+    const int nb = (int)sv->solvers.size();
+    const int64_t D = sv->solvers[0]->D;
+    // admit queued requests into free slots, then start them and launch every busy
+    // solver's iteration graph, each on its own stream
+    for (int b = 0; b < nb; ++b) {
+        cpm_solver_s *s = sv->solvers[b];
+        SolverScope sc(s);
+        cudaStream_t st = stream();
+        bool admitted = false;
+        for (int j = 0; j < 32 && !sv->queue.empty(); ++j) {
+            cpm_server_s::Busy &bz = sv->busy[32 * b + j];
+            if (bz.used) continue;
+            cpm_server_s::Req r = std::move(sv->queue.front());
+            sv->queue.pop_front();
+            double *hs = sv->h_stage + (size_t)(32 * b + j) * D, *ds = sv->d_stage.p + (size_t)(32 * b + j) * D;
+            const double *src = r.b_dev;
+            if (!src) {
+                memcpy(hs, r.b.data(), sizeof(double) * D);
+                CPM_CUDA_TRY(cudaMemcpyAsync(ds, hs, sizeof(double) * D, cudaMemcpyHostToDevice, st));
+                src = ds;
+            }
+            k_scatter_col<<<nblk(D), BS, 0, st>>>(D, 32, j, src, s->b64.p);
             count_launches(1);
+            memset(&s->h_slots[j], 0, sizeof(Slot));
+            s->h_slots[j].phase = PH_START;
+            CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p + j, &s->h_slots[j], sizeof(Slot), cudaMemcpyHostToDevice, st));
+            bz.used = true;
+            bz.tag = r.tag;
+            bz.x_dev = r.x_dev;
+            bz.t_submit = r.t_submit;
+            bz.t_admit = std::chrono::steady_clock::now();
+            admitted = true;
+        }
+        if (admitted) {
+            if (sv->P.mixed) {
+                mixed_start<32>(s, sv->P);
+            } else {
+                k_init<double, 32><<<s->G, BS, 0, st>>>(s->op->view<double>(), s->slots.p, sv->P, PH_START, s->b64.p, s->x64.p,
+                                                        s->dr.p, s->dr0.p, s->dp.p, s->dv.p, s->partial.p, s->counter.p);
+                count_launches(1);
+            }
+        }
+        int n_busy = 0;
+        for (int j = 0; j < 32; ++j) n_busy += sv->busy[32 * b + j].used;
+        if (n_busy) {
+            cudaGraphExec_t g = nullptr;
+            CPM_TRY(prepare_graph<32>(s, sv->P, &g));
+            CPM_CUDA_TRY(cudaGraphLaunch(g, st));
+            count_launches(graph_launches(s, sv->P));
+        }
+        CPM_CUDA_TRY(cudaMemcpyAsync(s->h_slots.data(), s->slots.p, sizeof(Slot) * 32, cudaMemcpyDeviceToHost, st));
+    }
+    int n_fin = 0;
+    for (int b = 0; b < nb; ++b) {
+        cpm_solver_s *s = sv->solvers[b];
+        SolverScope sc(s);
+        cudaStream_t st = stream();
+        CPM_CUDA_TRY(cudaStreamSynchronize(st));
+        if (!sv->P.mixed) {  // the plain path's restarts run between graphs (as in run_solve)
+            bool restart = false;
+            for (int j = 0; j < 32; ++j) restart = restart || s->h_slots[j].phase == PH_RESTART;
+            if (restart) {
+                plain_restart<32>(s);
+                count_launches(2);
+                CPM_CUDA_TRY(cudaGetLastError());
+            }
+        }
+        // harvest finished slots
+        std::vector<int> fin;
+        std::vector<cpm_solve_stats> fb_st(32);
+        std::vector<char> fb(32, 0);
+        for (int j = 0; j < 32; ++j) {
+            const Slot &S = s->h_slots[j];
+            cpm_server_s::Busy &bz = sv->busy[32 * b + j];
+            if (!bz.used) continue;
+            const bool over = S.phase == PH_DONE || S.iters >= sv->P.max_iters || S.refinements >= sv->P.max_refine;
+            if (!over) continue;
+            double *ds = bz.x_dev ? bz.x_dev : sv->d_stage.p + (size_t)(32 * b + j) * D;
+            if (S.phase == PH_DONE && (S.status == 0 || !sv->P.mixed)) {
+                k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->x64.p, ds);
+                count_launches(1);
+            } else {
+                // the FP32 inner iteration could not solve this right-hand side:
+                // solve it again with the plain FP64 path (one slot, blocking)
+                if (!sv->fallback) CPM_TRY(cpm_solver_create(s->op, s->m, s->n, 1, &sv->fallback));
+                double *bj = sv->d_stage.p + (size_t)(32 * b + j) * D;
+                k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->b64.p, bj);
+                count_launches(1);
+                cpm_solve_opts o64 = sv->opts;
+                o64.precision = 0;
+                CPM_TRY(cpm_solve_device(sv->fallback, 1, bj, ds, &o64, &fb_st[j]));
+                fb[j] = 1;
+            }
+            if (!bz.x_dev)
+                CPM_CUDA_TRY(cudaMemcpyAsync(sv->h_stage + (size_t)(32 * b + j) * D, ds, sizeof(double) * D,
+                                             cudaMemcpyDeviceToHost, st));
+            fin.push_back(j);
+        }
+        if (!fin.empty()) {
+            CPM_CUDA_TRY(cudaStreamSynchronize(st));
+            const auto now = std::chrono::steady_clock::now();
+            for (int j : fin) {
+                cpm_server_s::Busy &bz = sv->busy[32 * b + j];
+                cpm_server_s::Done d;
+                d.tag = bz.tag;
+                if (!bz.x_dev)
+                    d.x.assign(sv->h_stage + (size_t)(32 * b + j) * D, sv->h_stage + (size_t)(32 * b + j + 1) * D);
+                slot_stats(s->h_slots[j], sv->P.mixed != 0, 0.0f, &d.st);
+                if (fb[j]) {
+                    const int it = d.st.iterations, rf = d.st.refinements;
+                    d.st = fb_st[j];
+                    d.st.iterations += it;
+                    d.st.refinements = rf;
+                    d.st.fp64_fallback = 1;
+                }
+                d.latency = std::chrono::duration<double>(now - bz.t_submit).count();
+                d.st.seconds = std::chrono::duration<double>(now - bz.t_admit).count();
+                sv->done.push_back(std::move(d));
+                bz.used = false;
+                s->h_slots[j].phase = PH_IDLE;
+                CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p + j, &s->h_slots[j], sizeof(Slot), cudaMemcpyHostToDevice, st));
+                ++n_fin;
+            }
         }
     }
     int n_busy = 0;
-    for (int j = 0; j < 32; ++j) n_busy += sv->busy[j].used;
-    if (n_busy) {
-        cudaGraphExec_t g = nullptr;
-        CPM_TRY(prepare_graph<32>(s, sv->P, &g));
-        CPM_CUDA_TRY(cudaGraphLaunch(g, st));
-        count_launches(graph_launches(s, sv->P));
-    }
-    CPM_CUDA_TRY(cudaMemcpyAsync(s->h_slots.data(), s->slots.p, sizeof(Slot) * 32, cudaMemcpyDeviceToHost, st));
-    CPM_CUDA_TRY(cudaStreamSynchronize(st));
-    if (!sv->P.mixed) {  // the plain path's restarts run between graphs (as in run_solve)
-        bool restart = false;
-        for (int j = 0; j < 32; ++j) restart = restart || s->h_slots[j].phase == PH_RESTART;
-        if (restart) {
-            plain_restart<32>(s);
-            count_launches(2);
-            CPM_CUDA_TRY(cudaGetLastError());
-        }
-    }
-    // harvest finished slots
-    int n_fin = 0;
-    std::vector<int> fin;
-    std::vector<cpm_solve_stats> fb_st(32);
-    std::vector<char> fb(32, 0);
-    for (int j = 0; j < 32; ++j) {
-        const Slot &S = s->h_slots[j];
-        if (!sv->busy[j].used) continue;
-        const bool over = S.phase == PH_DONE || S.iters >= sv->P.max_iters || S.refinements >= sv->P.max_refine;
-        if (!over) continue;
-        double *ds = sv->busy[j].x_dev ? sv->busy[j].x_dev : sv->d_stage.p + (size_t)j * D;
-        if (S.phase == PH_DONE && (S.status == 0 || !sv->P.mixed)) {
-            k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->x64.p, ds);
-            count_launches(1);
-        } else {
-            // the FP32 inner iteration could not solve this right-hand side:
-            // solve it again with the plain FP64 path (one slot, blocking)
-            if (!sv->fallback) CPM_TRY(cpm_solver_create(s->op, s->m, s->n, 1, &sv->fallback));
-            double *bj = sv->d_stage.p + (size_t)j * D;
-            k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->b64.p, bj);
-            count_launches(1);
-            cpm_solve_opts o64 = sv->opts;
-            o64.precision = 0;
-            CPM_TRY(cpm_solve_device(sv->fallback, 1, bj, ds, &o64, &fb_st[j]));
-            fb[j] = 1;
-        }
-        if (!sv->busy[j].x_dev)
-            CPM_CUDA_TRY(cudaMemcpyAsync(sv->h_stage + (size_t)j * D, ds, sizeof(double) * D, cudaMemcpyDeviceToHost, st));
-        fin.push_back(j);
-    }
-    if (!fin.empty()) {
-        CPM_CUDA_TRY(cudaStreamSynchronize(st));
-        const auto now = std::chrono::steady_clock::now();
-        for (int j : fin) {
-            cpm_server_s::Done d;
-            d.tag = sv->busy[j].tag;
-            if (!sv->busy[j].x_dev) d.x.assign(sv->h_stage + (size_t)j * D, sv->h_stage + (size_t)(j + 1) * D);
-            slot_stats(s->h_slots[j], sv->P.mixed != 0, 0.0f, &d.st);
-            if (fb[j]) {
-                const int it = d.st.iterations, rf = d.st.refinements;
-                d.st = fb_st[j];
-                d.st.iterations += it;
-                d.st.refinements = rf;
-                d.st.fp64_fallback = 1;
-            }
-            d.latency = std::chrono::duration<double>(now - sv->busy[j].t_submit).count();
-            d.st.seconds = std::chrono::duration<double>(now - sv->busy[j].t_admit).count();
-            sv->done.push_back(std::move(d));
-            sv->busy[j].used = false;
-            s->h_slots[j].phase = PH_IDLE;
-            CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p + j, &s->h_slots[j], sizeof(Slot), cudaMemcpyHostToDevice, st));
-            ++n_fin;
-        }
-    }
-    n_busy = 0;
-    for (int j = 0; j < 32; ++j) n_busy += sv->busy[j].used;
+    for (auto &bz : sv->busy) n_busy += bz.used;
     if (active) *active = n_busy;
     if (queued) *queued = (int32_t)sv->queue.size();
     if (finished) *finished = n_fin;
@@ -2058,7 +2121,6 @@ extern "C" int cpm_server_poll(cpm_server_t sv, int64_t *tag, double *x, cpm_sol
 }
 
 extern "C" int cpm_server_destroy(cpm_server_t sv) {
-    if (sv) cudaStreamSynchronize(stream());
     delete sv;
     return 0;
 }
@@ -2066,9 +2128,8 @@ extern "C" int cpm_server_destroy(cpm_server_t sv) {
 extern "C" int64_t cpm_server_device_bytes(cpm_opset_t op) {
     if (!op) return -1;
     const int64_t D = op->D;
-    // FP32 Krylov vectors (10), FP64 b, x, r, E~x (4), staging, reduction scratch
-    // the larger of the two precisions: FP32 Krylov vectors (10) + FP64 b, x, r, E~x
-    // (4), or FP64 Krylov vectors (8) + the same 4; staging; reduction scratch
+    // per 32-slot batch, the larger of the two precisions: FP32 Krylov vectors (10) + FP64
+    // b, x, r, E~x (4), or FP64 Krylov vectors (8) + the same 4; staging; reduction scratch
     return D * 32 * (12 * 8 + 8) + D * (8 + 4) + (int64_t)(1 << 20);
 }
 

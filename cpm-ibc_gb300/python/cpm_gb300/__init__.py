@@ -179,6 +179,7 @@ def lib():
         L.cpm_solve_device.argtypes = [vp, ctypes.c_int32, vp, vp, P(SolveOpts), P(SolveStats)]
         L.cpm_solver_destroy.argtypes = [vp]
         L.cpm_server_create.argtypes = [vp, ctypes.c_double, ctypes.c_double, P(SolveOpts), P(vp)]
+        L.cpm_server_create_batches.argtypes = [vp, ctypes.c_double, ctypes.c_double, P(SolveOpts), ctypes.c_int32, P(vp)]
         L.cpm_server_submit.argtypes = [vp, vp, ctypes.c_int64]
         L.cpm_server_submit_device.argtypes = [vp, vp, vp, ctypes.c_int64]
         L.cpm_server_step.argtypes = [vp, vp, vp, vp]
@@ -554,17 +555,18 @@ class Server:
     updates; 0: plain FP64), admitted as slots free up."""
 
     def __init__(self, opset, m, n, tol=1e-10, inner_tol=0.0, max_refine=400, refine_every=0, max_iters=100000,
-                 precision=1):
-        self.opset, self.D, self.precision = opset, opset.D, precision
+                 precision=1, batches=1):
+        """batches: 32-slot solvers run concurrently, each on its own stream"""
+        self.opset, self.D, self.precision, self.batches = opset, opset.D, precision, batches
         o = SolveOpts(tol=tol, max_iters=max_iters, precision=precision, precond=DIAGONAL, precond_iters=0,
                       inner_tol=inner_tol, max_refine=max_refine, refine_every=refine_every)
         h = ctypes.c_void_p()
-        _check(lib().cpm_server_create(opset.h, m, n, ctypes.byref(o), ctypes.byref(h)))
+        _check(lib().cpm_server_create_batches(opset.h, m, n, ctypes.byref(o), int(batches), ctypes.byref(h)))
         self.h = h
 
     @staticmethod
-    def device_bytes(opset):
-        return int(lib().cpm_server_device_bytes(opset.h))
+    def device_bytes(opset, batches=1):
+        return batches * int(lib().cpm_server_device_bytes(opset.h))
 
     def __del__(self):
         try:

@@ -379,10 +379,17 @@ int cpm_geodesic_nearest_destroy(cpm_geodesic_nearest_t g);
  * harvest, queueing included).  submit_device takes a device right-hand side
  * (D doubles, read when the request is admitted) and a device destination for
  * its solution (written when it finishes; poll then returns no x).
- * device_bytes estimates the device memory a server on `op` allocates, for
- * admission by free HBM. */
+ * device_bytes estimates the device memory one 32-slot batch of a server on
+ * `op` allocates, for admission by free HBM.  Solvers and servers run on
+ * streams of their own, ordered after the work the calling thread queued on
+ * the library stream; every call returns with its work complete. */
 typedef struct cpm_server_s *cpm_server_t;
 int cpm_server_create(cpm_opset_t op, double m, double n, const cpm_solve_opts *opts, cpm_server_t *out);
+/* The same server over `batches` (1 to 8) 32-slot solvers, each on its own
+ * stream: every step launches each busy batch's iteration graph before waiting
+ * for any, so the batches' kernels overlap on the GPU (32 x batches slots). */
+int cpm_server_create_batches(cpm_opset_t op, double m, double n, const cpm_solve_opts *opts, int32_t batches,
+                              cpm_server_t *out);
 int cpm_server_submit(cpm_server_t s, const double *b, int64_t tag);
 int cpm_server_submit_device(cpm_server_t s, const void *b_dev, void *x_dev, int64_t tag);
 int cpm_server_step(cpm_server_t s, int32_t *active, int32_t *queued, int32_t *finished);

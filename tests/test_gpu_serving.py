@@ -88,3 +88,36 @@ def test_server_plain_fp64_mode(gpu):
         assert st["status"] == 0 and st["fp64_fallback"] == 0
         x64, _ = ref.solve(B[k], tol=1e-12, precision=0)
         assert _rel(x, x64[0]) <= 1e-9
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_server_two_concurrent_batches(gpu, precision):
+    """A server over two 32-slot batches on their own streams (cpm_server_create_batches):
+    80 requests, each within 1e-8 of its FP64 solve (tol 1e-12); with device right-hand
+    sides and destinations as well as host ones."""
+    import torch
+
+    T, O, rows = _setup(gpu, dx=0.05)
+    rng = np.random.default_rng(33)
+    n_req = 80
+    B = np.stack([_rhs(rows, rng.uniform(0, 1, 2)) for _ in range(n_req)])
+    srv = gpu.Server(O, 0.0, -1.0, precision=precision, batches=2)
+    b_dev = torch.from_numpy(B[40:]).cuda()
+    x_dev = torch.zeros_like(b_dev)
+    torch.cuda.synchronize()
+    for k in range(40):
+        srv.submit(B[k], k)
+    for k in range(40, n_req):
+        srv.submit_device(b_dev[k - 40].data_ptr(), x_dev[k - 40].data_ptr(), k)
+    out = srv.drain()
+    assert sorted(out) == list(range(n_req))
+    xd = x_dev.cpu().numpy()
+    ref = gpu.Solver(O, 0.0, -1.0, kslots=32)
+    for lo in range(0, n_req, 32):
+        X64, _ = ref.solve(B[lo:lo + 32], tol=1e-12, precision=0)
+        for j in range(len(X64)):
+            k = lo + j
+            x, st = out[k]
+            assert st["status"] == 0 and st["rel_residual"] <= 1e-10
+            got = x if k < 40 else xd[k - 40]
+            assert _rel(got, X64[j]) <= 1e-8
