@@ -287,6 +287,61 @@ def run_profile(what):
     torch.cuda.synchronize()
 
 
+def serving_mix(cg, requests, rate, seed=11):
+    """The serving stream over the three resident surfaces (the sphere with two circles at
+    dx 0.025, the torus at dx 0.01, the perturbed icosphere at dx 0.005): `requests` seeded
+    Poisson arrivals at `rate` per second, one in 32 a geodesic, the rest IBC Laplace solves
+    with values U[0,1]; served by the serving loop (continuous batching, mixed precision) and,
+    on the same stream and arrival times, one request at a time by the plain FP64 path.
+    Returns the summary (solves/s, p50/p99 latency of both)."""
+    from cpm_gb300 import serving as SV
+    from cpm_gb300 import workloads as W
+
+    t = time.perf_counter()
+    surfaces = W.serving_surfaces(cg)
+    t_setup = time.perf_counter() - t
+    loop = SV.ServingLoop(surfaces)
+    reqs = SV.poisson_stream(surfaces, requests, rate=rate, geodesic_every=32, seed=seed)
+    warm = SV.poisson_stream(surfaces, 12, rate=0.0, geodesic_every=0, seed=seed + 1)
+    for r in warm:
+        r["id"] = -1 - r["id"]
+    loop.run(warm)
+    t = time.perf_counter()
+    out = loop.run(reqs)
+    span = time.perf_counter() - t
+    lat = {k: [o["latency"] for o in out.values() if o["kind"] == k] for k in ("laplace", "geodesic")}
+    fb = sum(1 for o in out.values() if o["kind"] == "laplace" and o["stats"].get("fp64_fallback"))
+    t = time.perf_counter()
+    out64 = SV.serve_fp64_one_at_a_time(surfaces, reqs)
+    span64 = time.perf_counter() - t
+    lat64 = {k: [o["latency"] for o in out64.values() if o["kind"] == k] for k in ("laplace", "geodesic")}
+    all_lat = [o["latency"] for o in out.values()]
+    all_lat64 = [o["latency"] for o in out64.values()]
+
+    def pct(v):
+        return {k: {"p50": float(np.percentile(x, 50) * 1e3), "p99": float(np.percentile(x, 99) * 1e3), "n": len(x)}
+                for k, x in v.items() if x}
+
+    return {
+        "config": {"surfaces": {s.name: {"tube_nodes": s.tube.N, "rows": s.opset.D, "curves": s.n_ibc,
+                                         "server_bytes": s.bytes} for s in surfaces},
+                   "requests": requests, "rate_per_s": rate, "geodesic_every": 32, "arrivals": "seeded Poisson process",
+                   "slots_per_surface": 32, "tol": TOL},
+        "setup_s": t_setup, "makespan_s": span, "solves_per_s": len(out) / span,
+        "latency_ms": {"p50": float(np.percentile(all_lat, 50) * 1e3), "p99": float(np.percentile(all_lat, 99) * 1e3),
+                       "by_kind": pct(lat)},
+        "laplace_fp64_fallbacks": fb, "admissions": loop.admissions, "evictions": loop.evictions,
+        "precision_switches": loop.precision_switches,
+        "final_precision": {s.name: ("mixed" if s.precision else "fp64") for s in surfaces},
+        "solo_fp64_solves": loop.solo_solves,
+        "fp64_one_at_a_time": {"makespan_s": span64, "solves_per_s": len(out64) / span64,
+                               "latency_ms": {"p50": float(np.percentile(all_lat64, 50) * 1e3),
+                                              "p99": float(np.percentile(all_lat64, 99) * 1e3), "by_kind": pct(lat64)},
+                               "path": "the same stream and arrival times, each request solved alone in FP64"},
+        "speedup_solves_per_s": (len(out) / span) / (len(out64) / span64),
+    }
+
+
 def run_workload(args):
     """One JSON line for a configuration other than the headline one."""
     import build_ext
@@ -388,44 +443,7 @@ def run_workload(args):
                                                for c in range(3))),
         })
     else:  # serving-mix
-        t = time.perf_counter()
-        surfaces = W.serving_surfaces(cg)
-        t_setup = time.perf_counter() - t
-        loop = SV.ServingLoop(surfaces)
-        reqs = SV.poisson_stream(surfaces, args.requests, rate=args.rate, geodesic_every=32, seed=11)
-        warm = SV.poisson_stream(surfaces, 12, rate=0.0, geodesic_every=0, seed=12)
-        for r in warm:
-            r["id"] = -1 - r["id"]
-        loop.run(warm)
-        t = time.perf_counter()
-        out = loop.run(reqs)
-        span = time.perf_counter() - t
-        lat = {k: [o["latency"] for o in out.values() if o["kind"] == k] for k in ("laplace", "geodesic")}
-        fb = sum(1 for o in out.values() if o["kind"] == "laplace" and o["stats"].get("fp64_fallback"))
-        t = time.perf_counter()
-        out64 = SV.serve_fp64_one_at_a_time(surfaces, reqs)
-        span64 = time.perf_counter() - t
-        lat64 = {k: [o["latency"] for o in out64.values() if o["kind"] == k] for k in ("laplace", "geodesic")}
-
-        def pct(v):
-            return {k: {"p50": float(np.percentile(x, 50) * 1e3), "p99": float(np.percentile(x, 99) * 1e3), "n": len(x)}
-                    for k, x in v.items() if x}
-
-        line.update({
-            "config": {"surfaces": {s.name: {"tube_nodes": s.tube.N, "rows": s.opset.D, "curves": s.n_ibc,
-                                             "server_bytes": s.bytes} for s in surfaces},
-                       "requests": args.requests, "rate_per_s": args.rate, "geodesic_every": 32,
-                       "arrivals": "seeded Poisson process", "slots_per_surface": 32, "tol": TOL},
-            "setup_s": t_setup, "makespan_s": span, "solves_per_s": len(out) / span,
-            "latency_ms": pct(lat),
-            "laplace_fp64_fallbacks": fb, "admissions": loop.admissions, "evictions": loop.evictions,
-            "precision_switches": loop.precision_switches,
-            "final_precision": {s.name: ("mixed" if s.precision else "fp64") for s in surfaces},
-            "solo_fp64_solves": loop.solo_solves,
-            "fp64_one_at_a_time": {"makespan_s": span64, "solves_per_s": len(out64) / span64, "latency_ms": pct(lat64),
-                                   "path": "the same stream and arrival times, each request solved alone in FP64"},
-            "note": "geodesics run one at a time on their own point-IBC operator between server steps",
-        })
+        line.update(serving_mix(cg, args.requests, args.rate))
     print(json.dumps(line), flush=True)
 
 
@@ -446,6 +464,9 @@ def main():
     ap.add_argument("--solo", type=int, default=2, help="torus-geodesic: sources also run one at a time")
     ap.add_argument("--rate", type=float, default=8.0, help="serving-mix: mean arrivals per second")
     ap.add_argument("--batches", type=int, default=2, help="32-slot batches of the server, run concurrently")
+    ap.add_argument("--mix-requests", type=int, default=64,
+                    help="requests of the serving-stream sample in the default line (0: none)")
+    ap.add_argument("--mix-rate", type=float, default=4.0, help="its mean arrivals per second")
     ap.add_argument("--refine-every", type=int, default=0,
                     help="mixed precision: reliable-update period in iterations (0: the library default)")
     ap.add_argument("--inner-tol", type=float, default=0.0,
@@ -599,6 +620,11 @@ def main():
     if os.path.exists(prof):
         traffic = json.load(open(prof)).get("bytes_per_apply")
 
+    # ---- the serving stream over three surfaces (bounded sample; rank 0, N = 1 only)
+    mix = None
+    if rank == 0 and world == 1 and args.mix_requests > 0:
+        mix = serving_mix(cg, args.mix_requests, args.mix_rate)
+
     # ---- CPU baseline and the error against the oracle (rank 0, N = 1 only): whole oracle solves
     cpu, rel_err_oracle = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -670,6 +696,7 @@ def main():
                          "traffic": traffic, "kernel": "L.E apply (E pass + IBC patch rows + L pass), FP32, 32 RHS",
                          "apply_us": apply_s * 1e6, "alg_bytes_per_apply": alg_bytes, "peak_source": peak_src},
             "cpu_baseline": cpu,
+            "serving_mix": mix,
             "gpu_launches": int(launches),
             "clocks": clocks,
             "setup_s": setup_s,
