@@ -18,14 +18,9 @@ enum RowFlags : uint8_t {
     F_SLOTP = 64,  // tube row with per-slot patch records (a batch with one point IBC per slot)
 };
 
-// Schedule of the brick-staged E pass (k_ebrick32, FP32, 32 slots).  Rows are
-// grouped by base point and the groups by the 4^3 brick of grid points their
-// base lies in (a base brick).  The stencils of a base brick's groups cover the
-// 2 x 2 x 2 node bricks at its corner, whose nodes are contiguous runs of the
-// tube's node order, so a unit of work stages them with eight bulk copies (plus
-// one per IBC column its patch entries read) and computes every row of its
-// groups from shared memory.  Offsets are bytes into the unit's stage, one
-// 128-byte row (32 FP32 slots) per staged node.
+// Device view of an operator set in one arithmetic type: the rows of E and L
+// (bulk stencils, IBC patches), the apply schedule (rows sorted into base
+// groups, identity rows, neighbour table) and the per-slot patches of a batch.
 template <class T>
 struct OpView {
     BrickView bv;
@@ -307,6 +302,12 @@ __device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
+
+// round-to-nearest fma and difference, never re-associated by the compiler
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 
 // four consecutive values from 16-byte aligned shared memory, as vector loads
 __device__ __forceinline__ void lds4(const float *p, float (&o)[4]) {

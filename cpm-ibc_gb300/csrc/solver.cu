@@ -326,6 +326,48 @@ __global__ void __launch_bounds__(128) k_epass32s(OpView<T> op, const Slot *__re
         }
 }
 
+// IBC patch of one row of a 32-slot E pass (warp per row, lane = slot): patch-
+// list row q's value from its bulk value acc, sign (acc + sum_e w_e (x[new_e] -
+// x[old_e])) + xval x[xcol]: moved stencil points read the IBC DOF column
+// instead of the tube node (IBCMatrixManipulations::AddIBCExtension's column
+// moves, src/IBCMatrixManipulations.cpp:118-186).  The lanes load 32 entries at
+// once and broadcast them, so a row's x loads are all in flight together.
+// q is the same in every lane; inactive slots (act false) load nothing.
+template <class T>
+__device__ __forceinline__ T patch_row(const OpView<T> &op, int q, T acc, int lane, bool act, const T *__restrict__ x) {
+    const int e0 = op.pl_off[q], e1 = op.pl_off[q + 1], xc = op.pl_xcol[q], neg = op.pl_neg[q];
+    const T xv = op.pl_xval[q];
+    const T xe = (act && xc >= 0) ? x[(uint32_t)xc * 32u + lane] : T(0);
+    for (int base = e0; base < e1; base += 32) {
+        const int cnt = min(32, e1 - base);
+        int nc = 0, oc = 0;
+        T w = 0;
+        if (lane < cnt) {
+            nc = op.pe_new[base + lane];
+            oc = op.pe_old[base + lane];
+            w = op.pe_w[base + lane];
+        }
+        for (int u0 = 0; u0 < cnt; u0 += 8) {
+            T xn[8], xo[8], ww[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int k = u0 + u;
+                const uint32_t ncu = (uint32_t)__shfl_sync(FULL, nc, k & 31), ocu = (uint32_t)__shfl_sync(FULL, oc, k & 31);
+                ww[u] = __shfl_sync(FULL, w, k & 31);
+                const bool ok = act && k < cnt;
+                xn[u] = ok ? x[ncu * 32u + lane] : T(0);
+                xo[u] = ok ? x[ocu * 32u + lane] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (u0 + u < cnt) acc = fma_rn(ww[u], sub_rn(xn[u], xo[u]), acc);
+        }
+    }
+    if (neg) acc = -acc;
+    if (xc >= 0) acc = fma_rn(xv, xe, acc);
+    return acc;
+}
+
 // 32 FP32 slots, warp per base group: the warp gathers the group's 64 x
 // values plane by plane (16 columns each) and keeps each pair of rows' sum in
 // registers (f32x2): plane i adds wx_i (sum_j wy_j sum_k wz_k x_ijk) in the
@@ -427,12 +469,8 @@ __global__ void k_epass1(OpView<T> op, const Slot *__restrict__ sl, int ph, cons
     }
 }
 
-// IBC patch of the 32-slot E passes: for each row on the patch list (warp per
-// row, lane = slot), t_r = sign (bulk t_r + sum_e w_e (x[new_e] - x[old_e]))
-// + xval x[xcol]: moved stencil points read the IBC DOF column instead of the
-// tube node (IBCMatrixManipulations::AddIBCExtension's column moves,
-// src/IBCMatrixManipulations.cpp:118-186).  The lanes load 32 entries at once
-// and broadcast them, so a row's x loads are all in flight together.
+// the patch as a pass of its own after a bulk E pass (the FP64 32-slot pass),
+// warp per patch-list row
 template <class T>
 __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x,
                                                   T *__restrict__ t) {
@@ -440,54 +478,11 @@ __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__re
     const bool act = (ph < 0) || sl[lane].phase == ph;
     if (!__any_sync(FULL, act)) return;  // the same slots in every warp: block-uniform
     const int64_t warps = (int64_t)gridDim.x * 4;
-    int64_t q = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (q >= op.n_pl) return;
-    // the row's list record, loaded one row ahead
-    uint32_t r_n = (uint32_t)op.pl_row[q];
-    int e0_n = op.pl_off[q], e1_n = op.pl_off[q + 1], xc_n = op.pl_xcol[q], neg_n = op.pl_neg[q];
-    T xv_n = op.pl_xval[q];
-    for (; q < op.n_pl; q += warps) {
-        const uint32_t r = r_n;
-        const int e0 = e0_n, e1 = e1_n, xc = xc_n, neg = neg_n;
-        const T xv = xv_n;
-        if (q + warps < op.n_pl) {
-            r_n = (uint32_t)op.pl_row[q + warps];
-            e0_n = op.pl_off[q + warps];
-            e1_n = op.pl_off[q + warps + 1];
-            xc_n = op.pl_xcol[q + warps];
-            neg_n = op.pl_neg[q + warps];
-            xv_n = op.pl_xval[q + warps];
-        }
-        T acc = act ? t[r * 32u + lane] : T(0);
-        const T xe = (act && xc >= 0) ? x[(uint32_t)xc * 32u + lane] : T(0);
-        for (int base = e0; base < e1; base += 32) {
-            const int cnt = min(32, e1 - base);
-            int nc = 0, oc = 0;
-            T w = 0;
-            if (lane < cnt) {
-                nc = op.pe_new[base + lane];
-                oc = op.pe_old[base + lane];
-                w = op.pe_w[base + lane];
-            }
-            for (int u0 = 0; u0 < cnt; u0 += 8) {
-                T xn[8], xo[8], ww[8];
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int k = u0 + u;
-                    const uint32_t ncu = (uint32_t)__shfl_sync(FULL, nc, k & 31), ocu = (uint32_t)__shfl_sync(FULL, oc, k & 31);
-                    ww[u] = __shfl_sync(FULL, w, k & 31);
-                    const bool ok = act && k < cnt;
-                    xn[u] = ok ? x[ncu * 32u + lane] : T(0);
-                    xo[u] = ok ? x[ocu * 32u + lane] : T(0);
-                }
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (u0 + u < cnt) acc += ww[u] * (xn[u] - xo[u]);
-            }
-        }
-        if (neg) acc = -acc;
-        if (xc >= 0) acc += xv * xe;
-        if (act) t[r * 32u + lane] = acc;
+    for (int64_t q = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5); q < op.n_pl; q += warps) {
+        const uint32_t r = (uint32_t)op.pl_row[q];
+        const T acc = act ? t[r * 32u + lane] : T(0);
+        const T v = patch_row<T>(op, (int)q, acc, lane, act, x);
+        if (act) t[r * 32u + lane] = v;
     }
 }
 

@@ -182,11 +182,13 @@ def test_golden_order_through_device_solver(gpu, oracle):
 
 
 @pytest.mark.parametrize("dx", [0.05, 0.025])
-def test_brick_staged_e_pass_equals_gather_pass_bitwise(gpu, dx):
-    """The brick-staged FP32 32-slot E pass (k_ebrick32: TMA-staged node bricks,
-    IBC patch in registers) gives the same bits as the gather pass it replaces
-    (k_epass32w then k_epatch32), which cpm_apply_device still runs for an input
-    that is not 16-byte aligned."""
+def test_fp32_batched_apply_against_fp64_and_alignment(gpu, dx):
+    """The FP32 32-slot apply (E pass, IBC patch pass, L pass) of x in [-1, 1]:
+    within 1e-5 of the FP64 32-slot apply of the same values (relative to max |y|;
+    the FP32 row keeps its O(1/dx^2) terms apart, so the error stays near FP32
+    rounding); for an input 4 bytes past a 16-byte boundary (the L pass then
+    reads slots one at a time instead of four) the same E-pass bits and y within
+    1e-6, on two consecutive calls."""
     import torch
 
     O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), two_circle_ibcs(gpu, dx))
@@ -196,12 +198,18 @@ def test_brick_staged_e_pass_equals_gather_pass_bitwise(gpu, dx):
     xm = buf[1:1 + O.D * 32].view(O.D, 32)  # 4 bytes past a 16-byte boundary
     xm.copy_(x)
     assert xm.data_ptr() % 16 == 4
-    t_new, y_new = torch.full_like(x, float("nan")), torch.empty_like(x)
-    t_old, y_old = torch.full_like(x, float("nan")), torch.empty_like(x)
+    t_a, y_a = torch.full_like(x, float("nan")), torch.empty_like(x)
+    t_m, y_m = torch.full_like(x, float("nan")), torch.empty_like(x)
+    x64 = x.double()
+    t64, y64 = torch.empty_like(x64), torch.empty_like(x64)
     torch.cuda.synchronize()
-    for _ in range(2):  # the second launch checks that the work counters were reset
-        O.apply_device(0.0, -1.0, 32, True, x.data_ptr(), t_new.data_ptr(), y_new.data_ptr())
-        O.apply_device(0.0, -1.0, 32, True, xm.data_ptr(), t_old.data_ptr(), y_old.data_ptr())
+    for _ in range(2):
+        O.apply_device(0.0, -1.0, 32, True, x.data_ptr(), t_a.data_ptr(), y_a.data_ptr())
+        O.apply_device(0.0, -1.0, 32, True, xm.data_ptr(), t_m.data_ptr(), y_m.data_ptr())
         gpu.sync()
-        assert torch.equal(t_new, t_old)
-    assert _rel_inf(y_new.cpu().double().numpy(), y_old.cpu().double().numpy()) <= 1e-6
+        assert torch.equal(t_a, t_m)
+        assert _rel_inf(y_m.cpu().double().numpy(), y_a.cpu().double().numpy()) <= 1e-6
+    O.apply_device(0.0, -1.0, 32, False, x64.data_ptr(), t64.data_ptr(), y64.data_ptr())
+    gpu.sync()
+    assert _rel_inf(y_a.cpu().double().numpy(), y64.cpu().numpy()) <= 1e-5
+    assert _rel_inf(t_a.cpu().double().numpy(), t64.cpu().numpy()) <= 1e-6
