@@ -615,6 +615,10 @@ def main():
     if os.path.exists(peaks_path):
         peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
     achieved = alg_bytes / apply_s / 1e9
+    # FP32 arithmetic of the same apply: the separable E sum is 143 flops per stencil row and RHS
+    # (per plane i: 4 x (1 mul + 3 fma) over k, 1 mul + 3 fma over j, 1 mul by wx_i, 1 add into the row
+    # sum, less the first add; fma = 2 flops), the L row 16 flops per row and RHS
+    fp32_flops = stencil_rows * KSLOTS * 143 + D * KSLOTS * 16
     traffic = None
     prof = os.path.join(ROOT, "profiles", "apply_traffic.json")
     if os.path.exists(prof):
@@ -656,6 +660,11 @@ def main():
                "ebcg": EBCG_NOTE}
 
     clocks = clk.summary()
+    # nominal FP32 peak at the SM clock seen under load: 152 SMs x 128 FP32 lanes x 2 flops per fma
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    props = torch.cuda.get_device_properties(dev)
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_achieved = fp32_flops / apply_s / 1e12
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -694,7 +703,10 @@ def main():
                     "path": f"cpm_server_submit / cpm_server_step / cpm_server_poll with host arrays, {n_e2e} requests"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "kernel": "L.E apply (E pass + IBC patch rows + L pass), FP32, 32 RHS",
-                         "apply_us": apply_s * 1e6, "alg_bytes_per_apply": alg_bytes, "peak_source": peak_src},
+                         "apply_us": apply_s * 1e6, "alg_bytes_per_apply": alg_bytes, "peak_source": peak_src,
+                         "fp32": {"achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                                  "frac": fp32_achieved / fp32_peak, "flops_per_apply": int(fp32_flops),
+                                  "peak_source": "nominal: SMs x 128 FP32 lanes x 2 flops x median SM clock under load"}},
             "cpu_baseline": cpu,
             "serving_mix": mix,
             "gpu_launches": int(launches),

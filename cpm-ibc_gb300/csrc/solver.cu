@@ -469,8 +469,9 @@ __global__ void k_epass1(OpView<T> op, const Slot *__restrict__ sl, int ph, cons
     }
 }
 
-// the patch as a pass of its own after a bulk E pass (the FP64 32-slot pass),
-// warp per patch-list row
+// the patch as a pass of its own after the bulk 32-slot E pass, warp per
+// patch-list row (consecutive rows on neighbouring warps, whose gathers share
+// cache lines)
 template <class T>
 __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x,
                                                   T *__restrict__ t) {
