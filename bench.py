@@ -287,12 +287,13 @@ def run_profile(what):
     torch.cuda.synchronize()
 
 
-def serving_mix(cg, requests, rate, seed=11):
+def serving_mix(cg, requests, rate, seed=11, concurrent=True):
     """The serving stream over the three resident surfaces (the sphere with two circles at
     dx 0.025, the torus at dx 0.01, the perturbed icosphere at dx 0.005): `requests` seeded
     Poisson arrivals at `rate` per second, one in 32 a geodesic, the rest IBC Laplace solves
-    with values U[0,1]; served by the serving loop (continuous batching, mixed precision) and,
-    on the same stream and arrival times, one request at a time by the plain FP64 path.
+    with values U[0,1]; served by the serving loop (continuous batching, mixed precision; with
+    `concurrent`, one worker thread and CUDA stream per surface) and, on the same stream and
+    arrival times, one request at a time by the plain FP64 path.
     Returns the summary (solves/s, p50/p99 latency of both)."""
     from cpm_gb300 import serving as SV
     from cpm_gb300 import workloads as W
@@ -305,9 +306,10 @@ def serving_mix(cg, requests, rate, seed=11):
     warm = SV.poisson_stream(surfaces, 12, rate=0.0, geodesic_every=0, seed=seed + 1)
     for r in warm:
         r["id"] = -1 - r["id"]
-    loop.run(warm)
+    serve = loop.run_concurrent if concurrent else loop.run
+    serve(warm)
     t = time.perf_counter()
-    out = loop.run(reqs)
+    out = serve(reqs)
     span = time.perf_counter() - t
     lat = {k: [o["latency"] for o in out.values() if o["kind"] == k] for k in ("laplace", "geodesic")}
     fb = sum(1 for o in out.values() if o["kind"] == "laplace" and o["stats"].get("fp64_fallback"))
@@ -326,6 +328,7 @@ def serving_mix(cg, requests, rate, seed=11):
         "config": {"surfaces": {s.name: {"tube_nodes": s.tube.N, "rows": s.opset.D, "curves": s.n_ibc,
                                          "server_bytes": s.bytes} for s in surfaces},
                    "requests": requests, "rate_per_s": rate, "geodesic_every": 32, "arrivals": "seeded Poisson process",
+                   "workers": "one thread and CUDA stream per surface" if concurrent else "one loop for all surfaces",
                    "slots_per_surface": 32, "tol": TOL},
         "setup_s": t_setup, "makespan_s": span, "solves_per_s": len(out) / span,
         "latency_ms": {"p50": float(np.percentile(all_lat, 50) * 1e3), "p99": float(np.percentile(all_lat, 99) * 1e3),
@@ -443,7 +446,7 @@ def run_workload(args):
                                                for c in range(3))),
         })
     else:  # serving-mix
-        line.update(serving_mix(cg, args.requests, args.rate))
+        line.update(serving_mix(cg, args.requests, args.rate, concurrent=args.serve == "concurrent"))
     print(json.dumps(line), flush=True)
 
 
@@ -467,6 +470,8 @@ def main():
     ap.add_argument("--mix-requests", type=int, default=64,
                     help="requests of the serving-stream sample in the default line (0: none)")
     ap.add_argument("--mix-rate", type=float, default=4.0, help="its mean arrivals per second")
+    ap.add_argument("--serve", choices=["concurrent", "sequential"], default="concurrent",
+                    help="serving stream: one worker thread and CUDA stream per surface, or one loop for all")
     ap.add_argument("--refine-every", type=int, default=0,
                     help="mixed precision: reliable-update period in iterations (0: the library default)")
     ap.add_argument("--inner-tol", type=float, default=0.0,
@@ -499,6 +504,7 @@ def main():
     O = cg.OpSet(T, circles(cg, DX))
     cg.sync()
     setup_s = time.perf_counter() - t0
+    tuning = O.autotune(reps=10, fp64=True)  # launch shapes of the E passes, kept with the operator
     D = O.D
     rows = O.rows()
     rng = np.random.default_rng(1000 + rank)
@@ -627,7 +633,7 @@ def main():
     # ---- the serving stream over three surfaces (bounded sample; rank 0, N = 1 only)
     mix = None
     if rank == 0 and world == 1 and args.mix_requests > 0:
-        mix = serving_mix(cg, args.mix_requests, args.mix_rate)
+        mix = serving_mix(cg, args.mix_requests, args.mix_rate, concurrent=args.serve == "concurrent")
 
     # ---- CPU baseline and the error against the oracle (rank 0, N = 1 only): whole oracle solves
     cpu, rel_err_oracle = None, None
@@ -709,6 +715,7 @@ def main():
                                   "peak_source": "nominal: SMs x 128 FP32 lanes x 2 flops x median SM clock under load"}},
             "cpu_baseline": cpu,
             "serving_mix": mix,
+            "launch_shapes": {k: (round(v, 2) if isinstance(v, float) else v) for k, v in tuning.items()},
             "gpu_launches": int(launches),
             "clocks": clocks,
             "setup_s": setup_s,

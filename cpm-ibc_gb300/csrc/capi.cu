@@ -62,11 +62,16 @@ extern "C" int cpm_device_info(char *name, int64_t name_len, int64_t *free_bytes
 }
 
 extern "C" int cpm_sync(void) {
-    CPM_CUDA_TRY(cudaStreamSynchronize(cpm::library_stream()));
+    CPM_CUDA_TRY(cudaStreamSynchronize(cpm::stream()));
     return 0;
 }
 
-extern "C" void *cpm_get_stream(void) { return (void *)cpm::library_stream(); }
+extern "C" void *cpm_get_stream(void) { return (void *)cpm::stream(); }
+
+extern "C" int cpm_set_thread_stream(void *s) {
+    cpm::g_scope = (cudaStream_t)s;
+    return 0;
+}
 
 namespace cpm {
 static std::atomic<long long> g_launches{0};

@@ -69,6 +69,9 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
     v.pe_w = pe_w;
     v.n_pl = o->n_pl;
     v.n_sp_rows = o->n_sp_rows;
+    v.e32_bps = o->e32_bps;
+    v.patch_bps = o->patch_bps;
+    v.e64_bps = o->e64_bps;
     v.sp_ptr = o->n_sp_rows ? o->sp_ptr.p : nullptr;
     v.sp_rec = o->sp_rec.p;
     v.sp_w = sp_w;

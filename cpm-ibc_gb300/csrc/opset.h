@@ -68,6 +68,9 @@ struct OpView {
     const T *sp_w;
     const int32_t *sp_rows;                   // rows with records
     int64_t n_sp_rows;
+    // launch shapes of the 32-slot E passes, blocks per SM (0: the built-in
+    // defaults; cpm_opset_autotune / cpm_opset_set_launch).  Never the arithmetic.
+    int e32_bps, patch_bps, e64_bps;
 };
 
 // the per-slot L corrections of row r, slot s (K-wide batch): a moved neighbour
@@ -540,6 +543,7 @@ struct CpOverrides;
 struct cpm_opset_s {
     cpm_tube_s *tube = nullptr;  // not owned
     int64_t N = 0, D = 0, total_ibc = 0, num2 = 0, n_ibc = 0, n_patched = 0, n_moved = 0;
+    int e32_bps = 0, patch_bps = 0, e64_bps = 0;  // E-pass launch shapes (see OpView)
     double dx = 0;
     cpm::DBuf<uint32_t> base;
     cpm::DBuf<double> w;

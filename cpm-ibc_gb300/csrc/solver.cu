@@ -518,6 +518,10 @@ static void slot_epatch(const OpView<T> &op, const Slot *sl, int ph, const T *x,
     k_slot_epatch32<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
 }
 
+// default launch shapes of the 32-slot E passes (blocks per SM caps of the
+// grid-stride loops), measured best on the sphere with two circles at dx 0.025
+constexpr int E32_BPS = 32, PATCH_BPS = 16, E64_BPS = 16;
+
 // kernels one E pass of x launches
 template <class T, int K>
 static inline int epass_kernels(const OpView<T> &op, const T *) {
@@ -530,10 +534,12 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
     static_assert(K == 1 || K == 32, "slot widths 1 and 32");
     if constexpr (K == 32) {
         if constexpr (sizeof(T) == 4) {
-            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_grp + 3) / 4, 32LL * sm_count()));
+            const int64_t bps = op.e32_bps > 0 ? op.e32_bps : E32_BPS;
+            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_grp + 3) / 4, bps * sm_count()));
             k_epass32w<<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
         } else {
-            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(op.n_grp, 16LL * sm_count()));
+            const int64_t bps = op.e64_bps > 0 ? op.e64_bps : E64_BPS;
+            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(op.n_grp, bps * sm_count()));
             k_epass32s<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
         }
     } else {
@@ -541,7 +547,8 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
         k_epass1<T><<<(unsigned)((threads + BS - 1) / BS), BS, 0, st>>>(op, sl, ph, x, t);
     }
     if (K == 32 && op.n_pl > 0) {  // the gather passes correct the IBC patch rows afterwards
-        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_pl + 3) / 4, 16LL * sm_count()));
+        const int64_t bps = op.patch_bps > 0 ? op.patch_bps : PATCH_BPS;
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_pl + 3) / 4, bps * sm_count()));
         k_epatch32<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
     }
     if (K == 32 && op.n_sp_rows > 0) slot_epatch(op, sl, ph, x, t, st);
@@ -2259,6 +2266,112 @@ extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslo
                                               : epass_kernels<double, 32>(op->view<double>(), (const double *)x_dev))
                                       : 1));
     CPM_CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+// ================================================================= launch-shape autotuner
+// Times each 32-slot E-pass kernel of one operator over candidate grid sizes
+// (blocks per SM of its grid-stride loop) on scratch vectors, keeps the
+// fastest with the operator, and reports the times.  The grid sizes change no
+// arithmetic: every row and slot is summed by the same code in the same order.
+namespace {
+__global__ void k_tune_fill(int64_t n, float *__restrict__ a, double *__restrict__ b) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float v = (float)((i * 2654435761ull) % 2001ull) * 1e-3f - 1.0f;  // deterministic values in [-1, 1]
+    if (a) a[i] = v;
+    if (b) b[i] = (double)v;
+}
+
+template <class F>
+float time_launches(cudaStream_t st, int reps, F launch) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    launch();  // warm
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < reps; ++r) launch();
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms * 1000.f / (float)reps;
+}
+}  // namespace
+
+extern "C" int cpm_opset_set_launch(cpm_opset_t op, int32_t e32_bps, int32_t patch_bps, int32_t e64_bps) {
+    if (!op || e32_bps < 0 || patch_bps < 0 || e64_bps < 0 || e32_bps > 1024 || patch_bps > 1024 || e64_bps > 1024)
+        return fail(CPM_ERR_INVALID_ARG, "opset_set_launch: null operator or blocks per SM outside 0..1024");
+    op->e32_bps = e32_bps;
+    op->patch_bps = patch_bps;
+    op->e64_bps = e64_bps;
+    return 0;
+}
+
+extern "C" int cpm_opset_autotune(cpm_opset_t op, int32_t reps, int32_t with_fp64, cpm_tune_result *out) {
+    if (!op || reps < 1 || reps > 1000) return fail(CPM_ERR_INVALID_ARG, "opset_autotune: null operator or reps outside 1..1000");
+    const int64_t D = op->D, n = D * 32;
+    cudaStream_t st = stream();
+    DBuf<float> x32, t32;
+    DBuf<double> x64, t64;
+    CPM_TRY(x32.alloc(n));
+    CPM_TRY(t32.alloc(n));
+    if (with_fp64) {
+        CPM_TRY(x64.alloc(n));
+        CPM_TRY(t64.alloc(n));
+    }
+    k_tune_fill<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x32.p, with_fp64 ? x64.p : nullptr);
+    CPM_CUDA_TRY(cudaGetLastError());
+    cpm_tune_result res;
+    memset(&res, 0, sizeof(res));
+    const int sms = sm_count();
+    const int e32c[] = {8, 16, 24, 32, 48, 64}, pc[] = {4, 8, 16, 32}, e64c[] = {4, 8, 16, 32};
+    const OpView<float> v32 = op->view<float>();
+    auto pick = [&](const int *c, int nc, int dflt, auto launch_with, float &best_us, float &dflt_us, int32_t &best) {
+        best_us = 0.f;
+        dflt_us = 0.f;
+        best = dflt;
+        for (int i = 0; i < nc; ++i) {
+            const float us = time_launches(st, reps, [&] { launch_with(c[i]); });
+            if (c[i] == dflt) dflt_us = us;
+            if (best_us == 0.f || us < best_us) {
+                best_us = us;
+                best = c[i];
+            }
+        }
+        // keep the default unless another shape is at least 2 % faster
+        if (dflt_us > 0.f && best_us > 0.98f * dflt_us) {
+            best = dflt;
+            best_us = dflt_us;
+        }
+    };
+    if (op->n_grp > 0) {
+        pick(e32c, 6, E32_BPS, [&](int bps) {
+            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((v32.n_grp + 3) / 4, (int64_t)bps * sms));
+            k_epass32w<<<(unsigned)blocks, 128, 0, st>>>(v32, nullptr, -1, x32.p, t32.p);
+        }, res.e32_us, res.e32_default_us, res.e32_blocks_per_sm);
+    }
+    if (op->n_pl > 0) {
+        pick(pc, 4, PATCH_BPS, [&](int bps) {
+            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((v32.n_pl + 3) / 4, (int64_t)bps * sms));
+            k_epatch32<float><<<(unsigned)blocks, 128, 0, st>>>(v32, nullptr, -1, x32.p, t32.p);
+        }, res.patch_us, res.patch_default_us, res.patch_blocks_per_sm);
+    }
+    if (with_fp64 && op->n_grp > 0) {
+        const OpView<double> v64 = op->view<double>();
+        pick(e64c, 4, E64_BPS, [&](int bps) {
+            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(v64.n_grp, (int64_t)bps * sms));
+            k_epass32s<double><<<(unsigned)blocks, 128, 0, st>>>(v64, nullptr, -1, x64.p, t64.p);
+        }, res.e64_us, res.e64_default_us, res.e64_blocks_per_sm);
+    }
+    CPM_CUDA_TRY(cudaGetLastError());
+    CPM_CUDA_TRY(cudaStreamSynchronize(st));
+    op->e32_bps = res.e32_blocks_per_sm;
+    op->patch_bps = res.patch_blocks_per_sm;
+    if (with_fp64) op->e64_bps = res.e64_blocks_per_sm;
+    if (out) *out = res;
     return 0;
 }
 

@@ -74,6 +74,13 @@ class TubeInfo(ctypes.Structure):
                 ("radius", ctypes.c_double), ("p", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("e32_blocks_per_sm", ctypes.c_int32), ("patch_blocks_per_sm", ctypes.c_int32),
+                ("e64_blocks_per_sm", ctypes.c_int32), ("e32_us", ctypes.c_float), ("patch_us", ctypes.c_float),
+                ("e64_us", ctypes.c_float), ("e32_default_us", ctypes.c_float), ("patch_default_us", ctypes.c_float),
+                ("e64_default_us", ctypes.c_float)]
+
+
 class SolveOpts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iters", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("precond", ctypes.c_int32), ("precond_iters", ctypes.c_int32), ("inner_tol", ctypes.c_double),
@@ -174,6 +181,9 @@ def lib():
         L.cpm_get_stream.restype = ctypes.c_void_p
         L.cpm_launch_count.restype = ctypes.c_int64
         L.cpm_sync.restype = ctypes.c_int
+        L.cpm_set_thread_stream.argtypes = [vp]
+        L.cpm_opset_autotune.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, P(TuneResult)]
+        L.cpm_opset_set_launch.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
         L.cpm_solver_create.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, P(vp)]
         L.cpm_solve.argtypes = [vp, ctypes.c_int32, vp, vp, P(SolveOpts), P(SolveStats)]
         L.cpm_solve_device.argtypes = [vp, ctypes.c_int32, vp, vp, P(SolveOpts), P(SolveStats)]
@@ -376,8 +386,20 @@ class OpSet:
         return y
 
     def apply_device(self, m, n, kslots, fp32, x_ptr, t_ptr, y_ptr):
-        """Asynchronous device apply on the library stream ([D][kslots] arrays)."""
+        """Asynchronous device apply on the calling thread's library stream ([D][kslots] arrays)."""
         _check(lib().cpm_apply_device(self.h, m, n, kslots, int(fp32), x_ptr, t_ptr, y_ptr))
+
+    def autotune(self, reps=20, fp64=False):
+        """Time the 32-slot E passes over candidate launch shapes, keep the fastest with
+        this operator (cpm_opset_autotune) and return the chosen shapes and times."""
+        r = TuneResult()
+        _check(lib().cpm_opset_autotune(self.h, int(reps), int(bool(fp64)), ctypes.byref(r)))
+        return {k: getattr(r, k) for k, _ in TuneResult._fields_}
+
+    def set_launch(self, e32_blocks_per_sm=0, patch_blocks_per_sm=0, e64_blocks_per_sm=0):
+        """Set the 32-slot E passes' launch shapes by hand (0: the defaults)."""
+        _check(lib().cpm_opset_set_launch(self.h, int(e32_blocks_per_sm), int(patch_blocks_per_sm),
+                                          int(e64_blocks_per_sm)))
 
 
 class Geodesic:
@@ -486,8 +508,14 @@ def set_device(dev):
 
 
 def stream_ptr():
-    """The library's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+    """The calling thread's library cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
     return lib().cpm_get_stream()
+
+
+def set_thread_stream(ptr):
+    """Queue this thread's library work on the cudaStream_t `ptr` (an integer, e.g.
+    torch.cuda.Stream().cuda_stream); None or 0 goes back to the library stream."""
+    _check(lib().cpm_set_thread_stream(ptr or None))
 
 
 def launch_count():

@@ -32,6 +32,7 @@ continues on a plain FP64 32-slot server.
 Latency is measured from a request's arrival to the harvest of its result.
 """
 import heapq
+import threading
 import time
 
 import numpy as np
@@ -48,9 +49,11 @@ class ServedSurface:
     """A device-resident surface: its tube, operator (with IBC curves) and, while
     admitted, its server."""
 
-    def __init__(self, name, tube, ibcs, m=0.0, n=-1.0, tol=1e-10):
+    def __init__(self, name, tube, ibcs, m=0.0, n=-1.0, tol=1e-10, autotune=True):
         self.name, self.tube = name, tube
         self.opset = OpSet(tube, ibcs)
+        # launch shapes of this surface's E passes, timed once and kept with the operator
+        self.tuning = self.opset.autotune(reps=10, fp64=True) if autotune else None
         self.rows = self.opset.rows()
         self.n_ibc = len(ibcs)
         self.m, self.n, self.tol = m, n, tol
@@ -68,6 +71,7 @@ class ServedSurface:
         self.fp64_iters = None  # running mean iterations of a solo FP64 solve
         self.mixed_iters = None  # running mean iterations of a batched mixed solve
         self._cp = None
+        self.busy = threading.Lock()  # held while a unit of this surface's work runs
 
     def break_even(self):
         """requests waiting from which a 32-slot batch beats solving them one by one
@@ -109,28 +113,36 @@ class ServingLoop:
         self.evictions = 0
         self.precision_switches = 0
         self.solo_solves = 0
+        self._lock = threading.RLock()  # admissions and counters shared by the worker threads
 
     def _held(self):
         return sum(s.bytes for s in self.surfaces.values() if s.server is not None)
 
     def _admit(self, s):
-        """Create s's server if the HBM budget allows, releasing idle servers first."""
+        """Create s's server if the HBM budget allows, releasing idle servers first
+        (a server whose surface is in the middle of a unit of work is never released)."""
         if s.server is not None:
             return True
         if s.bytes > self.budget:
             raise MemoryError(f"surface {s.name}: a server needs {s.bytes} bytes, the budget is {self.budget}")
-        if self._held() + s.bytes > self.budget:
-            for o in self.surfaces.values():
-                if o is not s and o.server is not None and not o.active and not o.waiting:
-                    o.server = None
-                    self.evictions += 1
+        with self._lock:
+            if self._held() + s.bytes > self.budget:
+                for o in self.surfaces.values():
+                    if o is s or o.server is None or o.active or o.waiting or not o.busy.acquire(blocking=False):
+                        continue
+                    try:
+                        if o.server is not None and not o.active and not o.waiting:
+                            o.server = None
+                            self.evictions += 1
+                    finally:
+                        o.busy.release()
                     if self._held() + s.bytes <= self.budget:
                         break
-        if self._held() + s.bytes > self.budget:
-            return False
-        cap = max(200, int(6 * s.fp64_iters)) if (s.precision == 1 and s.fp64_iters) else 100000
-        s.server = Server(s.opset, s.m, s.n, tol=s.tol, precision=s.precision, max_iters=cap)
-        self.admissions += 1
+            if self._held() + s.bytes > self.budget:
+                return False
+            cap = max(200, int(6 * s.fp64_iters)) if (s.precision == 1 and s.fp64_iters) else 100000
+            s.server = Server(s.opset, s.m, s.n, tol=s.tol, precision=s.precision, max_iters=cap)
+            self.admissions += 1
         return True
 
     def _solo(self, s, keep_solutions, t0, out):
@@ -143,7 +155,8 @@ class ServingLoop:
         dt = time.perf_counter() - t
         it = float(st[0]["iterations"])
         s.fp64_iters = it if s.fp64_iters is None else 0.7 * s.fp64_iters + 0.3 * it
-        self.solo_solves += 1
+        with self._lock:
+            self.solo_solves += 1
         done = time.perf_counter() - t0
         rec = dict(kind="laplace", surface=s.name, arrival=arr, completion=done, latency=done - arr,
                    stats=dict(st[0], service=dt), precision=0, mode="solo")
@@ -201,26 +214,12 @@ class ServingLoop:
                     s.waiting.append((r["id"], s.rhs(r["values"]), r["t"]))
                 else:
                     geo_wait.append(r)
-            for s in self.surfaces.values():
-                if s.switch_pending and s.server is not None and not s.active:
-                    s.server = None
-                    s.precision = 0
-                    s.switch_pending = False
-                    self.precision_switches += 1
             # candidate units of work, keyed by the arrival of their oldest request
             cands = []
             for s in self.surfaces.values():
-                if s.server is not None and s.active:
-                    cands.append((min(s.inflight_arrival.values(), default=now), 0, s.name, "step"))
-                if not s.waiting:
-                    continue
-                idle = s.server is None or not s.active
-                probing = s.precision == 1 and s.finished < PROBE and s.submitted >= PROBE
-                be = s.break_even()
-                if be is None or s.switch_pending or probing or (idle and len(s.waiting) < be):
-                    cands.append((s.waiting[0][2], 1, s.name, "solo"))
-                elif len(s.inflight_arrival) < 2 * MAX_SLOTS:
-                    cands.append((s.waiting[0][2], 1, s.name, "submit"))
+                c = self._candidate(s, now)
+                if c is not None:
+                    cands.append((c[0], c[1], s.name, c[2]))
             if geo_wait:
                 cands.append((geo_wait[0]["t"], 2, None, "geodesic"))
             if not cands:
@@ -230,39 +229,132 @@ class ServingLoop:
             _, _, name, what = min(cands)
             if what == "geodesic":
                 r = geo_wait.pop(0)
-                s = self.surfaces[r["surface"]]
-                # a surface whose Laplace solves left mixed precision runs its geodesics in FP64 too
-                prec = min(self.geodesic_precision, s.precision)
-                phi, its = Geodesic(s.tube, r["source"]).run(self.dt_scale * s.tube.dx ** 2, precision=prec, tol=s.tol)
-                done = time.perf_counter() - t0
-                rec = dict(kind="geodesic", surface=s.name, arrival=r["t"], completion=done, latency=done - r["t"],
-                           stats=dict(iterations=its))
-                if keep_solutions:
-                    rec["x"] = phi
-                out[r["id"]] = rec
+                self._geodesic(self.surfaces[r["surface"]], r, keep_solutions, t0, out)
                 continue
-            s = self.surfaces[name]
-            if what == "solo":
-                self._solo(s, keep_solutions, t0, out)
-            elif what == "step":
+            self._unit(self.surfaces[name], what, keep_solutions, t0, out)
+        return out
+
+    def _geodesic(self, s, r, keep_solutions, t0, out):
+        # a surface whose Laplace solves left mixed precision runs its geodesics in FP64 too
+        prec = min(self.geodesic_precision, s.precision)
+        phi, its = Geodesic(s.tube, r["source"]).run(self.dt_scale * s.tube.dx ** 2, precision=prec, tol=s.tol)
+        done = time.perf_counter() - t0
+        rec = dict(kind="geodesic", surface=s.name, arrival=r["t"], completion=done, latency=done - r["t"],
+                   stats=dict(iterations=its))
+        if keep_solutions:
+            rec["x"] = phi
+        out[r["id"]] = rec
+
+    def _unit(self, s, what, keep_solutions, t0, out):
+        """one unit of work of surface s: 'solo', 'step' or 'submit'"""
+        with s.busy:
+            self._unit_locked(s, what, keep_solutions, t0, out)
+
+    def _unit_locked(self, s, what, keep_solutions, t0, out):
+        if what == "solo":
+            self._solo(s, keep_solutions, t0, out)
+        elif what == "step":
+            self._step(s, keep_solutions, t0, out)
+        elif self._admit(s):
+            # at most two batches in the server, so a precision switch takes effect within two batches
+            take = max(0, min(len(s.waiting), 2 * MAX_SLOTS - len(s.inflight_arrival)))
+            if s.precision == 1 and s.finished < PROBE:
+                take = min(take, max(0, PROBE - s.submitted))
+            if s.precision == 1:
+                s.submitted += take
+            for rid, b, arr in s.waiting[:take]:
+                s.server.submit(b, rid)
+                s.inflight_arrival[rid] = arr
+            s.waiting = s.waiting[take:]
+            s.active = s.active or take > 0
+            if s.active:
                 self._step(s, keep_solutions, t0, out)
-            elif self._admit(s):
-                # at most two batches in the server, so a precision switch takes effect within two batches
-                take = max(0, min(len(s.waiting), 2 * MAX_SLOTS - len(s.inflight_arrival)))
-                if s.precision == 1 and s.finished < PROBE:
-                    take = min(take, max(0, PROBE - s.submitted))
-                if s.precision == 1:
-                    s.submitted += take
-                for rid, b, arr in s.waiting[:take]:
-                    s.server.submit(b, rid)
-                    s.inflight_arrival[rid] = arr
-                s.waiting = s.waiting[take:]
-                s.active = s.active or take > 0
-                if s.active:
-                    self._step(s, keep_solutions, t0, out)
+        else:
+            # no room on the device for this surface's server: serve the request alone
+            self._solo(s, keep_solutions, t0, out)
+
+    def _candidate(self, s, now):
+        """(arrival of its oldest request, kind) of surface s's next unit of Laplace work, or None"""
+        if s.switch_pending and s.server is not None and not s.active:
+            s.server = None
+            s.precision = 0
+            s.switch_pending = False
+            with self._lock:
+                self.precision_switches += 1
+        best = None
+        if s.server is not None and s.active:
+            best = (min(s.inflight_arrival.values(), default=now), 0, "step")
+        if s.waiting:
+            idle = s.server is None or not s.active
+            probing = s.precision == 1 and s.finished < PROBE and s.submitted >= PROBE
+            be = s.break_even()
+            if be is None or s.switch_pending or probing or (idle and len(s.waiting) < be):
+                c = (s.waiting[0][2], 1, "solo")
+            elif len(s.inflight_arrival) < 2 * MAX_SLOTS:
+                c = (s.waiting[0][2], 1, "submit")
             else:
-                # no room on the device for this surface's server: serve the request alone
-                self._solo(s, keep_solutions, t0, out)
+                c = None
+            if c is not None and (best is None or c < best):
+                best = c
+        return best
+
+    def run_concurrent(self, requests, keep_solutions=False):
+        """run() with one worker thread per surface, each queueing its surface's work
+        on a CUDA stream of its own (cpm_set_thread_stream), so the surfaces' solves
+        overlap on the device.  Within a surface: earliest arrival first, with the same
+        batching, probe and precision rules as run()."""
+        import threading
+
+        import torch
+
+        from . import set_thread_stream
+
+        order = sorted(requests, key=lambda r: r["t"])
+        by = {name: [r for r in order if r["surface"] == name] for name in self.surfaces}
+        out = {}
+        t0 = time.perf_counter()
+        errors = []
+        dev = torch.cuda.current_device()
+
+        def worker(s, reqs):
+            try:
+                torch.cuda.set_device(dev)
+                st = torch.cuda.Stream()
+                set_thread_stream(st.cuda_stream)
+                s.inflight_arrival = {}
+                geo, i = [], 0
+                want = {r["id"] for r in reqs}
+                while not want.issubset(out.keys()):
+                    now = time.perf_counter() - t0
+                    while i < len(reqs) and reqs[i]["t"] <= now:
+                        r = reqs[i]
+                        i += 1
+                        if r["kind"] == "laplace":
+                            s.waiting.append((r["id"], s.rhs(r["values"]), r["t"]))
+                        else:
+                            geo.append(r)
+                    c = self._candidate(s, now)
+                    if geo and (c is None or geo[0]["t"] < c[0]):
+                        self._geodesic(s, geo.pop(0), keep_solutions, t0, out)
+                        continue
+                    if c is None:
+                        wait = reqs[i]["t"] - (time.perf_counter() - t0) if i < len(reqs) else 0.0
+                        time.sleep(max(0.0001, min(0.002, wait)))
+                        continue
+                    self._unit(s, c[2], keep_solutions, t0, out)
+                set_thread_stream(None)
+                st.synchronize()
+            except BaseException as e:  # reported on the calling thread
+                errors.append(e)
+
+        threads = [threading.Thread(target=worker, args=(self.surfaces[name], reqs), daemon=True)
+                   for name, reqs in by.items() if reqs]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        if errors:
+            raise errors[0]
         return out
 
 

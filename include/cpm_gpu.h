@@ -247,6 +247,24 @@ int cpm_gray_scott_step(cpm_opset_t op, double dt, double F, double k, double *u
 int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslots, int32_t fp32, const void *x_dev, void *t_dev,
                      void *y_dev);
 
+/* Launch shapes of an operator's 32-slot E passes, as blocks per SM of their
+ * grid-stride loops: the FP32 bulk pass, the IBC patch pass and the FP64 bulk
+ * pass (0 keeps the built-in default).  They never change results.  No
+ * counterpart in the reference, whose E is a CPU sparse product. */
+typedef struct {
+    int32_t e32_blocks_per_sm, patch_blocks_per_sm, e64_blocks_per_sm;
+    float e32_us, patch_us, e64_us;                      /* the chosen shapes' mean launch times */
+    float e32_default_us, patch_default_us, e64_default_us; /* the defaults' */
+} cpm_tune_result;
+/* Set the shapes by hand (0: default). */
+int cpm_opset_set_launch(cpm_opset_t op, int32_t e32_blocks_per_sm, int32_t patch_blocks_per_sm, int32_t e64_blocks_per_sm);
+/* The autotuner: time each pass over candidate shapes (reps launches each, on
+ * scratch vectors it allocates and frees; the FP64 pass only when with_fp64)
+ * on the calling thread's stream, keep the fastest with the operator (the
+ * default unless another is at least 2 % faster) and report the times in
+ * *out (may be NULL).  Blocks until done. */
+int cpm_opset_autotune(cpm_opset_t op, int32_t reps, int32_t with_fp64, cpm_tune_result *out);
+
 /* Allocation-free variant of cpm_apply_device.  It has no counterpart in the
  * reference; it exists for callers that cannot allocate device memory when
  * they apply the operator: applications whose device memory is entirely owned
@@ -397,12 +415,22 @@ int cpm_server_poll(cpm_server_t s, int64_t *tag, double *x, cpm_solve_stats *st
 int cpm_server_destroy(cpm_server_t s);
 int64_t cpm_server_device_bytes(cpm_opset_t op);
 
-/* Synchronise the library stream. */
+/* Synchronise the calling thread's stream (the library stream unless
+ * cpm_set_thread_stream chose another). */
 int cpm_sync(void);
 
-/* The library's CUDA stream (a cudaStream_t), for callers that order their
- * own work or timing events with the library's. */
+/* The calling thread's CUDA stream (a cudaStream_t): the library stream unless
+ * cpm_set_thread_stream chose another.  For callers that order their own work
+ * or timing events with the library's. */
 void *cpm_get_stream(void);
+
+/* Queue the calling thread's library work (builds, applies, geodesics, the
+ * entry ordering of solver calls) on `stream`, a cudaStream_t of the current
+ * device that outlives its use here, instead of the library stream; NULL goes
+ * back to the library stream.  Threads that each set a stream of their own
+ * run their surfaces' work concurrently on the device.  No counterpart in the
+ * reference, whose calls are blocking and single-threaded. */
+int cpm_set_thread_stream(void *stream);
 
 /* Number of kernels this library has launched in this process (graph
  * launches count their kernel nodes). */

@@ -57,3 +57,66 @@ def test_sparse_stream_solves_alone_in_fp64(gpu):
         assert np.max(np.abs(rec["x"] - x64[0])) / np.max(np.abs(x64[0])) <= 1e-8
     base = SV.serve_fp64_one_at_a_time(surfaces, reqs)
     assert sorted(base) == sorted(out)
+
+
+def test_concurrent_workers_results_and_admission(gpu):
+    """run_concurrent: one worker thread and CUDA stream per surface
+    (cpm_set_thread_stream), with the same HBM budget of two servers. Every
+    result within 1e-8 of the FP64 device solve (Laplace) or the FP64 geodesic."""
+    surfaces = W.serving_surfaces(gpu, dx_scale=5.0, mesh_level=3, n_curves=2)
+    by = {s.name: s for s in surfaces}
+    sizes = sorted(s.bytes for s in surfaces)
+    loop = SV.ServingLoop(surfaces, hbm_budget=sizes[-1] + sizes[-2])
+    reqs = SV.poisson_stream(surfaces, 64, rate=400.0, geodesic_every=16, seed=6)
+    lib_stream = gpu.stream_ptr()
+    out = loop.run_concurrent(reqs, keep_solutions=True)
+    assert sorted(out) == sorted(r["id"] for r in reqs)
+    assert gpu.stream_ptr() == lib_stream  # the calling thread keeps the library stream
+    for r in reqs:
+        rec = out[r["id"]]
+        s = by[r["surface"]]
+        assert rec["latency"] >= 0
+        if r["kind"] == "laplace":
+            assert rec["stats"]["status"] == 0
+            x64, _ = gpu.Solver(s.opset, 0.0, -1.0).solve(s.rhs(r["values"]), tol=1e-12, precision=0)
+            assert np.max(np.abs(rec["x"] - x64[0])) / np.max(np.abs(x64[0])) <= 1e-8
+        else:
+            g = gpu.Geodesic(s.tube, r["source"])
+            p64, _ = g.run(s.tube.dx ** 2, precision=0)
+            assert np.max(np.abs(rec["x"] - p64)) / np.max(np.abs(p64)) <= 1e-8
+
+
+def test_thread_stream_orders_the_calling_threads_work(gpu):
+    """cpm_set_thread_stream: an apply queued from a thread on its own stream
+    gives the same bits as on the library stream; the library stream is back
+    after the thread resets it."""
+    import threading
+
+    import torch
+
+    T = gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, 0.1)
+    O = gpu.OpSet(T)
+    x = torch.rand((O.D, 32), dtype=torch.float64, device="cuda")
+    t0, y0 = torch.empty_like(x), torch.empty_like(x)
+    t1, y1 = torch.empty_like(x), torch.empty_like(x)
+    lib_stream = gpu.stream_ptr()
+    torch.cuda.synchronize()
+    O.apply_device(1.0, -1.0, 32, False, x.data_ptr(), t0.data_ptr(), y0.data_ptr())
+    gpu.sync()
+    seen = {}
+
+    def work():
+        st = torch.cuda.Stream()
+        gpu.set_thread_stream(st.cuda_stream)
+        seen["stream"] = gpu.stream_ptr()
+        seen["own"] = st.cuda_stream
+        O.apply_device(1.0, -1.0, 32, False, x.data_ptr(), t1.data_ptr(), y1.data_ptr())
+        gpu.sync()
+        gpu.set_thread_stream(None)
+        seen["after"] = gpu.stream_ptr()
+
+    th = threading.Thread(target=work)
+    th.start()
+    th.join()
+    assert seen["stream"] == seen["own"] and seen["after"] == lib_stream
+    assert torch.equal(y0, y1)
