@@ -318,41 +318,172 @@ static std::vector<double> interp_unoriented(const HostTube &ht, const QueryRows
     return out;
 }
 
-// Geometry::EigenDecompositionOfJcp on a subset (src/Geometry.cpp:27-69): Dc and E
-// restricted to the subset, J = E (Dc_c cp_r), frames of 0.5 (J + J^T).
-static std::vector<Eig3> subset_jcp(const HostTube &ht, const IBCData &ib, const QueryRows &qr) {
-    size_t ns = ib.tag_set.size();
-    std::vector<double> g(9 * ns, 0.0);
-    const double cplus = 0.5 / ht.dx, cminus = -0.5 / ht.dx;
-    for (size_t i = 0; i < ns; ++i)
-        for (int c = 0; c < 3; ++c) {
-            int np = ht.nbr(ib.tag_set[i], 2 * c), nm = ht.nbr(ib.tag_set[i], 2 * c + 1);
-            int64_t sp = np >= 0 ? ib.tag_sub[np] : -1, sm = nm >= 0 ? ib.tag_sub[nm] : -1;
-            for (int r = 0; r < 3; ++r) {
-                double s = 0.0;
-                if (sp >= 0) s += cplus * ib.tag_cpc[3 * sp + r];
-                if (sm >= 0) s += cminus * ib.tag_cpc[3 * sm + r];
-                g[9 * i + 3 * r + c] = s;
-            }
+// ---------------------------------------------------------------- IBC frames on the device
+// ComputeFrameBasedDirections (src/IBCSubset.cpp:190-268) for a tagging subset:
+// the surface normals interpolated at the IBC closest points as
+// Geometry::InterpolateUnorientedVectors + ApplyInterpolationToUnorientedVectors
+// (src/Geometry.cpp:205-266; the arithmetic of interp_unoriented above, in the
+// same order), and the frames of Geometry::EigenDecompositionOfJcp restricted to
+// the subset (src/Geometry.cpp:27-69: Dc and E on the subset, J = E (Dc_c cp_r),
+// eigen-frames of 0.5 (J + J^T)).
+
+__device__ inline double ddot3(const double *a, const double *b) {
+    double s = 0.0;
+    for (int d = 0; d < 3; ++d) s += a[d] * b[d];
+    return s;
+}
+
+// Dc_c cp_r restricted to the subset: g[9 i + 3 r + c] per tagging index i
+__global__ void k_subset_grad(BrickView bv, int64_t nt, const uint32_t *__restrict__ key, const int32_t *__restrict__ tag_set,
+                              const int32_t *__restrict__ tag_sub, const double *__restrict__ tag_cpc, double dx,
+                              double *__restrict__ g) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    const double cplus = 0.5 / dx, cminus = -0.5 / dx;
+    const uint32_t kk = key[tag_set[i]];
+    const int a[3] = {unpack_i(kk), unpack_j(kk), unpack_k(kk)};
+    for (int c = 0; c < 3; ++c) {
+        int pp[3] = {a[0], a[1], a[2]}, mm[3] = {a[0], a[1], a[2]};
+        pp[c] += 1;
+        mm[c] -= 1;
+        const int np = node_at(bv, pp[0], pp[1], pp[2]), nm = node_at(bv, mm[0], mm[1], mm[2]);
+        const int32_t sp = np >= 0 ? tag_sub[np] : -1, sm = nm >= 0 ? tag_sub[nm] : -1;
+        for (int r = 0; r < 3; ++r) {
+            double s = 0.0;
+            if (sp >= 0) s += cplus * tag_cpc[3 * (int64_t)sp + r];
+            if (sm >= 0) s += cminus * tag_cpc[3 * (int64_t)sm + r];
+            g[9 * i + 3 * r + c] = s;
         }
-    std::vector<Eig3> out(ns);
-    for (size_t i = 0; i < ns; ++i) {
-        double J[9] = {0};
-        for (int s = 0; s < 64; ++s) {
-            int col;
-            double val;
-            stencil_entry(ht, qr, (int64_t)i, s, col, val);
-            if (col < 0) continue;
-            int64_t c = ib.tag_sub[col];
-            if (c < 0) continue;
-            for (int t = 0; t < 9; ++t) J[t] += val * g[9 * c + t];
-        }
-        double A[3][3];
-        for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) A[r][c] = 0.5 * (J[3 * r + c] + J[3 * c + r]);
-        out[i] = sym_eig3(A);
     }
-    return out;
+}
+
+// per tagging index: the unoriented surface normal interpolated at its IBC
+// closest point (stencil entries in ascending column order, each signed to the
+// first), the symmetrised J = E (Dc cp) and its eigen-frame, then the direction
+// and binormal
+__global__ void k_tag_frames(BrickView bv, int64_t nt, const uint32_t *__restrict__ qbase, const double *__restrict__ qw,
+                             const int32_t *__restrict__ tag_sub, const double *__restrict__ g,
+                             const double *__restrict__ normals, const double *__restrict__ tag_cpdiff,
+                             double *__restrict__ tag_dir, double *__restrict__ tag_binormal) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    const uint32_t b = qbase[i];
+    const int bi = unpack_i(b), bj = unpack_j(b), bk = unpack_k(b);
+    const double *w = qw + 12 * i;
+    // the stencil's bricks in rank order: nodes ascend with the rank, then with l
+    int rk[8], bx[8], by[8], bz[8], nbk = 0;
+    const int X0 = bi >> 2, Y0 = bj >> 2, Z0 = bk >> 2;
+    const int nx = ((bi + 3) >> 2) - X0 + 1, ny = ((bj + 3) >> 2) - Y0 + 1, nz = ((bk + 3) >> 2) - Z0 + 1;
+    for (int ox = 0; ox < nx; ++ox)
+        for (int oy = 0; oy < ny; ++oy)
+            for (int oz = 0; oz < nz; ++oz) {
+                const int X = X0 + ox, Y = Y0 + oy, Z = Z0 + oz;
+                if (X >= bv.NB || Y >= bv.NB || Z >= bv.NB) continue;
+                const int r = bv.bmap[((size_t)X * bv.NB + Y) * bv.NB + Z];
+                if (r < 0) continue;
+                int p = nbk++;
+                while (p > 0 && rk[p - 1] > r) {
+                    rk[p] = rk[p - 1];
+                    bx[p] = bx[p - 1];
+                    by[p] = by[p - 1];
+                    bz[p] = bz[p - 1];
+                    --p;
+                }
+                rk[p] = r;
+                bx[p] = X;
+                by[p] = Y;
+                bz[p] = Z;
+            }
+    double first[3] = {0, 0, 0}, acc[3] = {0, 0, 0};
+    bool have = false;
+    for (int e = 0; e < nbk; ++e) {
+        const uint64_t m = bv.bmask[rk[e]];
+        const int st = bv.bstart[rk[e]];
+        for (int l = 0; l < 64; ++l) {
+            if (!((m >> l) & 1ull)) continue;
+            const int si = 4 * bx[e] + (l >> 4) - bi, sj = 4 * by[e] + ((l >> 2) & 3) - bj, sk = 4 * bz[e] + (l & 3) - bk;
+            if (si < 0 || si > 3 || sj < 0 || sj > 3 || sk < 0 || sk > 3) continue;
+            const int col = st + __popcll(m & ((1ull << l) - 1ull));
+            const double val = w[8 + sk] * w[4 + sj] * w[si];
+            const double *v = normals + 3 * (int64_t)col;
+            if (!have) {
+                for (int k = 0; k < 3; ++k) first[k] = v[k];
+                have = true;
+            }
+            const bool plus = ddot3(first, v) > 0.0;
+            for (int k = 0; k < 3; ++k) acc[k] = plus ? acc[k] + val * v[k] : acc[k] - val * v[k];
+        }
+    }
+    double n[3];
+    const double nn = sqrt(ddot3(acc, acc));
+    for (int k = 0; k < 3; ++k) n[k] = (nn > 0.0) ? acc[k] / nn : 0.0;
+    // J over the stencil in s order, restricted to the subset
+    double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int s = 0; s < 64; ++s) {
+        const int si = s >> 4, sj = (s >> 2) & 3, sk = s & 3;
+        const int col = node_at(bv, bi + si, bj + sj, bk + sk);
+        if (col < 0) continue;
+        const int32_t c = tag_sub[col];
+        if (c < 0) continue;
+        const double val = w[8 + sk] * w[4 + sj] * w[si];
+        for (int t = 0; t < 9; ++t) J[t] += val * g[9 * (int64_t)c + t];
+    }
+    double A[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) A[r][c] = 0.5 * (J[3 * r + c] + J[3 * c + r]);
+    const Eig3 eg = sym_eig3(A);
+    const double *cd = tag_cpdiff + 3 * i;
+    double *dir = tag_dir + 3 * i, *bn = tag_binormal + 3 * i;
+    if (fabs(eg.val[2]) < 1e-8) {
+        const double dn = ddot3(n, cd);
+        for (int k = 0; k < 3; ++k) {
+            dir[k] = cd[k] - dn * n[k];
+            bn[k] = 0.0;
+        }
+    } else {
+        const double tg[3] = {eg.vec[0][2], eg.vec[1][2], eg.vec[2][2]};
+        const double bb[3] = {tg[1] * n[2] - tg[2] * n[1], tg[2] * n[0] - tg[0] * n[2], tg[0] * n[1] - tg[1] * n[0]};
+        const double bc = ddot3(bb, cd);
+        for (int k = 0; k < 3; ++k) {
+            bn[k] = bb[k];
+            dir[k] = bc * bb[k];
+        }
+    }
+}
+
+// the frame directions of an IBC's tagging subset, computed on the device from
+// the tube's unoriented normals (3 N, device)
+static int tag_frames_dev(cpm_tube_s *t, IBCData &ib, const double *normals_dev) {
+    const int64_t nt = (int64_t)ib.tag_set.size();
+    ib.tag_dir.assign(3 * nt, 0.0);
+    ib.tag_binormal.assign(3 * nt, 0.0);
+    if (nt == 0) return 0;
+    std::vector<int32_t> set(ib.tag_set.begin(), ib.tag_set.end()), sub(ib.tag_sub.begin(), ib.tag_sub.end());
+    DBuf<int32_t> dset, dsub, derr;
+    DBuf<double> dcpc, dcd, dg, ddir, dbn, dw;
+    DBuf<uint32_t> db;
+    CPM_TRY(dset.upload(set));
+    CPM_TRY(dsub.upload(sub));
+    CPM_TRY(dcpc.upload(ib.tag_cpc));
+    CPM_TRY(dcd.upload(ib.tag_cpdiff));
+    CPM_TRY(db.alloc(nt));
+    CPM_TRY(dw.alloc(12 * nt));
+    CPM_TRY(derr.alloc(1));
+    CPM_TRY(derr.zero());
+    CPM_TRY(interp_weights_dev(t, nt, dcpc.p, db.p, dw.p, derr.p));
+    std::vector<int32_t> he;
+    CPM_TRY(derr.download(he, 1));
+    if (he[0]) return fail(CPM_ERR_BASEPOINT_OUTSIDE_TUBE, "Tube::ComputeBasePoints - Interpolation base point is not within the tube");
+    CPM_TRY(dg.alloc(9 * nt));
+    CPM_TRY(ddir.alloc(3 * nt));
+    CPM_TRY(dbn.alloc(3 * nt));
+    const unsigned nb = (unsigned)((nt + 127) / 128);
+    k_subset_grad<<<nb, 128, 0, stream()>>>(t->view(), nt, t->key.p, dset.p, dsub.p, dcpc.p, t->g.dx, dg.p);
+    k_tag_frames<<<nb, 128, 0, stream()>>>(t->view(), nt, db.p, dw.p, dsub.p, dg.p, normals_dev, dcd.p, ddir.p, dbn.p);
+    CPM_CUDA_TRY(cudaGetLastError());
+    CPM_TRY(ddir.download(ib.tag_dir, 3 * nt));
+    CPM_TRY(dbn.download(ib.tag_binormal, 3 * nt));
+    return 0;
 }
 
 // Geometry::UnorientedSurfaceNormals (src/Geometry.cpp:101-126) with its defaults
@@ -472,7 +603,7 @@ struct CpOverrides {
     CpTable surface;           // the tube surface's closest points at the cp-bar projections
 };
 
-static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_desc &desc, const std::vector<double> &normals,
+static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_desc &desc, const double *normals_dev,
                           const DBuf<double> &xdev, const CpTable *cpt, const CpTable *surf_cpt,
                           IBCData &ib) {
     const int64_t N = ht.N;
@@ -593,28 +724,8 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
         ib.tag_dir = ib.tag_cpdiff;
         ib.tag_binormal.assign(3 * nt, 0.0);
     } else {
-    // ComputeFrameBasedDirections (src/IBCSubset.cpp:190-268)
-    QueryRows qc;
-    CPM_TRY(query_weights(t, ib.tag_cpc, qc));
-    std::vector<double> nrm = interp_unoriented(ht, qc, normals, nullptr);
-    std::vector<Eig3> eig = subset_jcp(ht, ib, qc);
-    ib.tag_dir.assign(3 * nt, 0.0);
-    ib.tag_binormal.assign(3 * nt, 0.0);
-    for (size_t i = 0; i < nt; ++i) {
-        const double *n = &nrm[3 * i], *cd = &ib.tag_cpdiff[3 * i];
-        if (std::fabs(eig[i].val[2]) < 1e-8) {
-            double dn = hdot(n, cd);
-            for (int k = 0; k < 3; ++k) ib.tag_dir[3 * i + k] = cd[k] - dn * n[k];
-        } else {
-            double tg[3] = {eig[i].vec[0][2], eig[i].vec[1][2], eig[i].vec[2][2]};
-            double b[3] = {tg[1] * n[2] - tg[2] * n[1], tg[2] * n[0] - tg[0] * n[2], tg[0] * n[1] - tg[1] * n[0]};
-            double bc = hdot(b, cd);
-            for (int k = 0; k < 3; ++k) {
-                ib.tag_binormal[3 * i + k] = b[k];
-                ib.tag_dir[3 * i + k] = bc * b[k];
-            }
-        }
-    }
+        // ComputeFrameBasedDirections (src/IBCSubset.cpp:190-268), on the device
+        CPM_TRY(tag_frames_dev(t, ib, normals_dev));
     }
     // IBCDOFSubset::ComputeDOFSubset (src/IBCDOFSubset.cpp:10-93)
     const double rad = desc.dof_radius_scale * r;
@@ -735,6 +846,91 @@ static inline bool tagged(const IBCData &ib, const double *dir_r, int col, doubl
     return flip * hdot(dir_r, &ib.tag_dir[3 * sp]) < 0.0;
 }
 
+// ---------------------------------------------------------------- TagStencils on the device
+// One IBC's tagging as the device kernels read it.
+struct IbcTagDev {
+    const int32_t *tag_sub;  // N: tagging index or -1
+    const uint8_t *tag_bdy;  // per tagging index: 0, or 1 / 2 at an open polyline's end points
+    const double *tag_dir;   // 3 per tagging index
+    const int32_t *dof_sub;  // N: DOF index or -1
+    int64_t col_start;
+};
+
+// tagged() on the device: the same products and sums, in the same order
+__device__ inline bool tagged_dev(const IbcTagDev &ib, const double *dir_r, int col, double flip) {
+    const int32_t sp = ib.tag_sub[col];
+    if (sp < 0 || ib.tag_bdy[sp] != 0) return false;
+    const double *d = ib.tag_dir + 3 * (int64_t)sp;
+    double s = 0.0;
+    for (int k = 0; k < 3; ++k) s += dir_r[k] * d[k];
+    return flip * s < 0.0;
+}
+
+// the one IBC column a tube row's entry (column col) moves to, -1 for none, -2
+// when it would move to two IBCs (MoveToIBCColumns, src/IBCMatrixManipulations.cpp:189-216)
+__device__ inline int64_t tube_entry_target(const IbcTagDev *ibs, int n_ibc, int64_t q, int col) {
+    int hits = 0;
+    int64_t tgt = -1;
+    for (int c = 0; c < n_ibc; ++c) {
+        const int32_t tq = ibs[c].tag_sub[q];
+        if (tq < 0 || col < 0) continue;
+        if (tagged_dev(ibs[c], ibs[c].tag_dir + 3 * (int64_t)tq, col, 1.0) && ibs[c].dof_sub[col] >= 0) {
+            ++hits;
+            tgt = ibs[c].col_start + ibs[c].dof_sub[col];
+        }
+    }
+    return hits > 1 ? -2 : (hits == 1 ? tgt : -1);
+}
+
+// tube row q's moved E stencil entries (bit s = 16 i + 4 j + k) and L neighbours
+// (bit d, order +x -x +y -y +z -z); with moved != null also their target
+// columns, E entries in s order then L entries in d order, from moved[off[q]]
+__global__ void k_tube_moves(BrickView bv, int64_t N, const uint32_t *__restrict__ key, const uint32_t *__restrict__ base,
+                             const IbcTagDev *__restrict__ ibs, int n_ibc, uint64_t *__restrict__ emask,
+                             uint8_t *__restrict__ lmask, int32_t *__restrict__ count, const int32_t *__restrict__ off,
+                             int32_t *__restrict__ moved, int *__restrict__ err) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    bool any = false;
+    for (int c = 0; c < n_ibc && !any; ++c) any = ibs[c].tag_sub[q] >= 0;
+    uint64_t em = 0;
+    uint8_t lm = 0;
+    int cnt = 0;
+    int32_t *out = moved ? moved + off[q] : nullptr;
+    if (any) {
+        const uint32_t b = base[q];
+        const int bi = unpack_i(b), bj = unpack_j(b), bk = unpack_k(b);
+        for (int s = 0; s < 64; ++s) {
+            const int col = node_at(bv, bi + (s >> 4), bj + ((s >> 2) & 3), bk + (s & 3));
+            const int64_t tgt = tube_entry_target(ibs, n_ibc, q, col);
+            if (tgt == -2) atomicOr(err, 1);
+            if (tgt >= 0) {
+                em |= 1ull << s;
+                if (out) out[cnt] = (int32_t)tgt;
+                ++cnt;
+            }
+        }
+        const uint32_t kk = key[q];
+        const int i = unpack_i(kk), j = unpack_j(kk), k = unpack_k(kk);
+        for (int d = 0; d < 6; ++d) {
+            const int col = node_at(bv, i + (d == 0) - (d == 1), j + (d == 2) - (d == 3), k + (d == 4) - (d == 5));
+            if (col < 0) continue;
+            const int64_t tgt = tube_entry_target(ibs, n_ibc, q, col);
+            if (tgt == -2) atomicOr(err, 1);
+            if (tgt >= 0) {
+                lm |= (uint8_t)(1u << d);
+                if (out) out[cnt] = (int32_t)tgt;
+                ++cnt;
+            }
+        }
+    }
+    if (!moved) {
+        emask[q] = em;
+        lmask[q] = lm;
+        count[q] = cnt;
+    }
+}
+
 static int build_base(cpm_opset_s *o) {
     cpm_tube_s *t = o->tube;
     o->N = t->N;
@@ -819,14 +1015,18 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
         CPM_TRY(tube_normals(o, normals));
         CPM_TRY(o->normals.upload(normals));
     }
-    if (need_xn) normals_x = unoriented_normals(ht);
+    DBuf<double> dnx;
+    if (need_xn) {
+        normals_x = unoriented_normals(ht);
+        CPM_TRY(dnx.upload(normals_x));
+    }
     DBuf<double> xdev;
     CPM_TRY(xdev.alloc(3 * N));
     k_node_coords<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, t->key.p, t->g.xstart, t->g.dx, xdev.p);
     CPM_CUDA_TRY(cudaGetLastError());
     std::vector<IBCData> ibs(n_ibc);
     for (int c = 0; c < n_ibc; ++c)
-        CPM_TRY(build_ibc_data(t, ht, descs[c], descs[c].use_Jcp_surface_normals ? normals : normals_x, xdev,
+        CPM_TRY(build_ibc_data(t, ht, descs[c], descs[c].use_Jcp_surface_normals ? o->normals.p : dnx.p, xdev,
                                ovr ? &ovr->ibc[c] : nullptr, ovr ? &ovr->surface : nullptr, ibs[c]));
     o->ibc_desc.assign(descs, descs + n_ibc);
     o->ibc_verts.assign(n_ibc, {});
@@ -900,68 +1100,73 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
         for (int k = 0; k < 3; ++k) point[3 * q + k] = ht.cp[3 * q + k];
     }
 
-    // ---- tube rows: moved E / L columns (MoveToIBCColumns, src/IBCMatrixManipulations.cpp:189-216)
+    // ---- tube rows: moved E / L columns (MoveToIBCColumns, src/IBCMatrixManipulations.cpp:189-216),
+    // on the device (k_tube_moves): masks and counts, then the targets at scanned offsets
     int64_t nmoved = 0;
-    for (int64_t q = 0; q < N; ++q) {
-        uint64_t emask = 0;
-        uint8_t lmask = 0;
-        std::vector<int32_t> etarget, ltarget;
-        bool any = false;
-        for (int c = 0; c < n_ibc && !any; ++c)
-            if (ibs[c].tag_sub[q] >= 0) any = true;
-        if (!any) continue;
-        // E row of q: stencil at cp(q) in s order
-        for (int s = 0; s < 64; ++s) {
-            int i = s >> 4, j = (s >> 2) & 3, k = s & 3;
-            int col = ht.node(unpack_i(base[q]) + i, unpack_j(base[q]) + j, unpack_k(base[q]) + k);
-            int hits = 0;
-            int64_t tgt = -1;
-            for (int c = 0; c < n_ibc; ++c) {
-                int64_t tq = ibs[c].tag_sub[q];
-                if (tq < 0 || col < 0) continue;
-                if (tagged(ibs[c], &ibs[c].tag_dir[3 * tq], col, 1.0) && ibs[c].dof_sub[col] >= 0) {
-                    ++hits;
-                    tgt = o->col_start[c] + ibs[c].dof_sub[col];
-                }
-            }
-            if (hits > 1) return fail(CPM_ERR_UNSUPPORTED, "IBCs too close together: a stencil entry moves to two IBCs");
-            if (hits == 1) {
-                emask |= 1ull << s;
-                etarget.push_back((int32_t)tgt);
-            }
+    if (n_ibc > 0) {
+        std::vector<DBuf<int32_t>> d_tag_sub(n_ibc), d_dof_sub(n_ibc);
+        std::vector<DBuf<uint8_t>> d_tag_bdy(n_ibc);
+        std::vector<DBuf<double>> d_tag_dir(n_ibc);
+        std::vector<IbcTagDev> hib(n_ibc);
+        for (int c = 0; c < n_ibc; ++c) {
+            const IBCData &ib = ibs[c];
+            std::vector<int32_t> ts(ib.tag_sub.begin(), ib.tag_sub.end()), ds(ib.dof_sub.begin(), ib.dof_sub.end());
+            CPM_TRY(d_tag_sub[c].upload(ts));
+            CPM_TRY(d_dof_sub[c].upload(ds));
+            std::vector<uint8_t> tb = ib.tag_bdy;
+            std::vector<double> td = ib.tag_dir;
+            if (tb.empty()) tb.push_back(0);
+            if (td.empty()) td.assign(3, 0.0);
+            CPM_TRY(d_tag_bdy[c].upload(tb));
+            CPM_TRY(d_tag_dir[c].upload(td));
+            hib[c] = IbcTagDev{d_tag_sub[c].p, d_tag_bdy[c].p, d_tag_dir[c].p, d_dof_sub[c].p, o->col_start[c]};
         }
-        for (int d = 0; d < 6; ++d) {
-            int col = ht.nbr(q, d);
-            if (col < 0) continue;
-            int hits = 0;
-            int64_t tgt = -1;
-            for (int c = 0; c < n_ibc; ++c) {
-                int64_t tq = ibs[c].tag_sub[q];
-                if (tq < 0) continue;
-                if (tagged(ibs[c], &ibs[c].tag_dir[3 * tq], col, 1.0) && ibs[c].dof_sub[col] >= 0) {
-                    ++hits;
-                    tgt = o->col_start[c] + ibs[c].dof_sub[col];
-                }
-            }
-            if (hits > 1) return fail(CPM_ERR_UNSUPPORTED, "IBCs too close together: a stencil entry moves to two IBCs");
-            if (hits == 1) {
-                lmask |= (uint8_t)(1u << d);
-                ltarget.push_back((int32_t)tgt);
-            }
+        DBuf<IbcTagDev> d_ibs;
+        CPM_TRY(d_ibs.upload(hib));
+        DBuf<uint64_t> d_em;
+        DBuf<uint8_t> d_lm;
+        DBuf<int32_t> d_cnt, d_off, d_moved;
+        DBuf<int> d_err;
+        CPM_TRY(d_em.alloc(N));
+        CPM_TRY(d_lm.alloc(N));
+        CPM_TRY(d_cnt.alloc(N));
+        CPM_TRY(d_err.alloc(1));
+        CPM_TRY(d_err.zero());
+        const unsigned nb = (unsigned)((N + 127) / 128);
+        k_tube_moves<<<nb, 128, 0, stream()>>>(t->view(), N, t->key.p, t->base.p, d_ibs.p, n_ibc, d_em.p, d_lm.p, d_cnt.p,
+                                               nullptr, nullptr, d_err.p);
+        CPM_CUDA_TRY(cudaGetLastError());
+        std::vector<uint64_t> em;
+        std::vector<uint8_t> lm;
+        std::vector<int32_t> cnt, he;
+        CPM_TRY(d_err.download(he, 1));
+        if (he[0]) return fail(CPM_ERR_UNSUPPORTED, "IBCs too close together: a stencil entry moves to two IBCs");
+        CPM_TRY(d_em.download(em, N));
+        CPM_TRY(d_lm.download(lm, N));
+        CPM_TRY(d_cnt.download(cnt, N));
+        std::vector<int32_t> off(N);
+        for (int64_t q = 0; q < N; ++q) {
+            off[q] = (int32_t)nmoved;
+            nmoved += cnt[q];
+            if (!em[q] && !lm[q]) continue;
+            patch[q] = (int32_t)p_emask.size();
+            p_emask.push_back(em[q]);
+            p_lmask.push_back(lm[q]);
+            p_eoff.push_back(off[q]);
+            p_loff.push_back(off[q] + __builtin_popcountll(em[q]));
+            p_xcol.push_back(0);
+            p_xval.push_back(0.0);
+            if (em[q]) flags[q] |= F_EMOVE;
+            if (lm[q]) flags[q] |= F_LMOVE;
         }
-        if (!emask && !lmask) continue;
-        patch[q] = (int32_t)p_emask.size();
-        p_emask.push_back(emask);
-        p_lmask.push_back(lmask);
-        p_eoff.push_back((int32_t)moved.size());
-        moved.insert(moved.end(), etarget.begin(), etarget.end());
-        p_loff.push_back((int32_t)moved.size());
-        moved.insert(moved.end(), ltarget.begin(), ltarget.end());
-        p_xcol.push_back(0);
-        p_xval.push_back(0.0);
-        if (emask) flags[q] |= F_EMOVE;
-        if (lmask) flags[q] |= F_LMOVE;
-        nmoved += (int64_t)etarget.size() + (int64_t)ltarget.size();
+        if (nmoved > 0) {
+            CPM_TRY(d_off.upload(off));
+            CPM_TRY(d_moved.alloc(nmoved));
+            k_tube_moves<<<nb, 128, 0, stream()>>>(t->view(), N, t->key.p, t->base.p, d_ibs.p, n_ibc, nullptr, nullptr,
+                                                   nullptr, d_off.p, d_moved.p, d_err.p);
+            CPM_CUDA_TRY(cudaGetLastError());
+            CPM_TRY(d_moved.download(moved, nmoved));
+        }
     }
     const int64_t n_tube_patched = (int64_t)p_emask.size();
 
@@ -1390,7 +1595,7 @@ static int build_point_batch(cpm_opset_s *o, int n_src, const double *sources, P
         pd.on_ibc_tolerance = 0.1 * t->g.dx * t->g.dx;
         pd.dof_radius_scale = 1.0;
         IBCData ib;
-        CPM_TRY(build_ibc_data(t, ht, pd, normals, xdev, nullptr, nullptr, ib));
+        CPM_TRY(build_ibc_data(t, ht, pd, o->normals.p, xdev, nullptr, nullptr, ib));
         M = std::max<int64_t>(M, (int64_t)ib.dof_set.size());
         // MoveToIBCColumns for this slot's IBC alone (one IBC: a stencil entry moves at most once)
         for (size_t i = 0; i < ib.tag_set.size(); ++i) {
@@ -1680,13 +1885,21 @@ extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp
     bool need_normals = false, need_xn = false;
     for (int c = 0; c < n_ibc; ++c)
         if (!op->ibc_desc[c].use_cp_diff_directions) (op->ibc_desc[c].use_Jcp_surface_normals ? need_normals : need_xn) = true;
+    DBuf<double> dn, dnx;
+    const double *normals_dev = op->normals.p;
     if (need_normals) {
-        if (op->normals.n >= (size_t)(3 * N))
+        if (op->normals.n >= (size_t)(3 * N)) {
             CPM_TRY(op->normals.download(normals, 3 * N));
-        else
+        } else {
             CPM_TRY(tube_normals(op, normals));
+            CPM_TRY(dn.upload(normals));
+            normals_dev = dn.p;
+        }
     }
-    if (need_xn) normals_x = unoriented_normals(ht);
+    if (need_xn) {
+        normals_x = unoriented_normals(ht);
+        CPM_TRY(dnx.upload(normals_x));
+    }
     DBuf<double> xdev;
     CPM_TRY(xdev.alloc(3 * N));
     k_node_coords<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, t->key.p, t->g.xstart, t->g.dx, xdev.p);
@@ -1694,7 +1907,7 @@ extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp
     std::vector<IBCData> ibs(n_ibc);
     const CpOverrides *ovr = op->cp_ovr.get();
     for (int c = 0; c < n_ibc; ++c)
-        CPM_TRY(build_ibc_data(t, ht, op->ibc_desc[c], op->ibc_desc[c].use_Jcp_surface_normals ? normals : normals_x, xdev,
+        CPM_TRY(build_ibc_data(t, ht, op->ibc_desc[c], op->ibc_desc[c].use_Jcp_surface_normals ? normals_dev : dnx.p, xdev,
                                ovr ? &ovr->ibc[c] : nullptr, ovr ? &ovr->surface : nullptr, ibs[c]));
     std::vector<double> hx(xp, xp + 3 * n);
     DBuf<double> dxp;
