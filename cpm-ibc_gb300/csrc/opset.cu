@@ -931,6 +931,50 @@ __global__ void k_tube_moves(BrickView bv, int64_t N, const uint32_t *__restrict
     }
 }
 
+// an IBC's DOF rows (AddExtensionIBCRows, src/IBCMatrixManipulations.cpp:118-186;
+// AddFiniteDifferenceIBCRows, :219-251): per DOF i, the E_ibc stencil entries
+// (at dbase[i], in s order) tagged against the DOF's direction with flip -1 that
+// move to a DOF column, and the six L columns (-1: dropped): across the curve
+// the tube node itself, same side and in the DOF subset that DOF's column.
+// With moved != null the E targets from moved[off[i]] instead.
+__global__ void k_dof_moves(BrickView bv, int64_t nd, const uint32_t *__restrict__ key, const int32_t *__restrict__ dof_set,
+                            const uint32_t *__restrict__ dbase, const double *__restrict__ dof_dir, IbcTagDev ib,
+                            uint64_t *__restrict__ emask, int32_t *__restrict__ count, int32_t *__restrict__ lcols,
+                            const int32_t *__restrict__ off, int32_t *__restrict__ moved) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nd) return;
+    const uint32_t b = dbase[i];
+    const int bi = unpack_i(b), bj = unpack_j(b), bk = unpack_k(b);
+    uint64_t em = 0;
+    int cnt = 0;
+    for (int s = 0; s < 64; ++s) {
+        const int col = node_at(bv, bi + (s >> 4), bj + ((s >> 2) & 3), bk + (s & 3));
+        if (col >= 0 && tagged_dev(ib, dof_dir + 3 * i, col, -1.0) && ib.dof_sub[col] >= 0) {
+            em |= 1ull << s;
+            if (moved) moved[off[i] + cnt] = (int32_t)(ib.col_start + ib.dof_sub[col]);
+            ++cnt;
+        }
+    }
+    if (moved) return;
+    emask[i] = em;
+    count[i] = cnt;
+    const int node = dof_set[i];
+    const uint32_t kk = key[node];
+    const int x = unpack_i(kk), y = unpack_j(kk), z = unpack_k(kk);
+    const int32_t tq = ib.tag_sub[node];
+    for (int d = 0; d < 6; ++d) {
+        const int col = node_at(bv, x + (d == 0) - (d == 1), y + (d == 2) - (d == 3), z + (d == 4) - (d == 5));
+        int32_t lc = -1;
+        if (col >= 0) {
+            if (tq >= 0 && tagged_dev(ib, ib.tag_dir + 3 * (int64_t)tq, col, 1.0))
+                lc = col;
+            else if (ib.dof_sub[col] >= 0)
+                lc = (int32_t)(ib.col_start + ib.dof_sub[col]);
+        }
+        lcols[6 * i + d] = lc;
+    }
+}
+
 static int build_base(cpm_opset_s *o) {
     cpm_tube_s *t = o->tube;
     o->N = t->N;
@@ -1103,24 +1147,25 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
     // ---- tube rows: moved E / L columns (MoveToIBCColumns, src/IBCMatrixManipulations.cpp:189-216),
     // on the device (k_tube_moves): masks and counts, then the targets at scanned offsets
     int64_t nmoved = 0;
+    // every IBC's tagging on the device, for the TagStencils kernels
+    std::vector<DBuf<int32_t>> d_tag_sub(n_ibc), d_dof_sub(n_ibc);
+    std::vector<DBuf<uint8_t>> d_tag_bdy(n_ibc);
+    std::vector<DBuf<double>> d_tag_dir(n_ibc);
+    std::vector<IbcTagDev> hib(n_ibc);
+    for (int c = 0; c < n_ibc; ++c) {
+        const IBCData &ib = ibs[c];
+        std::vector<int32_t> ts(ib.tag_sub.begin(), ib.tag_sub.end()), ds(ib.dof_sub.begin(), ib.dof_sub.end());
+        CPM_TRY(d_tag_sub[c].upload(ts));
+        CPM_TRY(d_dof_sub[c].upload(ds));
+        std::vector<uint8_t> tb = ib.tag_bdy;
+        std::vector<double> td = ib.tag_dir;
+        if (tb.empty()) tb.push_back(0);
+        if (td.empty()) td.assign(3, 0.0);
+        CPM_TRY(d_tag_bdy[c].upload(tb));
+        CPM_TRY(d_tag_dir[c].upload(td));
+        hib[c] = IbcTagDev{d_tag_sub[c].p, d_tag_bdy[c].p, d_tag_dir[c].p, d_dof_sub[c].p, o->col_start[c]};
+    }
     if (n_ibc > 0) {
-        std::vector<DBuf<int32_t>> d_tag_sub(n_ibc), d_dof_sub(n_ibc);
-        std::vector<DBuf<uint8_t>> d_tag_bdy(n_ibc);
-        std::vector<DBuf<double>> d_tag_dir(n_ibc);
-        std::vector<IbcTagDev> hib(n_ibc);
-        for (int c = 0; c < n_ibc; ++c) {
-            const IBCData &ib = ibs[c];
-            std::vector<int32_t> ts(ib.tag_sub.begin(), ib.tag_sub.end()), ds(ib.dof_sub.begin(), ib.dof_sub.end());
-            CPM_TRY(d_tag_sub[c].upload(ts));
-            CPM_TRY(d_dof_sub[c].upload(ds));
-            std::vector<uint8_t> tb = ib.tag_bdy;
-            std::vector<double> td = ib.tag_dir;
-            if (tb.empty()) tb.push_back(0);
-            if (td.empty()) td.assign(3, 0.0);
-            CPM_TRY(d_tag_bdy[c].upload(tb));
-            CPM_TRY(d_tag_dir[c].upload(td));
-            hib[c] = IbcTagDev{d_tag_sub[c].p, d_tag_bdy[c].p, d_tag_dir[c].p, d_dof_sub[c].p, o->col_start[c]};
-        }
         DBuf<IbcTagDev> d_ibs;
         CPM_TRY(d_ibs.upload(hib));
         DBuf<uint64_t> d_em;
@@ -1175,9 +1220,46 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
     for (int c = 0; c < n_ibc; ++c) {
         const IBCData &ib = ibs[c];
         const int64_t nd = (int64_t)ib.dof_set.size();
+        // the DOF rows' moved E entries and L columns, on the device (k_dof_moves)
+        std::vector<uint64_t> dem;
+        std::vector<int32_t> dcnt, dlc, dmoved;
+        if (nd > 0) {
+            std::vector<int32_t> dset(ib.dof_set.begin(), ib.dof_set.end());
+            DBuf<int32_t> d_set, d_cnt, d_lc, d_off, d_mv;
+            DBuf<uint32_t> d_base;
+            DBuf<double> d_dir;
+            DBuf<uint64_t> d_em;
+            CPM_TRY(d_set.upload(dset));
+            CPM_TRY(d_base.upload(ib.dof_rows.base));
+            CPM_TRY(d_dir.upload(ib.dof_dir));
+            CPM_TRY(d_em.alloc(nd));
+            CPM_TRY(d_cnt.alloc(nd));
+            CPM_TRY(d_lc.alloc(6 * nd));
+            const unsigned nb = (unsigned)((nd + 127) / 128);
+            k_dof_moves<<<nb, 128, 0, stream()>>>(t->view(), nd, t->key.p, d_set.p, d_base.p, d_dir.p, hib[c], d_em.p, d_cnt.p,
+                                                  d_lc.p, nullptr, nullptr);
+            CPM_CUDA_TRY(cudaGetLastError());
+            CPM_TRY(d_em.download(dem, nd));
+            CPM_TRY(d_cnt.download(dcnt, nd));
+            CPM_TRY(d_lc.download(dlc, 6 * nd));
+            std::vector<int32_t> doff(nd);
+            int64_t tot = 0;
+            for (int64_t i = 0; i < nd; ++i) {
+                doff[i] = (int32_t)tot;
+                tot += dcnt[i];
+            }
+            if (tot > 0) {
+                CPM_TRY(d_off.upload(doff));
+                CPM_TRY(d_mv.alloc(tot));
+                k_dof_moves<<<nb, 128, 0, stream()>>>(t->view(), nd, t->key.p, d_set.p, d_base.p, d_dir.p, hib[c], nullptr,
+                                                      nullptr, nullptr, d_off.p, d_mv.p);
+                CPM_CUDA_TRY(cudaGetLastError());
+                CPM_TRY(d_mv.download(dmoved, tot));
+            }
+            for (int64_t i = 0; i < nd; ++i) dcnt[i] = doff[i];  // now each DOF's first moved entry
+        }
         for (int64_t i = 0; i < nd; ++i) {
             const int64_t row = o->col_start[c] + i;
-            const int64_t node = ib.dof_set[i];
             for (int k = 0; k < 3; ++k) point[3 * row + k] = ib.dof_cp[3 * i + k];
             rowibc[row] = c;
             rowside[row] = desc_side(ib, i);
@@ -1195,24 +1277,15 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
             // (AddExtensionIBCRows, src/IBCMatrixManipulations.cpp:118-186).
             base[row] = ib.dof_rows.base[i];
             for (int k = 0; k < 12; ++k) w[12 * row + k] = ib.dof_rows.w[12 * i + k];
-            uint64_t emask = 0;
-            std::vector<int32_t> etarget;
-            for (int s = 0; s < 64; ++s) {
-                int ii = s >> 4, jj = (s >> 2) & 3, kk = s & 3;
-                uint32_t b = base[row];
-                int col = ht.node(unpack_i(b) + ii, unpack_j(b) + jj, unpack_k(b) + kk);
-                if (col >= 0 && tagged(ib, &ib.dof_dir[3 * i], col, -1.0) && ib.dof_sub[col] >= 0) {
-                    emask |= 1ull << s;
-                    etarget.push_back((int32_t)(o->col_start[c] + ib.dof_sub[col]));
-                }
-            }
+            const uint64_t emask = dem[i];
+            const int ne = __builtin_popcountll(emask);
             patch[row] = (int32_t)p_emask.size();
             p_emask.push_back(emask);
             p_lmask.push_back(0);
             p_eoff.push_back((int32_t)moved.size());
-            moved.insert(moved.end(), etarget.begin(), etarget.end());
+            moved.insert(moved.end(), dmoved.begin() + dcnt[i], dmoved.begin() + dcnt[i] + ne);
             p_loff.push_back((int32_t)moved.size());
-            nmoved += (int64_t)etarget.size();
+            nmoved += ne;
             uint8_t f = F_LCSR;
             if (emask) f |= F_EMOVE;
             if (ib.dof_dirichlet(i)) {
@@ -1228,19 +1301,11 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
             // L row (AddFiniteDifferenceIBCRows, src/IBCMatrixManipulations.cpp:219-251):
             // across the curve -> the original tube node; same side and in the DOF
             // subset -> that DOF's column; otherwise dropped.
-            const int64_t tq = ib.tag_sub[node];
-            for (int d = 0; d < 6; ++d) {
-                int col = ht.nbr(node, d);
-                if (col < 0) continue;
-                bool tg = tq >= 0 && tagged(ib, &ib.tag_dir[3 * tq], col, 1.0);
-                if (tg) {
-                    lcol.push_back(col);
-                    lval.push_back(Lof);
-                } else if (ib.dof_sub[col] >= 0) {
-                    lcol.push_back((int32_t)(o->col_start[c] + ib.dof_sub[col]));
+            for (int d = 0; d < 6; ++d)
+                if (dlc[6 * i + d] >= 0) {
+                    lcol.push_back(dlc[6 * i + d]);
                     lval.push_back(Lof);
                 }
-            }
             lptr.push_back((int32_t)lcol.size());
             ldiag.push_back(Ldg);
         }
