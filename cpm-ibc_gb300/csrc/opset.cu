@@ -603,6 +603,124 @@ struct CpOverrides {
     CpTable surface;           // the tube surface's closest points at the cp-bar projections
 };
 
+// ---------------------------------------------------------------- tagging walk on the device
+// IBCSubset::ComputeSubsetNearIBC (src/IBCSubset.cpp:39-109): a breadth-first
+// walk over tube neighbours from `start`, keeping the nodes with dist < lim, in
+// the order a FIFO queue discovers them.  One thread block walks level by level:
+// a node of the next level belongs to the smallest (frontier position p,
+// neighbour d) that reaches it while it is unvisited (t = 6 p + d, by atomicMin),
+// and the level's accepted nodes are compacted in increasing t, which is the
+// queue's discovery order.  `start` begins unvisited, as in the reference, so
+// it joins the subset if the walk reaches it again.  Every loop is bounded
+// (each level visits new nodes; at most cap accepted); err = 1 if cap is hit.
+constexpr int BFS_T = 1024;
+__global__ void __launch_bounds__(BFS_T) k_tag_walk(BrickView bv, const uint32_t *__restrict__ key, int start,
+                                                   const double *__restrict__ dist, double lim, uint8_t *__restrict__ visited,
+                                                   int32_t *__restrict__ kmin, int32_t *__restrict__ front0,
+                                                   int32_t *__restrict__ front1, int32_t *__restrict__ tag_set, int32_t cap,
+                                                   int32_t *__restrict__ n_out, int *__restrict__ err) {
+    __shared__ int32_t warp_sum[BFS_T / 32];
+    __shared__ int32_t s_carry, s_F, s_nt;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) {
+        front0[0] = start;
+        s_F = 1;
+        s_nt = 0;
+    }
+    __syncthreads();
+    int32_t *front = front0, *next = front1;
+    for (int level = 0; level < cap + 1; ++level) {
+        const int F = s_F;
+        if (F == 0) break;
+        const int T = 6 * F;
+        for (int t = tid; t < T; t += BFS_T) {
+            const uint32_t kk = key[front[t / 6]];
+            const int d = t % 6;
+            const int nb = node_at(bv, unpack_i(kk) + (d == 0) - (d == 1), unpack_j(kk) + (d == 2) - (d == 3),
+                                   unpack_k(kk) + (d == 4) - (d == 5));
+            if (nb >= 0 && !visited[nb]) atomicMin(&kmin[nb], t);
+        }
+        if (tid == 0) s_carry = 0;
+        __syncthreads();
+        for (int base = 0; base < T; base += BFS_T) {
+            const int t = base + tid;
+            int nb = -1, acc = 0;
+            bool own = false;
+            if (t < T) {
+                const uint32_t kk = key[front[t / 6]];
+                const int d = t % 6;
+                nb = node_at(bv, unpack_i(kk) + (d == 0) - (d == 1), unpack_j(kk) + (d == 2) - (d == 3),
+                             unpack_k(kk) + (d == 4) - (d == 5));
+                own = nb >= 0 && !visited[nb] && kmin[nb] == t;
+                acc = (own && dist[nb] < lim) ? 1 : 0;
+            }
+            // exclusive scan of acc over the block
+            int x = acc;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) warp_sum[wid] = x;
+            __syncthreads();
+            if (wid == 0) {
+                int w = warp_sum[lane];
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, w, o);
+                    if (lane >= o) w += y;
+                }
+                warp_sum[lane] = w;  // inclusive over warps
+            }
+            __syncthreads();
+            const int before = (wid > 0 ? warp_sum[wid - 1] : 0) + x - acc;
+            const int chunk = warp_sum[BFS_T / 32 - 1];
+            const int carry = s_carry;
+            if (acc) {
+                const int pos = carry + before, slot = s_nt + pos;
+                if (slot < cap && pos < cap) {
+                    next[pos] = nb;
+                    tag_set[slot] = nb;
+                } else {
+                    atomicOr(err, 1);
+                }
+            }
+            if (own) {
+                visited[nb] = 1;
+                kmin[nb] = 0x7fffffff;
+            }
+            __syncthreads();
+            if (tid == 0) s_carry = carry + chunk;
+            __syncthreads();
+        }
+        if (tid == 0) {
+            const int nF = s_carry;
+            s_nt = min(cap, s_nt + nF);
+            s_F = (*err) ? 0 : min(nF, cap);
+        }
+        __syncthreads();
+        int32_t *tmp = front;
+        front = next;
+        next = tmp;
+    }
+    if (tid == 0) *n_out = s_nt;
+}
+
+// tag_cpc / tag_dist of the walked subset from the IBC closest points of all tube nodes
+__global__ void k_tag_gather(int64_t nt, const int32_t *__restrict__ tag_set, const double *__restrict__ cp,
+                             const double *__restrict__ dist, double *__restrict__ tag_cpc, double *__restrict__ tag_dist) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    const int64_t q = tag_set[i];
+    for (int k = 0; k < 3; ++k) tag_cpc[3 * i + k] = cp[3 * q + k];
+    tag_dist[i] = dist[q];
+}
+
+__global__ void k_count_below(int64_t n, const double *__restrict__ v, double lim, unsigned long long *__restrict__ cnt) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool b = i < n && v[i] < lim;
+    const unsigned m = __ballot_sync(0xffffffffu, b);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(cnt, (unsigned long long)__popc(m));
+}
+
 static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_desc &desc, const double *normals_dev,
                           const DBuf<double> &xdev, const CpTable *cpt, const CpTable *surf_cpt,
                           IBCData &ib) {
@@ -620,15 +738,19 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
     CPM_TRY(dcp.alloc(3 * N));
     CPM_TRY(dd.alloc(N));
     CPM_TRY(closest_points_dev(s.params(), N, xdev.p, dcp.p, dd.p, 2.0 * r * (1.0 + 1e-12)));
-    std::vector<double> cpc, distc;
-    CPM_TRY(dcp.download(cpc, 3 * N));
-    CPM_TRY(dd.download(distc, N));
-    if (cpt && !cpt->empty())
+    if (cpt && !cpt->empty()) {
+        // the caller's closest points for the nodes its table holds (parity checks)
+        std::vector<double> cpc, distc;
+        CPM_TRY(dcp.download(cpc, 3 * N));
+        CPM_TRY(dd.download(distc, N));
         for (int64_t q = 0; q < N; ++q) {
             double xq[3];
             ht.x(q, xq);
             cpt->lookup(xq, &cpc[3 * q], &distc[q]);
         }
+        CPM_TRY(dcp.upload(cpc));
+        CPM_TRY(dd.upload(distc));
+    }
     // open polylines tag closest points at their end points (src/Surface.cpp:2614-2637)
     bool open_poly = false;
     if (desc.kind == CPM_POLYLINE && desc.nverts > 1) {
@@ -643,36 +765,60 @@ static int build_ibc_data(cpm_tube_s *t, const HostTube &ht, const cpm_surface_d
     ibc_xp0(desc, verts, xp0);
     int64_t start = ht.nearest(xp0);
     if (start < 0) return fail(CPM_ERR_INVALID_ARG, "IBC start point is not near the tube");
-    ib.tag_sub.assign(N, -1);
-    std::vector<uint8_t> visited(N, 0);
-    std::vector<int64_t> queue{start};
-    for (size_t h = 0; h < queue.size(); ++h) {
-        int64_t cur = queue[h];
-        for (int d = 0; d < 6; ++d) {
-            int nb = ht.nbr(cur, d);
-            if (nb < 0 || visited[nb]) continue;
-            visited[nb] = 1;
-            if (distc[nb] < 2.0 * r) {
-                ib.tag_sub[nb] = (int64_t)ib.tag_set.size();
-                ib.tag_set.push_back(nb);
-                queue.push_back(nb);
-            }
+    {
+        // the walk on the device (k_tag_walk), sized by the nodes within 2r
+        DBuf<unsigned long long> dcnt;
+        CPM_TRY(dcnt.alloc(1));
+        CPM_TRY(dcnt.zero());
+        k_count_below<<<(unsigned)((N + 255) / 256), 256, 0, stream()>>>(N, dd.p, 2.0 * r, dcnt.p);
+        std::vector<unsigned long long> hc;
+        CPM_TRY(dcnt.download(hc, 1));
+        const int32_t cap = (int32_t)hc[0] + 1;
+        DBuf<uint8_t> vis;
+        DBuf<int32_t> kmin, f0, f1, dset, dn;
+        DBuf<int> derr;
+        CPM_TRY(vis.alloc(N));
+        CPM_TRY(vis.zero());
+        CPM_TRY(kmin.alloc(N));
+        CPM_CUDA_TRY(cudaMemsetAsync(kmin.p, 0x7f, N * sizeof(int32_t), stream()));  // 0x7f7f7f7f > any 6 p + d
+        CPM_TRY(f0.alloc(cap));
+        CPM_TRY(f1.alloc(cap));
+        CPM_TRY(dset.alloc(cap));
+        CPM_TRY(dn.alloc(1));
+        CPM_TRY(derr.alloc(1));
+        CPM_TRY(derr.zero());
+        k_tag_walk<<<1, BFS_T, 0, stream()>>>(t->view(), t->key.p, (int)start, dd.p, 2.0 * r, vis.p, kmin.p, f0.p, f1.p,
+                                              dset.p, cap, dn.p, derr.p);
+        CPM_CUDA_TRY(cudaGetLastError());
+        std::vector<int32_t> hn, he, hs;
+        CPM_TRY(derr.download(he, 1));
+        if (he[0]) return fail(CPM_ERR_CUDA, "internal: the tagging walk outgrew its bound");
+        CPM_TRY(dn.download(hn, 1));
+        const int64_t ntw = hn[0];
+        CPM_TRY(dset.download(hs, ntw));
+        ib.tag_set.assign(hs.begin(), hs.end());
+        ib.tag_sub.assign(N, -1);
+        for (int64_t i = 0; i < ntw; ++i) ib.tag_sub[hs[i]] = i;
+        DBuf<double> dtc, dtd;
+        CPM_TRY(dtc.alloc(3 * std::max<int64_t>(1, ntw)));
+        CPM_TRY(dtd.alloc(std::max<int64_t>(1, ntw)));
+        if (ntw > 0) {
+            k_tag_gather<<<(unsigned)((ntw + 255) / 256), 256, 0, stream()>>>(ntw, dset.p, dcp.p, dd.p, dtc.p, dtd.p);
+            CPM_CUDA_TRY(cudaGetLastError());
         }
+        CPM_TRY(dtc.download(ib.tag_cpc, 3 * ntw));
+        CPM_TRY(dtd.download(ib.tag_dist, ntw));
     }
     const size_t nt = ib.tag_set.size();
-    ib.tag_cpc.resize(3 * nt);
-    ib.tag_dist.resize(nt);
     ib.tag_bdy.assign(nt, 0);
     for (size_t i = 0; i < nt; ++i) {
-        int64_t q = ib.tag_set[i];
-        for (int k = 0; k < 3; ++k) ib.tag_cpc[3 * i + k] = cpc[3 * q + k];
-        ib.tag_dist[i] = distc[q];
         if (open_poly) {
             const double *v0 = desc.verts, *vl = desc.verts + 3 * (desc.nverts - 1);
             double d0 = 0, d1 = 0;
+            const double *cq = &ib.tag_cpc[3 * i];
             for (int k = 0; k < 3; ++k) {
-                d0 += (v0[k] - cpc[3 * q + k]) * (v0[k] - cpc[3 * q + k]);
-                d1 += (vl[k] - cpc[3 * q + k]) * (vl[k] - cpc[3 * q + k]);
+                d0 += (v0[k] - cq[k]) * (v0[k] - cq[k]);
+                d1 += (vl[k] - cq[k]) * (vl[k] - cq[k]);
             }
             if (std::sqrt(d0) < 1e-7)
                 ib.tag_bdy[i] = 1;
