@@ -1990,7 +1990,7 @@ extern "C" int cpm_opset_ibc_export(cpm_opset_t o, int32_t c, int64_t *tag_set, 
 
 // Lfull / Efull as CSR (sorted columns) reconstructed from the device rows.
 extern "C" int cpm_opset_export_csr(cpm_opset_t o, int32_t which, int64_t *nnz, int64_t *ptr, int64_t *idx, double *val) {
-    if (!o || !nnz || (which != 0 && which != 1)) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
+    if (!o || !nnz || !(which == 0 || which == 1 || (which >= 5 && which <= 7))) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
     HostTube ht;
     CPM_TRY(ht.load(o->tube));
     const int64_t D = o->D, N = o->N;
@@ -2025,7 +2025,15 @@ extern "C" int cpm_opset_export_csr(cpm_opset_t o, int32_t which, int64_t *nnz, 
         // Lfull keeps the L rows of the tube and of the IBC DOFs, and the 2nd-order Dirichlet value rows
         // hold their 1 (src/IBCMatrixManipulations.cpp:54-62)
         const bool ident_row = (f & F_IDENT) && (which == 1 || r >= N + o->total_ibc);
-        if (ident_row) {
+        if (which >= 5) {
+            // the gradient matrix Dc_d of the tube rows (FDMatrices::BuildGradientMatrices,
+            // src/FDMatrices.cpp:66-92): (-1)^nbr 0.5 at the +/- e_d neighbours, then / dx
+            if (r < N)
+                for (int e = 0; e < 2; ++e) {
+                    const int col = ht.nbr(r, 2 * (which - 5) + e);
+                    if (col >= 0) row.push_back({col, (e ? -0.5 : 0.5) / o->dx});
+                }
+        } else if (ident_row) {
             row.push_back({r, 1.0});
         } else if (which == 1) {
             int pi = patch[r];

@@ -202,8 +202,10 @@ int cpm_opset_row_sides(cpm_opset_t op, int32_t *side);
 int cpm_opset_ibc_sizes(cpm_opset_t op, int32_t c, int64_t *sizes);
 int cpm_opset_ibc_export(cpm_opset_t op, int32_t c, int64_t *tag_set, int64_t *dof_set, double *dof_cp);
 
-/* Assembled Lfull / Efull (which = 0 / 1) as CSR in device row/column order,
- * for oracle comparison (columns sorted ascending). nnz query with ptr = NULL. */
+/* Assembled Lfull / Efull (which = 0 / 1), or the gradient matrices Dc_x, Dc_y,
+ * Dc_z of the tube rows (which = 5, 6, 7; FDMatrices::BuildGradientMatrices,
+ * src/FDMatrices.cpp:66-92; rows past the tube empty) as CSR in device row/column
+ * order, for oracle comparison (columns sorted ascending). nnz query with ptr = NULL. */
 int cpm_opset_export_csr(cpm_opset_t op, int32_t which, int64_t *nnz, int64_t *ptr, int64_t *idx, double *val);
 
 /* Evaluation of a solution at surface points (replaces Helpers::GetPlotInterpMatrix

@@ -85,6 +85,7 @@ struct Handle {
     std::vector<int64_t> vis_bdy;
     SpMat plot;
     bool plot_built = false;
+    std::vector<SpMat> dc;  // whole-tube gradient matrices, built on first use
     double last_setup_s = 0;
 };
 
@@ -222,6 +223,11 @@ static const SpMat &Pick(Handle *h, int which) {
         case 1: return P.Efull;
         case 2: return P.L;
         case 3: return P.E;
+        case 5:
+        case 6:
+        case 7:  // FDMatrices::BuildGradientMatrices on the whole tube (src/FDMatrices.cpp:66-92)
+            if (h->dc.empty()) BuildGradientMatrices(P.tube, h->dc);
+            return h->dc[which - 5];
         default:
             if (!h->plot_built) {
                 h->plot = P.PlotMatrix();

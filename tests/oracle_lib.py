@@ -216,7 +216,8 @@ class RefProblem:
         return w
 
     def csr(self, which):
-        """which: 0 Lfull, 1 Efull, 2 L, 3 E, 4 plot interpolation (with IBC columns)."""
+        """which: 0 Lfull, 1 Efull, 2 L, 3 E, 4 plot interpolation (with IBC columns),
+        5 / 6 / 7 the whole-tube gradient matrices Dc_x / Dc_y / Dc_z."""
         L = lib()
         nnz = int(L.cpmref_csr_nnz(self.h, which))
         rows = int(L.cpmref_csr_rows(self.h, which))

@@ -127,6 +127,14 @@ def test_c2_operator_rows_bit_exact(c2, which):
     assert_rows_bit_exact(P, O, gr, which)
 
 
+@pytest.mark.parametrize("which", [5, 6, 7])
+def test_c2_gradient_rows_bit_exact(c2, which):
+    """The gradient matrices Dc_x, Dc_y, Dc_z (FDMatrices::BuildGradientMatrices) of the tube
+    rows equal the oracle's entry by entry."""
+    P, T, O, gr = c2
+    assert_rows_bit_exact(P, O, gr, which)
+
+
 def test_c2_plain_fp64_solve_within_1e10(gpu, c2):
     """The plain FP64 GPU path against the oracle's solve of the same system:
     Laplace with circle values U[0,1], both to relative residual 1e-12."""

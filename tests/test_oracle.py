@@ -191,3 +191,21 @@ def test_heat_sphere_circle_neumann_golden_order(oracle):
     errs = [S.heat_sphere_circle_error(dx, 1, boundary_type=1) for dx in S.DX_HEAT_3D]
     avg, _ = S.convergence_order(errs, S.DX_HEAT_3D)
     assert abs(avg - S.GOLDEN_HEAT_SPHERE_CIRCLE_NEUMANN[1]) < 1e-2
+
+
+def test_gradient_matrices_difference_linear_functions(oracle):
+    """Dc_x, Dc_y, Dc_z (FDMatrices::BuildGradientMatrices): central differences of the grid
+    coordinates give 1 along their own axis and 0 across it, on every tube node whose two
+    neighbours along the axis are in the tube."""
+    import numpy as np
+
+    P = oracle.RefProblem(oracle.sphere_desc(), [], 3, 0.2)
+    t = P.tube()
+    for d in range(3):
+        ptr, idx, val = P.csr(5 + d)
+        full = np.diff(ptr) == 2
+        for a in range(3):
+            g = oracle.csr_matvec(ptr, idx, val, t["x"][:, a])
+            want = 1.0 if a == d else 0.0
+            assert np.allclose(g[full], want, atol=1e-12)
+        assert set(np.round(val * P.dx, 12)) <= {0.5, -0.5}
