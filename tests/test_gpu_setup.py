@@ -245,44 +245,51 @@ def test_plot_interpolation_with_ibc_columns_matches_oracle(gpu, oracle, dx):
     assert moved > 0
 
 
-def test_explicit_heat_step_matches_lfull_efull(gpu, oracle):
-    """HeatWithIBC's explicit step u <- Efull (u + dt Lfull u) on the device equals the
-    same products of the exported Lfull / Efull (whose rows match the oracle's),
-    identity rows included (Lfull and Efull hold 1 on their diagonal there)."""
-    dx = 0.1
+def _oracle_pair(gpu, oracle, dx):
+    from test_gpu_parity_c2 import same_cp_pair
+
+    return same_cp_pair(gpu, oracle, dx, two_circle_ibcs(oracle, dx), two_circle_ibcs(gpu, dx))
+
+
+def test_explicit_heat_step_matches_oracle(gpu, oracle):
+    """HeatWithIBC's explicit step u <- Efull (u + dt Lfull u) on the device equals the same
+    products of the oracle's Lfull / Efull (identity rows included: both hold 1 on their
+    diagonal there), on a device operator built from the oracle's closest points."""
+    dx = 0.05
     dt = 0.1 * dx * dx
-    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), two_circle_ibcs(gpu, dx))
+    P, T, O, gr = _oracle_pair(gpu, oracle, dx)
     rng = np.random.default_rng(3)
     u = rng.standard_normal((2, O.D))
     got = O.explicit_step(dt, u)
-    Lp, Li, Lv = O.csr(0)
-    Ep, Ei, Ev = O.csr(1)
+    Lp, Li, Lv = P.csr(0)
+    Ep, Ei, Ev = P.csr(1)
     for j in range(2):
-        v = u[j] + dt * oracle.csr_matvec(Lp, Li, Lv, u[j])
-        want = oracle.csr_matvec(Ep, Ei, Ev, v)
-        assert np.max(np.abs(got[j] - want)) <= 1e-13 * np.max(np.abs(want))
+        ur = u[j][gr]
+        want = oracle.csr_matvec(Ep, Ei, Ev, ur + dt * oracle.csr_matvec(Lp, Li, Lv, ur))
+        assert np.max(np.abs(got[j][gr] - want)) <= 1e-13 * np.max(np.abs(want))
 
 
-def test_gray_scott_step_matches_lfull_efull(gpu, oracle):
+def test_gray_scott_step_matches_oracle(gpu, oracle):
     """ReactionDiffusionWithIBC's Gray-Scott step on the device equals
-    Efull (u + nu_u dt Lfull u + dt R_u), Efull (v + nu_v dt Lfull v + dt R_v) from the
-    exported Lfull / Efull, the reaction terms from the old u, v."""
-    dx = 0.1
+    Efull (u + nu_u dt Lfull u + dt R_u), Efull (v + nu_v dt Lfull v + dt R_v) with the
+    oracle's Lfull / Efull, the reaction terms from the old u, v."""
+    dx = 0.05
     dt = 0.2
-    O = gpu.OpSet(gpu.Tube(gpu.desc(gpu.SPHERE, [1.0]), 3, dx), two_circle_ibcs(gpu, dx))
+    P, T, O, gr = _oracle_pair(gpu, oracle, dx)
     rng = np.random.default_rng(4)
     u, v = rng.uniform(0, 1, O.D), rng.uniform(0, 0.5, O.D)
     gu, gv = O.gray_scott_step(dt, u, v)
-    Lp, Li, Lv = O.csr(0)
-    Ep, Ei, Ev = O.csr(1)
+    Lp, Li, Lv = P.csr(0)
+    Ep, Ei, Ev = P.csr(1)
     nu_u = (dx / 3.0) ** 2
     nu_v = nu_u / 3.0
     F, k = 0.054, 0.063
-    un = u + nu_u * dt * oracle.csr_matvec(Lp, Li, Lv, u) + dt * (-u * v * v + F * (1 - u))
-    vn = v + nu_v * dt * oracle.csr_matvec(Lp, Li, Lv, v) + dt * (u * v * v - (F + k) * v)
+    ur, vr = u[gr], v[gr]
+    un = ur + nu_u * dt * oracle.csr_matvec(Lp, Li, Lv, ur) + dt * (-ur * vr * vr + F * (1 - ur))
+    vn = vr + nu_v * dt * oracle.csr_matvec(Lp, Li, Lv, vr) + dt * (ur * vr * vr - (F + k) * vr)
     wu, wv = oracle.csr_matvec(Ep, Ei, Ev, un), oracle.csr_matvec(Ep, Ei, Ev, vn)
-    assert np.max(np.abs(gu - wu)) <= 1e-13 * np.max(np.abs(wu))
-    assert np.max(np.abs(gv - wv)) <= 1e-13 * np.max(np.abs(wv))
+    assert np.max(np.abs(gu[gr] - wu)) <= 1e-13 * np.max(np.abs(wu))
+    assert np.max(np.abs(gv[gr] - wv)) <= 1e-13 * np.max(np.abs(wv))
 
 
 def test_nearest_baseline_operator_matches_oracle(gpu, oracle):
