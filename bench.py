@@ -467,7 +467,7 @@ def main():
     ap.add_argument("--solo", type=int, default=2, help="torus-geodesic: sources also run one at a time")
     ap.add_argument("--rate", type=float, default=8.0, help="serving-mix: mean arrivals per second")
     ap.add_argument("--batches", type=int, default=1, help="32-slot batches of the server, run concurrently")
-    ap.add_argument("--mix-requests", type=int, default=64,
+    ap.add_argument("--mix-requests", type=int, default=256,
                     help="requests of the serving-stream sample in the default line (0: none)")
     ap.add_argument("--mix-rate", type=float, default=4.0, help="its mean arrivals per second")
     ap.add_argument("--serve", choices=["concurrent", "sequential"], default="concurrent",
