@@ -323,8 +323,9 @@ class ServingLoop:
                 set_thread_stream(st.cuda_stream)
                 s.inflight_arrival = {}
                 geo, i = [], 0
-                want = {r["id"] for r in reqs}
-                while not want.issubset(out.keys()):
+                want = [r["id"] for r in reqs]
+                # membership tests only: other workers insert into `out` meanwhile
+                while any(rid not in out for rid in want):
                     now = time.perf_counter() - t0
                     while i < len(reqs) and reqs[i]["t"] <= now:
                         r = reqs[i]
