@@ -313,6 +313,7 @@ def serving_mix(cg, requests, rate, seed=11, concurrent=True):
     span = time.perf_counter() - t
     lat = {k: [o["latency"] for o in out.values() if o["kind"] == k] for k in ("laplace", "geodesic")}
     fb = sum(1 for o in out.values() if o["kind"] == "laplace" and o["stats"].get("fp64_fallback"))
+    geo_batched = sum(1 for o in out.values() if o["kind"] == "geodesic" and o["stats"].get("batched", 1) > 1)
     t = time.perf_counter()
     out64 = SV.serve_fp64_one_at_a_time(surfaces, reqs)
     span64 = time.perf_counter() - t
@@ -333,7 +334,8 @@ def serving_mix(cg, requests, rate, seed=11, concurrent=True):
         "setup_s": t_setup, "makespan_s": span, "solves_per_s": len(out) / span,
         "latency_ms": {"p50": float(np.percentile(all_lat, 50) * 1e3), "p99": float(np.percentile(all_lat, 99) * 1e3),
                        "by_kind": pct(lat)},
-        "laplace_fp64_fallbacks": fb, "admissions": loop.admissions, "evictions": loop.evictions,
+        "laplace_fp64_fallbacks": fb, "geodesics_batched": geo_batched, "admissions": loop.admissions,
+        "evictions": loop.evictions,
         "precision_switches": loop.precision_switches,
         "final_precision": {s.name: ("mixed" if s.precision else "fp64") for s in surfaces},
         "solo_fp64_solves": loop.solo_solves,

@@ -10,7 +10,9 @@ fixed IBC curves) on the device.  Requests arrive over time:
   FP64 reliable updates; slots refill as solves finish);
 * ``geodesic``: heat-method distance from a tube node
   (GeodesicDistance::ComputeDistance, problems/GeodesicDistance.cpp:11-69),
-  which carries its own point-IBC operator and runs as one pipeline.
+  which carries its own point-IBC operator and runs as one pipeline; the
+  geodesics waiting on one surface run together (up to 32) as one batch on a
+  slot-patched operator.
 
 A surface's server is admitted only while the device has room for it (its
 estimated bytes within the HBM budget); an idle server is released to make
@@ -37,7 +39,7 @@ import time
 
 import numpy as np
 
-from . import DIAGONAL, Geodesic, OpSet, Server, Solver, device_info
+from . import DIAGONAL, Geodesic, GeodesicBatch, OpSet, Server, Solver, device_info
 
 MAX_SLOTS = 32
 PROBE = 2  # requests in a surface's first mixed-precision batch
@@ -228,22 +230,36 @@ class ServingLoop:
                 continue
             _, _, name, what = min(cands)
             if what == "geodesic":
-                r = geo_wait.pop(0)
-                self._geodesic(self.surfaces[r["surface"]], r, keep_solutions, t0, out)
+                name0 = geo_wait[0]["surface"]
+                take = [r for r in geo_wait if r["surface"] == name0][:MAX_SLOTS]
+                geo_wait = [r for r in geo_wait if r not in take]
+                self._geodesics(self.surfaces[name0], take, keep_solutions, t0, out)
                 continue
             self._unit(self.surfaces[name], what, keep_solutions, t0, out)
         return out
 
-    def _geodesic(self, s, r, keep_solutions, t0, out):
-        # a surface whose Laplace solves left mixed precision runs its geodesics in FP64 too
-        prec = min(self.geodesic_precision, s.precision)
-        phi, its = Geodesic(s.tube, r["source"]).run(self.dt_scale * s.tube.dx ** 2, precision=prec, tol=s.tol)
+    def _geodesics(self, s, batch, keep_solutions, t0, out):
+        """the waiting geodesics of surface s: one alone (its own point-IBC operator), two or
+        more as one batch on a slot-patched operator (GeodesicBatch, FP64).  Results are the
+        distances on the tube rows."""
+        N = s.tube.N
+        if len(batch) == 1:
+            r = batch[0]
+            # a surface whose Laplace solves left mixed precision runs its geodesics in FP64 too
+            prec = min(self.geodesic_precision, s.precision)
+            phi, its = Geodesic(s.tube, r["source"]).run(self.dt_scale * s.tube.dx ** 2, precision=prec, tol=s.tol)
+            phis, stats = [phi], [dict(iterations=its, batched=1)]
+        else:
+            B = GeodesicBatch(s.tube, np.stack([r["source"] for r in batch]))
+            phib, itsb = B.run(self.dt_scale * s.tube.dx ** 2, tol=s.tol)
+            phis = list(phib)
+            stats = [dict(iterations=itsb[k].tolist(), batched=len(batch)) for k in range(len(batch))]
         done = time.perf_counter() - t0
-        rec = dict(kind="geodesic", surface=s.name, arrival=r["t"], completion=done, latency=done - r["t"],
-                   stats=dict(iterations=its))
-        if keep_solutions:
-            rec["x"] = phi
-        out[r["id"]] = rec
+        for r, phi, st in zip(batch, phis, stats):
+            rec = dict(kind="geodesic", surface=s.name, arrival=r["t"], completion=done, latency=done - r["t"], stats=st)
+            if keep_solutions:
+                rec["x"] = phi[:N]
+            out[r["id"]] = rec
 
     def _unit(self, s, what, keep_solutions, t0, out):
         """one unit of work of surface s: 'solo', 'step' or 'submit'"""
@@ -336,7 +352,8 @@ class ServingLoop:
                             geo.append(r)
                     c = self._candidate(s, now)
                     if geo and (c is None or geo[0]["t"] < c[0]):
-                        self._geodesic(s, geo.pop(0), keep_solutions, t0, out)
+                        take, geo = geo[:MAX_SLOTS], geo[MAX_SLOTS:]
+                        self._geodesics(s, take, keep_solutions, t0, out)
                         continue
                     if c is None:
                         wait = reqs[i]["t"] - (time.perf_counter() - t0) if i < len(reqs) else 0.0
