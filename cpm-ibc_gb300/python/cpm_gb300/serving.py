@@ -314,29 +314,45 @@ class ServingLoop:
                 best = c
         return best
 
+    @staticmethod
+    def _worker_stream():
+        """for the calling thread: opens a CUDA stream of its own on the caller's device
+        for the library's work (cpm_set_thread_stream); returns the function that
+        waits for it and hands the thread back to the library stream"""
+        import torch
+
+        from . import set_thread_stream
+
+        dev = torch.cuda.current_device()
+
+        def open_stream():
+            torch.cuda.set_device(dev)
+            st = torch.cuda.Stream()
+            set_thread_stream(st.cuda_stream)
+
+            def close():
+                set_thread_stream(None)
+                st.synchronize()
+
+            return close
+
+        return open_stream
+
     def run_concurrent(self, requests, keep_solutions=False):
         """run() with one worker thread per surface, each queueing its surface's work
         on a CUDA stream of its own (cpm_set_thread_stream), so the surfaces' solves
         overlap on the device.  Within a surface: earliest arrival first, with the same
         batching, probe and precision rules as run()."""
-        import threading
-
-        import torch
-
-        from . import set_thread_stream
-
         order = sorted(requests, key=lambda r: r["t"])
         by = {name: [r for r in order if r["surface"] == name] for name in self.surfaces}
         out = {}
         t0 = time.perf_counter()
         errors = []
-        dev = torch.cuda.current_device()
+        open_stream = self._worker_stream()
 
         def worker(s, reqs):
             try:
-                torch.cuda.set_device(dev)
-                st = torch.cuda.Stream()
-                set_thread_stream(st.cuda_stream)
+                close_stream = open_stream()
                 s.inflight_arrival = {}
                 geo, i = [], 0
                 want = [r["id"] for r in reqs]
@@ -360,8 +376,7 @@ class ServingLoop:
                         time.sleep(max(0.0001, min(0.002, wait)))
                         continue
                     self._unit(s, c[2], keep_solutions, t0, out)
-                set_thread_stream(None)
-                st.synchronize()
+                close_stream()
             except BaseException as e:  # reported on the calling thread
                 errors.append(e)
 
