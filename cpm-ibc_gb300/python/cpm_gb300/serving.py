@@ -10,9 +10,9 @@ fixed IBC curves) on the device.  Requests arrive over time:
   FP64 reliable updates; slots refill as solves finish);
 * ``geodesic``: heat-method distance from a tube node
   (GeodesicDistance::ComputeDistance, problems/GeodesicDistance.cpp:11-69),
-  which carries its own point-IBC operator and runs as one pipeline; the
-  geodesics waiting on one surface run together (up to 32) as one batch on a
-  slot-patched operator.
+  which carries its own point-IBC operator and runs as one pipeline; once
+  GEO_BATCH_MIN geodesics wait on one surface they run together (up to 32) as one
+  batch on a slot-patched operator.
 
 A surface's server is admitted only while the device has room for it (its
 estimated bytes within the HBM budget); an idle server is released to make
@@ -45,6 +45,10 @@ MAX_SLOTS = 32
 PROBE = 2  # requests in a surface's first mixed-precision batch
 K32_MIXED = 2.3  # 32-slot FP32 iteration (reliable updates amortised) / one-RHS FP64 iteration
 K32_FP64 = 14.0  # 32-slot FP64 iteration / one-RHS FP64 iteration
+# geodesics waiting on one surface from which a batch beats solving them one by one: the
+# 32-source batch costs the same with 2 or 32 sources (FP64, lane = source), 146.9 s on the
+# torus against 6.27 s for one source alone
+GEO_BATCH_MIN = 24
 
 
 class ServedSurface:
@@ -104,8 +108,10 @@ class ServingLoop:
     hbm_budget: bytes the servers may hold together (default: the device's free
     memory when the loop is created, less ``reserve`` bytes)."""
 
-    def __init__(self, surfaces, hbm_budget=None, reserve=1 << 30, geodesic_precision=1, dt_scale=1.0):
+    def __init__(self, surfaces, hbm_budget=None, reserve=1 << 30, geodesic_precision=1, dt_scale=1.0,
+                 geodesic_batch_min=GEO_BATCH_MIN):
         self.surfaces = {s.name: s for s in surfaces}
+        self.geodesic_batch_min = geodesic_batch_min
         if hbm_budget is None:
             hbm_budget = max(0, device_info()["free"] - reserve)
         self.budget = int(hbm_budget)
@@ -231,12 +237,17 @@ class ServingLoop:
             _, _, name, what = min(cands)
             if what == "geodesic":
                 name0 = geo_wait[0]["surface"]
-                take = [r for r in geo_wait if r["surface"] == name0][:MAX_SLOTS]
+                take = self._geo_take([r for r in geo_wait if r["surface"] == name0])
                 geo_wait = [r for r in geo_wait if r not in take]
                 self._geodesics(self.surfaces[name0], take, keep_solutions, t0, out)
                 continue
             self._unit(self.surfaces[name], what, keep_solutions, t0, out)
         return out
+
+    def _geo_take(self, waiting):
+        """the geodesics to run next from those waiting on one surface (oldest first): up
+        to 32 as one batch once geodesic_batch_min wait, else the oldest alone"""
+        return waiting[:MAX_SLOTS] if len(waiting) >= self.geodesic_batch_min else waiting[:1]
 
     def _geodesics(self, s, batch, keep_solutions, t0, out):
         """the waiting geodesics of surface s: one alone (its own point-IBC operator), two or
@@ -368,7 +379,8 @@ class ServingLoop:
                             geo.append(r)
                     c = self._candidate(s, now)
                     if geo and (c is None or geo[0]["t"] < c[0]):
-                        take, geo = geo[:MAX_SLOTS], geo[MAX_SLOTS:]
+                        take = self._geo_take(geo)
+                        geo = geo[len(take):]
                         self._geodesics(s, take, keep_solutions, t0, out)
                         continue
                     if c is None:

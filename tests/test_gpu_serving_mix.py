@@ -133,7 +133,7 @@ def test_waiting_geodesics_run_as_one_batch(gpu, concurrent):
     cp = s.closest_points()
     rng = np.random.default_rng(8)
     reqs = [dict(id=k, t=0.0, surface=s.name, kind="geodesic", source=cp[int(rng.integers(len(cp)))]) for k in range(4)]
-    loop = SV.ServingLoop(surfaces)
+    loop = SV.ServingLoop(surfaces, geodesic_batch_min=2)
     out = (loop.run_concurrent if concurrent else loop.run)(reqs, keep_solutions=True)
     assert sorted(out) == list(range(4))
     assert max(o["stats"]["batched"] for o in out.values()) >= 2

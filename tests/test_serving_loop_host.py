@@ -135,8 +135,20 @@ def test_every_request_once_with_its_own_result(fakes, concurrent):
 def test_waiting_geodesics_of_a_surface_form_one_batch(fakes, concurrent):
     s = _surface("a", 60, 2)
     reqs = [dict(id=k, t=0.0, surface="a", kind="geodesic", source=s._cp[k]) for k in range(40)]
-    loop = SV.ServingLoop([s], hbm_budget=1 << 30)
+    loop = SV.ServingLoop([s], hbm_budget=1 << 30, geodesic_batch_min=8)
     out = (loop.run_concurrent if concurrent else loop.run)(reqs, keep_solutions=True)
     assert sorted(out) == list(range(40))
     assert FakeGeodesicBatch.calls == [32, 8] and not FakeGeodesic.calls
     assert all(out[k]["x"][0] == s._cp[k].sum() for k in range(40))
+
+
+@pytest.mark.parametrize("concurrent", [False, True])
+def test_few_waiting_geodesics_run_alone(fakes, concurrent):
+    """below geodesic_batch_min waiting, each geodesic runs alone (a batch costs as much as 32)"""
+    s = _surface("a", 60, 2)
+    reqs = [dict(id=k, t=0.0, surface="a", kind="geodesic", source=s._cp[k]) for k in range(5)]
+    loop = SV.ServingLoop([s], hbm_budget=1 << 30)
+    out = (loop.run_concurrent if concurrent else loop.run)(reqs, keep_solutions=True)
+    assert sorted(out) == list(range(5))
+    assert not FakeGeodesicBatch.calls and len(FakeGeodesic.calls) == 5
+    assert all(out[k]["x"][0] == s._cp[k].sum() for k in range(5))
