@@ -2327,7 +2327,7 @@ extern "C" int cpm_opset_autotune(cpm_opset_t op, int32_t reps, int32_t with_fp6
     cpm_tune_result res;
     memset(&res, 0, sizeof(res));
     const int sms = sm_count();
-    const int e32c[] = {8, 16, 24, 32, 48, 64}, pc[] = {4, 8, 16, 32}, e64c[] = {4, 8, 16, 32};
+    const int e32c[] = {8, 16, 24, 32, 48, 64, 96, 128}, pc[] = {4, 8, 16, 32, 64, 128}, e64c[] = {4, 8, 16, 32, 64};
     const OpView<float> v32 = op->view<float>();
     auto pick = [&](const int *c, int nc, int dflt, auto launch_with, float &best_us, float &dflt_us, int32_t &best) {
         best_us = 0.f;
@@ -2348,20 +2348,20 @@ extern "C" int cpm_opset_autotune(cpm_opset_t op, int32_t reps, int32_t with_fp6
         }
     };
     if (op->n_grp > 0) {
-        pick(e32c, 6, E32_BPS, [&](int bps) {
+        pick(e32c, 8, E32_BPS, [&](int bps) {
             const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((v32.n_grp + 3) / 4, (int64_t)bps * sms));
             k_epass32w<<<(unsigned)blocks, 128, 0, st>>>(v32, nullptr, -1, x32.p, t32.p);
         }, res.e32_us, res.e32_default_us, res.e32_blocks_per_sm);
     }
     if (op->n_pl > 0) {
-        pick(pc, 4, PATCH_BPS, [&](int bps) {
+        pick(pc, 6, PATCH_BPS, [&](int bps) {
             const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((v32.n_pl + 3) / 4, (int64_t)bps * sms));
             k_epatch32<float><<<(unsigned)blocks, 128, 0, st>>>(v32, nullptr, -1, x32.p, t32.p);
         }, res.patch_us, res.patch_default_us, res.patch_blocks_per_sm);
     }
     if (with_fp64 && op->n_grp > 0) {
         const OpView<double> v64 = op->view<double>();
-        pick(e64c, 4, E64_BPS, [&](int bps) {
+        pick(e64c, 5, E64_BPS, [&](int bps) {
             const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(v64.n_grp, (int64_t)bps * sms));
             k_epass32s<double><<<(unsigned)blocks, 128, 0, st>>>(v64, nullptr, -1, x64.p, t64.p);
         }, res.e64_us, res.e64_default_us, res.e64_blocks_per_sm);
