@@ -520,8 +520,8 @@ static void slot_epatch(const OpView<T> &op, const Slot *sl, int ph, const T *x,
 
 // default launch shapes of the 32-slot E passes (blocks per SM caps of the
 // grid-stride loops): the FP32 bulk pass's best on the sphere with two circles at
-// dx 0.025, the patch and FP64 passes' best or within 2 % of it on the sphere,
-// the torus and the mesh of the serving stream
+// dx 0.025; for the patch and FP64 passes the autotuner chose 64 or more blocks
+// per SM on the sphere, the torus and the mesh of the serving stream
 constexpr int E32_BPS = 32, PATCH_BPS = 64, E64_BPS = 64;
 
 // kernels one E pass of x launches
