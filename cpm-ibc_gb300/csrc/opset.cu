@@ -25,7 +25,7 @@ namespace cpm {
 
 template <class T>
 static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, const T *lval, const T *ldiag, const T *w_ord,
-                           const T *pl_xval, const T *pe_w, const T *sp_w) {
+                           const T *pl_xval, const T *pe_w, const T *sp_w, const T *ov_w) {
     OpView<T> v;
     v.bv = o->tube->view();
     v.N = o->N;
@@ -76,6 +76,9 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
     v.sp_rec = o->sp_rec.p;
     v.sp_w = sp_w;
     v.sp_rows = o->sp_rows.p;
+    v.ov_ptr = o->ov_ptr.p;
+    v.ov_col = o->ov_col.p;
+    v.ov_w = ov_w;
     return v;
 }
 
@@ -83,11 +86,11 @@ static OpView<T> make_view(const cpm_opset_s *o, const T *w, const T *xval, cons
 
 template <>
 cpm::OpView<double> cpm_opset_s::view<double>() const {
-    return cpm::make_view<double>(this, w.p, p_xval.p, lval.p, ldiag.p, w_ord.p, pl_xval.p, pe_w.p, sp_w.p);
+    return cpm::make_view<double>(this, w.p, p_xval.p, lval.p, ldiag.p, w_ord.p, pl_xval.p, pe_w.p, sp_w.p, ov_w.p);
 }
 template <>
 cpm::OpView<float> cpm_opset_s::view<float>() const {
-    return cpm::make_view<float>(this, w32.p, p_xval32.p, lval32.p, ldiag32.p, w_ord32.p, pl_xval32.p, pe_w32.p, sp_w32.p);
+    return cpm::make_view<float>(this, w32.p, p_xval32.p, lval32.p, ldiag32.p, w_ord32.p, pl_xval32.p, pe_w32.p, sp_w32.p, ov_w32.p);
 }
 
 namespace cpm {
@@ -1012,61 +1015,79 @@ __device__ inline bool tagged_dev(const IbcTagDev &ib, const double *dir_r, int 
     return flip * s < 0.0;
 }
 
-// the one IBC column a tube row's entry (column col) moves to, -1 for none, -2
-// when it would move to two IBCs (MoveToIBCColumns, src/IBCMatrixManipulations.cpp:189-216)
-__device__ inline int64_t tube_entry_target(const IbcTagDev *ibs, int n_ibc, int64_t q, int col) {
+// the IBC columns a tube row's entry (column col) moves to: one copy of the
+// entry for every IBC whose tag crosses it and whose DOF subset holds col
+// (MoveToIBCColumns, src/IBCMatrixManipulations.cpp:189-216), in IBC order.
+// Returns their count; the first target in *first, the others in xout.
+__device__ inline int tube_entry_targets(const IbcTagDev *ibs, int n_ibc, int64_t q, int col, int64_t *first,
+                                         int32_t *xout) {
     int hits = 0;
-    int64_t tgt = -1;
+    if (col < 0) return 0;
     for (int c = 0; c < n_ibc; ++c) {
         const int32_t tq = ibs[c].tag_sub[q];
-        if (tq < 0 || col < 0) continue;
+        if (tq < 0) continue;
         if (tagged_dev(ibs[c], ibs[c].tag_dir + 3 * (int64_t)tq, col, 1.0) && ibs[c].dof_sub[col] >= 0) {
+            const int64_t tgt = ibs[c].col_start + ibs[c].dof_sub[col];
+            if (hits == 0)
+                *first = tgt;
+            else if (xout)
+                xout[hits - 1] = (int32_t)tgt;
             ++hits;
-            tgt = ibs[c].col_start + ibs[c].dof_sub[col];
         }
     }
-    return hits > 1 ? -2 : (hits == 1 ? tgt : -1);
+    return hits;
 }
 
 // tube row q's moved E stencil entries (bit s = 16 i + 4 j + k) and L neighbours
-// (bit d, order +x -x +y -y +z -z); with moved != null also their target
-// columns, E entries in s order then L entries in d order, from moved[off[q]]
+// (bit d, order +x -x +y -y +z -z) with their counts, and the number of extra
+// targets of entries that move to more than one IBC (xcount[2q]: E, [2q+1]: L).
+// With moved != null instead the targets: first targets from moved[off[q]], E
+// entries in s order then L entries in d order; extra targets from xcol[xoff[q]]
+// in the same order, each with its s or d in xsd.
 __global__ void k_tube_moves(BrickView bv, int64_t N, const uint32_t *__restrict__ key, const uint32_t *__restrict__ base,
                              const IbcTagDev *__restrict__ ibs, int n_ibc, uint64_t *__restrict__ emask,
-                             uint8_t *__restrict__ lmask, int32_t *__restrict__ count, const int32_t *__restrict__ off,
-                             int32_t *__restrict__ moved, int *__restrict__ err) {
+                             uint8_t *__restrict__ lmask, int32_t *__restrict__ count, int32_t *__restrict__ xcount,
+                             const int32_t *__restrict__ off, int32_t *__restrict__ moved, const int32_t *__restrict__ xoff,
+                             int32_t *__restrict__ xcol, int32_t *__restrict__ xsd) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= N) return;
     bool any = false;
     for (int c = 0; c < n_ibc && !any; ++c) any = ibs[c].tag_sub[q] >= 0;
     uint64_t em = 0;
     uint8_t lm = 0;
-    int cnt = 0;
+    int cnt = 0, xe = 0, xl = 0;
     int32_t *out = moved ? moved + off[q] : nullptr;
+    int32_t *xo = (moved && xcol) ? xcol + xoff[q] : nullptr;
+    int32_t *xs = (moved && xcol) ? xsd + xoff[q] : nullptr;
     if (any) {
         const uint32_t b = base[q];
         const int bi = unpack_i(b), bj = unpack_j(b), bk = unpack_k(b);
         for (int s = 0; s < 64; ++s) {
             const int col = node_at(bv, bi + (s >> 4), bj + ((s >> 2) & 3), bk + (s & 3));
-            const int64_t tgt = tube_entry_target(ibs, n_ibc, q, col);
-            if (tgt == -2) atomicOr(err, 1);
-            if (tgt >= 0) {
+            int64_t tgt = -1;
+            const int h = tube_entry_targets(ibs, n_ibc, q, col, &tgt, xo ? xo + xe : nullptr);
+            if (h > 0) {
                 em |= 1ull << s;
                 if (out) out[cnt] = (int32_t)tgt;
                 ++cnt;
+                if (xs)
+                    for (int e = 0; e < h - 1; ++e) xs[xe + e] = s;
+                xe += h - 1;
             }
         }
         const uint32_t kk = key[q];
         const int i = unpack_i(kk), j = unpack_j(kk), k = unpack_k(kk);
         for (int d = 0; d < 6; ++d) {
             const int col = node_at(bv, i + (d == 0) - (d == 1), j + (d == 2) - (d == 3), k + (d == 4) - (d == 5));
-            if (col < 0) continue;
-            const int64_t tgt = tube_entry_target(ibs, n_ibc, q, col);
-            if (tgt == -2) atomicOr(err, 1);
-            if (tgt >= 0) {
+            int64_t tgt = -1;
+            const int h = tube_entry_targets(ibs, n_ibc, q, col, &tgt, xo ? xo + xe + xl : nullptr);
+            if (h > 0) {
                 lm |= (uint8_t)(1u << d);
                 if (out) out[cnt] = (int32_t)tgt;
                 ++cnt;
+                if (xs)
+                    for (int e = 0; e < h - 1; ++e) xs[xe + xl + e] = d;
+                xl += h - 1;
             }
         }
     }
@@ -1074,6 +1095,8 @@ __global__ void k_tube_moves(BrickView bv, int64_t N, const uint32_t *__restrict
         emask[q] = em;
         lmask[q] = lm;
         count[q] = cnt;
+        xcount[2 * q] = xe;
+        xcount[2 * q + 1] = xl;
     }
 }
 
@@ -1165,6 +1188,7 @@ static int make_float_copies(cpm_opset_s *o) {
     CPM_TRY(conv(o->ldiag, o->ldiag32));
     CPM_TRY(conv(o->pl_xval, o->pl_xval32));
     CPM_TRY(conv(o->pe_w, o->pe_w32));
+    if (o->ov_w.n) CPM_TRY(conv(o->ov_w, o->ov_w32));
     return 0;
 }
 
@@ -1311,34 +1335,37 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
         CPM_TRY(d_tag_dir[c].upload(td));
         hib[c] = IbcTagDev{d_tag_sub[c].p, d_tag_bdy[c].p, d_tag_dir[c].p, d_dof_sub[c].p, o->col_start[c]};
     }
+    // extra targets (entries that move to several IBCs), per tube patch record
+    std::vector<int32_t> ov_ptr{0}, ov_col, ov_s;
+    std::vector<double> ov_w;
     if (n_ibc > 0) {
         DBuf<IbcTagDev> d_ibs;
         CPM_TRY(d_ibs.upload(hib));
         DBuf<uint64_t> d_em;
         DBuf<uint8_t> d_lm;
-        DBuf<int32_t> d_cnt, d_off, d_moved;
-        DBuf<int> d_err;
+        DBuf<int32_t> d_cnt, d_xcnt, d_off, d_moved, d_xoff, d_xcol, d_xsd;
         CPM_TRY(d_em.alloc(N));
         CPM_TRY(d_lm.alloc(N));
         CPM_TRY(d_cnt.alloc(N));
-        CPM_TRY(d_err.alloc(1));
-        CPM_TRY(d_err.zero());
+        CPM_TRY(d_xcnt.alloc(2 * N));
         const unsigned nb = (unsigned)((N + 127) / 128);
         k_tube_moves<<<nb, 128, 0, stream()>>>(t->view(), N, t->key.p, t->base.p, d_ibs.p, n_ibc, d_em.p, d_lm.p, d_cnt.p,
-                                               nullptr, nullptr, d_err.p);
+                                               d_xcnt.p, nullptr, nullptr, nullptr, nullptr, nullptr);
         CPM_CUDA_TRY(cudaGetLastError());
         std::vector<uint64_t> em;
         std::vector<uint8_t> lm;
-        std::vector<int32_t> cnt, he;
-        CPM_TRY(d_err.download(he, 1));
-        if (he[0]) return fail(CPM_ERR_UNSUPPORTED, "IBCs too close together: a stencil entry moves to two IBCs");
+        std::vector<int32_t> cnt, xcnt;
         CPM_TRY(d_em.download(em, N));
         CPM_TRY(d_lm.download(lm, N));
         CPM_TRY(d_cnt.download(cnt, N));
-        std::vector<int32_t> off(N);
+        CPM_TRY(d_xcnt.download(xcnt, 2 * N));
+        std::vector<int32_t> off(N), xoff(N);
+        int64_t nx = 0;
         for (int64_t q = 0; q < N; ++q) {
             off[q] = (int32_t)nmoved;
             nmoved += cnt[q];
+            xoff[q] = (int32_t)nx;
+            nx += xcnt[2 * q] + xcnt[2 * q + 1];
             if (!em[q] && !lm[q]) continue;
             patch[q] = (int32_t)p_emask.size();
             p_emask.push_back(em[q]);
@@ -1347,16 +1374,41 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
             p_loff.push_back(off[q] + __builtin_popcountll(em[q]));
             p_xcol.push_back(0);
             p_xval.push_back(0.0);
+            ov_ptr.push_back(ov_ptr.back() + xcnt[2 * q]);
+            ov_ptr.push_back(ov_ptr.back() + xcnt[2 * q + 1]);
             if (em[q]) flags[q] |= F_EMOVE;
             if (lm[q]) flags[q] |= F_LMOVE;
+            if (xcnt[2 * q] + xcnt[2 * q + 1]) flags[q] |= F_OVL;
         }
         if (nmoved > 0) {
             CPM_TRY(d_off.upload(off));
             CPM_TRY(d_moved.alloc(nmoved));
+            int32_t *xc = nullptr, *xs = nullptr;
+            if (nx > 0) {
+                CPM_TRY(d_xoff.upload(xoff));
+                CPM_TRY(d_xcol.alloc(nx));
+                CPM_TRY(d_xsd.alloc(nx));
+                xc = d_xcol.p;
+                xs = d_xsd.p;
+            }
             k_tube_moves<<<nb, 128, 0, stream()>>>(t->view(), N, t->key.p, t->base.p, d_ibs.p, n_ibc, nullptr, nullptr,
-                                                   nullptr, d_off.p, d_moved.p, d_err.p);
+                                                   nullptr, nullptr, d_off.p, d_moved.p, d_xoff.p, xc, xs);
             CPM_CUDA_TRY(cudaGetLastError());
             CPM_TRY(d_moved.download(moved, nmoved));
+            if (nx > 0) {
+                CPM_TRY(d_xcol.download(ov_col, nx));
+                CPM_TRY(d_xsd.download(ov_s, nx));
+            }
+        }
+        // E extras carry the stencil weight of their point, as the patch entries do
+        ov_w.assign(ov_col.size(), 0.0);
+        for (int64_t q = 0; q < N; ++q) {
+            if (patch[q] < 0) continue;
+            const int pi = patch[q];
+            for (int e = ov_ptr[2 * pi]; e < ov_ptr[2 * pi + 1]; ++e) {
+                const int sx = ov_s[e], i = sx >> 4, j = (sx >> 2) & 3, k = sx & 3;
+                ov_w[e] = (w[12 * q + i] * w[12 * q + 4 + j]) * w[12 * q + 8 + k];
+            }
         }
     }
     const int64_t n_tube_patched = (int64_t)p_emask.size();
@@ -1493,6 +1545,17 @@ static int build_ibc(cpm_opset_s *o, int n_ibc, const cpm_surface_desc *descs, c
     if (lcol.empty()) {
         lcol.push_back(0);
         lval.push_back(0);
+    }
+    // the DOF rows' patch records (after the tube rows') have no extra targets
+    ov_ptr.resize(2 * p_emask.size() + 1, ov_ptr.back());
+    o->n_ov = (int64_t)ov_col.size();
+    o->h_ov_ptr = ov_ptr;
+    o->h_ov_col = ov_col;
+    o->h_ov_s = ov_s;
+    if (o->n_ov > 0) {
+        CPM_TRY(o->ov_ptr.upload(ov_ptr));
+        CPM_TRY(o->ov_col.upload(ov_col));
+        CPM_TRY(o->ov_w.upload(ov_w));
     }
     CPM_TRY(o->p_emask.upload(p_emask));
     CPM_TRY(o->p_lmask.upload(p_lmask));
@@ -1632,7 +1695,8 @@ static int build_patch_list(cpm_opset_s *o, const std::vector<uint8_t> &flags) {
             if (pi < 0 || (size_t)pi >= p_emask.size()) return fail(CPM_ERR_CUDA, "internal: patched row without a patch record");
             rows.push_back((int32_t)r);
             off.push_back(off.back() + ((f & F_EMOVE) ? __builtin_popcountll(p_emask[pi]) : 0));
-            neg.push_back((f & F_ENEG) ? 1 : 0);
+            const bool ex = (f & F_OVL) && o->h_ov_ptr[2 * pi + 1] > o->h_ov_ptr[2 * pi];
+            neg.push_back((uint8_t)(((f & F_ENEG) ? 1 : 0) | (ex ? 2 : 0)));
             xcol.push_back((f & F_EXTRA) ? p_xcol[pi] : -1);
             xval.push_back((f & F_EXTRA) ? p_xval[pi] : 0.0);
         }
@@ -2047,6 +2111,11 @@ extern "C" int cpm_opset_export_csr(cpm_opset_t o, int32_t which, int64_t *nnz, 
                                                     : ht.node(unpack_i(b) + i, unpack_j(b) + j, unpack_k(b) + k);
                 row.push_back({col, sg * (w[12 * r + 8 + k] * w[12 * r + 4 + j] * w[12 * r + i])});
             }
+            if (f & F_OVL)  // the further copies of entries that move to several IBCs
+                for (int e = o->h_ov_ptr[2 * pi]; e < o->h_ov_ptr[2 * pi + 1]; ++e) {
+                    const int sx = o->h_ov_s[e], i = sx >> 4, j = (sx >> 2) & 3, k = sx & 3;
+                    row.push_back({o->h_ov_col[e], sg * (w[12 * r + 8 + k] * w[12 * r + 4 + j] * w[12 * r + i])});
+                }
             if (f & F_EXTRA) row.push_back({p_xcol[pi], p_xval[pi]});
         } else if (r < N) {
             int pi = patch[r];
@@ -2057,6 +2126,8 @@ extern "C" int cpm_opset_export_csr(cpm_opset_t o, int32_t which, int64_t *nnz, 
                 int64_t col = ((lm >> d) & 1) ? moved[loff + __builtin_popcount((unsigned)lm & ((1u << d) - 1u))] : ht.nbr(r, d);
                 if (col >= 0) row.push_back({col, Lof});
             }
+            if (f & F_OVL)
+                for (int e = o->h_ov_ptr[2 * pi + 1]; e < o->h_ov_ptr[2 * pi + 2]; ++e) row.push_back({o->h_ov_col[e], Lof});
         } else {
             int64_t q = r - N;
             row.push_back({r, ldiag[q]});
@@ -2187,7 +2258,7 @@ extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp
                     tgt = op->col_start[c] + ibs[c].dof_sub[col];
                 }
             }
-            if (hits > 1) return fail(CPM_ERR_UNSUPPORTED, "IBCs too close together: a stencil entry moves to two IBCs");
+            if (hits > 1) return fail(CPM_ERR_UNSUPPORTED, "an evaluation stencil entry lies across two IBCs (64 entries per point)");
             if (hits == 1) cols[64 * i + e] = tgt;
         }
     return 0;

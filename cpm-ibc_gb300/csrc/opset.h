@@ -16,6 +16,7 @@ enum RowFlags : uint8_t {
     F_ENEG = 16,   // E row negated (2nd-order Dirichlet DOF rows)
     F_EXTRA = 32,  // E row has one extra entry (2 * Dirichlet value)
     F_SLOTP = 64,  // tube row with per-slot patch records (a batch with one point IBC per slot)
+    F_OVL = 128,   // tube row with entries that move to more than one IBC (extra targets)
 };
 
 // Device view of an operator set in one arithmetic type: the rows of E and L
@@ -54,7 +55,7 @@ struct OpView {
     // IBC patch list of the rows whose E row differs from the bulk stencil:
     // t_r = sign (bulk + sum_e w_e (x[new_e] - x[old_e])) + xval x[xcol]
     const int32_t *pl_row, *pl_off, *pl_xcol;  // n_pl rows; entries pl_off[i] .. pl_off[i+1]
-    const uint8_t *pl_neg;                    // 1: negated (2nd-order Dirichlet DOF rows)
+    const uint8_t *pl_neg;                    // bit 0: negated (2nd-order Dirichlet DOF rows); bit 1: E extras (F_OVL)
     const T *pl_xval;
     const int32_t *pe_new, *pe_old;           // moved column and the bulk column it replaces
     const T *pe_w;                            // stencil weight (wx_i wy_j) wz_k of the moved point
@@ -68,6 +69,13 @@ struct OpView {
     const T *sp_w;
     const int32_t *sp_rows;                   // rows with records
     int64_t n_sp_rows;
+    // extra targets of the F_OVL rows (patch index pi): an entry that lies across
+    // several IBCs moves to every one of their DOF columns (MoveToIBCColumns keeps
+    // one copy per IBC), the first in the moved list, the others here.  E extras
+    // ov_col[ov_ptr[2 pi] .. ov_ptr[2 pi + 1]) with stencil weight ov_w, L extras
+    // ov_col[ov_ptr[2 pi + 1] .. ov_ptr[2 pi + 2]) with weight Loff.
+    const int32_t *ov_ptr, *ov_col;
+    const T *ov_w;
     // launch shapes of the 32-slot E passes, blocks per SM (0: the built-in
     // defaults; cpm_opset_autotune / cpm_opset_set_launch).  Never the arithmetic.
     int e32_bps, patch_bps, e64_bps;
@@ -83,6 +91,15 @@ __device__ __forceinline__ T slot_l_correction(const OpView<T> &op, int64_t r, i
         if (rec.x == s && rec.y == 1) c += t[(int64_t)rec.w * K + s] - t[(int64_t)rec.z * K + s];
     }
     return n * (op.Loff * c);
+}
+
+// sum of x (K-wide, slot s) at an F_OVL row's E extras, weighted
+template <class T, int K>
+__device__ __forceinline__ T ovl_e_sum(const int32_t *ov_ptr, const int32_t *ov_col, const T *ov_w, int pi, int s,
+                                       const T *__restrict__ x) {
+    T a = 0;
+    for (int e = ov_ptr[2 * pi]; e < ov_ptr[2 * pi + 1]; ++e) a += ov_w[e] * x[(int64_t)ov_col[e] * K + s];
+    return a;
 }
 
 // ---------------------------------------------------------------------------
@@ -148,7 +165,7 @@ __device__ __forceinline__ T e_row_thread(const OpView<T> &op, int64_t r, int s,
     }
     uint64_t emask = 0;
     int eoff = 0, pi = -1;
-    if (fl & (F_EMOVE | F_EXTRA)) {
+    if (fl & (F_EMOVE | F_EXTRA | F_OVL)) {
         pi = op.patch[r];
         emask = op.p_emask[pi];
         eoff = op.p_eoff[pi];
@@ -183,6 +200,7 @@ __device__ __forceinline__ T e_row_thread(const OpView<T> &op, int64_t r, int s,
         }
         acc += wx[i] * ay;
     }
+    if (fl & F_OVL) acc += ovl_e_sum<T, K>(op.ov_ptr, op.ov_col, op.ov_w, pi, s, x);
     if (fl & F_ENEG) acc = -acc;
     if (fl & F_EXTRA) acc += op.p_xval[pi] * x[(int64_t)op.p_xcol[pi] * K + s];
     return acc;
@@ -206,7 +224,7 @@ __device__ __forceinline__ T e_row(const OpView<T> &op, int64_t r, int s, const 
     }
     uint64_t emask = 0;
     int eoff = 0, pi = -1;
-    if (fl & (F_EMOVE | F_EXTRA)) {
+    if (fl & (F_EMOVE | F_EXTRA | F_OVL)) {
         pi = op.patch[r];
         emask = op.p_emask[pi];
         eoff = op.p_eoff[pi];
@@ -233,6 +251,7 @@ __device__ __forceinline__ T e_row(const OpView<T> &op, int64_t r, int s, const 
         }
         acc += wx[i] * ay;
     }
+    if (fl & F_OVL) acc += ovl_e_sum<T, K>(op.ov_ptr, op.ov_col, op.ov_w, pi, s, x);
     if (fl & F_ENEG) acc = -acc;
     if (fl & F_EXTRA) acc += op.p_xval[pi] * x[(int64_t)op.p_xcol[pi] * K + s];
     return acc;
@@ -420,6 +439,18 @@ __device__ __forceinline__ void e_group_split(const OpView<T> &op, int p0, int p
     }
 }
 
+// The extra L targets of an F_OVL row r (OpView::ov_*), added to a finished
+// row as n Loff sum_e t_e: after the row's own sum, when its neighbour columns
+// are no longer live, so the row loops of operators without overlaps keep
+// their registers.
+template <class T, int K>
+__device__ __forceinline__ T ovl_l_term(const OpView<T> &op, int64_t r, int s, T n, const T *__restrict__ t) {
+    const int pi = op.patch[r];
+    T a = 0;
+    for (int e = op.ov_ptr[2 * pi + 1]; e < op.ov_ptr[2 * pi + 2]; ++e) a += t[(int64_t)op.ov_col[e] * K + s];
+    return n * (op.Loff * a);
+}
+
 // y_r = m x_r + n (Ldiag x_r + Loff sum_d t_{c_d}), identity rows y = x
 // (GeneralizedBiCGStabSystem::Multiply, src/GeneralizedBiCGStabSystem.h:191-233)
 // for slot s of a K-wide row-major batch and U rows at once: the flags, x and
@@ -479,13 +510,18 @@ __device__ __forceinline__ void l_rows(const OpView<T> &op, const int64_t (&r)[U
             if ((fl[u] & F_SLOTP) && act) y[u] += slot_l_correction<T, K>(op, r[u], s, n, t);
         }
     }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+        if ((fl[u] & F_OVL) && act) y[u] += ovl_l_term<T, K>(op, r[u], s, n, t);
 }
 
 // l_rows for 32 FP32 slots, four per thread: slots 4q .. 4q+3 of U rows, as
 // two f32x2 pairs (slots 4q, 4q+1 in .x; 4q+2, 4q+3 in .y).  One 16-byte load
 // per vector and row, the neighbour columns shared by the four slots, and the
 // difference form of the FP32 row on slot pairs.  Rows >= D produce nothing.
-template <int U>
+// OVL: the operator has extra L targets (OpView::ov_*); only then is their
+// code compiled in, so the hot kernels of other operators are unchanged.
+template <int U, bool OVL>
 __device__ __forceinline__ void l_rows4(const OpView<float> &op, const int64_t (&r)[U], int q, float m, float n,
                                         const float *__restrict__ x, const float *__restrict__ t, ulonglong2 (&y)[U]) {
     uint8_t fl[U];
@@ -533,6 +569,20 @@ __device__ __forceinline__ void l_rows4(const OpView<float> &op, const int64_t (
             y[u].y = f2_fma(n2, f2_mul(l2, o1), f2_mul(m2, xr[u].y));
         }
     }
+    if constexpr (OVL)
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+        if (fl[u] & F_OVL) {  // extra L targets, n Loff sum_e t_e (never an identity row)
+            const int pi = op.patch[r[u]];
+            uint64_t a0 = 0ull, a1 = 0ull;
+            for (int e = op.ov_ptr[2 * pi + 1]; e < op.ov_ptr[2 * pi + 2]; ++e) {
+                const ulonglong2 tv = *(const ulonglong2 *)(t + (uint32_t)op.ov_col[e] * 32u + 4 * q);
+                a0 = f2_add(a0, tv.x);
+                a1 = f2_add(a1, tv.y);
+            }
+            y[u].x = f2_fma(n2, f2_mul(l2, a0), y[u].x);
+            y[u].y = f2_fma(n2, f2_mul(l2, a1), y[u].y);
+        }
 }
 
 // caller-supplied closest points of an operator set built by cpm_opset_create_from_cp
@@ -587,6 +637,14 @@ struct cpm_opset_s {
     cpm::DBuf<double> sp_w;
     cpm::DBuf<float> sp_w32;
     int64_t n_sp_rows = 0;
+    // extra targets of entries that move to several IBCs (OpView::ov_*); the
+    // host copy keeps each E extra's stencil index (s = 16 i + 4 j + k) or L
+    // neighbour (d) in h_ov_s
+    cpm::DBuf<int32_t> ov_ptr, ov_col;
+    cpm::DBuf<double> ov_w;
+    cpm::DBuf<float> ov_w32;
+    std::vector<int32_t> h_ov_ptr, h_ov_col, h_ov_s;
+    int64_t n_ov = 0;  // extra targets in all
 
     template <class T>
     cpm::OpView<T> view() const;

@@ -330,11 +330,22 @@ __global__ void __launch_bounds__(128) k_epass32s(OpView<T> op, const Slot *__re
 // list row q's value from its bulk value acc, sign (acc + sum_e w_e (x[new_e] -
 // x[old_e])) + xval x[xcol]: moved stencil points read the IBC DOF column
 // instead of the tube node (IBCMatrixManipulations::AddIBCExtension's column
-// moves, src/IBCMatrixManipulations.cpp:118-186).  The lanes load 32 entries at
+// moves, src/IBCMatrixManipulations.cpp:118-186); a point that moves to
+// several IBCs adds w x[target] for each further IBC (OpView::ov_*).  The lanes load 32 entries at
 // once and broadcast them, so a row's x loads are all in flight together.
 // q is the same in every lane; inactive slots (act false) load nothing.
 template <class T>
-__device__ __forceinline__ T patch_row(const OpView<T> &op, int q, T acc, int lane, bool act, const T *__restrict__ x) {
+__device__ __forceinline__ T ovl_e_patch(const int32_t *patch, const int32_t *ov_ptr, const int32_t *ov_col, const T *ov_w,
+                                         uint32_t r, T acc, int lane, bool act, const T *__restrict__ x) {
+    const int pi = patch[r];
+    for (int e = ov_ptr[2 * pi]; e < ov_ptr[2 * pi + 1]; ++e)
+        acc = fma_rn(ov_w[e], act ? x[(uint32_t)ov_col[e] * 32u + lane] : T(0), acc);
+    return acc;
+}
+
+template <class T, bool OVL>
+__device__ __forceinline__ T patch_row(const OpView<T> &op, int q, uint32_t r, T acc, int lane, bool act,
+                                       const T *__restrict__ x) {
     const int e0 = op.pl_off[q], e1 = op.pl_off[q + 1], xc = op.pl_xcol[q], neg = op.pl_neg[q];
     const T xv = op.pl_xval[q];
     const T xe = (act && xc >= 0) ? x[(uint32_t)xc * 32u + lane] : T(0);
@@ -363,7 +374,9 @@ __device__ __forceinline__ T patch_row(const OpView<T> &op, int q, T acc, int la
                 if (u0 + u < cnt) acc = fma_rn(ww[u], sub_rn(xn[u], xo[u]), acc);
         }
     }
-    if (neg) acc = -acc;
+    if constexpr (OVL)
+        if (neg & 2) acc = ovl_e_patch<T>(op.patch, op.ov_ptr, op.ov_col, op.ov_w, r, acc, lane, act, x);
+    if (neg & 1) acc = -acc;
     if (xc >= 0) acc = fma_rn(xv, xe, acc);
     return acc;
 }
@@ -472,7 +485,7 @@ __global__ void k_epass1(OpView<T> op, const Slot *__restrict__ sl, int ph, cons
 // the patch as a pass of its own after the bulk 32-slot E pass, warp per
 // patch-list row (consecutive rows on neighbouring warps, whose gathers share
 // cache lines)
-template <class T>
+template <class T, bool OVL>
 __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__restrict__ sl, int ph, const T *__restrict__ x,
                                                   T *__restrict__ t) {
     const int lane = threadIdx.x & 31;
@@ -482,7 +495,7 @@ __global__ void __launch_bounds__(128) k_epatch32(OpView<T> op, const Slot *__re
     for (int64_t q = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5); q < op.n_pl; q += warps) {
         const uint32_t r = (uint32_t)op.pl_row[q];
         const T acc = act ? t[r * 32u + lane] : T(0);
-        const T v = patch_row<T>(op, (int)q, acc, lane, act, x);
+        const T v = patch_row<T, OVL>(op, (int)q, r, acc, lane, act, x);
         if (act) t[r * 32u + lane] = v;
     }
 }
@@ -551,7 +564,10 @@ static void launch_epass(const OpView<T> &op, const Slot *sl, int ph, const T *x
     if (K == 32 && op.n_pl > 0) {  // the gather passes correct the IBC patch rows afterwards
         const int64_t bps = op.patch_bps > 0 ? op.patch_bps : PATCH_BPS;
         const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((op.n_pl + 3) / 4, bps * sm_count()));
-        k_epatch32<T><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
+        if (op.ov_ptr)
+            k_epatch32<T, true><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
+        else
+            k_epatch32<T, false><<<(unsigned)blocks, 128, 0, st>>>(op, sl, ph, x, t);
     }
     if (K == 32 && op.n_sp_rows > 0) slot_epatch(op, sl, ph, x, t, st);
 }
@@ -1008,14 +1024,15 @@ __device__ __forceinline__ bool grid_reduce4(const Dot4<N> &acc, double *partial
     return grid_reduce<32, N, true>(v, partial, counter, out);
 }
 
-// k_lpass for 32 FP32 slots (every slot)
+// k_lpass for 32 FP32 slots (every slot); OVL as in l_rows4
+template <bool OVL>
 __global__ void __launch_bounds__(BS, 4) k_lpass4(OpView<float> op, float m, float n, const float *__restrict__ x,
                                                const float *__restrict__ t, float *__restrict__ y) {
     GRID_LOOP4
     ROWS4(op.D, V4_UN) {
         ROWS4_OF_TRIP(rr, V4_UN)
         ulonglong2 v[V4_UN];
-        l_rows4<V4_UN>(op, rr, q, m, n, x, t, v);
+        l_rows4<V4_UN, OVL>(op, rr, q, m, n, x, t, v);
 #pragma unroll
         for (int u = 0; u < V4_UN; ++u)
             if (rr[u] < op.D) st4(y, rr[u], q, v[u], 15u);
@@ -1029,6 +1046,7 @@ static inline bool lpass4_ok(int64_t D, const void *a, const void *b, const void
 }
 
 // k_apply_alpha for 32 FP32 slots
+template <bool OVL>
 __global__ void __launch_bounds__(BS, 4) k_apply_alpha4(OpView<float> op, Slot *sl, float m, float n, const float *__restrict__ y,
                                                      const float *__restrict__ te, const float *__restrict__ r0,
                                                      float *__restrict__ v, double *partial, unsigned int *counter) {
@@ -1043,7 +1061,7 @@ __global__ void __launch_bounds__(BS, 4) k_apply_alpha4(OpView<float> op, Slot *
             ulonglong2 r0v[V4_UN], vv[V4_UN];
 #pragma unroll
             for (int u = 0; u < V4_UN; ++u) r0v[u] = rr[u] < op.D ? ld4(r0, rr[u], q) : make_ulonglong2(0ull, 0ull);
-            l_rows4<V4_UN>(op, rr, q, m, n, y, te, vv);
+            l_rows4<V4_UN, OVL>(op, rr, q, m, n, y, te, vv);
 #pragma unroll
             for (int u = 0; u < V4_UN; ++u)
                 if (rr[u] < op.D) {
@@ -1056,6 +1074,7 @@ __global__ void __launch_bounds__(BS, 4) k_apply_alpha4(OpView<float> op, Slot *
 }
 
 // k_apply_omega for 32 FP32 slots
+template <bool OVL>
 __global__ void __launch_bounds__(BS, 4) k_apply_omega4(OpView<float> op, Slot *sl, float m, float n, const float *__restrict__ z,
                                                      const float *__restrict__ te, const float *__restrict__ sv,
                                                      float *__restrict__ tv, double *partial, unsigned int *counter) {
@@ -1070,7 +1089,7 @@ __global__ void __launch_bounds__(BS, 4) k_apply_omega4(OpView<float> op, Slot *
             ulonglong2 svv[V4_UN], tt[V4_UN];
 #pragma unroll
             for (int u = 0; u < V4_UN; ++u) svv[u] = rr[u] < op.D ? ld4(sv, rr[u], q) : make_ulonglong2(0ull, 0ull);
-            l_rows4<V4_UN>(op, rr, q, m, n, z, te, tt);
+            l_rows4<V4_UN, OVL>(op, rr, q, m, n, z, te, tt);
 #pragma unroll
             for (int u = 0; u < V4_UN; ++u)
                 if (rr[u] < op.D) {
@@ -1513,14 +1532,20 @@ static void mixed_iteration(cpm_solver_s *s, const SolveParams &P) {
     k_update_p<float, K><<<s->G, BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fp.p, s->fy.p, s->fr0.p);
     launch_epass<float, K>(op, sl, PH_ITER, s->fy.p, s->fte.p, st);
     if (v4)
-        k_apply_alpha4<<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p, s->counter.p);
+        if (op.ov_ptr)
+            k_apply_alpha4<true><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p, s->counter.p);
+        else
+            k_apply_alpha4<false><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p, s->counter.p);
     else
         k_apply_alpha<float, K><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fy.p, s->fte.p, s->fr0.p, s->fv.p, s->partial.p,
                                                      s->counter.p);
     k_update_s<float, K><<<s->G, BS, 0, st>>>(D, sl, pden, 1.0f, s->fr.p, s->fv.p, s->fs.p, s->fz.p);
     launch_epass<float, K>(op, sl, PH_ITER, s->fz.p, s->fte.p, st);
     if (v4) {
-        k_apply_omega4<<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p, s->counter.p);
+        if (op.ov_ptr)
+            k_apply_omega4<true><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p, s->counter.p);
+        else
+            k_apply_omega4<false><<<s->G, BS, 0, st>>>(op, sl, m, n, s->fz.p, s->fte.p, s->fs.p, s->ft.p, s->partial.p, s->counter.p);
         k_update_xr4<<<s->G, BS, 0, st>>>(D, sl, P, s->fy.p, s->fz.p, s->fs.p, s->ft.p, s->fr0.p, s->fx.p, s->fr.p,
                                           s->partial.p, s->counter.p);
     } else {
@@ -2248,7 +2273,10 @@ extern "C" int cpm_apply_device(cpm_opset_t op, double m, double n, int32_t kslo
         } else {
             launch_epass<float, 32>(v, nullptr, -1, x, t, st);
             if (lpass4_ok(D, x, t, y))
-                k_lpass4<<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
+                if (v.ov_ptr)
+                    k_lpass4<true><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
+                else
+                    k_lpass4<false><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
             else
                 k_lpass<float, 32><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, t, y);
         }
@@ -2358,7 +2386,10 @@ extern "C" int cpm_opset_autotune(cpm_opset_t op, int32_t reps, int32_t with_fp6
     if (op->n_pl > 0) {
         pick(pc, 6, PATCH_BPS, [&](int bps) {
             const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((v32.n_pl + 3) / 4, (int64_t)bps * sms));
-            k_epatch32<float><<<(unsigned)blocks, 128, 0, st>>>(v32, nullptr, -1, x32.p, t32.p);
+            if (v32.ov_ptr)
+                k_epatch32<float, true><<<(unsigned)blocks, 128, 0, st>>>(v32, nullptr, -1, x32.p, t32.p);
+            else
+                k_epatch32<float, false><<<(unsigned)blocks, 128, 0, st>>>(v32, nullptr, -1, x32.p, t32.p);
         }, res.patch_us, res.patch_default_us, res.patch_blocks_per_sm);
     }
     if (with_fp64 && op->n_grp > 0) {
@@ -2428,7 +2459,10 @@ extern "C" int cpm_apply_device_noalloc(cpm_opset_t op, double m, double n, int3
         } else {
             launch_epass<float, 32>(v, nullptr, -1, x, tt, st);
             if (lpass4_ok(D, x, tt, y))
-                k_lpass4<<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
+                if (v.ov_ptr)
+                    k_lpass4<true><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
+                else
+                    k_lpass4<false><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
             else
                 k_lpass<float, 32><<<row_grid(D, 32), BS, 0, st>>>(v, (float)m, (float)n, x, tt, y);
         }

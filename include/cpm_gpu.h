@@ -157,7 +157,12 @@ int cpm_tube_destroy(cpm_tube_t t);
  * (src/IBCSubsets.h:23) and IBCMatrixManipulations::AddIBCFiniteDifference /
  * AddIBCExtension (src/IBCMatrixManipulations.cpp:12-71) as one object whose
  * rows are: tube rows (device order), then IBC DOF rows and Dirichlet value
- * rows in the reference's column layout (src/IBCSubsets.cpp:74-116). */
+ * rows in the reference's column layout (src/IBCSubsets.cpp:74-116).  A stencil
+ * entry that lies across several IBCs moves to each of their DOF columns, as
+ * MoveToIBCColumns keeps it (src/IBCMatrixManipulations.cpp:189-216).
+ * CPM_ERR_UNSUPPORTED for IBCs of different boundary orders in one set (the
+ * reference's identity-row numbering has no place for an order-1 IBC's rows once
+ * another IBC is of order 2). */
 int cpm_opset_create(cpm_tube_t t, int32_t n_ibc, const cpm_surface_desc *ibcs, cpm_opset_t *out);
 
 /* Closest points computed by the caller: n query points x (3n), their closest
@@ -214,7 +219,8 @@ int cpm_opset_export_csr(cpm_opset_t op, int32_t which, int64_t *nnz, int64_t *p
  * xp[3i..3i+2] its 64 interpolation entries cols[64i..], vals[64i..] in the
  * operator's column layout, the stencil nodes that lie across an IBC from the
  * point moved to that IBC's DOF columns.  u(xp_i) = sum_e vals[64i+e] x[cols[64i+e]].
- * CPM_ERR_BASEPOINT_OUTSIDE_TUBE if a stencil leaves the tube. */
+ * CPM_ERR_BASEPOINT_OUTSIDE_TUBE if a stencil leaves the tube; CPM_ERR_UNSUPPORTED if
+ * an entry lies across two IBCs (it would need a 65th entry). */
 int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp, int64_t *cols, double *vals);
 
 /* The operator of the nearest-node baselines (PoissonWithIBCNearest,

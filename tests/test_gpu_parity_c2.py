@@ -1,6 +1,7 @@
 """Parity with the oracle at the size of the two-circle Laplace configuration
 (unit sphere, Dirichlet circles z = 0.3 and z = -0.5, dx = 0.025: 166,390 tube
-nodes, 215,662 rows) and on the Neumann IBC rows.
+nodes, 215,662 rows), and on the reference's other IBC options: Neumann rows,
+oriented curves, and curves close enough that a stencil entry moves to both.
 
 "Given the same closest points" means: the tube is built from the oracle's
 closest points (cpm_tube_build_from_cp), and the IBC build takes the oracle's
@@ -279,3 +280,84 @@ def test_ibc_direction_options_rows_bit_exact(gpu, oracle, option):
     assert O.D == P.D and O.total_ibc_dofs == P.total_ibc_dofs
     for which in (0, 1):
         assert_rows_bit_exact(P, O, gr, which)
+
+
+# ---- IBCs close enough that one stencil entry lies across both: MoveToIBCColumns
+# (src/IBCMatrixManipulations.cpp:189-216) keeps one copy of the entry for every IBC
+# whose tag crosses it, each in that IBC's DOF column.  The circles z = 0.3 and
+# z = 0.3 + gap on the unit sphere; gap < dx also doubles L entries.
+
+def _close_circles(mod, dx, gap, order):
+    zs = (0.3, 0.3 + gap)
+    if hasattr(mod, "circle3d_desc"):
+        return [mod.circle3d_desc(math.sqrt(1 - z * z), (0, 0, z), (0, 0, 1), dx, boundary_order=order) for z in zs]
+    return [mod.desc(mod.CIRCLE3D, [math.sqrt(1 - z * z), 0, 0, z, 0, 0, 1], (-1.0, 1.0), boundary_order=order,
+                     on_ibc_tolerance=0.1 * dx * dx) for z in zs]
+
+
+def _close_pair(gpu, oracle, dx, gap, order):
+    return same_cp_pair(gpu, oracle, dx, _close_circles(oracle, dx, gap, order), _close_circles(gpu, dx, gap, order))
+
+
+@pytest.mark.parametrize("dx,gap,order", [(0.05, 0.06, 2), (0.05, 0.04, 2), (0.05, 0.04, 1), (0.1, 0.08, 2)])
+def test_close_circles_rows_bit_exact(gpu, oracle, dx, gap, order):
+    P, T, O, gr = _close_pair(gpu, oracle, dx, gap, order)
+    assert (np.diff(P.csr(1)[0])[:P.N] > 64).any()  # E entries that move to both circles
+    assert (np.diff(P.csr(0)[0])[:P.N] > 7).any() == (gap < dx)  # and L entries
+    assert O.D == P.D and O.total_ibc_dofs == P.total_ibc_dofs and O.num2 == P.num2
+    rr, gg = P.rows(), O.rows()
+    for k in ("identity", "kind", "ibc"):
+        assert np.array_equal(rr[k], gg[k][gr]), k
+    for which in (0, 1):
+        assert_rows_bit_exact(P, O, gr, which)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_close_circles_applies_and_solves_match_oracle(gpu, oracle, order):
+    """The operator with doubled E and L entries: the FP64 apply (1 and 32 slots)
+    within 1e-13 of the oracle's, the FP32 32-slot apply within 1e-5; Laplace with
+    a value per circle: the plain FP64 solve within 1e-10 of the oracle's (both to
+    tol 1e-12), the 32-slot mixed-precision solves within 1e-8."""
+    import torch
+
+    dx, gap = 0.05, 0.04
+    P, T, O, gr = _close_pair(gpu, oracle, dx, gap, order)
+    rng = np.random.default_rng(12)
+    x = rng.standard_normal(P.D)
+    xg = np.empty(O.D)
+    xg[gr] = x
+    for m, n in ((1.0, -0.1 * dx), (0.0, -1.0)):
+        assert _rel_inf(O.apply(m, n, xg)[0][gr], P.apply(m, n, x)) <= 1e-13
+    X = rng.uniform(-1, 1, (32, P.D))
+    Xg = np.empty((O.D, 32))
+    Xg[gr] = X.T
+    x64 = torch.from_numpy(Xg).cuda()
+    t64, y64 = torch.empty_like(x64), torch.empty_like(x64)
+    x32 = x64.float()
+    t32, y32 = torch.empty_like(x32), torch.empty_like(x32)
+    torch.cuda.synchronize()
+    O.apply_device(0.0, -1.0, 32, False, x64.data_ptr(), t64.data_ptr(), y64.data_ptr())
+    O.apply_device(0.0, -1.0, 32, True, x32.data_ptr(), t32.data_ptr(), y32.data_ptr())
+    gpu.sync()
+    Y64, Y32 = y64.cpu().numpy(), y32.cpu().double().numpy()
+    for k in (0, 17, 31):
+        assert _rel_inf(Y64[gr, k], P.apply(0.0, -1.0, X[k])) <= 1e-13
+    assert _rel_inf(Y32, Y64) <= 1e-5
+    rows = P.rows()
+    vals = rng.uniform(0, 1, (32, 2))
+
+    def rhs(v):
+        return S.build_rhs(rows, lambda p: np.zeros(len(p)), lambda c, p: np.full(len(p), v[c]))
+
+    B = np.stack([rhs(v) for v in vals])
+    Bg = np.empty((32, O.D))
+    Bg[:, gr] = B
+    x_ref, _ = P.solve(0.0, -1.0, B[0], tol=FP64_SOLVE_TOL)
+    x1, st = gpu.Solver(O, 0.0, -1.0).solve(Bg[0], tol=FP64_SOLVE_TOL, precision=0)
+    assert st[0]["status"] == 0
+    assert _rel_inf(x1[0][gr], x_ref) <= FP64_PARITY
+    Xm, stm = gpu.Solver(O, 0.0, -1.0, kslots=32).solve(Bg, precision=1)
+    assert all(s_["status"] == 0 for s_ in stm), stm
+    for k in (0, 31):
+        xr = x_ref if k == 0 else P.solve(0.0, -1.0, B[k], tol=FP64_SOLVE_TOL)[0]
+        assert _rel_inf(Xm[k][gr], xr) <= 1e-8
