@@ -2158,9 +2158,15 @@ extern "C" int cpm_opset_destroy(cpm_opset_t o) {
 // the stencil nodes that lie across an IBC from the point moved to that IBC's
 // DOF columns, as the operator's E rows are.  The IBC subsets are derived again
 // from the stored descriptions (this is a post-processing query, not a solve).
-extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp, int64_t *cols, double *vals) {
-    if (!op || n < 0 || (n > 0 && (!xp || !cols || !vals))) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
-    if (n == 0) return 0;
+// the evaluation rows: per point its 64 (column, value) entries with the moves
+// applied, and the further copies of entries that lie across several IBCs as
+// (point, column, value) extras in point and stencil order
+struct PlotExtras {
+    std::vector<int64_t> row, col;
+    std::vector<double> val;
+};
+
+static int plot_interp_rows(cpm_opset_t op, int64_t n, const double *xp, int64_t *cols, double *vals, PlotExtras &ex) {
     CPM_TRY(cpm_interp_query(op->tube, n, xp, cols, vals));
     for (int64_t e = 0; e < 64 * n; ++e)
         if (cols[e] < 0) return fail(CPM_ERR_BASEPOINT_OUTSIDE_TUBE, "plot interpolation stencil leaves the tube");
@@ -2249,18 +2255,59 @@ extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp
         for (int e = 0; e < 64; ++e) {
             const int col = (int)cols[64 * i + e];
             int hits = 0;
-            int64_t tgt = -1;
             for (int c = 0; c < n_ibc; ++c) {
                 const int64_t si = sub[c][i];
                 if (si < 0) continue;
                 if (tagged(ibs[c], &dirs[c][3 * si], col, 1.0) && ibs[c].dof_sub[col] >= 0) {
-                    ++hits;
-                    tgt = op->col_start[c] + ibs[c].dof_sub[col];
+                    const int64_t tgt = op->col_start[c] + ibs[c].dof_sub[col];
+                    if (hits++ == 0) {
+                        cols[64 * i + e] = tgt;
+                    } else {  // MoveToIBCColumns: one copy of the entry per IBC
+                        ex.row.push_back(i);
+                        ex.col.push_back(tgt);
+                        ex.val.push_back(vals[64 * i + e]);
+                    }
                 }
             }
-            if (hits > 1) return fail(CPM_ERR_UNSUPPORTED, "an evaluation stencil entry lies across two IBCs (64 entries per point)");
-            if (hits == 1) cols[64 * i + e] = tgt;
         }
+    return 0;
+}
+
+extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp, int64_t *cols, double *vals) {
+    if (!op || n < 0 || (n > 0 && (!xp || !cols || !vals))) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
+    if (n == 0) return 0;
+    PlotExtras ex;
+    CPM_TRY(plot_interp_rows(op, n, xp, cols, vals, ex));
+    if (!ex.row.empty())
+        return fail(CPM_ERR_UNSUPPORTED, "an evaluation stencil entry lies across two IBCs: use cpm_opset_plot_interp_csr");
+    return 0;
+}
+
+// the same rows as CSR: each point's 64 entries, then its extra copies
+extern "C" int cpm_opset_plot_interp_csr(cpm_opset_t op, int64_t n, const double *xp, int64_t *nnz, int64_t *ptr,
+                                         int64_t *cols, double *vals) {
+    if (!op || n < 0 || !nnz || (n > 0 && !xp) || (ptr && (!cols || !vals)))
+        return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
+    std::vector<int64_t> c64(64 * (size_t)n);
+    std::vector<double> v64(64 * (size_t)n);
+    PlotExtras ex;
+    if (n > 0) CPM_TRY(plot_interp_rows(op, n, xp, c64.data(), v64.data(), ex));
+    *nnz = 64 * n + (int64_t)ex.row.size();
+    if (!ptr) return 0;
+    size_t x = 0;
+    int64_t k = 0;
+    ptr[0] = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        for (int e = 0; e < 64; ++e, ++k) {
+            cols[k] = c64[64 * i + e];
+            vals[k] = v64[64 * i + e];
+        }
+        for (; x < ex.row.size() && ex.row[x] == i; ++x, ++k) {
+            cols[k] = ex.col[x];
+            vals[k] = ex.val[x];
+        }
+        ptr[i + 1] = k;
+    }
     return 0;
 }
 

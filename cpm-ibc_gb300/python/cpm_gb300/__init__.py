@@ -173,6 +173,7 @@ def lib():
         L.cpm_opset_ibc_export.argtypes = [vp, ctypes.c_int32, vp, vp, vp]
         L.cpm_opset_export_csr.argtypes = [vp, ctypes.c_int32, vp, vp, vp, vp]
         L.cpm_opset_plot_interp.argtypes = [vp, ctypes.c_int64, vp, vp, vp]
+        L.cpm_opset_plot_interp_csr.argtypes = [vp, ctypes.c_int64, vp, vp, vp, vp, vp]
         L.cpm_explicit_step.argtypes = [vp, ctypes.c_double, ctypes.c_int32, vp, vp]
         L.cpm_gray_scott_step.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp, vp]
         L.cpm_opset_destroy.argtypes = [vp]
@@ -373,10 +374,24 @@ class OpSet:
         _check(lib().cpm_gray_scott_step(self.h, dt, F, k, _p(u), _p(v)))
         return u, v
 
+    def plot_interp_csr(self, xp):
+        """The evaluation rows as CSR (ptr, cols, vals): each point's 64 entries, then the
+        further copies of entries that lie across several IBCs."""
+        xp = np.ascontiguousarray(xp, np.float64)
+        n = xp.shape[0]
+        nnz = ctypes.c_int64(0)
+        _check(lib().cpm_opset_plot_interp_csr(self.h, n, _p(xp), ctypes.byref(nnz), None, None, None))
+        ptr = np.zeros(n + 1, np.int64)
+        cols = np.zeros(nnz.value, np.int64)
+        vals = np.zeros(nnz.value)
+        _check(lib().cpm_opset_plot_interp_csr(self.h, n, _p(xp), ctypes.byref(nnz), _p(ptr), _p(cols), _p(vals)))
+        return ptr, cols, vals
+
     def evaluate(self, x, xp):
         """u at evaluation points xp from a solution x on the operator's rows"""
-        cols, vals = self.plot_interp(xp)
-        return np.einsum("pe,pe->p", vals, np.asarray(x, np.float64)[cols])
+        ptr, cols, vals = self.plot_interp_csr(xp)
+        prod = vals * np.asarray(x, np.float64)[cols]
+        return np.add.reduceat(prod, ptr[:-1]) if len(prod) else np.zeros(len(ptr) - 1)
 
     def apply(self, m, n, x):
         """Solver::Multiply (src/Solver.cpp:122-138); x: (D,) or (k, D)."""

@@ -223,6 +223,13 @@ int cpm_opset_export_csr(cpm_opset_t op, int32_t which, int64_t *nnz, int64_t *p
  * an entry lies across two IBCs (it would need a 65th entry). */
 int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp, int64_t *cols, double *vals);
 
+/* The same evaluation rows as CSR (ptr: n + 1): each point's 64 entries, then one more
+ * copy of every entry that lies across several IBCs for each further IBC, in that IBC's
+ * DOF column (MoveToIBCColumns keeps one copy per IBC, src/IBCMatrixManipulations.cpp:189-216).
+ * nnz query with ptr = NULL. */
+int cpm_opset_plot_interp_csr(cpm_opset_t op, int64_t n, const double *xp, int64_t *nnz, int64_t *ptr, int64_t *cols,
+                              double *vals);
+
 /* The operator of the nearest-node baselines (PoissonWithIBCNearest,
  * problems/PoissonWithIBCNearest.cpp:73-89): the tube's plain L and E with
  * identity rows (Dirichlet values) at the n_rows given tube rows (device

@@ -399,13 +399,15 @@ class SystemOperator {
         std::vector<Scalar> pts(3 * (size_t)n);
         for (size_t i = 0; i < xp.size(); ++i)
             for (int k = 0; k < 3; ++k) pts[3 * i + (size_t)k] = xp[i][(size_t)k];
-        std::vector<int64_t> cols(64 * (size_t)n);
-        std::vector<Scalar> vals(64 * (size_t)n);
-        check(cpm_opset_plot_interp(h_.get(), n, pts.data(), cols.data(), vals.data()));
+        int64_t nnz = 0;
+        check(cpm_opset_plot_interp_csr(h_.get(), n, pts.data(), &nnz, nullptr, nullptr, nullptr));
+        std::vector<int64_t> ptr((size_t)n + 1), cols((size_t)nnz);
+        std::vector<Scalar> vals((size_t)nnz);
+        check(cpm_opset_plot_interp_csr(h_.get(), n, pts.data(), &nnz, ptr.data(), cols.data(), vals.data()));
         const VectorX ud = to_device(u);
         VectorX out((size_t)n, 0.0);
         for (size_t i = 0; i < (size_t)n; ++i)
-            for (size_t e = 0; e < 64; ++e) out[i] += vals[64 * i + e] * ud[(size_t)cols[64 * i + e]];
+            for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) out[i] += vals[(size_t)e] * ud[(size_t)cols[(size_t)e]];
         return out;
     }
 

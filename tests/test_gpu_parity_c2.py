@@ -361,3 +361,29 @@ def test_close_circles_applies_and_solves_match_oracle(gpu, oracle, order):
     for k in (0, 31):
         xr = x_ref if k == 0 else P.solve(0.0, -1.0, B[k], tol=FP64_SOLVE_TOL)[0]
         assert _rel_inf(Xm[k][gr], xr) <= 1e-8
+
+
+def test_close_circles_evaluation_rows_match_oracle(gpu, oracle):
+    """Evaluation rows (GetPlotInterpMatrix + AddIBCPlotInterpolation) at the
+    sphere's plot points: the CSR query carries the doubled entries (points with
+    more than 64), with the oracle's columns and values within 1e-14; the fixed
+    64-entry query refuses these points."""
+    dx, gap = 0.05, 0.04
+    P, T, O, gr = _close_pair(gpu, oracle, dx, gap, 2)
+    ref_of_g = np.empty(O.D, np.int64)
+    ref_of_g[gr] = np.arange(O.D)
+    xp = P.xp()
+    rp, ri, rv = P.csr(4)
+    ptr, cols, vals = O.plot_interp_csr(xp)
+    assert (np.diff(rp) > 64).sum() == (np.diff(ptr) > 64).sum() > 0
+    a = _csr_triplets(rp, ri, rv)
+    b = _csr_triplets(ptr, cols, vals, col_map=ref_of_g)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.all(np.abs(a[2] - b[2]) <= 1e-14 * np.maximum(1.0, np.abs(a[2])))
+    with pytest.raises(RuntimeError):
+        O.plot_interp(xp)
+    keep = np.diff(ptr) == 64  # points with no doubled entry: the two queries agree
+    c64, v64 = O.plot_interp(xp[keep][:500])
+    sel = np.flatnonzero(keep)[:500]
+    assert np.array_equal(c64, cols[ptr[sel][:, None] + np.arange(64)])
+    assert np.array_equal(v64, vals[ptr[sel][:, None] + np.arange(64)])
