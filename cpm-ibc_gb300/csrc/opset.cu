@@ -2286,14 +2286,14 @@ extern "C" int cpm_opset_plot_interp(cpm_opset_t op, int64_t n, const double *xp
 // the same rows as CSR: each point's 64 entries, then its extra copies
 extern "C" int cpm_opset_plot_interp_csr(cpm_opset_t op, int64_t n, const double *xp, int64_t *nnz, int64_t *ptr,
                                          int64_t *cols, double *vals) {
-    if (!op || n < 0 || !nnz || (n > 0 && !xp) || (ptr && (!cols || !vals)))
-        return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
+    if (!op || n < 0 || !nnz || (n > 0 && !xp)) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
     std::vector<int64_t> c64(64 * (size_t)n);
     std::vector<double> v64(64 * (size_t)n);
     PlotExtras ex;
     if (n > 0) CPM_TRY(plot_interp_rows(op, n, xp, c64.data(), v64.data(), ex));
     *nnz = 64 * n + (int64_t)ex.row.size();
     if (!ptr) return 0;
+    if (*nnz > 0 && (!cols || !vals)) return fail(CPM_ERR_INVALID_ARG, "invalid arguments");
     size_t x = 0;
     int64_t k = 0;
     ptr[0] = 0;
