@@ -387,3 +387,22 @@ def test_close_circles_evaluation_rows_match_oracle(gpu, oracle):
     sel = np.flatnonzero(keep)[:500]
     assert np.array_equal(c64, cols[ptr[sel][:, None] + np.arange(64)])
     assert np.array_equal(v64, vals[ptr[sel][:, None] + np.arange(64)])
+
+
+@pytest.mark.parametrize("scale", [0.6, 1.5])
+def test_dof_radius_scale_rows_bit_exact(gpu, oracle, scale):
+    """IBCMetaData::ibc_DOFSubset_radius_scale (src/IBCDOFSubset.cpp:20,44): the DOF subset is
+    the tagged nodes within scale * r of the curve; subsets and every Lfull / Efull row equal
+    the oracle's."""
+    dx = 0.05
+    oi, gi = two_circle_ibcs(oracle, dx), two_circle_ibcs(gpu, dx)
+    for d in oi + gi:
+        d.dof_radius_scale = scale
+    P, T, O, gr = same_cp_pair(gpu, oracle, dx, oi, gi)
+    ref, g = P.tube(), T.export()
+    assert O.D == P.D and O.total_ibc_dofs == P.total_ibc_dofs and O.num2 == P.num2
+    for c in range(2):
+        rs, gs = P.ibc_subsets(c), O.ibc_subsets(c)
+        assert np.array_equal(g["rec"][gs["dof_set"]], ref["rec"][rs["dof_set"]])
+    for which in (0, 1):
+        assert_rows_bit_exact(P, O, gr, which)
