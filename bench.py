@@ -6,9 +6,10 @@ circles z = 0.3 and z = -0.5, dx = 0.025 (~166k tube nodes, 215,662 rows with
 the IBC DOF and Dirichlet value rows), tricubic extension, 2nd-order IBCs.
 Requests are right-hand sides with random circle values U[0,1] (seeded).
 
-A step is 32 requests served by the continuous-batching server: FP32
-BiCGStab inside FP64 iterative refinement to ||b - A x|| <= 1e-10 ||b||
-(the reference's relative residual), slots refilled as solves finish.
+A step is 64 requests served by the continuous-batching server over two
+32-slot batches on their own streams (--batches): FP32 BiCGStab inside FP64
+iterative refinement to ||b - A x|| <= 1e-10 ||b|| (the reference's relative
+residual), slots refilled as solves finish.
 `value` is solves/s with every right-hand side resident in HBM (CUDA events on
 the library stream).  Reported beside it: the plain FP64 one-request-at-a-time
 GPU path (the reference algorithm on the device), latencies, the error against
@@ -468,7 +469,8 @@ def main():
     ap.add_argument("--sources", type=int, default=32, help="torus-geodesic: sources of the batched run")
     ap.add_argument("--solo", type=int, default=2, help="torus-geodesic: sources also run one at a time")
     ap.add_argument("--rate", type=float, default=8.0, help="serving-mix: mean arrivals per second")
-    ap.add_argument("--batches", type=int, default=1, help="32-slot batches of the server, run concurrently")
+    ap.add_argument("--batches", type=int, default=2,
+                    help="32-slot batches of the server, run concurrently on their own streams")
     ap.add_argument("--mix-requests", type=int, default=256,
                     help="requests of the serving-stream sample in the default line (0: none)")
     ap.add_argument("--mix-rate", type=float, default=4.0, help="its mean arrivals per second")

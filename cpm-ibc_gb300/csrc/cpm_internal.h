@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <string>
 #include <vector>
@@ -98,6 +99,38 @@ struct DBuf {
         CPM_CUDA_TRY(cudaStreamSynchronize(stream()));
         return 0;
     }
+};
+
+// Host array in page-locked memory.  A device-to-host cudaMemcpyAsync into
+// pageable memory returns only once the copy (and so all earlier work on its
+// stream) is done; into a PinnedArray it is queued like any other stream work.
+template <class T>
+struct PinnedArray {
+    T *p = nullptr;
+    size_t n = 0;
+    PinnedArray() = default;
+    PinnedArray(const PinnedArray &) = delete;
+    PinnedArray &operator=(const PinnedArray &) = delete;
+    ~PinnedArray() {
+        if (p) cudaFreeHost(p);
+    }
+    int alloc(size_t count) {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMallocHost((void **)&p, (count ? count : 1) * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(CPM_ERR_OOM, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+        }
+        n = count;
+        memset(p, 0, (count ? count : 1) * sizeof(T));
+        return 0;
+    }
+    T *data() { return p; }
+    const T *data() const { return p; }
+    T &operator[](size_t i) { return p[i]; }
+    const T &operator[](size_t i) const { return p[i]; }
 };
 
 // ---------------------------------------------------------------- geometry

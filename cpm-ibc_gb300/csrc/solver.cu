@@ -1426,7 +1426,7 @@ struct cpm_solver_s {
     int64_t D = 0;
     int G = 1;
     DBuf<Slot> slots;
-    std::vector<Slot> h_slots;
+    PinnedArray<Slot> h_slots;  // pinned: the slot read-back after a graph does not block the host
     DBuf<double> partial;
     DBuf<unsigned int> counter;
     // FP64 Krylov vectors (plain path) and FP64 refinement state (mixed path)
@@ -1836,13 +1836,12 @@ extern "C" int cpm_solver_create(cpm_opset_t op, double m, double n, int32_t ksl
     s->K = (kslots == 1) ? 1 : 32;
     s->D = op->D;
     s->G = row_grid(s->D, s->K);
-    s->h_slots.assign(s->K, Slot());
     auto bail = [&](int rc) {
         delete s;
         return rc;
     };
     int rc;
-    if ((rc = s->slots.alloc(s->K)) || (rc = s->partial.alloc((size_t)(s->G + reduce_groups(s->G)) * s->K * 2)) ||
+    if ((rc = s->h_slots.alloc(s->K)) || (rc = s->slots.alloc(s->K)) || (rc = s->partial.alloc((size_t)(s->G + reduce_groups(s->G)) * s->K * 2)) ||
         (rc = s->counter.alloc((size_t)(1 + reduce_groups(s->G)))) ||
         (rc = s->counter.zero()) || (rc = s->b64.alloc((size_t)s->D * s->K)) || (rc = s->x64.alloc((size_t)s->D * s->K)) ||
         (rc = s->r64.alloc((size_t)s->D * s->K)) || (rc = s->te64.alloc((size_t)s->D * s->K)) || (rc = s->pden64.alloc(s->D)))
