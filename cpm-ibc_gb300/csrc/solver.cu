@@ -1916,19 +1916,27 @@ struct cpm_server_s {
     };
     struct Done {
         int64_t tag;
-        std::vector<double> x;
+        std::vector<double> x;          // the solution, once moved out of the result columns
+        const double *pend = nullptr;   // or still in batch pb's pinned result column
+        int pb = -1;
         cpm_solve_stats st;
         double latency;
     };
     std::deque<Req> queue;
     std::vector<Busy> busy;     // 32 per solver
     std::deque<Done> done;
-    double *h_stage = nullptr;  // pinned, [32 nb][D]: one staging column per slot
+    double *h_stage = nullptr;  // pinned, [32 nb][D]: one right-hand-side staging column per slot
+    double *h_res = nullptr;    // pinned, [32 nb][D]: one result column per slot
     DBuf<double> d_stage;       // device, [32 nb][D]
+    std::vector<char> inflight;         // per batch: launched, not yet harvested
+    std::vector<cudaEvent_t> res_ev;    // per batch: its last harvest's copies are done
     ~cpm_server_s() {
         for (auto *s : solvers)
             if (s) cudaStreamSynchronize(s->own);
         if (h_stage) cudaFreeHost(h_stage);
+        if (h_res) cudaFreeHost(h_res);
+        for (cudaEvent_t e : res_ev)
+            if (e) cudaEventDestroy(e);
         for (auto *s : solvers) delete s;
         delete fallback;
     }
@@ -1952,8 +1960,14 @@ static int server_create(cpm_opset_t op, double m, double n, const cpm_solve_opt
     for (int b = 0; b < nb && !rc; ++b) rc = cpm_solver_create(op, m, n, 32, &sv->solvers[b]);
     if (rc) return bail(rc);
     const int64_t D = op->D;
-    if (cudaMallocHost((void **)&sv->h_stage, sizeof(double) * 32 * nb * (size_t)D) != cudaSuccess)
+    if (cudaMallocHost((void **)&sv->h_stage, sizeof(double) * 32 * nb * (size_t)D) != cudaSuccess ||
+        cudaMallocHost((void **)&sv->h_res, sizeof(double) * 32 * nb * (size_t)D) != cudaSuccess)
         return bail(fail(CPM_ERR_OOM, "server_create: pinned staging"));
+    sv->inflight.assign(nb, 0);
+    sv->res_ev.assign(nb, nullptr);
+    for (int b = 0; b < nb; ++b)
+        if (cudaEventCreateWithFlags(&sv->res_ev[b], cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(CPM_ERR_CUDA, "server_create: event"));
     if ((rc = sv->d_stage.alloc(32 * nb * (size_t)D))) return bail(rc);
     sv->busy.assign(32 * nb, cpm_server_s::Busy());
     for (cpm_solver_s *s : sv->solvers) {
@@ -2002,138 +2016,192 @@ extern "C" int cpm_server_submit_device(cpm_server_t sv, const void *b_dev, void
     return 0;
 }
 
-extern "C" int cpm_server_step(cpm_server_t sv, int32_t *active, int32_t *queued, int32_t *finished) {
-    if (!sv) return fail(CPM_ERR_INVALID_ARG, "server_step: null server");
-    const int nb = (int)sv->solvers.size();
+// admit queued requests into batch b's free slots, start them and launch its
+// iteration graph (when any slot is busy) and the read-back of its slot states,
+// all on the batch's stream without waiting
+static int server_launch(cpm_server_t sv, int b) {
     const int64_t D = sv->solvers[0]->D;
-    // admit queued requests into free slots, then start them and launch every busy
-    // solver's iteration graph, each on its own stream
-    for (int b = 0; b < nb; ++b) {
-        cpm_solver_s *s = sv->solvers[b];
-        SolverScope sc(s);
-        cudaStream_t st = stream();
-        bool admitted = false;
-        for (int j = 0; j < 32 && !sv->queue.empty(); ++j) {
-            cpm_server_s::Busy &bz = sv->busy[32 * b + j];
-            if (bz.used) continue;
-            cpm_server_s::Req r = std::move(sv->queue.front());
-            sv->queue.pop_front();
-            double *hs = sv->h_stage + (size_t)(32 * b + j) * D, *ds = sv->d_stage.p + (size_t)(32 * b + j) * D;
-            const double *src = r.b_dev;
-            if (!src) {
-                memcpy(hs, r.b.data(), sizeof(double) * D);
-                CPM_CUDA_TRY(cudaMemcpyAsync(ds, hs, sizeof(double) * D, cudaMemcpyHostToDevice, st));
-                src = ds;
-            }
-            k_scatter_col<<<nblk(D), BS, 0, st>>>(D, 32, j, src, s->b64.p);
+    cpm_solver_s *s = sv->solvers[b];
+    SolverScope sc(s);
+    cudaStream_t st = stream();
+    bool admitted = false;
+    for (int j = 0; j < 32 && !sv->queue.empty(); ++j) {
+        cpm_server_s::Busy &bz = sv->busy[32 * b + j];
+        if (bz.used) continue;
+        cpm_server_s::Req r = std::move(sv->queue.front());
+        sv->queue.pop_front();
+        double *hs = sv->h_stage + (size_t)(32 * b + j) * D, *ds = sv->d_stage.p + (size_t)(32 * b + j) * D;
+        const double *src = r.b_dev;
+        if (!src) {
+            memcpy(hs, r.b.data(), sizeof(double) * D);
+            CPM_CUDA_TRY(cudaMemcpyAsync(ds, hs, sizeof(double) * D, cudaMemcpyHostToDevice, st));
+            src = ds;
+        }
+        k_scatter_col<<<nblk(D), BS, 0, st>>>(D, 32, j, src, s->b64.p);
+        count_launches(1);
+        memset(&s->h_slots[j], 0, sizeof(Slot));
+        s->h_slots[j].phase = PH_START;
+        CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p + j, &s->h_slots[j], sizeof(Slot), cudaMemcpyHostToDevice, st));
+        bz.used = true;
+        bz.tag = r.tag;
+        bz.x_dev = r.x_dev;
+        bz.t_submit = r.t_submit;
+        bz.t_admit = std::chrono::steady_clock::now();
+        admitted = true;
+    }
+    if (admitted) {
+        if (sv->P.mixed) {
+            mixed_start<32>(s, sv->P);
+        } else {
+            k_init<double, 32><<<s->G, BS, 0, st>>>(s->op->view<double>(), s->slots.p, sv->P, PH_START, s->b64.p, s->x64.p,
+                                                    s->dr.p, s->dr0.p, s->dp.p, s->dv.p, s->partial.p, s->counter.p);
             count_launches(1);
-            memset(&s->h_slots[j], 0, sizeof(Slot));
-            s->h_slots[j].phase = PH_START;
-            CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p + j, &s->h_slots[j], sizeof(Slot), cudaMemcpyHostToDevice, st));
-            bz.used = true;
-            bz.tag = r.tag;
-            bz.x_dev = r.x_dev;
-            bz.t_submit = r.t_submit;
-            bz.t_admit = std::chrono::steady_clock::now();
-            admitted = true;
-        }
-        if (admitted) {
-            if (sv->P.mixed) {
-                mixed_start<32>(s, sv->P);
-            } else {
-                k_init<double, 32><<<s->G, BS, 0, st>>>(s->op->view<double>(), s->slots.p, sv->P, PH_START, s->b64.p, s->x64.p,
-                                                        s->dr.p, s->dr0.p, s->dp.p, s->dv.p, s->partial.p, s->counter.p);
-                count_launches(1);
-            }
-        }
-        int n_busy = 0;
-        for (int j = 0; j < 32; ++j) n_busy += sv->busy[32 * b + j].used;
-        if (n_busy) {
-            cudaGraphExec_t g = nullptr;
-            CPM_TRY(prepare_graph<32>(s, sv->P, &g));
-            CPM_CUDA_TRY(cudaGraphLaunch(g, st));
-            count_launches(graph_launches(s, sv->P));
-        }
-        CPM_CUDA_TRY(cudaMemcpyAsync(s->h_slots.data(), s->slots.p, sizeof(Slot) * 32, cudaMemcpyDeviceToHost, st));
-    }
-    int n_fin = 0;
-    for (int b = 0; b < nb; ++b) {
-        cpm_solver_s *s = sv->solvers[b];
-        SolverScope sc(s);
-        cudaStream_t st = stream();
-        CPM_CUDA_TRY(cudaStreamSynchronize(st));
-        if (!sv->P.mixed) {  // the plain path's restarts run between graphs (as in run_solve)
-            bool restart = false;
-            for (int j = 0; j < 32; ++j) restart = restart || s->h_slots[j].phase == PH_RESTART;
-            if (restart) {
-                plain_restart<32>(s);
-                count_launches(2);
-                CPM_CUDA_TRY(cudaGetLastError());
-            }
-        }
-        // harvest finished slots
-        std::vector<int> fin;
-        std::vector<cpm_solve_stats> fb_st(32);
-        std::vector<char> fb(32, 0);
-        for (int j = 0; j < 32; ++j) {
-            const Slot &S = s->h_slots[j];
-            cpm_server_s::Busy &bz = sv->busy[32 * b + j];
-            if (!bz.used) continue;
-            const bool over = S.phase == PH_DONE || S.iters >= sv->P.max_iters || S.refinements >= sv->P.max_refine;
-            if (!over) continue;
-            double *ds = bz.x_dev ? bz.x_dev : sv->d_stage.p + (size_t)(32 * b + j) * D;
-            if (S.phase == PH_DONE && (S.status == 0 || !sv->P.mixed)) {
-                k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->x64.p, ds);
-                count_launches(1);
-            } else {
-                // the FP32 inner iteration could not solve this right-hand side:
-                // solve it again with the plain FP64 path (one slot, blocking)
-                if (!sv->fallback) CPM_TRY(cpm_solver_create(s->op, s->m, s->n, 1, &sv->fallback));
-                double *bj = sv->d_stage.p + (size_t)(32 * b + j) * D;
-                k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->b64.p, bj);
-                count_launches(1);
-                cpm_solve_opts o64 = sv->opts;
-                o64.precision = 0;
-                CPM_TRY(cpm_solve_device(sv->fallback, 1, bj, ds, &o64, &fb_st[j]));
-                fb[j] = 1;
-            }
-            if (!bz.x_dev)
-                CPM_CUDA_TRY(cudaMemcpyAsync(sv->h_stage + (size_t)(32 * b + j) * D, ds, sizeof(double) * D,
-                                             cudaMemcpyDeviceToHost, st));
-            fin.push_back(j);
-        }
-        if (!fin.empty()) {
-            CPM_CUDA_TRY(cudaStreamSynchronize(st));
-            const auto now = std::chrono::steady_clock::now();
-            for (int j : fin) {
-                cpm_server_s::Busy &bz = sv->busy[32 * b + j];
-                cpm_server_s::Done d;
-                d.tag = bz.tag;
-                if (!bz.x_dev)
-                    d.x.assign(sv->h_stage + (size_t)(32 * b + j) * D, sv->h_stage + (size_t)(32 * b + j + 1) * D);
-                slot_stats(s->h_slots[j], sv->P.mixed != 0, 0.0f, &d.st);
-                if (fb[j]) {
-                    const int it = d.st.iterations, rf = d.st.refinements;
-                    d.st = fb_st[j];
-                    d.st.iterations += it;
-                    d.st.refinements = rf;
-                    d.st.fp64_fallback = 1;
-                }
-                d.latency = std::chrono::duration<double>(now - bz.t_submit).count();
-                d.st.seconds = std::chrono::duration<double>(now - bz.t_admit).count();
-                sv->done.push_back(std::move(d));
-                bz.used = false;
-                s->h_slots[j].phase = PH_IDLE;
-                CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p + j, &s->h_slots[j], sizeof(Slot), cudaMemcpyHostToDevice, st));
-                ++n_fin;
-            }
         }
     }
+    int n_busy = 0;
+    for (int j = 0; j < 32; ++j) n_busy += sv->busy[32 * b + j].used;
+    if (n_busy) {
+        cudaGraphExec_t g = nullptr;
+        CPM_TRY(prepare_graph<32>(s, sv->P, &g));
+        CPM_CUDA_TRY(cudaGraphLaunch(g, st));
+        count_launches(graph_launches(s, sv->P));
+    }
+    CPM_CUDA_TRY(cudaMemcpyAsync(s->h_slots.data(), s->slots.p, sizeof(Slot) * 32, cudaMemcpyDeviceToHost, st));
+    sv->inflight[b] = 1;
+    return 0;
+}
+
+// wait for batch b's last launch and harvest its finished slots: each solution
+// gathered to its device destination, or copied into the batch's pinned result
+// columns (poll copies it out once the batch's result event has passed); the
+// caller's stream is ordered after the gathers.  Results of the batch still
+// unpolled are moved out of those columns first.
+static int server_harvest(cpm_server_t sv, int b, cudaStream_t caller, int *n_fin) {
+    const int64_t D = sv->solvers[0]->D;
+    cpm_solver_s *s = sv->solvers[b];
+    SolverScope sc(s);
+    cudaStream_t st = stream();
+    CPM_CUDA_TRY(cudaStreamSynchronize(st));
+    sv->inflight[b] = 0;
+    for (cpm_server_s::Done &d : sv->done)
+        if (d.pend && d.pb == b) {
+            d.x.assign(d.pend, d.pend + D);
+            d.pend = nullptr;
+        }
+    if (!sv->P.mixed) {  // the plain path's restarts run between graphs (as in run_solve)
+        bool restart = false;
+        for (int j = 0; j < 32; ++j) restart = restart || s->h_slots[j].phase == PH_RESTART;
+        if (restart) {
+            plain_restart<32>(s);
+            count_launches(2);
+            CPM_CUDA_TRY(cudaGetLastError());
+        }
+    }
+    std::vector<int> fin;
+    std::vector<cpm_solve_stats> fb_st(32);
+    std::vector<char> fb(32, 0);
+    for (int j = 0; j < 32; ++j) {
+        const Slot &S = s->h_slots[j];
+        cpm_server_s::Busy &bz = sv->busy[32 * b + j];
+        if (!bz.used) continue;
+        const bool over = S.phase == PH_DONE || S.iters >= sv->P.max_iters || S.refinements >= sv->P.max_refine;
+        if (!over) continue;
+        double *ds = bz.x_dev ? bz.x_dev : sv->d_stage.p + (size_t)(32 * b + j) * D;
+        if (S.phase == PH_DONE && (S.status == 0 || !sv->P.mixed)) {
+            k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->x64.p, ds);
+            count_launches(1);
+        } else {
+            // the FP32 inner iteration could not solve this right-hand side:
+            // solve it again with the plain FP64 path (one slot, blocking)
+            if (!sv->fallback) CPM_TRY(cpm_solver_create(s->op, s->m, s->n, 1, &sv->fallback));
+            double *bj = sv->d_stage.p + (size_t)(32 * b + j) * D;
+            k_gather_col<<<nblk(D), BS, 0, st>>>(D, 32, j, s->b64.p, bj);
+            count_launches(1);
+            cpm_solve_opts o64 = sv->opts;
+            o64.precision = 0;
+            CPM_TRY(cpm_solve_device(sv->fallback, 1, bj, ds, &o64, &fb_st[j]));
+            fb[j] = 1;
+        }
+        if (!bz.x_dev)
+            CPM_CUDA_TRY(cudaMemcpyAsync(sv->h_res + (size_t)(32 * b + j) * D, ds, sizeof(double) * D,
+                                         cudaMemcpyDeviceToHost, st));
+        fin.push_back(j);
+    }
+    if (fin.empty()) return 0;
+    CPM_CUDA_TRY(cudaEventRecord(sv->res_ev[b], st));
+    CPM_CUDA_TRY(cudaStreamWaitEvent(caller, sv->res_ev[b], 0));
+    const auto now = std::chrono::steady_clock::now();
+    for (int j : fin) {
+        cpm_server_s::Busy &bz = sv->busy[32 * b + j];
+        cpm_server_s::Done d;
+        d.tag = bz.tag;
+        if (!bz.x_dev) {
+            d.pend = sv->h_res + (size_t)(32 * b + j) * D;
+            d.pb = b;
+        }
+        slot_stats(s->h_slots[j], sv->P.mixed != 0, 0.0f, &d.st);
+        if (fb[j]) {
+            const int it = d.st.iterations, rf = d.st.refinements;
+            d.st = fb_st[j];
+            d.st.iterations += it;
+            d.st.refinements = rf;
+            d.st.fp64_fallback = 1;
+        }
+        d.latency = std::chrono::duration<double>(now - bz.t_submit).count();
+        d.st.seconds = std::chrono::duration<double>(now - bz.t_admit).count();
+        sv->done.push_back(std::move(d));
+        bz.used = false;
+        s->h_slots[j].phase = PH_IDLE;
+        CPM_CUDA_TRY(cudaMemcpyAsync(s->slots.p + j, &s->h_slots[j], sizeof(Slot), cudaMemcpyHostToDevice, st));
+        ++*n_fin;
+    }
+    return 0;
+}
+
+static void server_counts(cpm_server_t sv, int n_fin, int32_t *active, int32_t *queued, int32_t *finished) {
     int n_busy = 0;
     for (auto &bz : sv->busy) n_busy += bz.used;
     if (active) *active = n_busy;
     if (queued) *queued = (int32_t)sv->queue.size();
     if (finished) *finished = n_fin;
+}
+
+// One round: admit queued requests into free slots, launch every busy batch's
+// iteration graph (each on its own stream, all queued before any is waited for),
+// then wait for them and harvest the finished requests.
+extern "C" int cpm_server_step(cpm_server_t sv, int32_t *active, int32_t *queued, int32_t *finished) {
+    if (!sv) return fail(CPM_ERR_INVALID_ARG, "server_step: null server");
+    const int nb = (int)sv->solvers.size();
+    cudaStream_t caller = stream();
+    int n_fin = 0;
+    for (int b = 0; b < nb; ++b)  // a previous cpm_server_step_async's launches
+        if (sv->inflight[b]) CPM_TRY(server_harvest(sv, b, caller, &n_fin));
+    for (int b = 0; b < nb; ++b) CPM_TRY(server_launch(sv, b));
+    for (int b = 0; b < nb; ++b) CPM_TRY(server_harvest(sv, b, caller, &n_fin));
+    for (int b = 0; b < nb; ++b) CPM_CUDA_TRY(cudaEventSynchronize(sv->res_ev[b]));
+    server_counts(sv, n_fin, active, queued, finished);
+    return 0;
+}
+
+// The same round, pipelined: harvest what the previous call launched, then admit
+// and launch and return without waiting, so the caller's polls (the host copies
+// of the finished solutions) overlap the graphs just launched.  A call that
+// leaves nothing busy waits for its own results, as cpm_server_step does.
+extern "C" int cpm_server_step_async(cpm_server_t sv, int32_t *active, int32_t *queued, int32_t *finished) {
+    if (!sv) return fail(CPM_ERR_INVALID_ARG, "server_step_async: null server");
+    const int nb = (int)sv->solvers.size();
+    cudaStream_t caller = stream();
+    int n_fin = 0;
+    for (int b = 0; b < nb; ++b)
+        if (sv->inflight[b]) CPM_TRY(server_harvest(sv, b, caller, &n_fin));
+    for (int b = 0; b < nb; ++b) CPM_TRY(server_launch(sv, b));
+    int n_busy = 0;
+    for (auto &bz : sv->busy) n_busy += bz.used;
+    if (n_busy == 0 && sv->queue.empty()) {  // idle: nothing left to overlap with
+        for (int b = 0; b < nb; ++b) CPM_TRY(server_harvest(sv, b, caller, &n_fin));
+        for (int b = 0; b < nb; ++b) CPM_CUDA_TRY(cudaEventSynchronize(sv->res_ev[b]));
+    }
+    server_counts(sv, n_fin, active, queued, finished);
     return 0;
 }
 
@@ -2142,7 +2210,12 @@ extern "C" int cpm_server_poll(cpm_server_t sv, int64_t *tag, double *x, cpm_sol
     if (sv->done.empty()) return 0;
     cpm_server_s::Done &d = sv->done.front();
     if (tag) *tag = d.tag;
-    if (x && !d.x.empty()) memcpy(x, d.x.data(), sizeof(double) * d.x.size());
+    if (x && d.pend) {
+        CPM_CUDA_TRY(cudaEventSynchronize(sv->res_ev[d.pb]));
+        memcpy(x, d.pend, sizeof(double) * sv->solvers[0]->D);
+    } else if (x && !d.x.empty()) {
+        memcpy(x, d.x.data(), sizeof(double) * d.x.size());
+    }
     if (stats) *stats = d.st;
     if (latency) *latency = d.latency;
     sv->done.pop_front();

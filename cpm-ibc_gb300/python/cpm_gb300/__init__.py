@@ -194,6 +194,7 @@ def lib():
         L.cpm_server_submit.argtypes = [vp, vp, ctypes.c_int64]
         L.cpm_server_submit_device.argtypes = [vp, vp, vp, ctypes.c_int64]
         L.cpm_server_step.argtypes = [vp, vp, vp, vp]
+        L.cpm_server_step_async.argtypes = [vp, vp, vp, vp]
         L.cpm_server_poll.argtypes = [vp, vp, vp, P(SolveStats), vp]
         L.cpm_server_destroy.argtypes = [vp]
         L.cpm_server_device_bytes.argtypes = [vp]
@@ -627,10 +628,13 @@ class Server:
         """device right-hand side and solution destination (D doubles each)"""
         _check(lib().cpm_server_submit_device(self.h, b_ptr, x_ptr, int(tag)))
 
-    def step(self):
-        """one admission + iteration-graph + harvest round: (active, queued, finished)"""
+    def step(self, pipelined=False):
+        """one admission + iteration-graph + harvest round: (active, queued, finished).
+        pipelined: harvest the previous call's graphs, launch the next ones and return
+        without waiting (cpm_server_step_async)"""
         a, q, f = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
-        _check(lib().cpm_server_step(self.h, ctypes.byref(a), ctypes.byref(q), ctypes.byref(f)))
+        fn = lib().cpm_server_step_async if pipelined else lib().cpm_server_step
+        _check(fn(self.h, ctypes.byref(a), ctypes.byref(q), ctypes.byref(f)))
         return a.value, q.value, f.value
 
     def poll(self, want_x=True):
@@ -649,11 +653,13 @@ class Server:
                                   status=st.status, rel_residual=st.rel_residual, service=st.seconds,
                                   latency=lat.value, fp64_fallback=st.fp64_fallback)
 
-    def drain(self, want_x=True):
-        """step until every submitted request has finished; returns {tag: (x, stats)}"""
+    def drain(self, want_x=True, pipelined=True):
+        """step until every submitted request has finished; returns {tag: (x, stats)}.
+        Pipelined steps (the default) copy each round's results out while the next
+        round's graphs run."""
         out = {}
         while True:
-            a, q, _ = self.step()
+            a, q, _ = self.step(pipelined)
             while True:
                 r = self.poll(want_x)
                 if r is None:

@@ -426,6 +426,14 @@ int cpm_server_create_batches(cpm_opset_t op, double m, double n, const cpm_solv
 int cpm_server_submit(cpm_server_t s, const double *b, int64_t tag);
 int cpm_server_submit_device(cpm_server_t s, const void *b_dev, void *x_dev, int64_t tag);
 int cpm_server_step(cpm_server_t s, int32_t *active, int32_t *queued, int32_t *finished);
+/* step, pipelined: harvests what the previous call launched, then admits and
+ * launches the next graphs and returns without waiting for them, so the caller's
+ * polls (the host copies of the finished solutions) overlap them; a finished
+ * request becomes visible one call later than with cpm_server_step.  A call that
+ * leaves no slot busy and nothing queued waits for its own work.  Device
+ * destinations are written in stream order before the calling thread's later
+ * work on its stream. */
+int cpm_server_step_async(cpm_server_t s, int32_t *active, int32_t *queued, int32_t *finished);
 int cpm_server_poll(cpm_server_t s, int64_t *tag, double *x, cpm_solve_stats *stats, double *latency);
 int cpm_server_destroy(cpm_server_t s);
 int64_t cpm_server_device_bytes(cpm_opset_t op);

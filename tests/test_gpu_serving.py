@@ -121,3 +121,45 @@ def test_server_two_concurrent_batches(gpu, precision):
             assert st["status"] == 0 and st["rel_residual"] <= 1e-10
             got = x if k < 40 else xd[k - 40]
             assert _rel(got, X64[j]) <= 1e-8
+
+
+def test_server_pipelined_steps(gpu):
+    """cpm_server_step_async: each call harvests what the previous one launched and
+    returns with the next graphs running; host and device destinations give every
+    request within 1e-8 of its FP64 solve, like the synchronous steps, and a
+    request's result appears one call later than with them."""
+    import torch
+
+    T, O, rows = _setup(gpu, dx=0.1)
+    rng = np.random.default_rng(21)
+    B = np.stack([_rhs(rows, rng.uniform(0, 1, 2)) for _ in range(48)])
+    b_dev = torch.from_numpy(B[24:]).cuda()
+    x_dev = torch.zeros_like(b_dev)
+    torch.cuda.synchronize()
+    out = {}
+    for pipelined in (True, False):
+        srv = gpu.Server(O, 0.0, -1.0, batches=2)
+        for k in range(24):
+            srv.submit(B[k], k)
+        for k in range(24, 48):
+            srv.submit_device(b_dev[k - 24].data_ptr(), x_dev[k - 24].data_ptr(), k)
+        out[pipelined] = srv.drain(pipelined=pipelined)
+        xd = x_dev.cpu().numpy()
+        for k in range(24, 48):
+            out[pipelined][k] = (xd[k - 24].copy(), out[pipelined][k][1])
+        x_dev.zero_()
+        torch.cuda.synchronize()
+    ref = gpu.Solver(O, 0.0, -1.0)
+    for pipelined in (True, False):
+        assert sorted(out[pipelined]) == list(range(48))
+        assert all(v[1]["status"] == 0 for v in out[pipelined].values())
+        for k in (0, 23, 24, 47):
+            x64, _ = ref.solve(B[k], tol=1e-12, precision=0)
+            assert _rel(out[pipelined][k][0], x64[0]) <= 1e-8
+    # the first pipelined call only launches; the synchronous call already harvests
+    srv = gpu.Server(O, 0.0, -1.0)
+    srv.submit(np.zeros(O.D), 0)  # zero right-hand side: done at its start
+    assert srv.step(pipelined=True)[2] == 0
+    assert srv.step(pipelined=True)[2] == 1 and srv.poll()[0] == 0
+    srv.submit(np.zeros(O.D), 1)
+    assert srv.step()[2] == 1 and srv.poll()[0] == 1
