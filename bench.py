@@ -559,6 +559,43 @@ def main():
     xs = x_dev[sel].cpu().numpy()
     rel_err = float(max(np.max(np.abs(xs[j] - x64[j])) / np.max(np.abs(x64[j])) for j in range(KSLOTS)))
 
+    # ---- the same requests served to relative residual 1e-8, the metric's error bound (the
+    # plain FP64 path keeps the reference's 1e-10): a second server, timed the same way
+    tol8 = None
+    if stol != 1e-8:
+        x8 = torch.zeros_like(b_dev)
+        srv8 = cg.Server(O, 0.0, -1.0, tol=1e-8, refine_every=args.refine_every, inner_tol=args.inner_tol,
+                         batches=args.batches)
+
+        def stream8(lo, hi):
+            for k in range(lo, hi):
+                srv8.submit_device(b_dev[k].data_ptr(), x8[k].data_ptr(), k)
+            return srv8.drain(want_x=False)
+
+        stream8(0, n_warm)
+        torch.cuda.synchronize()
+        e8a, e8b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e8a.record(st)
+        served8 = stream8(n_warm, n_warm + n_timed)
+        e8b.record(st)
+        e8b.synchronize()
+        torch.cuda.synchronize()
+        t8 = max_over_ranks(e8a.elapsed_time(e8b) * 1e-3, dist, dev)
+        st8 = [served8[k][1] for k in range(n_warm, n_warm + n_timed)]
+        x8s = x8[sel].cpu().numpy()
+        tol8 = {"tol": 1e-8, "solves_per_s": replicas_value(world, n_timed, t8),
+                "max_rel_err_vs_fp64": float(max(np.max(np.abs(x8s[j] - x64[j])) / np.max(np.abs(x64[j]))
+                                                 for j in range(KSLOTS))),
+                "err_what": f"relative l_inf against FP64 solves (tol 1e-12) of {KSLOTS} of the requests",
+                "latency_ms": {"p50": float(np.percentile([x["service"] for x in st8], 50) * 1e3),
+                               "p99": float(np.percentile([x["service"] for x in st8], 99) * 1e3)},
+                "iterations_p50": float(np.median([x["iterations"] for x in st8])),
+                "fp64_fallbacks": int(sum(x.get("fp64_fallback", 0) for x in st8)),
+                "converged": bool(all(x["status"] == 0 for x in st8)),
+                "what": "the same requests through a server at relative residual 1e-8 (the metric's error bound); "
+                        "the plain FP64 path keeps the reference's 1e-10"}
+        del srv8, x8
+
     # ---- one static batch of 32 (all slots start together; the batch ends with its slowest solve)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
     bstat = torch.from_numpy(np.ascontiguousarray(B[sel].T)).to(dev)
@@ -700,6 +737,8 @@ def main():
                            "iterations": int(np.median(plain_iters)),
                            "tube_node_iterations_per_s": float(O.N * np.sum(plain_iters) / np.sum(plain_t))},
             "speedup_vs_fp64_plain": value / world / plain_sps,
+            "served_tol_1e-8": (dict(tol8, speedup_vs_fp64_plain=tol8["solves_per_s"] / world / plain_sps)
+                                if tol8 else None),
             # tube nodes x BiCGStab iterations (per right-hand side) per second, the whole job
             "tube_node_iterations_per_s": float(world * O.N * np.sum(iters) / t_total),
             "static_batch_32": {"solves_per_s": KSLOTS / static_s, "ms": static_s * 1e3,
